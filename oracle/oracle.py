@@ -1,0 +1,293 @@
+"""ctypes front end of the CPU oracles (test infrastructure only).
+
+Two libraries sit behind the same calls:
+
+* ``port``      -- oracle/libphotic_oracle.so, the C restatement in
+                   photic_oracle.c of the reference's samodel_Rrs /
+                   samodel_error / nelmin / samodel_optimise.  It builds on
+                   any host and is the oracle on the GPU machine.
+* ``reference`` -- oracle/_ref/libphotic_ref.so, the reference's own
+                   model/samodel.c, asa047.c and common.c compiled in place
+                   (only where the reference sources are available).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU legs import this
+module; the product never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "libphotic_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libphotic_ref.so")
+NOUT = 40
+
+# Output record columns shared by the oracles and the GPU path.
+COL = dict(H=0, B=1, cost=2, rrs_error=3, K_min=4, iod=5, evals_kept=6, evals=7,
+           converged=8, status=9, n_scenes=10, P=11, G=19, X=27, restarts=35,
+           kept_start=36, ifault=37)
+
+OLI_BANDS = (443.0, 482.0, 561.0, 655.0)
+DEFAULT_HSTARTS = (40.0, 30.0, 20.0, 15.0, 10.0, 7.5, 2.5, 1.0)
+
+_dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
+_ip = C.POINTER(C.c_int)
+_i32p = C.POINTER(C.c_int32)
+
+
+def build(ref: bool = True) -> None:
+    """Compile the port (and the reference harness when its sources exist)."""
+    targets = ["all"] if ref else ["libphotic_oracle.so"]
+    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(t) if a is not None else None
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class _Lib:
+    def __init__(self, path: str, prefix: str):
+        self.path = path
+        self.lib = C.CDLL(path)
+        self.prefix = prefix
+
+    def fn(self, name):
+        return getattr(self.lib, self.prefix + name)
+
+
+_port = None
+_ref = None
+
+
+def port() -> _Lib:
+    global _port
+    if _port is None:
+        if not os.path.exists(PORT_SO):
+            build(ref=False)
+        _port = _Lib(PORT_SO, "po_")
+        L = _port.lib
+        L.po_cost.restype = C.c_double
+        L.po_interp_1d.restype = C.c_double
+        L.po_invert_batch.argtypes = [C.c_int, _dp, C.c_double, C.c_double, C.c_double, _fp,
+                                      C.c_int64, C.c_float, C.c_double, C.c_int, C.c_int,
+                                      C.c_int, _dp, _dp, C.c_int, _dp]
+        L.po_joint_invert_batch.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _i32p, _dp,
+                                            _fp, C.c_int64, C.c_float, C.c_int, C.c_double,
+                                            C.c_int, C.c_int, C.c_int, _dp, C.c_int, _dp]
+        L.po_generate_single.argtypes = [C.c_uint64, C.c_int64, C.c_int64, C.c_int, _dp,
+                                         C.c_double, C.c_double, C.c_double, C.c_double,
+                                         C.c_float, _fp, _dp]
+        L.po_joint_counts.argtypes = [C.c_uint64, C.c_int64, C.c_int, C.c_int, _i32p]
+        L.po_generate_joint.argtypes = [C.c_uint64, C.c_int64, C.c_int, _dp, C.c_double,
+                                        C.c_double, C.c_double, C.c_double, C.c_double,
+                                        C.c_float, _i32p, _dp, _fp, _dp]
+        L.po_cost.argtypes = [C.c_int, _dp, C.c_double, C.c_double, C.c_double, _dp, _dp, _dp,
+                              _dp]
+        L.po_nelmin_pixel.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _dp, _dp, _dp,
+                                      C.c_double, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _ip]
+        L.po_band_constants.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _dp]
+        L.po_interp_1d.argtypes = [_dp, _dp, C.c_int, C.c_double]
+        L.po_philox4x32.argtypes = [C.c_uint32] * 6 + [C.POINTER(C.c_uint32)]
+    return _port
+
+
+def reference_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+def reference() -> _Lib:
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_SO):
+            raise FileNotFoundError(
+                "oracle/_ref/libphotic_ref.so is not built (needs the reference sources)")
+        _ref = _Lib(REF_SO, "photic_ref_")
+        L = _ref.lib
+        L.photic_ref_cost.restype = C.c_double
+        L.photic_ref_interp_1d.restype = C.c_double
+        L.photic_ref_invert_batch.argtypes = [C.c_int, _dp, C.c_double, C.c_double, C.c_double,
+                                              _fp, C.c_longlong, C.c_float, C.c_int, C.c_double,
+                                              C.c_int, C.c_int, C.c_int, _dp]
+        L.photic_ref_joint_invert_batch.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _ip,
+                                                    _dp, _fp, C.c_longlong, C.c_float, C.c_int,
+                                                    C.c_double, C.c_int, C.c_int, C.c_int, _dp]
+        L.photic_ref_cost.argtypes = [C.c_int, _dp, C.c_double, C.c_double, C.c_double, _dp,
+                                      _dp, C.c_int, _dp, _dp]
+        L.photic_ref_nelmin.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _dp, _dp, _dp,
+                                        C.c_double, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _ip]
+        L.photic_ref_band_constants.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _dp]
+        L.photic_ref_interp_1d.argtypes = [_dp, _dp, C.c_int, C.c_double]
+    return _ref
+
+
+# --------------------------------------------------------------------------
+# Calls with identical meaning on both libraries.
+# --------------------------------------------------------------------------
+
+def invert_batch(rrs, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0, h_tide=0.0,
+                 nodata=-9999.0, reqmin=1e-10, konvge=100, kcount=2000, hstarts=None,
+                 seeds=None, nthreads=0, which="port"):
+    """Invert [npix, n_bands] float32 spectra; returns [npix, NOUT] float64.
+
+    ``which="reference"`` runs the reference's own samodel_optimise with the
+    tolerances swapped in at its nelmin call; ``reqmin=None`` keeps the
+    reference's hard-coded 1e-2 / 100 / 5000 there.
+    """
+    rrs = _f32(rrs)
+    npix, nb = rrs.shape
+    wl = _f64(wl)
+    out = np.zeros((npix, NOUT), dtype=np.float64)
+    if which == "reference":
+        L = reference().lib
+        override = 0 if reqmin is None else 1
+        L.photic_ref_invert_batch(nb, _ptr(wl, _dp), theta_sun, theta_view, h_tide,
+                                  _ptr(rrs, _fp), npix, nodata, override,
+                                  1e-2 if reqmin is None else reqmin, konvge, kcount, nthreads,
+                                  _ptr(out, _dp))
+        return out
+    L = port().lib
+    if reqmin is None:
+        reqmin, konvge, kcount = 1e-2, 100, 5000
+    hs = _f64(hstarts) if hstarts is not None else None
+    sd = _f64(seeds) if seeds is not None else None
+    rc = L.po_invert_batch(nb, _ptr(wl, _dp), theta_sun, theta_view, h_tide, _ptr(rrs, _fp),
+                           npix, nodata, reqmin, konvge, kcount,
+                           0 if hs is None else len(hs), _ptr(hs, _dp), _ptr(sd, _dp), nthreads,
+                           _ptr(out, _dp))
+    if rc:
+        raise ValueError(f"po_invert_batch failed ({rc})")
+    return out
+
+
+def joint_invert_batch(scene_offsets, theta_sun, rrs, *, wl=OLI_BANDS, theta_view=0.0,
+                       h_tide=0.0, nodata=-9999.0, layout=0, reqmin=1e-10, konvge=100,
+                       kcount=2000, nthreads=0, which="port"):
+    offs = np.ascontiguousarray(scene_offsets, dtype=np.int32)
+    th = _f64(theta_sun)
+    rrs = _f32(rrs)
+    npix = len(offs) - 1
+    wl = _f64(wl)
+    out = np.zeros((npix, NOUT), dtype=np.float64)
+    if which == "reference":
+        if layout != 0:
+            raise ValueError("the reference implements only the shared-bottom layout")
+        L = reference().lib
+        L.photic_ref_joint_invert_batch(rrs.shape[1], _ptr(wl, _dp), theta_view, h_tide,
+                                        offs.ctypes.data_as(_ip), _ptr(th, _dp),
+                                        _ptr(rrs, _fp), npix, nodata, 1, reqmin, konvge,
+                                        kcount, nthreads, _ptr(out, _dp))
+        return out
+    L = port().lib
+    rc = L.po_joint_invert_batch(rrs.shape[1], _ptr(wl, _dp), theta_view, h_tide,
+                                 offs.ctypes.data_as(_i32p), _ptr(th, _dp), _ptr(rrs, _fp),
+                                 npix, nodata, layout, reqmin, konvge, kcount, 0, None,
+                                 nthreads, _ptr(out, _dp))
+    if rc:
+        raise ValueError(f"po_joint_invert_batch failed ({rc})")
+    return out
+
+
+def cost(rrs_measured, params, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0, h_tide=0.0,
+         which="port"):
+    """Cost, modelled Rrs and K of one 6-parameter vector for one spectrum."""
+    r = _f64(rrs_measured)
+    p = _f64(params)
+    wl = _f64(wl)
+    nb = len(wl)
+    rm = np.zeros(nb)
+    K = np.zeros(nb)
+    if which == "reference":
+        c = reference().lib.photic_ref_cost(nb, _ptr(wl, _dp), theta_sun, theta_view, h_tide,
+                                            _ptr(r, _dp), _ptr(p, _dp), len(p), _ptr(rm, _dp),
+                                            _ptr(K, _dp))
+    else:
+        c = port().lib.po_cost(nb, _ptr(wl, _dp), theta_sun, theta_view, h_tide, _ptr(r, _dp),
+                               _ptr(p, _dp), _ptr(rm, _dp), _ptr(K, _dp))
+    return c, rm, K
+
+
+def nelmin(rrs_measured, start, step, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0,
+           reqmin=1e-10, konvge=100, kcount=2000, which="port"):
+    r = _f64(rrs_measured)
+    st = _f64(start).copy()
+    sp = _f64(step)
+    wl = _f64(wl)
+    xmin = np.zeros(6)
+    y = C.c_double()
+    ic, nr, fl = C.c_int(), C.c_int(), C.c_int()
+    f = (reference().lib.photic_ref_nelmin if which == "reference"
+         else port().lib.po_nelmin_pixel)
+    f(len(wl), _ptr(wl, _dp), theta_sun, theta_view, _ptr(r, _dp), _ptr(st, _dp),
+      _ptr(sp, _dp), reqmin, konvge, kcount, _ptr(xmin, _dp), C.byref(y), C.byref(ic),
+      C.byref(nr), C.byref(fl))
+    return xmin, y.value, ic.value, nr.value, fl.value
+
+
+def band_constants(*, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0, which="port"):
+    wl = _f64(wl)
+    out = np.zeros((len(wl), 8))
+    f = (reference().lib.photic_ref_band_constants if which == "reference"
+         else port().lib.po_band_constants)
+    f(len(wl), _ptr(wl, _dp), theta_sun, theta_view, _ptr(out, _dp))
+    return out
+
+
+def interp_1d(X, Y, x, which="port"):
+    X = _f64(X)
+    Y = _f64(Y)
+    f = (reference().lib.photic_ref_interp_1d if which == "reference"
+         else port().lib.po_interp_1d)
+    return f(_ptr(X, _dp), _ptr(Y, _dp), len(X), x)
+
+
+# --------------------------------------------------------------------------
+# Synthetic generator (port only; the reference has none).
+# --------------------------------------------------------------------------
+
+def generate_single(seed, npix, *, pix0=0, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0,
+                    mask_frac=0.15, noise_sigma=2e-4, nodata=-9999.0):
+    wl = _f64(wl)
+    rrs = np.zeros((npix, len(wl)), dtype=np.float32)
+    truth = np.zeros((npix, 5))
+    port().lib.po_generate_single(seed, pix0, npix, len(wl), _ptr(wl, _dp), theta_sun,
+                                  theta_view, mask_frac, noise_sigma, nodata, _ptr(rrs, _fp),
+                                  _ptr(truth, _dp))
+    return rrs, truth
+
+
+def generate_joint(seed, npix, *, kmin=2, kmax=8, wl=OLI_BANDS, theta_view=0.0,
+                   theta_sun_range=(25.0, 50.0), mask_frac=0.0, noise_sigma=2e-4,
+                   nodata=-9999.0):
+    wl = _f64(wl)
+    counts = np.zeros(npix, dtype=np.int32)
+    port().lib.po_joint_counts(seed, npix, kmin, kmax, counts.ctypes.data_as(_i32p))
+    offs = np.zeros(npix + 1, dtype=np.int32)
+    offs[1:] = np.cumsum(counts)
+    nobs = int(offs[-1])
+    th = np.zeros(nobs)
+    rrs = np.zeros((nobs, len(wl)), dtype=np.float32)
+    truth = np.zeros((nobs, 5))
+    port().lib.po_generate_joint(seed, npix, len(wl), _ptr(wl, _dp), theta_view,
+                                 theta_sun_range[0], theta_sun_range[1], mask_frac, noise_sigma,
+                                 nodata, offs.ctypes.data_as(_i32p), _ptr(th, _dp),
+                                 _ptr(rrs, _fp), _ptr(truth, _dp))
+    return offs, th, rrs, truth
+
+
+def philox4x32(c, k):
+    out = (C.c_uint32 * 4)()
+    port().lib.po_philox4x32(*(list(c) + list(k)), out)
+    return list(out)

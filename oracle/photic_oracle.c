@@ -1,0 +1,1005 @@
+/*
+ * photic_oracle.c -- CPU restatement of photic's per-pixel inversion.
+ *
+ * TEST INFRASTRUCTURE ONLY (see photic_oracle.h).  Only tests/,
+ * __graft_entry__.smoke() and bench.py's CPU legs load this library, and
+ * only as the checker or as the timed CPU baseline, never as the product.
+ *
+ * Every routine below states which reference lines it follows.  The
+ * arithmetic is written in the same association order as the reference so
+ * that, built with the same compiler flags and libm, it reproduces the
+ * reference's results bit for bit (checked against oracle/_ref by
+ * tests/test_oracle_vs_reference.py).  The one deliberate departure is the
+ * double -> long truncation inside nelmin's local-minimum test
+ * (model/asa047.c:438,445,460), whose result for NaN or |x| >= 2^63 is
+ * undefined in C: it is pinned here to the x86-64 behaviour (LONG_MIN) so
+ * that the oracle agrees with itself on every host.
+ */
+#include "photic_oracle.h"
+
+#include <limits.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#if _OPENMP
+#include <omp.h>
+#endif
+
+#define PO_PI 3.141592653589793 /* model/common.h:19 */
+
+/* ------------------------------------------------------------------------
+ * Spectral tables on the 41-point 400..800 nm grid.  Values are the
+ * published tables the reference tabulates in model/samodel.c:105-287:
+ * pure-water absorption (Pope & Fry 1997), pure-water backscatter
+ * (Morel 1974), Lee's a0/a1 phytoplankton coefficients (Lee 1994) and the
+ * eight HYDROLIGHT-averaged bottom reflectance spectra.  They must be equal
+ * to the reference's numbers for parity, so they are data, not design.
+ * ---------------------------------------------------------------------- */
+#define PO_NREF 41
+static const double po_ref_wl[PO_NREF] = {
+    400, 410, 420, 430, 440, 450, 460, 470, 480, 490, 500, 510, 520, 530,
+    540, 550, 560, 570, 580, 590, 600, 610, 620, 630, 640, 650, 660, 670,
+    680, 690, 700, 710, 720, 730, 740, 750, 760, 770, 780, 790, 800};
+static const double po_aw[PO_NREF] = {
+    0.00663, 0.00473, 0.00454, 0.00495, 0.00635, 0.00922, 0.00979, 0.0106, 0.0127,
+    0.015,   0.0204,  0.0325,  0.0409,  0.0434,  0.0474,  0.0565,  0.0619, 0.0695,
+    0.0896,  0.1351,  0.2224,  0.2644,  0.2755,  0.2916,  0.3108,  0.34,   0.41,
+    0.439,   0.465,   0.516,   0.624,   0.827,   1.231,   1.65768, 2.38147, 2.47014,
+    2.5045,  2.47509, 2.35431, 2.17654, 2.01226};
+static const double po_bbw[PO_NREF] = {
+    0.0038,      0.00341552,  0.00307784,  0.00278035,  0.00251749,  0.00228457,
+    0.00207763,  0.0018933,   0.0017287,   0.00158138,  0.00144921,  0.00133039,
+    0.00122334,  0.00112671,  0.0010393,   0.000960099, 0.000888199, 0.000822817,
+    0.000763262, 0.000708928, 0.000659279, 0.000613844, 0.000572204, 0.000533988,
+    0.000498868, 0.000466549, 0.00043677,  0.000409298, 0.000383923, 0.000360458,
+    0.000338734, 0.000318601, 0.000299921, 0.000282571, 0.000266441, 0.000251431,
+    0.000237448, 0.00022441,  0.000212243, 0.000200879, 0.000190254};
+static const double po_a0[PO_NREF] = {
+    0.684266, 0.778234, 0.86369,  0.960272, 1,        0.96339,  0.931107, 0.869651, 0.788982,
+    0.755811, 0.733335, 0.691062, 0.632722, 0.568079, 0.504551, 0.426236, 0.343342, 0.294978,
+    0.278405, 0.259509, 0.238935, 0.274531, 0.319712, 0.342135, 0.333133, 0.350196, 0.560974,
+    0.843456, 0.74852,  0.4,      0.15,     0.06,     0.026,    0.013,    0.013,    0.013,
+    0.013,    0.013,    0.013,    0.013,    0.013};
+static const double po_a1[PO_NREF] = {
+    0.0205345, 0.0129366, 0.0064013, 0.00168429, 0,         0.00602146, 0.0109083,
+    0.0157169, 0.0152315, 0.0255969, 0.0559074,  0.0865174, 0.098141,   0.0968975,
+    0.0899322, 0.0780758, 0.0658936, 0.0596445,  0.0581118, 0.0539721,  0.0494872,
+    0.057845,  0.0673832, 0.0717643, 0.0684625,  0.0713488, 0.112818,   0.159471,
+    0.138835,  0.0811786, 0.03,      0.012,      0.0054,    0.0028,     0.0028,
+    0.0028,    0.0028,    0.0028,    0.0028,     0.0028,    0.0028};
+/* Bottom table order: sand, seagrass, coral, macrophytes, dark sediment,
+ * coral sand, green algae, red algae (model/samodel.c:464-475). */
+static const double po_bottom[PO_N_BOTTOM_TYPES][PO_NREF] = {
+    {0.634432, 0.654965, 0.682443, 0.712079, 0.74123,  0.769656, 0.802245, 0.827992, 0.854624,
+     0.878036, 0.89898,  0.924542, 0.94899,  0.965671, 0.982481, 1.,       1.01237,  1.02994,
+     1.04658,  1.07139,  1.08139,  1.08884,  1.09447,  1.09916,  1.10557,  1.10758,  1.101,
+     1.08464,  1.08658,  1.12477,  1.17063,  1.20125,  1.21407,  1.22691,  1.23186,  1.24098,
+     1.24708,  1.25257,  1.25607,  1.26361,  1.26789},
+    {0.542201, 0.538755, 0.543345, 0.550218, 0.550218, 0.562483, 0.606813, 0.607225, 0.63619,
+     0.650873, 0.670997, 0.735138, 0.808387, 0.887508, 0.949743, 1.,       1.03488,  1.04312,
+     1.03199,  1.00882,  0.95964,  0.903696, 0.85915,  0.848253, 0.830917, 0.807567, 0.785207,
+     0.839027, 1.09213,  1.68562,  2.5015,   4.15478,  5.11731,  5.77383,  6.02484,  6.11441,
+     6.16467,  6.22648,  6.27581,  6.29811,  6.34481},
+    {0.437155, 0.381353, 0.353904, 0.339709, 0.358934, 0.382172, 0.390592, 0.407088, 0.462696,
+     0.522577, 0.60409,  0.707443, 0.764575, 0.826841, 0.892756, 1.,       1.15687,  1.3644,
+     1.44365,  1.40967,  1.48473,  1.53551,  1.41572,  1.32706,  1.25349,  1.20397,  0.955824,
+     0.643935, 0.669901, 1.38703,  2.42848,  3.3846,   3.6429,   3.89712,  4.10336,  4.23733,
+     4.32766,  4.37486,  4.43428,  4.47756,  4.52468},
+    {0.443737, 0.401082, 0.382427, 0.382427, 0.382427, 0.382427, 0.402497, 0.409674, 0.443211,
+     0.44772,  0.494445, 0.620241, 0.755823, 0.882367, 0.973539, 1.,       1.09947,  1.09321,
+     1.11723,  1.09127,  1.06283,  1.03064,  0.919521, 0.896435, 0.839186, 0.769511, 0.645607,
+     0.60577,  0.743085, 1.1217,   2.17169,  3.27124,  3.47565,  3.3989,   3.48151,  3.59713,
+     3.65614,  3.65521,  3.67159,  3.6131,   3.58176},
+    {0.57054,  0.564806, 0.583536, 0.596254, 0.616995, 0.640224, 0.669295, 0.691865, 0.722327,
+     0.740098, 0.765618, 0.801745, 0.850374, 0.901024, 0.943913, 1.,       1.05834,  1.10294,
+     1.13346,  1.17132,  1.20427,  1.20038,  1.16874,  1.16074,  1.14623,  1.14875,  1.03881,
+     0.903713, 0.894767, 1.05454,  1.30921,  1.49551,  1.58863,  1.64064,  1.65234,  1.66933,
+     1.68055,  1.69243,  1.70471,  1.72121,  1.72876},
+    {0.616201, 0.636915, 0.659543, 0.685341, 0.71562,  0.742639, 0.769601, 0.792999, 0.818446,
+     0.840791, 0.86273,  0.890834, 0.912898, 0.940877, 0.970795, 1.,       1.03073,  1.05991,
+     1.08887,  1.1141,   1.13666,  1.15865,  1.18297,  1.20189,  1.22277,  1.23953,  1.25598,
+     1.27532,  1.29161,  1.31127,  1.3302,   1.348,    1.36099,  1.37632,  1.38579,  1.39478,
+     1.40298,  1.41371,  1.42261,  1.43402,  1.44206},
+    {0.16848,  0.188393, 0.188646, 0.17936,  0.170655, 0.190607, 0.220843, 0.241126, 0.262068,
+     0.294282, 0.357834, 0.516557, 0.717781, 0.898626, 0.975598, 1.,       1.00009,  0.946152,
+     0.874696, 0.829798, 0.807546, 0.763138, 0.701775, 0.673854, 0.606387, 0.524554, 0.426766,
+     0.3044,   0.284069, 0.48541,  0.912011, 1.33421,  1.52307,  1.61754,  1.65643,  1.66741,
+     1.66741,  1.66741,  1.66741,  1.66741,  1.66298},
+    {1.25032,  1.13331,  1.06326,  1.00005,  0.925705, 0.983453, 1.,       1.,       0.975044,
+     0.877564, 0.877766, 0.987416, 1.04918,  1.03747,  1.,       1.,       1.01387,  1.16916,
+     1.56137,  2.08995,  2.44941,  2.40749,  2.30252,  2.33337,  2.48719,  2.53279,  2.21543,
+     1.72598,  1.80604,  2.72284,  4.35056,  5.67543,  6.32734,  6.72766,  6.90232,  6.98939,
+     7.04997,  7.09008,  7.11525,  7.09872,  7.04973}};
+
+/* ------------------------------------------------------------------------
+ * Tolerant comparisons in single precision (model/common.c:392-406) and
+ * piecewise-linear interpolation with end-segment extrapolation
+ * (interp_1d, model/common.c:298-335).  The float arguments are part of the
+ * behaviour: doubles are rounded to float before comparing.
+ * ---------------------------------------------------------------------- */
+static int f_close(float a, float b, float eps) {
+  double big = fabs(a) < fabs(b) ? fabs(b) : fabs(a);
+  return fabs(a - b) <= big * eps;
+}
+static int f_le(float a, float b, float eps) { return a < b || f_close(a, b, eps); }
+static int f_ge(float a, float b, float eps) { return a > b || f_close(a, b, eps); }
+
+double po_interp_1d(const double *X, const double *Y, int n, double x) {
+  double x0 = 0.0, x1 = 1.0, y0 = 0.0, y1 = 0.0, t;
+  int i;
+  if (f_close(x, X[0], 1.0e-5)) return Y[0];
+  if (f_close(x, X[n - 1], 1.0e-5)) return Y[n - 1];
+  if (X[0] < X[n - 1] && x < X[0]) {
+    x0 = X[0]; x1 = X[1]; y0 = Y[0]; y1 = Y[1];
+  } else if (X[n - 1] > X[0] && x > X[n - 1]) {
+    x0 = X[n - 2]; x1 = X[n - 1]; y0 = Y[n - 2]; y1 = Y[n - 1];
+  } else {
+    for (i = 0; i + 1 < n; i++) {
+      int up = f_le(X[i], x, 1.0e-5) && f_ge(X[i + 1], x, 1.0e-5);
+      int down = f_ge(X[i], x, 1.0e-5) && f_le(X[i + 1], x, 1.0e-5);
+      if (up || down) {
+        x0 = X[i]; x1 = X[i + 1]; y0 = Y[i]; y1 = Y[i + 1];
+        break;
+      }
+    }
+  }
+  t = (x - x0) / (x1 - x0);
+  return y0 * (1.0 - t) + y1 * t;
+}
+
+/* ------------------------------------------------------------------------
+ * Scene constants: band-wavelength interpolation of the tables and the
+ * subsurface angle secants, as samodel() prepares them
+ * (model/samodel.c:505, 534-548, 550-618).
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  int n_bands;
+  double wl[PO_MAX_BANDS];
+  double a0[PO_MAX_BANDS], a1[PO_MAX_BANDS], aw[PO_MAX_BANDS], bbw[PO_MAX_BANDS];
+  double refl[PO_N_BOTTOM_TYPES][PO_MAX_BANDS];
+  double sec_sun, sec_view, h_tide, aw640;
+} po_scene;
+
+static void scene_init(po_scene *sc, int n_bands, const double *wl, double theta_sun_deg,
+                       double theta_view_deg, double h_tide) {
+  int b, k;
+  double th;
+  sc->n_bands = n_bands;
+  th = theta_view_deg;
+  th *= PO_PI / 180.0;
+  sc->sec_view = 1.0 / cos(th);
+  th = theta_sun_deg;
+  th *= PO_PI / 180.0;
+  sc->sec_sun = 1.0 / cos(th);
+  sc->h_tide = h_tide;
+  sc->aw640 = po_interp_1d(po_ref_wl, po_aw, PO_NREF, 640.0);
+  for (b = 0; b < n_bands; b++) {
+    double l = wl[b];
+    sc->wl[b] = l;
+    sc->a0[b] = po_interp_1d(po_ref_wl, po_a0, PO_NREF, l);
+    sc->a1[b] = po_interp_1d(po_ref_wl, po_a1, PO_NREF, l);
+    sc->bbw[b] = po_interp_1d(po_ref_wl, po_bbw, PO_NREF, l);
+    sc->aw[b] = po_interp_1d(po_ref_wl, po_aw, PO_NREF, l);
+    for (k = 0; k < PO_N_BOTTOM_TYPES; k++)
+      sc->refl[k][b] = po_interp_1d(po_ref_wl, po_bottom[k], PO_NREF, l);
+  }
+}
+
+void po_band_constants(int n_bands, const double *wl, double theta_sun_deg,
+                       double theta_view_deg, double *out) {
+  po_scene sc;
+  int b;
+  scene_init(&sc, n_bands, wl, theta_sun_deg, theta_view_deg, 0.0);
+  for (b = 0; b < n_bands; b++) {
+    out[b * 8 + 0] = sc.a0[b];
+    out[b * 8 + 1] = sc.a1[b];
+    out[b * 8 + 2] = sc.aw[b];
+    out[b * 8 + 3] = sc.bbw[b];
+    out[b * 8 + 4] = sc.refl[0][b];
+    out[b * 8 + 5] = sc.sec_sun;
+    out[b * 8 + 6] = sc.sec_view;
+    out[b * 8 + 7] = sc.aw640;
+  }
+}
+
+/* ------------------------------------------------------------------------
+ * One pixel: its scenes, measured spectra, the interpolated Rrs at
+ * 440/490/550/640/750 nm, and the per-evaluation side outputs the
+ * reference keeps in model_data.
+ * ---------------------------------------------------------------------- */
+enum { PO_LAYOUT_REFERENCE = 0, PO_LAYOUT_PER_SCENE_B = 1 };
+
+typedef struct {
+  int n_scenes, n_bands, n_bottoms, layout;
+  const po_scene *sc[PO_MAX_SCENES];
+  double rrs[PO_MAX_SCENES][PO_MAX_BANDS];
+  double r440[PO_MAX_SCENES], r490[PO_MAX_SCENES], r550[PO_MAX_SCENES];
+  double r640[PO_MAX_SCENES], r750[PO_MAX_SCENES];
+  /* side outputs of the latest cost evaluation */
+  double Rm[PO_MAX_SCENES][PO_MAX_BANDS], rrs_mod[PO_MAX_SCENES][PO_MAX_BANDS];
+  double rrs_bot[PO_MAX_SCENES][PO_MAX_BANDS], K[PO_MAX_SCENES][PO_MAX_BANDS];
+  double bottom_albedo, rrs_error, model_error;
+} po_pixel;
+
+static int n_params_of(const po_pixel *px) {
+  if (px->layout == PO_LAYOUT_PER_SCENE_B) return 1 + 4 * px->n_scenes;
+  return 1 + 2 * px->n_bottoms + 3 * px->n_scenes; /* model/samodel.c:1833-1855 */
+}
+
+/* Rrs(440..750) of each scene from its measured bands, with the
+ * negative-440 guard (model/samodel.c:1785-1799). */
+static void pixel_reference_rrs(po_pixel *px) {
+  int s;
+  for (s = 0; s < px->n_scenes; s++) {
+    const double *wl = px->sc[s]->wl;
+    int n = px->n_bands;
+    px->r440[s] = po_interp_1d(wl, px->rrs[s], n, 440.0);
+    px->r490[s] = po_interp_1d(wl, px->rrs[s], n, 490.0);
+    px->r550[s] = po_interp_1d(wl, px->rrs[s], n, 550.0);
+    px->r640[s] = po_interp_1d(wl, px->rrs[s], n, 640.0);
+    px->r750[s] = po_interp_1d(wl, px->rrs[s], n, 750.0);
+    if (px->r440[s] < 0.0) px->r440[s] = 0.0001;
+  }
+}
+
+/* HOPE forward model for one band (samodel_Rrs, model/samodel.c:2846-2949).
+ * rho is the already mixed bottom term sum_i q_i B_i rho_i(lambda). */
+static double hope_band(const po_scene *sc, int b, double P, double G, double X, double rho,
+                        double H, double Delta, double r440, double r490, double *K_out,
+                        double *rrs_bottom, double *rrs_total) {
+  const double S = 0.015;
+  double a_phi, a_g, a, chi, Y, b_p, bb, u, K, rrs_dp, DuC, DuB, M, rrs_C, rrs_B, rrs;
+  double lambda = sc->wl[b];
+  a_phi = (sc->a0[b] + sc->a1[b] * log(fabs(P))) * fabs(P);
+  a_g = fabs(G) * exp(-S * (lambda - 440.0));
+  a = sc->aw[b] + a_phi + a_g;
+  chi = r440 / r490;
+  Y = 3.44 * (1.0 - 3.17 * exp(-2.01 * chi));
+  if (Y < 0.0) Y = 0.0;
+  if (Y > 2.5) Y = 2.5;
+  b_p = X * pow(440.0 / lambda, Y);
+  bb = sc->bbw[b] + b_p;
+  u = bb / (a + bb);
+  K = a + bb;
+  if (K < 0.0) K = 0.0;
+  if (K > 2.5) K = 2.5;
+  *K_out = K;
+  rrs_dp = (0.084 + 0.170 * u) * u;
+  DuC = 1.03 * sqrt(1.0 + 2.4 * u);
+  DuB = 1.04 * sqrt(1.0 + 5.4 * u);
+  M = sc->sec_sun + DuC * sc->sec_view;
+  rrs_C = rrs_dp * (1.0 - exp(-M * K * H));
+  M = sc->sec_sun + DuB * sc->sec_view;
+  rrs_B = rho / PO_PI * exp(-M * K * H);
+  *rrs_bottom = rrs_B;
+  rrs = rrs_C + rrs_B;
+  *rrs_total = rrs;
+  return 0.5 * rrs / (1.0 - 1.5 * rrs) + Delta;
+}
+
+/* Cost of one parameter vector (samodel_error, model/samodel.c:2432-2759)
+ * for a single spatial region.  With one region the depth- and
+ * bottom-continuity terms (model/samodel.c:2598-2692) compare each value
+ * with itself and are identically zero, and SAM is compiled out (SAM 0,
+ * model/samodel.c:96), so the weighted sum reduces to the spectral and K
+ * terms; both are restated here in the reference's operation order. */
+static double pixel_cost(const double *x, void *ctx) {
+  po_pixel *px = (po_pixel *)ctx;
+  const int nb = px->n_bottoms;
+  double err = 0.0, tot = 0.0, H, rrs_error, K_error, K_min = 1.0e4, model;
+  int s, b, k, nobs = 0;
+
+  H = fabs(x[0]);
+  for (s = 0; s < px->n_scenes; s++) {
+    const po_scene *sc = px->sc[s];
+    double P, G, X, B[PO_N_BOTTOM_TYPES], q[PO_N_BOTTOM_TYPES], q_sum = 0.0;
+    int nbs;
+    if (px->layout == PO_LAYOUT_PER_SCENE_B) {
+      B[0] = 0.01 * fabs(x[1 + 4 * s]);
+      P = 0.01 * fabs(x[1 + 4 * s + 1]);
+      G = 0.01 * fabs(x[1 + 4 * s + 2]);
+      X = 0.01 * fabs(x[1 + 4 * s + 3]);
+      q[0] = 1.0;
+      nbs = 1;
+    } else {
+      int off = 1 + 2 * nb;
+      P = 0.01 * fabs(x[off + 3 * s]);
+      G = 0.01 * fabs(x[off + 3 * s + 1]);
+      X = 0.01 * fabs(x[off + 3 * s + 2]);
+      for (k = 0; k < nb; k++) B[k] = 0.01 * fabs(x[1 + k]);
+      for (k = 0; k < nb; k++) {
+        q[k] = fabs(x[1 + nb + k]);
+        q_sum += q[k];
+      }
+      for (k = 0; k < nb; k++) q[k] /= q_sum;
+      nbs = nb;
+    }
+    for (b = 0; b < px->n_bands; b++) {
+      double rho = 0.0, albedo = 0.0, Rm, d;
+      for (k = 0; k < nbs; k++) {
+        albedo += q[k] * B[k];
+        rho += q[k] * B[k] * sc->refl[k][b];
+      }
+      px->bottom_albedo = albedo;
+      Rm = hope_band(sc, b, P, G, X, rho, H, 0.0, px->r440[s], px->r490[s], &px->K[s][b],
+                     &px->rrs_bot[s][b], &px->rrs_mod[s][b]);
+      px->Rm[s][b] = Rm;
+      d = Rm - px->rrs[s][b];
+      err += pow(d, 2.0);
+      tot += px->rrs[s][b];
+      nobs++;
+    }
+  }
+  rrs_error = 100.0 * sqrt(err / (double)nobs) / (tot / (double)nobs);
+  px->rrs_error = rrs_error;
+
+  /* Shallow/low-K and very-high-K penalties, model/samodel.c:2696-2732. */
+  {
+    const double mean_c = 0.275, min_c = 0.185;
+    K_error = 0.0;
+    for (s = 0; s < px->n_scenes; s++) {
+      K_min = 1.0e4;
+      for (b = 0; b < px->n_bands; b++)
+        if (!f_close((float)px->K[s][b], 0.0f, 1.0e-6f) && px->K[s][b] < K_min) K_min = px->K[s][b];
+      if (H < 1.0 && K_min < mean_c) {
+        K_error += 100.0 * pow(1.0 / (0.01 + K_min) - 1.0 / (0.01 + min_c), 2);
+      } else if (H < 2.0 && K_min < 0.5 * (1.5 * min_c + 0.5 * mean_c)) {
+        K_error += 100.0 * pow(1.0 / (0.01 + K_min) - 1.0 / (0.01 + 0.5 * (1.5 * min_c + 0.5 * mean_c)), 2);
+      } else if (H < 3.0 && K_min < 0.5 * (1.25 * min_c + 0.75 * mean_c)) {
+        K_error += 100.0 * pow(1.0 / (0.01 + K_min) - 1.0 / (0.01 + 0.5 * (1.25 * min_c + 0.75 * mean_c)), 2);
+      } else if (H < 4.0 && K_min < 0.5 * (1.5 * min_c + 0.5 * mean_c)) {
+        K_error += 100.0 * pow(1.0 / (0.01 + K_min) - 1.0 / (0.01 + 0.5 * (1.5 * min_c + 0.5 * mean_c)), 2);
+      } else if (H < 5.0 && K_min < 0.5 * (1.75 * min_c + 0.25 * mean_c)) {
+        K_error += 100.0 * pow(1.0 / (0.01 + K_min) - 1.0 / (0.01 + 0.5 * (1.75 * min_c + 0.25 * mean_c)), 2);
+      }
+    }
+    /* uses the last scene's K_min, as the reference does */
+    if (K_min > 0.7) K_error += 100.0 * pow(4.0 * (K_min - 0.7), 2);
+  }
+  /* weights 80/15/10/15 (model/samodel.c:2736-2744); depth/bottom terms 0 */
+  model = 80.0 * rrs_error + 15.0 * K_error;
+  model /= 120.0;
+  px->model_error = model;
+  return model;
+}
+
+/* ------------------------------------------------------------------------
+ * Nelder-Mead, AS 47 as modified in model/asa047.c:10-502: reflection 1,
+ * expansion 2, contraction 1/2, shrink towards the best vertex; variance
+ * test every konvge iterations against reqmin*n; then the +/- eps*step
+ * local-minimum probe on (long)(10*y) truncated costs, restarting from the
+ * probe point with a 1e-6 scaled simplex when it fails.
+ * ---------------------------------------------------------------------- */
+typedef double (*po_fn)(const double *x, void *ctx);
+
+/* (long)(10*y) with the x86-64 result for NaN and out-of-range values. */
+static long trunc_to_long(double v) {
+  if (!(v > -9.2233720368547758e18 && v < 9.2233720368547758e18)) return LONG_MIN;
+  return (long)v;
+}
+
+static void po_nelmin(po_fn fn, void *ctx, int n, double *start, double *xmin, double *ynewlo,
+                      double reqmin, const double *step, int konvge, int kcount, int *icount,
+                      int *numres, int *ifault) {
+  const double grow = 2.0, shrink = 0.5, eps = 1.0e-6;
+  double v[(PO_MAX_PARAMS + 1) * PO_MAX_PARAMS], f[PO_MAX_PARAMS + 1];
+  double cen[PO_MAX_PARAMS], refl[PO_MAX_PARAMS], trial[PO_MAX_PARAMS];
+  double scale = 1.0, fr, ft, fmean, var, delta, ylo;
+  const double nd = (double)n, n1d = (double)(n + 1), var_limit = reqmin * nd;
+  int i, j, lo, hi, countdown = konvge;
+  long floor_lo, floor_probe;
+
+  if (reqmin <= 0.0 || n < 1 || konvge < 1) {
+    *ifault = 1;
+    return;
+  }
+  *icount = 0;
+  *numres = 0;
+  for (;;) {
+    /* Simplex: vertex n is the start point, vertex j moves coordinate j. */
+    for (i = 0; i < n; i++) v[n * n + i] = start[i];
+    f[n] = fn(start, ctx);
+    (*icount)++;
+    for (j = 0; j < n; j++) {
+      double keep = start[j];
+      start[j] = start[j] + step[j] * scale;
+      for (i = 0; i < n; i++) v[j * n + i] = start[i];
+      f[j] = fn(start, ctx);
+      (*icount)++;
+      start[j] = keep;
+    }
+    /* ylo is kept apart from f[lo]: when every vertex ties, hi == lo and
+     * the reference keeps comparing against the old best value. */
+    ylo = f[0];
+    lo = 0;
+    for (j = 1; j <= n; j++)
+      if (f[j] < ylo) {
+        ylo = f[j];
+        lo = j;
+      }
+
+    for (;;) {
+      if (kcount <= *icount) break;
+      hi = 0;
+      for (j = 1; j <= n; j++)
+        if (f[hi] < f[j]) hi = j;
+      *ynewlo = f[hi];
+      for (i = 0; i < n; i++) {
+        double z = 0.0;
+        for (j = 0; j <= n; j++) z = z + v[j * n + i];
+        z = z - v[hi * n + i];
+        cen[i] = z / nd;
+      }
+      for (i = 0; i < n; i++) refl[i] = cen[i] + 1.0 * (cen[i] - v[hi * n + i]);
+      fr = fn(refl, ctx);
+      (*icount)++;
+
+      if (fr < ylo) {
+        for (i = 0; i < n; i++) trial[i] = cen[i] + grow * (refl[i] - cen[i]);
+        ft = fn(trial, ctx);
+        (*icount)++;
+        if (fr < ft) {
+          for (i = 0; i < n; i++) v[hi * n + i] = refl[i];
+          f[hi] = fr;
+        } else {
+          for (i = 0; i < n; i++) v[hi * n + i] = trial[i];
+          f[hi] = ft;
+        }
+      } else {
+        int worse = 0;
+        for (j = 0; j <= n; j++)
+          if (fr < f[j]) worse++;
+        if (worse > 1) {
+          for (i = 0; i < n; i++) v[hi * n + i] = refl[i];
+          f[hi] = fr;
+        } else if (worse == 0) {
+          for (i = 0; i < n; i++) trial[i] = cen[i] + shrink * (v[hi * n + i] - cen[i]);
+          ft = fn(trial, ctx);
+          (*icount)++;
+          if (f[hi] < ft) {
+            /* shrink every vertex towards the best one */
+            for (j = 0; j <= n; j++) {
+              for (i = 0; i < n; i++) {
+                v[j * n + i] = (v[j * n + i] + v[lo * n + i]) * 0.5;
+                xmin[i] = v[j * n + i];
+              }
+              f[j] = fn(xmin, ctx);
+              (*icount)++;
+            }
+            ylo = f[0];
+            lo = 0;
+            for (j = 1; j <= n; j++)
+              if (f[j] < ylo) {
+                ylo = f[j];
+                lo = j;
+              }
+            continue;
+          }
+          for (i = 0; i < n; i++) v[hi * n + i] = trial[i];
+          f[hi] = ft;
+        } else {
+          for (i = 0; i < n; i++) trial[i] = cen[i] + shrink * (refl[i] - cen[i]);
+          ft = fn(trial, ctx);
+          (*icount)++;
+          if (ft <= fr) {
+            for (i = 0; i < n; i++) v[hi * n + i] = trial[i];
+            f[hi] = ft;
+          } else {
+            for (i = 0; i < n; i++) v[hi * n + i] = refl[i];
+            f[hi] = fr;
+          }
+        }
+      }
+      if (f[hi] < ylo) {
+        ylo = f[hi];
+        lo = hi;
+      }
+      countdown--;
+      if (countdown > 0) continue;
+      if (*icount <= kcount) {
+        countdown = konvge;
+        fmean = 0.0;
+        for (j = 0; j <= n; j++) fmean = fmean + f[j];
+        fmean = fmean / n1d;
+        var = 0.0;
+        for (j = 0; j <= n; j++) var = var + pow(f[j] - fmean, 2);
+        if (var <= var_limit) break;
+      }
+    }
+
+    for (i = 0; i < n; i++) xmin[i] = v[lo * n + i];
+    *ynewlo = f[lo];
+    floor_lo = trunc_to_long(10.0 * f[lo]);
+    if (kcount < *icount) {
+      *ifault = 2;
+      break;
+    }
+    *ifault = 0;
+    for (i = 0; i < n; i++) {
+      delta = step[i] * eps;
+      xmin[i] = xmin[i] + delta;
+      floor_probe = trunc_to_long(10.0 * fn(xmin, ctx));
+      (*icount)++;
+      if (floor_probe < floor_lo) {
+        *ifault = 2;
+        break;
+      }
+      xmin[i] = xmin[i] - delta - delta;
+      floor_probe = trunc_to_long(10.0 * fn(xmin, ctx));
+      (*icount)++;
+      if (floor_probe < floor_lo) {
+        *ifault = 2;
+        break;
+      }
+      xmin[i] = xmin[i] + delta;
+    }
+    if (*ifault == 0) break;
+    for (i = 0; i < n; i++) start[i] = xmin[i];
+    scale = eps;
+    (*numres)++;
+  }
+}
+
+/* ------------------------------------------------------------------------
+ * Per-pixel driver (samodel_optimise + _one_bottom_combination, cold start,
+ * no empirical depth, model/samodel.c:1768-2115 and :2119-2427), or a
+ * single fit from a caller-given start vector (seeded).
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  double reqmin;
+  int konvge, kcount;
+  int n_hstarts;
+  const double *hstarts;
+} po_fit;
+
+static void cold_start(const po_pixel *px, double H0, double *start, double *step) {
+  const int nb = px->n_bottoms, ns = px->n_scenes;
+  double m490 = 0.0;
+  int s, k;
+  start[0] = H0;
+  step[0] = 1.25 * start[0];
+  for (s = 0; s < ns; s++) m490 += px->r490[s];
+  m490 /= (double)1 * ns;
+  if (px->layout == PO_LAYOUT_PER_SCENE_B) {
+    for (s = 0; s < ns; s++) {
+      double r490 = (0.0 + px->r490[s]) / (double)1;
+      double r550 = (0.0 + px->r550[s]) / (double)1;
+      double r640 = (0.0 + px->r640[s]) / (double)1;
+      double *z = start + 1 + 4 * s, *d = step + 1 + 4 * s;
+      z[0] = 100.0 * 4.0 * r490;
+      d[0] = 1.5 * z[0];
+      z[1] = 100.0 * 0.072 * pow(r490 / r550, -1.7);
+      z[2] = 1.5 * z[1];
+      z[3] = 100.0 * 30.0 * px->sc[s]->aw640 * r640;
+      d[1] = 2.0 * z[1];
+      d[2] = 2.0 * z[2];
+      d[3] = 2.0 * z[3];
+    }
+    return;
+  }
+  for (k = 0; k < nb; k++) {
+    start[1 + k] = 100.0 * 4.0 * m490;
+    step[1 + k] = 1.5 * start[1 + k];
+  }
+  for (k = 0; k < nb; k++) {
+    start[1 + nb + k] = 1.0;
+    step[1 + nb + k] = 0.5 * start[1 + nb + k];
+  }
+  for (s = 0; s < ns; s++) {
+    int o = 1 + 2 * nb + 3 * s;
+    double r490 = (0.0 + px->r490[s]) / (double)1;
+    double r550 = (0.0 + px->r550[s]) / (double)1;
+    double r640 = (0.0 + px->r640[s]) / (double)1;
+    start[o] = 100.0 * 0.072 * pow(r490 / r550, -1.7);
+    start[o + 1] = 1.5 * start[o];
+    start[o + 2] = 100.0 * 30.0 * px->sc[s]->aw640 * r640;
+    step[o] = 2.0 * start[o];
+    step[o + 1] = 2.0 * start[o + 1];
+    step[o + 2] = 2.0 * start[o + 2];
+  }
+}
+
+/* Steps of a seeded start: the same relative steps as the cold start. */
+static void seeded_start(const po_pixel *px, const double *seed, double *start, double *step) {
+  int n = n_params_of(px), i;
+  double rel_ref[6] = {1.25, 1.5, 0.5, 2.0, 2.0, 2.0};
+  for (i = 0; i < n; i++) {
+    double rel = (i < 6) ? rel_ref[i] : 2.0;
+    start[i] = seed[i];
+    step[i] = rel * start[i];
+  }
+}
+
+static void fit_pixel(po_pixel *px, const po_fit *fit, const double *seed, double *o) {
+  const int n = n_params_of(px);
+  double start[PO_MAX_PARAMS], step[PO_MAX_PARAMS], xm[PO_MAX_PARAMS], best[PO_MAX_PARAMS];
+  double lowest = 1.0e4, y = 0.0;
+  int icount = 0, numres = 0, ifault = 0, k, s, b, nst;
+  long total = 0;
+  int kept_evals = 0, kept_res = 0, kept_start = 0, kept_fault = 0, converged = 0;
+
+  pixel_reference_rrs(px);
+  memset(best, 0, sizeof best);
+  nst = seed ? 1 : fit->n_hstarts;
+  for (k = 0; k < nst; k++) {
+    if (seed)
+      seeded_start(px, seed, start, step);
+    else
+      cold_start(px, fit->hstarts[k], start, step);
+    po_nelmin(pixel_cost, px, n, start, xm, &y, fit->reqmin, step, fit->konvge, fit->kcount,
+              &icount, &numres, &ifault);
+    total += icount;
+    if (y < lowest) {
+      lowest = y;
+      memcpy(best, xm, n * sizeof(double));
+      kept_evals = icount;
+      kept_res = numres;
+      kept_start = k;
+      kept_fault = ifault;
+      converged = (ifault == 0);
+      if (lowest < 2.5 * ((float)px->n_scenes)) break; /* model/samodel.c:2404 */
+    }
+  }
+  /* Recompute the model at the kept optimum (model/samodel.c:2413). */
+  pixel_cost(best, px);
+
+  /* Post-fit products (model/samodel.c:1994-2079) for one region. */
+  {
+    double K_min = 1.0e10, iod = 0.0, nobs = 0.0, depth;
+    int found = 0;
+    for (s = 0; s < px->n_scenes; s++)
+      for (b = 0; b < px->n_bands; b++)
+        if (!f_close((float)px->K[s][b], (float)0.0, 1.0e-4f) && px->K[s][b] < K_min) {
+          K_min = px->K[s][b];
+          found = 1;
+        }
+    if (!found) K_min = 0.0;
+    depth = 0.0;
+    depth += sqrt(1.0) * fabs(best[0]);
+    depth /= sqrt(1.0) + 1.0 - 1.0;
+    for (s = 0; s < px->n_scenes; s++)
+      for (b = 0; b < px->n_bands; b++) {
+        iod += px->rrs_bot[s][b] / px->rrs_mod[s][b];
+        nobs += 1.0;
+      }
+    iod = 100.0 * iod / nobs;
+    o[0] = depth;
+    o[1] = px->bottom_albedo;
+    o[2] = px->model_error;
+    o[3] = px->rrs_error;
+    o[4] = K_min;
+    o[5] = iod;
+  }
+  o[6] = (double)kept_evals;
+  o[7] = (double)total;
+  o[8] = converged ? 1.0 : 0.0;
+  o[9] = 0.0;
+  o[10] = (double)px->n_scenes;
+  for (s = 0; s < px->n_scenes; s++) {
+    int idx = (px->layout == PO_LAYOUT_PER_SCENE_B) ? 1 + 4 * s + 1 : 1 + 2 * px->n_bottoms + 3 * s;
+    o[11 + s] = 0.01 * fabs(best[idx]);
+    o[19 + s] = 0.01 * fabs(best[idx + 1]);
+    o[27 + s] = 0.01 * fabs(best[idx + 2]);
+  }
+  o[35] = (double)kept_res;
+  o[36] = (double)kept_start;
+  o[37] = (double)kept_fault;
+}
+
+/* Mask test of model/samodel.c:937-941: nodata or negative in any band. */
+static int masked(const float *r, int n, float nodata) {
+  int b;
+  for (b = 0; b < n; b++)
+    if (f_close(r[b], nodata, 1.0e-6f) || r[b] < 0.0) return 1;
+  return 0;
+}
+
+static const double po_default_hstarts[8] = {40.0, 30.0, 20.0, 15.0, 10.0, 7.5, 2.5, 1.0};
+
+int po_nout(void) { return PO_NOUT; }
+
+int po_invert_batch(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
+                    double h_tide, const float *rrs, int64_t npix, float nodata, double reqmin,
+                    int konvge, int kcount, int n_hstarts, const double *hstarts,
+                    const double *seeds, int nthreads, double *out) {
+  po_scene sc;
+  po_fit fit;
+  int64_t p;
+  if (n_bands < 2 || n_bands > PO_MAX_BANDS) return 1;
+  scene_init(&sc, n_bands, wl, theta_sun_deg, theta_view_deg, h_tide);
+  fit.reqmin = reqmin;
+  fit.konvge = konvge;
+  fit.kcount = kcount;
+  fit.n_hstarts = (n_hstarts > 0 && hstarts) ? n_hstarts : 8;
+  fit.hstarts = (n_hstarts > 0 && hstarts) ? hstarts : po_default_hstarts;
+#if _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 8)
+#endif
+  for (p = 0; p < npix; p++) {
+    const float *r = rrs + p * n_bands;
+    double *o = out + p * PO_NOUT;
+    const double *seed = NULL;
+    po_pixel px;
+    int b;
+    memset(o, 0, PO_NOUT * sizeof(double));
+    if (masked(r, n_bands, nodata)) {
+      o[9] = 1.0;
+      continue;
+    }
+    memset(&px, 0, sizeof px);
+    px.n_scenes = 1;
+    px.n_bands = n_bands;
+    px.n_bottoms = 1;
+    px.layout = PO_LAYOUT_REFERENCE;
+    px.sc[0] = &sc;
+    for (b = 0; b < n_bands; b++) px.rrs[0][b] = r[b];
+    if (seeds && !isnan(seeds[p * 6])) seed = seeds + p * 6;
+    fit_pixel(&px, &fit, seed, o);
+  }
+  return 0;
+}
+
+int po_joint_invert_batch(int n_bands, const double *wl, double theta_view_deg, double h_tide,
+                          const int32_t *scene_offsets, const double *theta_sun_deg,
+                          const float *rrs, int64_t npix, float nodata, int layout,
+                          double reqmin, int konvge, int kcount, int n_hstarts,
+                          const double *hstarts, int nthreads, double *out) {
+  po_fit fit;
+  int64_t p;
+  if (n_bands < 2 || n_bands > PO_MAX_BANDS) return 1;
+  fit.reqmin = reqmin;
+  fit.konvge = konvge;
+  fit.kcount = kcount;
+  fit.n_hstarts = (n_hstarts > 0 && hstarts) ? n_hstarts : 8;
+  fit.hstarts = (n_hstarts > 0 && hstarts) ? hstarts : po_default_hstarts;
+#if _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 4)
+#endif
+  for (p = 0; p < npix; p++) {
+    int o0 = scene_offsets[p], k = scene_offsets[p + 1] - scene_offsets[p], s, b, m = 0;
+    double *o = out + p * PO_NOUT;
+    po_scene sc[PO_MAX_SCENES];
+    po_pixel px;
+    memset(o, 0, PO_NOUT * sizeof(double));
+    if (k < 1 || k > PO_MAX_SCENES) {
+      o[9] = 2.0;
+      continue;
+    }
+    for (s = 0; s < k; s++) m |= masked(rrs + (size_t)(o0 + s) * n_bands, n_bands, nodata);
+    if (m) {
+      o[9] = 1.0;
+      continue;
+    }
+    memset(&px, 0, sizeof px);
+    px.n_scenes = k;
+    px.n_bands = n_bands;
+    px.n_bottoms = 1;
+    px.layout = layout;
+    for (s = 0; s < k; s++) {
+      scene_init(&sc[s], n_bands, wl, theta_sun_deg[o0 + s], theta_view_deg, h_tide);
+      px.sc[s] = &sc[s];
+      for (b = 0; b < n_bands; b++) px.rrs[s][b] = rrs[(size_t)(o0 + s) * n_bands + b];
+    }
+    fit_pixel(&px, &fit, NULL, o);
+  }
+  return 0;
+}
+
+double po_cost(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
+               double h_tide, const double *rrs_measured, const double *params,
+               double *rrs_modelled, double *K_out) {
+  po_scene sc;
+  po_pixel px;
+  double c;
+  int b;
+  scene_init(&sc, n_bands, wl, theta_sun_deg, theta_view_deg, h_tide);
+  memset(&px, 0, sizeof px);
+  px.n_scenes = 1;
+  px.n_bands = n_bands;
+  px.n_bottoms = 1;
+  px.sc[0] = &sc;
+  for (b = 0; b < n_bands; b++) px.rrs[0][b] = rrs_measured[b];
+  pixel_reference_rrs(&px);
+  c = pixel_cost(params, &px);
+  for (b = 0; b < n_bands; b++) {
+    rrs_modelled[b] = px.Rm[0][b];
+    K_out[b] = px.K[0][b];
+  }
+  return c;
+}
+
+void po_nelmin_pixel(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
+                     const double *rrs_measured, const double *start_in, const double *step,
+                     double reqmin, int konvge, int kcount, double *xmin, double *ynewlo,
+                     int *icount, int *numres, int *ifault) {
+  po_scene sc;
+  po_pixel px;
+  double start[PO_MAX_PARAMS];
+  int b;
+  scene_init(&sc, n_bands, wl, theta_sun_deg, theta_view_deg, 0.0);
+  memset(&px, 0, sizeof px);
+  px.n_scenes = 1;
+  px.n_bands = n_bands;
+  px.n_bottoms = 1;
+  px.sc[0] = &sc;
+  for (b = 0; b < n_bands; b++) px.rrs[0][b] = rrs_measured[b];
+  pixel_reference_rrs(&px);
+  memcpy(start, start_in, 6 * sizeof(double));
+  po_nelmin(pixel_cost, &px, 6, start, xmin, ynewlo, reqmin, step, konvge, kcount, icount, numres,
+            ifault);
+}
+
+/* ------------------------------------------------------------------------
+ * Synthetic scenes.  Counter-based Philox4x32-10 (Salmon et al., SC'11)
+ * keyed by the 64-bit seed, with the pixel index and a draw index in the
+ * counter, so any pixel can be regenerated alone and the CUDA generator in
+ * photic_gb300/csrc produces the same uniforms.  Truth follows the
+ * synthetic prior of the plain-method workload: H~U(0.5,25) m,
+ * P~logU(0.005,0.1), G~logU(0.005,0.2), X~logU(0.001,0.05),
+ * B~U(0.05,0.5) on the sand spectrum; Rrs from the forward model with the
+ * spectral-shape exponent Y made self-consistent by fixed-point iteration
+ * (Y depends on the measured Rrs440/Rrs490, model/samodel.c:2898-2901),
+ * plus Gaussian noise.  This generator is new: the reference has none.
+ * ---------------------------------------------------------------------- */
+void po_philox4x32(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
+                   uint32_t *out4) {
+  int r;
+  for (r = 0; r < 10; r++) {
+    uint64_t m0 = (uint64_t)0xD2511F53u * c0, m1 = (uint64_t)0xCD9E8D57u * c2;
+    uint32_t n0 = (uint32_t)(m1 >> 32) ^ c1 ^ k0;
+    uint32_t n1 = (uint32_t)m1;
+    uint32_t n2 = (uint32_t)(m0 >> 32) ^ c3 ^ k1;
+    uint32_t n3 = (uint32_t)m0;
+    c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out4[0] = c0; out4[1] = c1; out4[2] = c2; out4[3] = c3;
+}
+
+static void draw4(uint64_t seed, uint64_t idx, uint32_t block, uint32_t stream, double *u) {
+  uint32_t w[4];
+  int i;
+  po_philox4x32((uint32_t)idx, (uint32_t)(idx >> 32), block, stream, (uint32_t)seed,
+                (uint32_t)(seed >> 32), w);
+  for (i = 0; i < 4; i++) u[i] = ((double)w[i] + 0.5) * 2.3283064365386963e-10; /* 2^-32 */
+}
+
+static double log_uniform(double u, double lo, double hi) {
+  return exp(log(lo) + u * (log(hi) - log(lo)));
+}
+
+/* Fixed-point synthesis of one scene's spectrum for truth (H,P,G,X,B). */
+static void synthesise(const po_scene *sc, double H, double P, double G, double X, double B,
+                       double *rrs) {
+  po_pixel px;
+  double x[6];
+  int it, b;
+  memset(&px, 0, sizeof px);
+  px.n_scenes = 1;
+  px.n_bands = sc->n_bands;
+  px.n_bottoms = 1;
+  px.sc[0] = sc;
+  x[0] = H; x[1] = 100.0 * B; x[2] = 1.0; x[3] = 100.0 * P; x[4] = 100.0 * G; x[5] = 100.0 * X;
+  for (b = 0; b < sc->n_bands; b++) px.rrs[0][b] = 0.01;
+  for (it = 0; it < 30; it++) {
+    pixel_reference_rrs(&px);
+    pixel_cost(x, &px);
+    for (b = 0; b < sc->n_bands; b++) px.rrs[0][b] = px.Rm[0][b];
+  }
+  for (b = 0; b < sc->n_bands; b++) rrs[b] = px.rrs[0][b];
+}
+
+static void add_noise(uint64_t seed, uint64_t idx, uint32_t stream, int n_bands, double sigma,
+                      double *rrs) {
+  int b;
+  for (b = 0; b < n_bands; b += 2) {
+    double u[4], r, a;
+    draw4(seed, idx, 2u + (uint32_t)(b / 4), stream, u);
+    r = sqrt(-2.0 * log(u[(b % 4)]));
+    a = 2.0 * PO_PI * u[(b % 4) + 1];
+    rrs[b] += sigma * r * cos(a);
+    if (b + 1 < n_bands) rrs[b + 1] += sigma * r * sin(a);
+  }
+}
+
+static void apply_mask(double u_mask, double u_kind, double mask_frac, int n_bands, float nodata,
+                       float *r) {
+  int b;
+  if (u_mask >= mask_frac) return;
+  if (u_kind < 0.5) {
+    for (b = 0; b < n_bands; b++) r[b] = nodata;
+  } else {
+    r[n_bands - 1] = -fabsf(r[n_bands - 1]) - 1.0e-3f;
+  }
+}
+
+void po_generate_single(uint64_t seed, int64_t pix0, int64_t npix, int n_bands, const double *wl,
+                        double theta_sun_deg, double theta_view_deg, double mask_frac,
+                        double noise_sigma, float nodata, float *rrs_out, double *truth_out) {
+  po_scene sc;
+  int64_t i;
+  scene_init(&sc, n_bands, wl, theta_sun_deg, theta_view_deg, 0.0);
+#if _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+  for (i = 0; i < npix; i++) {
+    uint64_t p = (uint64_t)(pix0 + i);
+    double u0[4], u1[4], H, P, G, X, B, r[PO_MAX_BANDS];
+    int b;
+    draw4(seed, p, 0u, 0u, u0);
+    draw4(seed, p, 1u, 0u, u1);
+    H = 0.5 + 24.5 * u0[0];
+    P = log_uniform(u0[1], 0.005, 0.1);
+    G = log_uniform(u0[2], 0.005, 0.2);
+    X = log_uniform(u0[3], 0.001, 0.05);
+    B = 0.05 + 0.45 * u1[0];
+    synthesise(&sc, H, P, G, X, B, r);
+    add_noise(seed, p, 0u, n_bands, noise_sigma, r);
+    for (b = 0; b < n_bands; b++) rrs_out[i * n_bands + b] = (float)r[b];
+    apply_mask(u1[1], u1[2], mask_frac, n_bands, nodata, rrs_out + i * n_bands);
+    if (truth_out) {
+      truth_out[i * 5 + 0] = H;
+      truth_out[i * 5 + 1] = P;
+      truth_out[i * 5 + 2] = G;
+      truth_out[i * 5 + 3] = X;
+      truth_out[i * 5 + 4] = B;
+    }
+  }
+}
+
+void po_joint_counts(uint64_t seed, int64_t npix, int kmin, int kmax, int32_t *counts) {
+  int64_t p;
+  for (p = 0; p < npix; p++) {
+    double u[4];
+    int k;
+    draw4(seed, (uint64_t)p, 0u, 1u, u);
+    k = kmin + (int)(u[0] * (double)(kmax - kmin + 1));
+    if (k > kmax) k = kmax;
+    counts[p] = k;
+  }
+}
+
+void po_generate_joint(uint64_t seed, int64_t npix, int n_bands, const double *wl,
+                       double theta_view_deg, double theta_sun_min, double theta_sun_max,
+                       double mask_frac, double noise_sigma, float nodata,
+                       const int32_t *scene_offsets, double *theta_sun_out, float *rrs_out,
+                       double *truth_out) {
+  int64_t p;
+#if _OPENMP
+#pragma omp parallel for schedule(dynamic, 64)
+#endif
+  for (p = 0; p < npix; p++) {
+    int o0 = scene_offsets[p], k = scene_offsets[p + 1] - o0, s, b;
+    double uH[4], H;
+    draw4(seed, (uint64_t)p, 1u, 1u, uH);
+    H = 0.5 + 24.5 * uH[0];
+    for (s = 0; s < k; s++) {
+      uint64_t obs = (uint64_t)(o0 + s);
+      double u0[4], u1[4], r[PO_MAX_BANDS], P, G, X, B, th;
+      po_scene sc;
+      draw4(seed, obs, 0u, 2u, u0);
+      draw4(seed, obs, 1u, 2u, u1);
+      P = log_uniform(u0[0], 0.005, 0.1);
+      G = log_uniform(u0[1], 0.005, 0.2);
+      X = log_uniform(u0[2], 0.001, 0.05);
+      B = 0.05 + 0.45 * u0[3];
+      th = theta_sun_min + (theta_sun_max - theta_sun_min) * u1[0];
+      theta_sun_out[obs] = th;
+      scene_init(&sc, n_bands, wl, th, theta_view_deg, 0.0);
+      synthesise(&sc, H, P, G, X, B, r);
+      add_noise(seed, obs, 2u, n_bands, noise_sigma, r);
+      for (b = 0; b < n_bands; b++) rrs_out[obs * n_bands + b] = (float)r[b];
+      if (s == 0) apply_mask(uH[1], uH[2], mask_frac, n_bands, nodata, rrs_out + obs * n_bands);
+      if (truth_out) {
+        truth_out[obs * 5 + 0] = H;
+        truth_out[obs * 5 + 1] = P;
+        truth_out[obs * 5 + 2] = G;
+        truth_out[obs * 5 + 3] = X;
+        truth_out[obs * 5 + 4] = B;
+      }
+    }
+  }
+}

@@ -1,0 +1,79 @@
+/*
+ * photic_oracle.h -- CPU restatement of photic's per-pixel inversion.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle that the tests, the smoke
+ * check and bench.py's CPU baseline compare the GPU path against.  Nothing
+ * in the product (photic_gb300/) includes, links or loads it.
+ *
+ * It restates, in plain C99 with double precision and the same order of
+ * floating-point operations, the reference's
+ *   samodel_Rrs        model/samodel.c:2846-2949   (HOPE forward model)
+ *   samodel_error      model/samodel.c:2432-2759   (cost)
+ *   nelmin             model/asa047.c:10-502       (modified AS 47)
+ *   samodel_optimise   model/samodel.c:1768-2115   (per-pixel driver) with
+ *   samodel_optimise_one_bottom_combination  model/samodel.c:2119-2427
+ *   interp_1d          model/common.c:298-335
+ * restricted to one spatial region per pixel (n_spatial <= 1), which is what
+ * every synthetic configuration uses.  It is pinned bit-for-bit against the
+ * reference compiled from its own sources (oracle/_ref, built by
+ * oracle/Makefile) and against the committed fixtures in tests/golden/.
+ */
+#ifndef PHOTIC_ORACLE_H
+#define PHOTIC_ORACLE_H
+
+#include <stdint.h>
+
+#define PO_MAX_BANDS 8
+#define PO_MAX_SCENES 8
+#define PO_MAX_PARAMS 40
+#define PO_N_BOTTOM_TYPES 8
+#define PO_NOUT 40
+
+/* Output record per pixel (doubles), shared with oracle/_ref and the GPU:
+ *  0 depth H   1 bottom albedo   2 model error (cost)   3 Rrs error (%)
+ *  4 K_min     5 index of optical depth   6 evaluations of the kept start
+ *  7 evaluations over all starts          8 converged (ifault == 0)
+ *  9 status (0 fitted, 1 masked, 2 invalid)   10 scene count
+ * 11..18 P per scene   19..26 G per scene   27..34 X per scene
+ * 35 restarts of the kept start   36 index of the kept start   37 ifault */
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+int po_nout(void);
+double po_interp_1d(const double *X, const double *Y, int n, double x);
+void po_band_constants(int n_bands, const double *wl, double theta_sun_deg,
+                       double theta_view_deg, double *out);
+double po_cost(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
+               double h_tide, const double *rrs_measured, const double *params,
+               double *rrs_modelled, double *K_out);
+void po_nelmin_pixel(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
+                     const double *rrs_measured, const double *start, const double *step,
+                     double reqmin, int konvge, int kcount, double *xmin, double *ynewlo,
+                     int *icount, int *numres, int *ifault);
+int po_invert_batch(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
+                    double h_tide, const float *rrs, int64_t npix, float nodata, double reqmin,
+                    int konvge, int kcount, int n_hstarts, const double *hstarts,
+                    const double *seeds, int nthreads, double *out);
+int po_joint_invert_batch(int n_bands, const double *wl, double theta_view_deg, double h_tide,
+                          const int32_t *scene_offsets, const double *theta_sun_deg,
+                          const float *rrs, int64_t npix, float nodata, int layout,
+                          double reqmin, int konvge, int kcount, int n_hstarts,
+                          const double *hstarts, int nthreads, double *out);
+void po_generate_single(uint64_t seed, int64_t pix0, int64_t npix, int n_bands, const double *wl,
+                        double theta_sun_deg, double theta_view_deg, double mask_frac,
+                        double noise_sigma, float nodata, float *rrs_out, double *truth_out);
+void po_joint_counts(uint64_t seed, int64_t npix, int kmin, int kmax, int32_t *counts);
+void po_generate_joint(uint64_t seed, int64_t npix, int n_bands, const double *wl,
+                       double theta_view_deg, double theta_sun_min, double theta_sun_max,
+                       double mask_frac, double noise_sigma, float nodata,
+                       const int32_t *scene_offsets, double *theta_sun_out, float *rrs_out,
+                       double *truth_out);
+void po_philox4x32(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
+                   uint32_t *out4);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
