@@ -1,0 +1,329 @@
+"""Benchmark: converged pixels/s of the batched plain-method inversion.
+
+Workload (one "step"): the whole synthetic 4096 x 4096 single scene of the
+plain method -- 4 OLI-like bands (443/482/561/655 nm), sun 35 deg, nadir,
+truth H~U(0.5,25) m, P~logU(0.005,0.1), G~logU(0.005,0.2),
+X~logU(0.001,0.05), B~U(0.05,0.5) on sand, N(0, 2e-4) noise, 15 % of pixels
+masked -- inverted with the cold-start Nelder-Mead at reqmin 1e-10,
+kcount 2000 on one GPU.  The scene is generated on the device with the
+seeded generator (synthetic data: the reference ships no dataset).
+
+metric: converged pixels per second whose depth is within 1 cm of the FP64
+oracle.  The full-scene FP64 reference is the FP64 kernel (its parity with
+the CPU oracle is what tests/test_gpu_invert.py asserts); a random sample
+of pixels is also re-fitted by the CPU oracle in the same run and the
+within-1-cm fraction of that sample is reported and applied.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl photic|reference]
+                  [--npix P] [--precision fp64|df64|fp32]
+
+Under torchrun each rank inverts its own scene shard of the same size
+(pixels are independent: weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SEED = 20260101
+METRIC = "converged pixels/s at |dH|<=1cm vs FP64 (plain cold-start Nelder-Mead, 1 GB300)"
+UNIT = "px/s"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons while timing."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) > 8:
+                for k, n in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.rows)}
+
+
+def cpu_oracle_rate(npix: int, seed: int):
+    """The CPU oracle (C restatement of the reference path, OpenMP over
+    pixels) on a bounded sample of the same workload."""
+    from oracle import oracle as O
+    rrs, _ = O.generate_single(seed, npix, pix0=7_000_000)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    out = O.invert_batch(rrs, nthreads=threads)
+    dt = time.perf_counter() - t0
+    conv = int(np.sum((out[:, 9] == 0) & (out[:, 8] == 1)))
+    return conv / dt, threads, dt, npix, out
+
+
+def run_reference(args, ws, rank):
+    """--impl reference: the reference path on the host cores (the oracle
+    port of it; the reference's own build needs sources absent here)."""
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    kind = "reference" if O.reference_available() else "port"
+    threads = os.cpu_count() or 1
+    n = args.ref_sample
+    rrs, _ = O.generate_single(SEED, n, pix0=7_000_000)
+    which = "reference" if kind == "reference" else "port"
+    for _ in range(args.warmup):
+        O.invert_batch(rrs[: max(1, n // 16)], which=which, nthreads=threads)
+    times, convs = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        out = O.invert_batch(rrs, which=which, nthreads=threads)
+        times.append(time.perf_counter() - t0)
+        convs.append(int(np.sum((out[:, 9] == 0) & (out[:, 8] == 1))))
+    t = float(np.mean(times))
+    value = float(np.mean(convs)) / t
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded generator, plain-method prior)",
+            "config": {"workload": "plain method, 4096x4096 single scene, 4 bands, "
+                                   "reqmin 1e-10 kcount 2000 (bounded sample per step)",
+                       "sample_pixels": n, "host_threads": threads},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                             "sample": f"{n} pixels of the same generator per step"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="photic", choices=["photic", "reference"])
+    ap.add_argument("--npix", type=int, default=4096 * 4096)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "df64", "fp32"])
+    ap.add_argument("--warmup-npix", type=int, default=1 << 20)
+    ap.add_argument("--sample", type=int, default=2048, help="pixels re-fitted by the CPU oracle")
+    ap.add_argument("--cpu-sample", type=int, default=1 << 16)
+    ap.add_argument("--ref-sample", type=int, default=1 << 16)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+
+    ws, rank, local = _dist()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+
+    import torch
+    import photic_gb300 as pg
+    from photic_gb300 import _lib as L
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pg_ = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+        pg_ = dist
+    stream = torch.cuda.current_stream()
+    cfg = pg.Config(precision=args.precision)
+    npix = args.npix
+    pix0 = rank * npix
+    rrs, truth = pg.generate_scene(npix, seed=SEED, config=cfg, pix0=pix0, device=dev)
+    out = pg.alloc_outputs(npix, dev, ("depth", "depth_f64", "P", "G", "X", "bottom_albedo",
+                                       "model_error", "evals", "status"))
+
+    # warm-up on a slice of the scene (W launches)
+    for _ in range(args.warmup):
+        pg.invert(rrs[: min(npix, args.warmup_npix)], cfg)
+    pg.sync()
+
+    def barrier():
+        if pg_ is not None:
+            pg_.barrier()
+
+    clocks = Clocks(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        pg.invert(rrs, cfg, out=out)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier()
+    pg.sync()
+    ms_step = ev0.elapsed_time(ev1) / args.steps
+    if pg_ is not None:
+        t = torch.tensor([ms_step], device=dev)
+        pg_.all_reduce(t, op=pg_.ReduceOp.MAX)
+        ms_step = float(t.item())
+
+    status = out["status"].cpu().numpy()
+    fitted = (status & 0xFF) == 0
+    conv = fitted & ((status >> 8) & 1).astype(bool)
+    evals = out["evals"].cpu().numpy().astype(np.int64)
+    h = out["depth_f64"].cpu().numpy()
+
+    # FP64 reference of the full scene: the FP64 kernel itself, or a run of it.
+    if args.precision == "fp64":
+        h64 = h
+    else:
+        ref = pg.invert(rrs, pg.Config(precision="fp64"),
+                        fields=("depth_f64", "status"))
+        pg.sync()
+        h64 = ref["depth_f64"].cpu().numpy()
+    within = conv & (np.abs(h - h64) <= 0.01)
+
+    # CPU-oracle sample: same pixels, FP64 C restatement of the reference.
+    sample_frac, sample_stats = 1.0, None
+    if rank == 0 and args.sample > 0:
+        from oracle import oracle as O
+        rng = np.random.default_rng(1)
+        idx = np.sort(rng.choice(npix, size=min(args.sample, npix), replace=False))
+        r_np = rrs[torch.tensor(idx, device=dev)].cpu().numpy()
+        o = O.invert_batch(r_np, nthreads=os.cpu_count() or 1)
+        m = (o[:, 9] == 0) & conv[idx]
+        d = np.abs(h[idx][m] - o[m, 0])
+        sample_frac = float(np.mean(d <= 0.01)) if m.any() else 1.0
+        sample_stats = {"pixels": int(m.sum()), "median_abs_dH_m": float(np.median(d)),
+                        "p99_abs_dH_m": float(np.quantile(d, 0.99)),
+                        "frac_within_1cm": sample_frac}
+    good = float(np.sum(within)) * sample_frac
+    if pg_ is not None:
+        t = torch.tensor([good], device=dev, dtype=torch.float64)
+        pg_.all_reduce(t)
+        good = float(t.item())
+    value = good / (ms_step * 1e-3)
+
+    # Roofline of the inversion kernel: FP64 pipe.
+    p64 = np.zeros(1)
+    p32 = np.zeros(1)
+    pmu = np.zeros(1)
+    import ctypes as C
+    L.check(L.lib().photic_measure_peaks(p64.ctypes.data_as(C.POINTER(C.c_double)),
+                                         p32.ctypes.data_as(C.POINTER(C.c_double)),
+                                         pmu.ctypes.data_as(C.POINTER(C.c_double))))
+    total_evals = float(evals.sum())
+    flops_per_eval = FLOPS_PER_EVAL_F64
+    achieved = total_evals * flops_per_eval / (ms_step * 1e-3) / 1e12
+    roof = {"bound": "fp64-pipe", "achieved": achieved, "peak": float(p64[0]),
+            "unit": "TFLOP/s", "frac": achieved / float(p64[0]), "traffic": None,
+            "peak_source": "measured by photic_measure_peaks (DFMA chains) in this run",
+            "evals_per_s": total_evals / (ms_step * 1e-3),
+            "flops_per_eval": flops_per_eval}
+
+    # End to end through the public API with host buffers.
+    e2e = None
+    if rank == 0:
+        host_in = rrs.cpu().pin_memory()
+        host_depth = torch.empty(npix, dtype=torch.float32).pin_memory()
+        host_status = torch.empty(npix, dtype=torch.int32).pin_memory()
+        dev_in = torch.empty_like(rrs)
+        o2 = pg.alloc_outputs(npix, dev, ("depth", "status"))
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t0.record(stream)
+        dev_in.copy_(host_in, non_blocking=True)
+        pg.invert(dev_in, cfg, out=o2)
+        host_depth.copy_(o2["depth"], non_blocking=True)
+        host_status.copy_(o2["status"], non_blocking=True)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = t0.elapsed_time(t1)
+        st2 = host_status.numpy()
+        conv2 = ((st2 & 0xFF) == 0) & ((st2 >> 8) & 1).astype(bool)
+        within2 = conv2 & (np.abs(host_depth.numpy().astype(np.float64) - h64) <= 0.01)
+        e2e = {"value": float(np.sum(within2)) * sample_frac / (e2e_ms * 1e-3), "unit": UNIT,
+               "h2d_bytes_per_step": int(host_in.numel() * 4),
+               "d2h_bytes_per_step": int(npix * 8), "ms_per_step": e2e_ms}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu and args.cpu_sample > 0:
+        rate, threads, dt, n, _ = cpu_oracle_rate(args.cpu_sample, SEED)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{n} pixels of the same generator, {dt:.1f} s on {threads} threads"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": {"fp64": "f64", "df64": "df64 (2 x f32)", "fp32": "f32"}[args.precision],
+                "data": "synthetic (seeded on-device generator, plain-method prior)",
+                "config": {"workload": "plain method, 4096x4096 single scene, 4 bands, "
+                                       "cold start, reqmin 1e-10, kcount 2000",
+                           "pixels_per_gpu": npix, "precision": args.precision,
+                           "l2": "inputs 268 MB > L2; compute-bound kernel"},
+                "gpu_launches": args.steps,
+                "pixels": {"fitted": int(fitted.sum()), "converged": int(conv.sum()),
+                           "within_1cm_of_fp64": int(within.sum()),
+                           "mean_evals": float(evals[fitted].mean()) if fitted.any() else 0.0},
+                "oracle_sample": sample_stats, "roofline": roof, "cpu_baseline": cpu,
+                "e2e": e2e, "clocks": clk}
+        print(json.dumps(line))
+    if pg_ is not None:
+        pg_.destroy_process_group()
+
+
+# Algorithmic double-precision operations of one cost evaluation at 4 bands
+# (adds, multiplies, divides, square roots; exp/log counted as one each):
+# 43 per band (photic_fp64.cuh cost_f64) + 9 in the tail.
+FLOPS_PER_EVAL_F64 = 4 * 43 + 9
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,183 @@
+/*
+ * photic.h -- C ABI of the GB300 implementation of photic's per-pixel
+ * semi-analytical inversion (HOPE forward model + Nelder-Mead fit).
+ *
+ * All entry points are extern "C", take plain pointers and sizes, return an
+ * int status (PHOTIC_OK == 0) and never exit the process.  Array arguments
+ * named d_* are device pointers; the batch calls are asynchronous on the
+ * given CUDA stream (pass NULL for the legacy default stream) and report
+ * launch-time errors in their return value.  Errors raised while the
+ * kernels run are read back with photic_sync().
+ *
+ * Mapping to the reference (file:line inside stblake/photic):
+ *   photic_invert_batch        replaces the pixel loop of samodel()
+ *                              model/samodel.c:901-1166 calling
+ *                              samodel_optimise() model/samodel.c:1768
+ *                              (cold start, no LUT, one region).
+ *   photic_joint_invert_batch  the same loop with n_scenes = k per pixel,
+ *                              the temporal joint fit
+ *                              model/samodel.c:2463-2491, 2312-2353.
+ *   photic_cost_batch          samodel_error() model/samodel.c:2432.
+ *   photic_forward_batch       samodel_Rrs() model/samodel.c:2846.
+ *   photic_interp_1d           interp_1d() model/common.c:298.
+ *   photic_generate_scene      (new) synthetic scenes; no counterpart.
+ * The link-compatible drop-ins samodel_Rrs / samodel_error /
+ * samodel_optimise keep the reference signatures; they are declared in
+ * photic_samodel.h together with the model_data layout they read.
+ */
+#ifndef PHOTIC_H
+#define PHOTIC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PHOTIC_MAX_BANDS 8
+#define PHOTIC_MAX_SCENES 8
+#define PHOTIC_MAX_HSTARTS 32
+
+/* Return codes. */
+enum {
+  PHOTIC_OK = 0,
+  PHOTIC_ERR_INVALID = 1,     /* bad argument or configuration */
+  PHOTIC_ERR_CUDA = 2,        /* a CUDA call failed (message: photic_last_error) */
+  PHOTIC_ERR_NOMEM = 3,       /* device allocation failed */
+  PHOTIC_ERR_TIMEOUT = 4,     /* a bounded device wait gave up */
+  PHOTIC_ERR_UNSUPPORTED = 5  /* configuration outside what the kernels implement */
+};
+
+/* Arithmetic of the cost evaluations. */
+enum {
+  PHOTIC_PREC_FP64 = 0, /* IEEE double in the reference's operation order */
+  PHOTIC_PREC_DF64 = 1, /* double-float (two FP32 words) on the FP32 pipes */
+  PHOTIC_PREC_FP32 = 2  /* FP32 forward model; FP64 for the convergence and
+                           local-minimum tests only */
+};
+
+/* Per-pixel status word: low byte is the pixel state, bit 8 is set when
+ * the kept start converged (nelmin ifault == 0), bits 16..23 hold the index
+ * of the kept depth start. */
+enum { PHOTIC_PX_FITTED = 0, PHOTIC_PX_MASKED = 1, PHOTIC_PX_INVALID = 2 };
+#define PHOTIC_PX_CONVERGED 0x100
+
+/* Parameter layouts of the temporal joint fit. */
+enum {
+  PHOTIC_LAYOUT_REFERENCE = 0, /* H, B, q shared; P, G, X per scene: n = 3 + 3k */
+  PHOTIC_LAYOUT_SCENE_B = 1    /* H shared; B, P, G, X per scene:   n = 1 + 4k */
+};
+
+typedef struct photic_config {
+  int32_t n_bands;                           /* bands per scene, 2..8 */
+  double wavelengths[PHOTIC_MAX_BANDS];      /* nm, ascending */
+  double theta_sun_deg;                      /* subsurface solar zenith (deg) */
+  double theta_view_deg;                     /* subsurface view angle (deg) */
+  double h_tide;                             /* tidal height added to depth */
+  float nodata_value;                        /* masked-pixel marker */
+  double reqmin;                             /* nelmin variance limit */
+  int32_t konvge;                            /* iterations per convergence check */
+  int32_t kcount;                            /* evaluation budget per nelmin call */
+  int32_t n_hstarts;                         /* cold-start depths tried in order */
+  double hstarts[PHOTIC_MAX_HSTARTS];
+  double early_exit_per_scene;               /* keep a start when cost < this * scenes */
+  int32_t precision;                         /* PHOTIC_PREC_* */
+  int32_t layout;                            /* PHOTIC_LAYOUT_* (joint fit) */
+  int32_t block_threads;                     /* launch shape; 0 = tuned default */
+  int32_t blocks_per_sm;                     /* 0 = tuned default */
+} photic_config;
+
+/* Outputs, structure of arrays.  Every pointer may be NULL (not written).
+ * Single-scene calls write [npix]; the joint call writes per-pixel arrays
+ * as [npix] and P/G/X as [n_obs] aligned with its inputs. */
+typedef struct photic_outputs {
+  float *depth;          /* H (m) */
+  double *depth_f64;     /* H (m) in double precision */
+  float *P, *G, *X;      /* 0.01 * |fitted parameter| */
+  float *bottom_albedo;  /* sum_i q_i B_i */
+  float *model_error;    /* cost at the kept optimum */
+  float *rrs_error;      /* spectral RMS relative error (%) */
+  float *K_min;          /* min over bands of K at the optimum */
+  float *iod;            /* index of optical depth (%) */
+  int32_t *evals;        /* cost evaluations over all starts */
+  int32_t *evals_kept;   /* evaluations of the kept start */
+  int32_t *status;       /* PHOTIC_PX_* | PHOTIC_PX_CONVERGED | start << 16 */
+} photic_outputs;
+
+/* Defaults: OLI-like bands 443/482/561/655 nm, sun 35 deg, nadir, the
+ * reference's 8 cold depth starts (model/samodel.c:2216-2218), early exit
+ * 2.5 per scene (:2404), reqmin 1e-10, konvge 100, kcount 2000, FP64. */
+void photic_config_default(photic_config *cfg);
+
+/* Validate cfg; PHOTIC_OK or PHOTIC_ERR_INVALID with a message. */
+int photic_config_check(const photic_config *cfg);
+
+/* Plain-method inversion of npix single-scene pixels.  Band b of pixel p
+ * is d_rrs[p * pixel_stride + b * band_stride] (float).  d_seeds is NULL
+ * (cold start) or [npix * 6] doubles: a start vector
+ * (H, 100B, q, 100P, 100G, 100X) per pixel, NaN in the first slot meaning
+ * cold start for that pixel. */
+int photic_invert_batch(const photic_config *cfg, const float *d_rrs, int64_t npix,
+                        int64_t pixel_stride, int64_t band_stride, const double *d_seeds,
+                        const photic_outputs *out, void *stream);
+
+/* Temporal joint fit: pixel p owns observations d_offsets[p] ..
+ * d_offsets[p+1]-1 (CSR, int32, device); observation o has spectrum
+ * d_rrs[o * n_bands .. +n_bands) and subsurface sun zenith
+ * d_theta_sun_deg[o].  k = d_offsets[p+1]-d_offsets[p] must be 1..8. */
+int photic_joint_invert_batch(const photic_config *cfg, const int32_t *d_offsets,
+                              const double *d_theta_sun_deg, const float *d_rrs, int64_t npix,
+                              int64_t n_obs, const photic_outputs *out, void *stream);
+
+/* Cost of n parameter vectors (6 doubles each) against spectra
+ * [n * n_bands] floats: samodel_error at one region. d_cost [n] doubles;
+ * d_rrs_modelled [n * n_bands] doubles (NULL to skip). */
+int photic_cost_batch(const photic_config *cfg, const float *d_rrs, const double *d_params,
+                      int64_t n, double *d_cost, double *d_rrs_modelled, void *stream);
+
+/* Synthetic scene of the plain-method workload (see photic_generate.cu):
+ * writes [npix * n_bands] floats and, if d_truth != NULL, [npix * 5]
+ * doubles (H, P, G, X, B). Pixels pix0 .. pix0+npix-1 of the scene. */
+int photic_generate_scene(const photic_config *cfg, uint64_t seed, int64_t pix0, int64_t npix,
+                          double mask_frac, double noise_sigma, float *d_rrs, double *d_truth,
+                          void *stream);
+
+/* Joint-fit synthetic stack: d_counts [npix] int32 scene counts in
+ * [kmin, kmax]; after the caller forms offsets (exclusive scan),
+ * photic_generate_joint fills theta_sun [n_obs], rrs [n_obs * n_bands] and
+ * truth [n_obs * 5] (H shared per pixel). */
+int photic_joint_counts(uint64_t seed, int64_t npix, int32_t kmin, int32_t kmax,
+                        int32_t *d_counts, void *stream);
+int photic_generate_joint(const photic_config *cfg, uint64_t seed, int64_t npix,
+                          const int32_t *d_offsets, double theta_sun_min, double theta_sun_max,
+                          double mask_frac, double noise_sigma, double *d_theta_sun,
+                          float *d_rrs, double *d_truth, void *stream);
+
+/* interp_1d of the reference (host function, no GPU needed). */
+double photic_interp_1d(const double *X, const double *Y, int32_t n, double x);
+
+/* Band constants of a configuration (host function): out[b*8 + 0..7] =
+ * a0, a1, a_w, b_bw, sand reflectance, sec(theta_sun), sec(theta_view),
+ * a_w(640). */
+int photic_band_constants(const photic_config *cfg, double *out);
+
+/* Waits for the stream, then reports any error recorded by the device
+ * (bounded-wait timeouts, invalid inputs) since the previous call. */
+int photic_sync(void *stream);
+
+/* Measured pipe throughput of the current device, for roofline
+ * denominators of the compute-bound kernels: FP64 and FP32 FMA (TFLOP/s,
+ * 2 flops per FMA) and MUFU ex2 (T ops/s).  Synchronous; ~0.1 s. */
+int photic_measure_peaks(double *fp64_tflops, double *fp32_tflops, double *mufu_tops);
+
+/* Message of the most recent error on this host thread. */
+const char *photic_last_error(void);
+
+/* Library version string. */
+const char *photic_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,8 @@
+"""photic_gb300: GB300 (sm_103a) implementation of photic's per-pixel
+semi-analytical inversion -- the HOPE forward model fitted per pixel by
+the reference's modified AS 47 Nelder-Mead -- behind a C ABI
+(include/photic.h) and this thin Python host layer over it.
+"""
+from . import api  # noqa: F401
+from .api import (Config, PhoticError, alloc_outputs, cost, generate_scene, invert,  # noqa: F401
+                  sync, version)

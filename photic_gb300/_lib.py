@@ -1,0 +1,126 @@
+"""ctypes binding of libphotic_gb300.so (the C ABI in include/photic.h).
+
+The structs below mirror include/photic.h field for field.  Loading fails
+loudly when the library has not been built: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libphotic_gb300.so")
+
+MAX_BANDS = 8
+MAX_SCENES = 8
+MAX_HSTARTS = 32
+
+OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT, ERR_UNSUPPORTED = range(6)
+PREC_FP64, PREC_DF64, PREC_FP32 = 0, 1, 2
+LAYOUT_REFERENCE, LAYOUT_SCENE_B = 0, 1
+PX_FITTED, PX_MASKED, PX_INVALID = 0, 1, 2
+PX_CONVERGED = 0x100
+
+
+class photic_config(C.Structure):
+    _fields_ = [
+        ("n_bands", C.c_int32),
+        ("wavelengths", C.c_double * MAX_BANDS),
+        ("theta_sun_deg", C.c_double),
+        ("theta_view_deg", C.c_double),
+        ("h_tide", C.c_double),
+        ("nodata_value", C.c_float),
+        ("reqmin", C.c_double),
+        ("konvge", C.c_int32),
+        ("kcount", C.c_int32),
+        ("n_hstarts", C.c_int32),
+        ("hstarts", C.c_double * MAX_HSTARTS),
+        ("early_exit_per_scene", C.c_double),
+        ("precision", C.c_int32),
+        ("layout", C.c_int32),
+        ("block_threads", C.c_int32),
+        ("blocks_per_sm", C.c_int32),
+    ]
+
+
+class photic_outputs(C.Structure):
+    _fields_ = [
+        ("depth", C.c_void_p),
+        ("depth_f64", C.c_void_p),
+        ("P", C.c_void_p),
+        ("G", C.c_void_p),
+        ("X", C.c_void_p),
+        ("bottom_albedo", C.c_void_p),
+        ("model_error", C.c_void_p),
+        ("rrs_error", C.c_void_p),
+        ("K_min", C.c_void_p),
+        ("iod", C.c_void_p),
+        ("evals", C.c_void_p),
+        ("evals_kept", C.c_void_p),
+        ("status", C.c_void_p),
+    ]
+
+
+class PhoticError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"photic error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+# name -> (restype, argtypes)
+_SIGS = {
+    "photic_version": (C.c_char_p, []),
+    "photic_last_error": (C.c_char_p, []),
+    "photic_config_default": (None, [C.POINTER(photic_config)]),
+    "photic_config_check": (C.c_int, [C.POINTER(photic_config)]),
+    "photic_invert_batch": (C.c_int, [C.POINTER(photic_config), C.c_void_p, C.c_int64,
+                                      C.c_int64, C.c_int64, C.c_void_p,
+                                      C.POINTER(photic_outputs), C.c_void_p]),
+    "photic_joint_invert_batch": (C.c_int, [C.POINTER(photic_config), C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.c_int64, C.c_int64,
+                                            C.POINTER(photic_outputs), C.c_void_p]),
+    "photic_cost_batch": (C.c_int, [C.POINTER(photic_config), C.c_void_p, C.c_void_p,
+                                    C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "photic_generate_scene": (C.c_int, [C.POINTER(photic_config), C.c_uint64, C.c_int64,
+                                        C.c_int64, C.c_double, C.c_double, C.c_void_p,
+                                        C.c_void_p, C.c_void_p]),
+    "photic_joint_counts": (C.c_int, [C.c_uint64, C.c_int64, C.c_int32, C.c_int32, C.c_void_p,
+                                      C.c_void_p]),
+    "photic_generate_joint": (C.c_int, [C.POINTER(photic_config), C.c_uint64, C.c_int64,
+                                        C.c_void_p, C.c_double, C.c_double, C.c_double,
+                                        C.c_double, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p]),
+    "photic_interp_1d": (C.c_double, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int32,
+                                      C.c_double]),
+    "photic_band_constants": (C.c_int, [C.POINTER(photic_config), C.POINTER(C.c_double)]),
+    "photic_sync": (C.c_int, [C.c_void_p]),
+    "photic_measure_peaks": (C.c_int, [C.POINTER(C.c_double)] * 3),
+}
+
+
+def lib() -> C.CDLL:
+    """The loaded library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; "
+                "g.build()'` (nvcc for sm_103a). There is no CPU fallback.")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def exported_symbols():
+    return list(_SIGS)
+
+
+def check(rc: int) -> None:
+    if rc != OK:
+        raise PhoticError(rc, lib().photic_last_error().decode(errors="replace"))

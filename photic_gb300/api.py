@@ -1,0 +1,193 @@
+"""Python host layer over the C ABI (include/photic.h).
+
+This is the user-facing mirror of the reference's per-pixel operator,
+``samodel_optimise`` (model/samodel.c:1768) applied over a scene the way
+the pixel loop of ``samodel`` does (model/samodel.c:901-1166): give it the
+band reflectances of many pixels, get back depth, P, G, X, bottom albedo,
+the model error and the convergence flag of every pixel.  Configuration
+names follow the reference (reqmin / konvge / kcount of nelmin, depth starts
+``hstarts``, subsurface ``theta_sun`` / ``theta_view``).
+
+Device memory and streams come from PyTorch; every computation runs in the
+CUDA library, and an error from it raises :class:`PhoticError`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Dict, Optional, Sequence
+
+import torch
+
+from . import _lib as L
+from ._lib import PhoticError  # noqa: F401
+
+PRECISIONS = {"fp64": L.PREC_FP64, "df64": L.PREC_DF64, "fp32": L.PREC_FP32}
+LAYOUTS = {"reference": L.LAYOUT_REFERENCE, "scene_b": L.LAYOUT_SCENE_B}
+OUTPUT_FIELDS = ("depth", "depth_f64", "P", "G", "X", "bottom_albedo", "model_error",
+                 "rrs_error", "K_min", "iod", "evals", "evals_kept", "status")
+_DTYPES = {"depth_f64": torch.float64, "evals": torch.int32, "evals_kept": torch.int32,
+           "status": torch.int32}
+
+
+@dataclass
+class Config:
+    """Mirror of ``photic_config``; the defaults are the plain-method
+    workload: OLI-like bands, sun 35 deg, nadir, reqmin 1e-10, kcount 2000
+    and the reference's eight cold depth starts (model/samodel.c:2216)."""
+    wavelengths: Sequence[float] = (443.0, 482.0, 561.0, 655.0)
+    theta_sun_deg: float = 35.0
+    theta_view_deg: float = 0.0
+    h_tide: float = 0.0
+    nodata_value: float = -9999.0
+    reqmin: float = 1.0e-10
+    konvge: int = 100
+    kcount: int = 2000
+    hstarts: Sequence[float] = (40.0, 30.0, 20.0, 15.0, 10.0, 7.5, 2.5, 1.0)
+    early_exit_per_scene: float = 2.5
+    precision: str = "fp64"
+    layout: str = "reference"
+    block_threads: int = 0
+    blocks_per_sm: int = 0
+
+    @classmethod
+    def reference_default(cls, **kw) -> "Config":
+        """The tolerances the reference hard-codes (model/samodel.c:2142-2144)."""
+        kw.setdefault("reqmin", 1.0e-2)
+        kw.setdefault("konvge", 100)
+        kw.setdefault("kcount", 5000)
+        return cls(**kw)
+
+    @property
+    def n_bands(self) -> int:
+        return len(self.wavelengths)
+
+    def to_c(self) -> L.photic_config:
+        c = L.photic_config()
+        L.lib().photic_config_default(C.byref(c))
+        c.n_bands = len(self.wavelengths)
+        if c.n_bands > L.MAX_BANDS:
+            raise ValueError(f"at most {L.MAX_BANDS} bands")
+        for i, w in enumerate(self.wavelengths):
+            c.wavelengths[i] = float(w)
+        c.theta_sun_deg = float(self.theta_sun_deg)
+        c.theta_view_deg = float(self.theta_view_deg)
+        c.h_tide = float(self.h_tide)
+        c.nodata_value = float(self.nodata_value)
+        c.reqmin = float(self.reqmin)
+        c.konvge = int(self.konvge)
+        c.kcount = int(self.kcount)
+        if len(self.hstarts) > L.MAX_HSTARTS:
+            raise ValueError(f"at most {L.MAX_HSTARTS} depth starts")
+        c.n_hstarts = len(self.hstarts)
+        for i, h in enumerate(self.hstarts):
+            c.hstarts[i] = float(h)
+        c.early_exit_per_scene = float(self.early_exit_per_scene)
+        c.precision = PRECISIONS[self.precision]
+        c.layout = LAYOUTS[self.layout]
+        c.block_threads = int(self.block_threads)
+        c.blocks_per_sm = int(self.blocks_per_sm)
+        return c
+
+
+def version() -> str:
+    return L.lib().photic_version().decode()
+
+
+def _stream_handle(stream: Optional[torch.cuda.Stream]) -> int:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return int(s.cuda_stream)
+
+
+def _ptr(t: Optional[torch.Tensor]) -> Optional[int]:
+    return None if t is None else int(t.data_ptr())
+
+
+def _check_cuda(t: torch.Tensor, name: str, dtype) -> None:
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError(f"{name} must be a CUDA tensor")
+    if t.dtype != dtype:
+        raise TypeError(f"{name} must be {dtype}, got {t.dtype}")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+
+
+def alloc_outputs(npix: int, device, fields: Sequence[str] = OUTPUT_FIELDS,
+                  n_obs: Optional[int] = None) -> Dict[str, torch.Tensor]:
+    out = {}
+    for f in fields:
+        n = n_obs if (n_obs is not None and f in ("P", "G", "X")) else npix
+        out[f] = torch.empty(n, dtype=_DTYPES.get(f, torch.float32), device=device)
+    return out
+
+
+def _outputs_struct(out: Dict[str, torch.Tensor]) -> L.photic_outputs:
+    s = L.photic_outputs()
+    for f in OUTPUT_FIELDS:
+        setattr(s, f, _ptr(out.get(f)))
+    return s
+
+
+def invert(rrs: torch.Tensor, config: Optional[Config] = None, *,
+           seeds: Optional[torch.Tensor] = None, out: Optional[Dict[str, torch.Tensor]] = None,
+           fields: Sequence[str] = OUTPUT_FIELDS,
+           stream: Optional[torch.cuda.Stream] = None) -> Dict[str, torch.Tensor]:
+    """Fit every pixel of ``rrs`` ([npix, n_bands] float32, CUDA).
+
+    ``seeds`` ([npix, 6] float64) starts a pixel's single fit from the given
+    vector (H, 100B, q, 100P, 100G, 100X); NaN in column 0 keeps that pixel
+    on the cold multi-start.  Asynchronous on ``stream``; call :func:`sync`
+    to surface device-side errors.
+    """
+    cfg = config or Config()
+    _check_cuda(rrs, "rrs", torch.float32)
+    if rrs.dim() != 2 or rrs.shape[1] != cfg.n_bands:
+        raise ValueError(f"rrs must be [npix, {cfg.n_bands}]")
+    npix = rrs.shape[0]
+    if seeds is not None:
+        _check_cuda(seeds, "seeds", torch.float64)
+        if tuple(seeds.shape) != (npix, 6):
+            raise ValueError("seeds must be [npix, 6]")
+    if out is None:
+        out = alloc_outputs(npix, rrs.device, fields)
+    c = cfg.to_c()
+    os_ = _outputs_struct(out)
+    L.check(L.lib().photic_invert_batch(C.byref(c), _ptr(rrs), npix, cfg.n_bands, 1,
+                                        _ptr(seeds), C.byref(os_), _stream_handle(stream)))
+    return out
+
+
+def cost(rrs: torch.Tensor, params: torch.Tensor, config: Optional[Config] = None, *,
+         stream: Optional[torch.cuda.Stream] = None):
+    """samodel_error of [n, 6] parameter vectors against [n, n_bands]
+    spectra; returns (cost [n] f64, modelled Rrs [n, n_bands] f64)."""
+    cfg = config or Config()
+    _check_cuda(rrs, "rrs", torch.float32)
+    _check_cuda(params, "params", torch.float64)
+    n = rrs.shape[0]
+    c_out = torch.empty(n, dtype=torch.float64, device=rrs.device)
+    rm = torch.empty(n, cfg.n_bands, dtype=torch.float64, device=rrs.device)
+    c = cfg.to_c()
+    L.check(L.lib().photic_cost_batch(C.byref(c), _ptr(rrs), _ptr(params), n, _ptr(c_out),
+                                      _ptr(rm), _stream_handle(stream)))
+    return c_out, rm
+
+
+def generate_scene(npix: int, seed: int = 20260101, config: Optional[Config] = None, *,
+                   pix0: int = 0, mask_frac: float = 0.15, noise_sigma: float = 2.0e-4,
+                   device="cuda", with_truth: bool = True,
+                   stream: Optional[torch.cuda.Stream] = None):
+    """Synthetic scene of the plain-method workload, generated on the GPU.
+    Returns (rrs [npix, n_bands] f32, truth [npix, 5] f64 = H, P, G, X, B)."""
+    cfg = config or Config()
+    rrs = torch.empty(npix, cfg.n_bands, dtype=torch.float32, device=device)
+    truth = torch.empty(npix, 5, dtype=torch.float64, device=device) if with_truth else None
+    c = cfg.to_c()
+    L.check(L.lib().photic_generate_scene(C.byref(c), seed, pix0, npix, mask_frac, noise_sigma,
+                                          _ptr(rrs), _ptr(truth), _stream_handle(stream)))
+    return rrs, truth
+
+
+def sync(stream: Optional[torch.cuda.Stream] = None) -> None:
+    """Wait for ``stream`` and raise if the device recorded an error."""
+    L.check(L.lib().photic_sync(_stream_handle(stream)))

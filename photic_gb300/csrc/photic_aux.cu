@@ -1,0 +1,220 @@
+// photic_aux.cu -- synthetic scene generator and the batched cost kernel.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "photic_fp64.cuh"
+#include "photic_kernels.h"
+
+namespace photic {
+
+namespace {
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): counter (idx, block,
+// stream), key = 64-bit seed.  Same stream of uniforms as the CPU generator
+// used by the tests.
+__device__ __forceinline__ void philox(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c[0]), lo0 = 0xD2511F53u * c[0];
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c[2]), lo1 = 0xCD9E8D57u * c[2];
+    const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0;
+    c[1] = lo1;
+    c[2] = n2;
+    c[3] = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
+__device__ __forceinline__ void draw4(uint64_t seed, uint64_t idx, uint32_t block, uint32_t stream,
+                                      double u[4]) {
+  uint32_t c[4] = {(uint32_t)idx, (uint32_t)(idx >> 32), block, stream};
+  philox(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+#pragma unroll
+  for (int i = 0; i < 4; i++) u[i] = ((double)c[i] + 0.5) * 2.3283064365386963e-10;
+}
+
+__device__ __forceinline__ double log_uniform(double u, double lo, double hi) {
+  return exp(log(lo) + u * (log(hi) - log(lo)));
+}
+
+// Self-consistent spectrum of truth (H, P, G, X, B): the forward model's Y
+// exponent depends on the spectrum itself, so iterate spectrum -> model.
+template <int NB>
+__device__ void synthesise(const FitParams &fp, const SceneConsts &sc, double H, double P,
+                           double G, double X, double B, double *rrs) {
+  double x[6] = {H, 100.0 * B, 1.0, 100.0 * P, 100.0 * G, 100.0 * X};
+  double cur[NB];
+#pragma unroll
+  for (int b = 0; b < NB; b++) cur[b] = 0.01;
+  for (int it = 0; it < 30; it++) {
+    PixelF64<NB> px;
+    pixel_setup_f64<NB>(fp, sc, cur, px);
+    CostDetailsF64 det;
+    cost_f64<true, NB>(fp, sc, px, x, &det);
+#pragma unroll
+    for (int b = 0; b < NB; b++) cur[b] = det.Rm[b];
+  }
+#pragma unroll
+  for (int b = 0; b < NB; b++) rrs[b] = cur[b];
+}
+
+template <int NB>
+__global__ void generate_kernel(GenArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.npix) return;
+  const int nb = a.fp.n_bands;
+  const uint64_t p = (uint64_t)(a.pix0 + i);
+  double u0[4], u1[4];
+  draw4(a.seed, p, 0u, 0u, u0);
+  draw4(a.seed, p, 1u, 0u, u1);
+  const double H = 0.5 + 24.5 * u0[0];
+  const double P = log_uniform(u0[1], 0.005, 0.1);
+  const double G = log_uniform(u0[2], 0.005, 0.2);
+  const double X = log_uniform(u0[3], 0.001, 0.05);
+  const double B = 0.05 + 0.45 * u1[0];
+  double r[NB];
+  synthesise<NB>(a.fp, a.sc, H, P, G, X, B, r);
+  for (int b = 0; b < nb; b += 2) {
+    double u[4];
+    draw4(a.seed, p, 2u + (uint32_t)(b / 4), 0u, u);
+    const double rad = sqrt(-2.0 * log(u[b % 4]));
+    const double ang = 2.0 * kPi * u[(b % 4) + 1];
+    r[b] += a.noise_sigma * rad * cos(ang);
+    if (b + 1 < nb) r[b + 1] += a.noise_sigma * rad * sin(ang);
+  }
+  float *o = a.rrs + i * nb;
+  for (int b = 0; b < nb; b++) o[b] = (float)r[b];
+  if (u1[1] < a.mask_frac) {
+    if (u1[2] < 0.5) {
+      for (int b = 0; b < nb; b++) o[b] = a.fp.nodata;
+    } else {
+      o[nb - 1] = -fabsf(o[nb - 1]) - 1.0e-3f;
+    }
+  }
+  if (a.truth) {
+    double *t = a.truth + i * 5;
+    t[0] = H;
+    t[1] = P;
+    t[2] = G;
+    t[3] = X;
+    t[4] = B;
+  }
+}
+
+template <int NB>
+__global__ void cost_kernel(CostArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int nb = a.fp.n_bands;
+  double r[NB];
+#pragma unroll
+  for (int b = 0; b < NB; b++) r[b] = b < nb ? (double)a.rrs[i * nb + b] : 0.0;
+  PixelF64<NB> px;
+  pixel_setup_f64<NB>(a.fp, a.sc, r, px);
+  double x[6];
+#pragma unroll
+  for (int k = 0; k < 6; k++) x[k] = a.params[i * 6 + k];
+  CostDetailsF64 det;
+  const double c = cost_f64<true, NB>(a.fp, a.sc, px, x, &det);
+  a.cost[i] = c;
+  if (a.rrs_modelled)
+    for (int b = 0; b < nb; b++) a.rrs_modelled[i * nb + b] = det.Rm[b];
+}
+
+}  // namespace
+
+cudaError_t launch_generate(const GenArgs &a, cudaStream_t s) {
+  if (a.npix <= 0) return cudaSuccess;
+  const int block = 128;
+  const int64_t grid = (a.npix + block - 1) / block;
+  if (a.fp.n_bands == 4) generate_kernel<4><<<(unsigned)grid, block, 0, s>>>(a);
+  else generate_kernel<8><<<(unsigned)grid, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cost(const CostArgs &a, cudaStream_t s) {
+  if (a.n <= 0) return cudaSuccess;
+  const int block = 128;
+  const int64_t grid = (a.n + block - 1) / block;
+  if (a.fp.n_bands == 4) cost_kernel<4><<<(unsigned)grid, block, 0, s>>>(a);
+  else cost_kernel<8><<<(unsigned)grid, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace photic
+
+// ---------------------------------------------------------------------------
+// Pipe-throughput probes for the roofline denominators of compute-bound
+// kernels: independent FMA chains (FP64 DFMA, FP32 FFMA) and MUFU ex2.
+// ---------------------------------------------------------------------------
+namespace photic {
+namespace {
+
+template <class T>
+__global__ void fma_probe(T *out, int iters, T x, T y) {
+  T a0 = (T)threadIdx.x * (T)1e-3, a1 = a0 + (T)1, a2 = a0 + (T)2, a3 = a0 + (T)3;
+  T a4 = a0 + (T)4, a5 = a0 + (T)5, a6 = a0 + (T)6, a7 = a0 + (T)7;
+  for (int i = 0; i < iters; i++) {
+    a0 = fma(a0, x, y); a1 = fma(a1, x, y); a2 = fma(a2, x, y); a3 = fma(a3, x, y);
+    a4 = fma(a4, x, y); a5 = fma(a5, x, y); a6 = fma(a6, x, y); a7 = fma(a7, x, y);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+__global__ void mufu_probe(float *out, int iters, float s) {
+  float a0 = threadIdx.x * 1e-6f, a1 = a0 + 0.1f, a2 = a0 + 0.2f, a3 = a0 + 0.3f;
+  for (int i = 0; i < iters; i++) {
+    a0 = exp2f(a0 * s); a1 = exp2f(a1 * s); a2 = exp2f(a2 * s); a3 = exp2f(a3 * s);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3;
+}
+
+}  // namespace
+
+cudaError_t measure_peaks(double *fp64_tflops, double *fp32_tflops, double *mufu_tops) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int block = 256, grid = sms * 8, n = grid * block;
+  void *buf = nullptr;
+  cudaError_t e = cudaMalloc(&buf, (size_t)n * sizeof(double));
+  if (e != cudaSuccess) return e;
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  float ms = 0.f;
+  // FP64: 8 DFMA per iteration per thread
+  const int it64 = 4096;
+  fma_probe<double><<<grid, block>>>((double *)buf, 16, 0.999999, 1e-7);
+  cudaEventRecord(t0);
+  fma_probe<double><<<grid, block>>>((double *)buf, it64, 0.999999, 1e-7);
+  cudaEventRecord(t1);
+  cudaEventSynchronize(t1);
+  cudaEventElapsedTime(&ms, t0, t1);
+  *fp64_tflops = 2.0 * 8.0 * it64 * (double)n / (ms * 1e-3) / 1e12;
+  const int it32 = 65536;
+  fma_probe<float><<<grid, block>>>((float *)buf, 16, 0.999999f, 1e-7f);
+  cudaEventRecord(t0);
+  fma_probe<float><<<grid, block>>>((float *)buf, it32, 0.999999f, 1e-7f);
+  cudaEventRecord(t1);
+  cudaEventSynchronize(t1);
+  cudaEventElapsedTime(&ms, t0, t1);
+  *fp32_tflops = 2.0 * 8.0 * it32 * (double)n / (ms * 1e-3) / 1e12;
+  const int itm = 16384;
+  mufu_probe<<<grid, block>>>((float *)buf, 16, 1e-3f);
+  cudaEventRecord(t0);
+  mufu_probe<<<grid, block>>>((float *)buf, itm, 1e-3f);
+  cudaEventRecord(t1);
+  cudaEventSynchronize(t1);
+  cudaEventElapsedTime(&ms, t0, t1);
+  *mufu_tops = 4.0 * itm * (double)n / (ms * 1e-3) / 1e12;
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  e = cudaGetLastError();
+  cudaFree(buf);
+  return e;
+}
+
+}  // namespace photic

@@ -1,0 +1,414 @@
+// photic_host.cu -- the extern "C" entry points of include/photic.h.
+//
+// Host work here is set-up only: validating the configuration, resolving
+// the table interpolation at the band wavelengths (interp_1d,
+// model/common.c:298) and the subsurface-angle secants once per call, and
+// launching the kernels.  No pixel is ever processed on the host.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/photic.h"
+#include "photic_kernels.h"
+#include "photic_params.h"
+#include "photic_tables.h"
+
+using namespace photic;
+
+namespace {
+
+constexpr double kPiHost = 3.141592653589793;  // model/common.h:19
+
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...) __attribute__((format(printf, 2, 3)));
+int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+  return fail(PHOTIC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// Tolerant single-precision comparisons of model/common.c:392-406.
+bool f_close(float a, float b, float eps) {
+  double big = fabs(a) < fabs(b) ? fabs(b) : fabs(a);
+  return fabs(a - b) <= big * eps;
+}
+bool f_le(float a, float b, float eps) { return a < b || f_close(a, b, eps); }
+bool f_ge(float a, float b, float eps) { return a > b || f_close(a, b, eps); }
+
+// Segment choice of interp_1d (model/common.c:298-330) for target x over
+// abscissae X[0..n): either an exact end point, or (i0, i1, t).
+InterpPlan resolve_interp(const double *X, int n, double x) {
+  InterpPlan p{};
+  if (f_close((float)x, (float)X[0], 1.0e-5f)) {
+    p.exact = 1;
+    p.i0 = p.i1 = 0;
+    return p;
+  }
+  if (f_close((float)x, (float)X[n - 1], 1.0e-5f)) {
+    p.exact = 1;
+    p.i0 = p.i1 = n - 1;
+    return p;
+  }
+  double x0 = 0.0, x1 = 1.0;
+  if (X[0] < X[n - 1] && x < X[0]) {
+    p.i0 = 0;
+    p.i1 = 1;
+  } else if (X[n - 1] > X[0] && x > X[n - 1]) {
+    p.i0 = n - 2;
+    p.i1 = n - 1;
+  } else {
+    p.i0 = 0;
+    p.i1 = 0;
+    for (int i = 0; i + 1 < n; i++) {
+      bool up = f_le((float)X[i], (float)x, 1.0e-5f) && f_ge((float)X[i + 1], (float)x, 1.0e-5f);
+      bool down = f_ge((float)X[i], (float)x, 1.0e-5f) && f_le((float)X[i + 1], (float)x, 1.0e-5f);
+      if (up || down) {
+        p.i0 = i;
+        p.i1 = i + 1;
+        break;
+      }
+    }
+  }
+  x0 = X[p.i0];
+  x1 = X[p.i1];
+  p.exact = 0;
+  p.t = (x - x0) / (x1 - x0);
+  p.one_minus_t = 1.0 - p.t;
+  return p;
+}
+
+double interp_apply(const InterpPlan &p, const double *Y) {
+  if (p.exact) return Y[p.i0];
+  return Y[p.i0] * p.one_minus_t + Y[p.i1] * p.t;
+}
+
+double table_at(const double *tab, double x) {
+  return interp_apply(resolve_interp(tables::wl, tables::kNRef, x), tab);
+}
+
+// Scene constants for a subsurface sun zenith (samodel():521-618).
+void make_scene(const photic_config &cfg, double theta_sun_deg, SceneConsts &sc) {
+  memset(&sc, 0, sizeof sc);
+  double th = cfg.theta_view_deg;
+  th *= kPiHost / 180.0;
+  sc.sec_view = 1.0 / cos(th);
+  th = theta_sun_deg;
+  th *= kPiHost / 180.0;
+  sc.sec_sun = 1.0 / cos(th);
+  sc.h_tide = cfg.h_tide;
+  const double S = 0.015;
+  for (int b = 0; b < cfg.n_bands; b++) {
+    const double l = cfg.wavelengths[b];
+    sc.wl[b] = l;
+    sc.a0[b] = table_at(tables::a0, l);
+    sc.a1[b] = table_at(tables::a1, l);
+    sc.bbw[b] = table_at(tables::bbw, l);
+    sc.aw[b] = table_at(tables::aw, l);
+    sc.refl[b] = table_at(tables::bottom[0], l);
+    sc.eS[b] = exp(-S * (l - 440.0));
+    sc.ratio440[b] = 440.0 / l;
+  }
+}
+
+void make_fit(const photic_config &cfg, FitParams &fp) {
+  memset(&fp, 0, sizeof fp);
+  fp.n_bands = cfg.n_bands;
+  fp.kcount = cfg.kcount;
+  fp.konvge = cfg.konvge;
+  fp.n_hstarts = cfg.n_hstarts;
+  fp.layout = cfg.layout;
+  fp.nodata = cfg.nodata_value;
+  fp.reqmin = cfg.reqmin;
+  fp.early_exit_per_scene = cfg.early_exit_per_scene;
+  fp.aw640 = table_at(tables::aw, 640.0);
+  for (int k = 0; k < cfg.n_hstarts; k++) fp.hstarts[k] = cfg.hstarts[k];
+  const double targets[kNRefTargets] = {440.0, 490.0, 550.0, 640.0, 750.0};
+  for (int t = 0; t < kNRefTargets; t++)
+    fp.plan[t] = resolve_interp(cfg.wavelengths, cfg.n_bands, targets[t]);
+  // K penalty (model/samodel.c:2696-2732): thresholds and targets.
+  const double mean_c = 0.275, min_c = 0.185;
+  const double t2 = 0.5 * (1.5 * min_c + 0.5 * mean_c);
+  const double t3 = 0.5 * (1.25 * min_c + 0.75 * mean_c);
+  const double t5 = 0.5 * (1.75 * min_c + 0.25 * mean_c);
+  const double thr[5] = {mean_c, t2, t3, t2, t5};
+  const double tgt[5] = {min_c, t2, t3, t2, t5};
+  for (int i = 0; i < 5; i++) {
+    fp.kp.k_thr[i] = thr[i];
+    fp.kp.inv_t[i] = 1.0 / (0.01 + tgt[i]);
+  }
+}
+
+// Sticky per-device error word the kernels OR their error bits into.
+std::mutex g_dev_mu;
+std::vector<unsigned int *> g_dev_err;
+std::vector<int> g_dev_sms;
+
+int device_state(unsigned int **err, int *sms) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  std::lock_guard<std::mutex> lk(g_dev_mu);
+  if ((int)g_dev_err.size() <= dev) {
+    g_dev_err.resize(dev + 1, nullptr);
+    g_dev_sms.resize(dev + 1, 0);
+  }
+  if (g_dev_err[dev] == nullptr) {
+    unsigned int *p = nullptr;
+    e = cudaMalloc(&p, sizeof(unsigned int));
+    if (e != cudaSuccess) return fail(PHOTIC_ERR_NOMEM, "error word: %s", cudaGetErrorString(e));
+    e = cudaMemset(p, 0, sizeof(unsigned int));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemset");
+    int n = 0;
+    e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+    g_dev_err[dev] = p;
+    g_dev_sms[dev] = n;
+  }
+  *err = g_dev_err[dev];
+  *sms = g_dev_sms[dev];
+  return PHOTIC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *photic_version(void) { return "photic-gb300 0.1"; }
+
+const char *photic_last_error(void) { return g_err.c_str(); }
+
+void photic_config_default(photic_config *cfg) {
+  memset(cfg, 0, sizeof *cfg);
+  cfg->n_bands = 4;
+  const double wl[4] = {443.0, 482.0, 561.0, 655.0};
+  for (int b = 0; b < 4; b++) cfg->wavelengths[b] = wl[b];
+  cfg->theta_sun_deg = 35.0;
+  cfg->theta_view_deg = 0.0;
+  cfg->h_tide = 0.0;
+  cfg->nodata_value = -9999.0f;
+  cfg->reqmin = 1.0e-10;
+  cfg->konvge = 100;
+  cfg->kcount = 2000;
+  const double hs[8] = {40.0, 30.0, 20.0, 15.0, 10.0, 7.5, 2.5, 1.0};
+  cfg->n_hstarts = 8;
+  for (int k = 0; k < 8; k++) cfg->hstarts[k] = hs[k];
+  cfg->early_exit_per_scene = 2.5;
+  cfg->precision = PHOTIC_PREC_FP64;
+  cfg->layout = PHOTIC_LAYOUT_REFERENCE;
+  cfg->block_threads = 0;
+  cfg->blocks_per_sm = 0;
+}
+
+int photic_config_check(const photic_config *cfg) {
+  if (!cfg) return fail(PHOTIC_ERR_INVALID, "config is NULL");
+  if (cfg->n_bands < 2 || cfg->n_bands > PHOTIC_MAX_BANDS)
+    return fail(PHOTIC_ERR_INVALID, "n_bands %d outside 2..%d", cfg->n_bands, PHOTIC_MAX_BANDS);
+  for (int b = 0; b < cfg->n_bands; b++) {
+    if (!(cfg->wavelengths[b] > 0.0) || !isfinite(cfg->wavelengths[b]))
+      return fail(PHOTIC_ERR_INVALID, "wavelength %d is not a positive number", b);
+    if (b && !(cfg->wavelengths[b] > cfg->wavelengths[b - 1]))
+      return fail(PHOTIC_ERR_INVALID, "wavelengths must be ascending");
+  }
+  if (!(cfg->reqmin > 0.0)) return fail(PHOTIC_ERR_INVALID, "reqmin must be > 0 (nelmin ifault 1)");
+  if (cfg->konvge < 1) return fail(PHOTIC_ERR_INVALID, "konvge must be >= 1 (nelmin ifault 1)");
+  if (cfg->kcount < 1) return fail(PHOTIC_ERR_INVALID, "kcount must be >= 1");
+  if (cfg->n_hstarts < 1 || cfg->n_hstarts > PHOTIC_MAX_HSTARTS)
+    return fail(PHOTIC_ERR_INVALID, "n_hstarts %d outside 1..%d", cfg->n_hstarts, PHOTIC_MAX_HSTARTS);
+  if (cfg->precision < PHOTIC_PREC_FP64 || cfg->precision > PHOTIC_PREC_FP32)
+    return fail(PHOTIC_ERR_INVALID, "unknown precision %d", cfg->precision);
+  if (cfg->layout != PHOTIC_LAYOUT_REFERENCE && cfg->layout != PHOTIC_LAYOUT_SCENE_B)
+    return fail(PHOTIC_ERR_INVALID, "unknown layout %d", cfg->layout);
+  if (cfg->block_threads != 0 && cfg->block_threads != 64 && cfg->block_threads != 128 &&
+      cfg->block_threads != 256)
+    return fail(PHOTIC_ERR_INVALID, "block_threads must be 0, 64, 128 or 256");
+  if (cfg->blocks_per_sm < 0 || cfg->blocks_per_sm > 32)
+    return fail(PHOTIC_ERR_INVALID, "blocks_per_sm outside 0..32");
+  return PHOTIC_OK;
+}
+
+double photic_interp_1d(const double *X, const double *Y, int32_t n, double x) {
+  if (!X || !Y || n < 2) return NAN;
+  return interp_apply(resolve_interp(X, n, x), Y);
+}
+
+int photic_band_constants(const photic_config *cfg, double *out) {
+  int rc = photic_config_check(cfg);
+  if (rc) return rc;
+  SceneConsts sc;
+  make_scene(*cfg, cfg->theta_sun_deg, sc);
+  const double aw640 = table_at(tables::aw, 640.0);
+  for (int b = 0; b < cfg->n_bands; b++) {
+    out[b * 8 + 0] = sc.a0[b];
+    out[b * 8 + 1] = sc.a1[b];
+    out[b * 8 + 2] = sc.aw[b];
+    out[b * 8 + 3] = sc.bbw[b];
+    out[b * 8 + 4] = sc.refl[b];
+    out[b * 8 + 5] = sc.sec_sun;
+    out[b * 8 + 6] = sc.sec_view;
+    out[b * 8 + 7] = aw640;
+  }
+  return PHOTIC_OK;
+}
+
+int photic_invert_batch(const photic_config *cfg, const float *d_rrs, int64_t npix,
+                        int64_t pixel_stride, int64_t band_stride, const double *d_seeds,
+                        const photic_outputs *out, void *stream) {
+  int rc = photic_config_check(cfg);
+  if (rc) return rc;
+  if (npix < 0) return fail(PHOTIC_ERR_INVALID, "npix < 0");
+  if (npix == 0) return PHOTIC_OK;
+  if (!d_rrs || !out) return fail(PHOTIC_ERR_INVALID, "NULL input or output");
+  if (pixel_stride < 1 || band_stride < 1)
+    return fail(PHOTIC_ERR_INVALID, "strides must be >= 1");
+  if (cfg->precision != PHOTIC_PREC_FP64)
+    return fail(PHOTIC_ERR_UNSUPPORTED, "precision %d not built in this version", cfg->precision);
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned int *err = nullptr;
+  int sms = 0;
+  rc = device_state(&err, &sms);
+  if (rc) return rc;
+
+  InvertArgs a;
+  memset(&a, 0, sizeof a);
+  make_fit(*cfg, a.fp);
+  make_scene(*cfg, cfg->theta_sun_deg, a.sc);
+  a.rrs = d_rrs;
+  a.npix = npix;
+  a.pixel_stride = pixel_stride;
+  a.band_stride = band_stride;
+  a.vec4 = (cfg->n_bands == 4 && pixel_stride == 4 && band_stride == 1 &&
+            ((uintptr_t)d_rrs & 15u) == 0);
+  a.seeds = d_seeds;
+  a.out = *out;
+  a.error = err;
+  a.early_exit = cfg->early_exit_per_scene * (double)(float)1;
+
+  const int block = cfg->block_threads ? cfg->block_threads : 128;
+  int per_sm = cfg->blocks_per_sm;
+  if (per_sm == 0) {
+    per_sm = invert_f64_blocks_per_sm(cfg->n_bands, block);
+    if (per_sm < 1) return fail(PHOTIC_ERR_CUDA, "kernel does not fit on the device");
+  }
+  int64_t grid = (int64_t)sms * per_sm;
+  const int64_t need = (npix + block - 1) / block;
+  if (grid > need) grid = need;
+
+  unsigned long long *queue = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&queue, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return fail(PHOTIC_ERR_NOMEM, "queue head: %s", cudaGetErrorString(e));
+  e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  a.queue = queue;
+  e = launch_invert_f64(a, block, (int)grid, s);
+  cudaError_t e2 = cudaFreeAsync(queue, s);
+  if (e != cudaSuccess) return cuda_fail(e, "invert kernel launch");
+  if (e2 != cudaSuccess) return cuda_fail(e2, "cudaFreeAsync");
+  return PHOTIC_OK;
+}
+
+int photic_joint_invert_batch(const photic_config *cfg, const int32_t *d_offsets,
+                              const double *d_theta_sun_deg, const float *d_rrs, int64_t npix,
+                              int64_t n_obs, const photic_outputs *out, void *stream) {
+  (void)cfg; (void)d_offsets; (void)d_theta_sun_deg; (void)d_rrs; (void)npix; (void)n_obs;
+  (void)out; (void)stream;
+  return fail(PHOTIC_ERR_UNSUPPORTED, "joint fit not built in this version");
+}
+
+int photic_cost_batch(const photic_config *cfg, const float *d_rrs, const double *d_params,
+                      int64_t n, double *d_cost, double *d_rrs_modelled, void *stream) {
+  int rc = photic_config_check(cfg);
+  if (rc) return rc;
+  if (n < 0 || !d_rrs || !d_params || !d_cost) return fail(PHOTIC_ERR_INVALID, "bad arguments");
+  CostArgs a;
+  memset(&a, 0, sizeof a);
+  make_fit(*cfg, a.fp);
+  make_scene(*cfg, cfg->theta_sun_deg, a.sc);
+  a.rrs = d_rrs;
+  a.params = d_params;
+  a.n = n;
+  a.cost = d_cost;
+  a.rrs_modelled = d_rrs_modelled;
+  cudaError_t e = launch_cost(a, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cost kernel launch");
+  return PHOTIC_OK;
+}
+
+int photic_generate_scene(const photic_config *cfg, uint64_t seed, int64_t pix0, int64_t npix,
+                          double mask_frac, double noise_sigma, float *d_rrs, double *d_truth,
+                          void *stream) {
+  int rc = photic_config_check(cfg);
+  if (rc) return rc;
+  if (npix < 0 || pix0 < 0 || !d_rrs) return fail(PHOTIC_ERR_INVALID, "bad arguments");
+  GenArgs a;
+  memset(&a, 0, sizeof a);
+  make_fit(*cfg, a.fp);
+  make_scene(*cfg, cfg->theta_sun_deg, a.sc);
+  a.seed = seed;
+  a.pix0 = pix0;
+  a.npix = npix;
+  a.mask_frac = mask_frac;
+  a.noise_sigma = noise_sigma;
+  a.rrs = d_rrs;
+  a.truth = d_truth;
+  cudaError_t e = launch_generate(a, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "generator launch");
+  return PHOTIC_OK;
+}
+
+int photic_joint_counts(uint64_t seed, int64_t npix, int32_t kmin, int32_t kmax,
+                        int32_t *d_counts, void *stream) {
+  (void)seed; (void)npix; (void)kmin; (void)kmax; (void)d_counts; (void)stream;
+  return fail(PHOTIC_ERR_UNSUPPORTED, "joint generator not built in this version");
+}
+
+int photic_generate_joint(const photic_config *cfg, uint64_t seed, int64_t npix,
+                          const int32_t *d_offsets, double theta_sun_min, double theta_sun_max,
+                          double mask_frac, double noise_sigma, double *d_theta_sun,
+                          float *d_rrs, double *d_truth, void *stream) {
+  (void)cfg; (void)seed; (void)npix; (void)d_offsets; (void)theta_sun_min; (void)theta_sun_max;
+  (void)mask_frac; (void)noise_sigma; (void)d_theta_sun; (void)d_rrs; (void)d_truth; (void)stream;
+  return fail(PHOTIC_ERR_UNSUPPORTED, "joint generator not built in this version");
+}
+
+int photic_measure_peaks(double *fp64_tflops, double *fp32_tflops, double *mufu_tops) {
+  if (!fp64_tflops || !fp32_tflops || !mufu_tops) return fail(PHOTIC_ERR_INVALID, "NULL output");
+  cudaError_t e = measure_peaks(fp64_tflops, fp32_tflops, mufu_tops);
+  if (e != cudaSuccess) return cuda_fail(e, "peak probes");
+  return PHOTIC_OK;
+}
+
+int photic_sync(void *stream) {
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+  unsigned int *err = nullptr;
+  int sms = 0;
+  int rc = device_state(&err, &sms);
+  if (rc) return rc;
+  unsigned int h = 0;
+  e = cudaMemcpy(&h, err, sizeof h, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy error word");
+  if (h) {
+    cudaMemset(err, 0, sizeof h);
+    if (h & PHOTIC_DEVERR_EVAL_CAP)
+      return fail(PHOTIC_ERR_TIMEOUT, "a pixel exceeded the evaluation cap (device error 0x%x)", h);
+    return fail(PHOTIC_ERR_INVALID, "device reported invalid input (device error 0x%x)", h);
+  }
+  return PHOTIC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,60 @@
+// photic_kernels.h -- launch arguments and launchers of the device code
+// (internal to the library; the public ABI is include/photic.h).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/photic.h"
+#include "photic_params.h"
+
+namespace photic {
+
+// Device error bits accumulated in the per-call error word.
+enum : unsigned {
+  PHOTIC_DEVERR_EVAL_CAP = 1u,   // a pixel exceeded the defensive evaluation cap
+  PHOTIC_DEVERR_BAD_SCENES = 2u  // a joint pixel had a scene count outside 1..8
+};
+
+struct InvertArgs {
+  FitParams fp;
+  SceneConsts sc;
+  const float *rrs;
+  int64_t npix, pixel_stride, band_stride;
+  int32_t vec4;  // rrs is [npix][4], 16-byte aligned
+  const double *seeds;
+  photic_outputs out;
+  unsigned long long *queue;
+  unsigned int *error;
+  double early_exit;  // early-exit cost threshold (per-scene value * scenes)
+};
+
+size_t smem_bytes_f64(int block, int nb);
+cudaError_t launch_invert_f64(const InvertArgs &a, int block, int grid, cudaStream_t s);
+int invert_f64_blocks_per_sm(int nb, int block);  // resident blocks per SM (0 on error)
+
+struct GenArgs {
+  FitParams fp;
+  SceneConsts sc;
+  uint64_t seed;
+  int64_t pix0, npix;
+  double mask_frac, noise_sigma;
+  float *rrs;
+  double *truth;
+};
+cudaError_t launch_generate(const GenArgs &a, cudaStream_t s);
+
+struct CostArgs {
+  FitParams fp;
+  SceneConsts sc;
+  const float *rrs;
+  const double *params;
+  int64_t n;
+  double *cost;
+  double *rrs_modelled;
+};
+cudaError_t launch_cost(const CostArgs &a, cudaStream_t s);
+
+// Throughput probes (TFLOP/s of FP64 and FP32 FMA, Tops/s of MUFU ex2).
+cudaError_t measure_peaks(double *fp64_tflops, double *fp32_tflops, double *mufu_tops);
+
+}  // namespace photic

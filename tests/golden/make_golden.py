@@ -1,0 +1,81 @@
+"""Regenerate the golden fixtures from the reference itself.
+
+Runs the reference's own samodel_optimise / samodel_error / nelmin, compiled
+from its sources by oracle/Makefile into oracle/_ref/libphotic_ref.so
+(needs the reference sources; run from the repository root):
+
+    make -C oracle all && python tests/golden/make_golden.py
+
+Inputs are synthetic spectra of the plain-method workload (the reference
+publishes no test vectors).  Every fixture stores its inputs next to the
+reference outputs, so the tests never need the reference at run time.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+from oracle import oracle as O  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+KEEP = [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 11, 19, 27]  # H B cost rrs_err Kmin iod evk ev conv status P G X
+
+
+def single():
+    rrs, truth = O.generate_single(20260101, 768, pix0=1000)
+    ref = O.invert_batch(rrs, which="reference", nthreads=os.cpu_count())
+    # the reference's own hard-coded tolerances on a smaller set
+    ref_d = O.invert_batch(rrs[:256], which="reference", reqmin=None, nthreads=os.cpu_count())
+    np.savez_compressed(os.path.join(OUT, "single_scene.npz"), rrs=rrs, truth=truth,
+                        ref=ref[:, KEEP], ref_default=ref_d[:, KEEP], cols=np.array(KEEP),
+                        seed=np.array(20260101), pix0=np.array(1000))
+
+
+def joint():
+    offs, th, rrs, truth = O.generate_joint(20260202, 96)
+    ref = O.joint_invert_batch(offs, th, rrs, which="reference", nthreads=os.cpu_count())
+    cols = list(range(0, 11)) + list(range(11, 35))
+    np.savez_compressed(os.path.join(OUT, "joint.npz"), offsets=offs, theta_sun=th, rrs=rrs,
+                        truth=truth, ref=ref[:, cols], cols=np.array(cols))
+
+
+def cost_and_nelmin():
+    rng = np.random.default_rng(7)
+    rrs, _ = O.generate_single(20260303, 64, mask_frac=0.0)
+    params = np.column_stack([rng.uniform(0.2, 40, 64), rng.uniform(1, 60, 64),
+                              rng.uniform(0.2, 2, 64), rng.uniform(0.1, 12, 64),
+                              rng.uniform(0.1, 25, 64), rng.uniform(0.05, 6, 64)])
+    params[::7] *= -1.0  # the cost takes |x|
+    costs, rm, K = [], [], []
+    for i in range(64):
+        c, r, k = O.cost(rrs[i].astype(np.float64), params[i], which="reference")
+        costs.append(c); rm.append(r); K.append(k)
+    starts = np.column_stack([np.full(16, 40.0), 400 * rrs[:16, 1], np.ones(16),
+                              np.full(16, 0.9), np.full(16, 1.35), 3000 * 0.3108 * rrs[:16, 3]])
+    steps = starts * np.array([1.25, 1.5, 0.5, 2, 2, 2])
+    nm = [O.nelmin(rrs[i].astype(np.float64), starts[i], steps[i], which="reference")
+          for i in range(16)]
+    bc = O.band_constants(which="reference")
+    np.savez_compressed(os.path.join(OUT, "cost_nelmin.npz"), rrs=rrs, params=params,
+                        cost=np.array(costs), rrs_modelled=np.array(rm), K=np.array(K),
+                        nm_start=starts, nm_step=steps,
+                        nm_xmin=np.array([r[0] for r in nm]),
+                        nm_y=np.array([r[1] for r in nm]),
+                        nm_counts=np.array([[r[2], r[3], r[4]] for r in nm]),
+                        band_constants=bc)
+
+
+if __name__ == "__main__":
+    O.build(ref=True)
+    if not O.reference_available():
+        sys.exit("reference library not built; the reference sources are required")
+    single()
+    joint()
+    cost_and_nelmin()
+    for f in sorted(os.listdir(OUT)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(OUT, f)), "bytes")

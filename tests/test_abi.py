@@ -1,0 +1,62 @@
+"""The C-ABI library: it loads, exports every function include/photic.h
+declares, and its host-side set-up agrees with the oracle.  No GPU needed
+(only host functions are called)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared(header):
+    txt = open(os.path.join(ROOT, "include", header)).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(photic_[a-z0-9_]+|samodel[a-z_]*)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from photic_gb300 import _lib
+    return _lib.lib()
+
+
+def test_exports_every_declared_symbol(lib):
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        for name in _declared(h):
+            assert hasattr(lib, name), f"{name} declared in include/{h} but not exported"
+
+
+def test_config_defaults_and_validation(lib):
+    from photic_gb300 import _lib as L
+    c = L.photic_config()
+    lib.photic_config_default(C.byref(c))
+    assert c.n_bands == 4 and c.kcount == 2000 and c.konvge == 100 and c.reqmin == 1e-10
+    assert list(c.hstarts[:8]) == [40.0, 30.0, 20.0, 15.0, 10.0, 7.5, 2.5, 1.0]
+    assert lib.photic_config_check(C.byref(c)) == 0
+    c.reqmin = 0.0  # nelmin's ifault 1 condition
+    assert lib.photic_config_check(C.byref(c)) == L.ERR_INVALID
+    assert b"reqmin" in lib.photic_last_error()
+    lib.photic_config_default(C.byref(c))
+    c.n_bands = 9
+    assert lib.photic_config_check(C.byref(c)) == L.ERR_INVALID
+
+
+def test_interp_matches_oracle(lib, port):
+    X = np.array([443.0, 482.0, 561.0, 655.0])
+    Y = np.array([0.011, 0.013, 0.009, 0.001])
+    Xp = X.ctypes.data_as(C.POINTER(C.c_double))
+    Yp = Y.ctypes.data_as(C.POINTER(C.c_double))
+    for x in [400.0, 440.0, 443.0, 482.0, 490.0, 550.0, 640.0, 655.0, 750.0]:
+        assert lib.photic_interp_1d(Xp, Yp, 4, x) == port.interp_1d(X, Y, x)
+
+
+@pytest.mark.parametrize("theta", [35.0, 25.0, 50.0])
+def test_band_constants_match_oracle(lib, port, theta):
+    import photic_gb300
+    cfg = photic_gb300.Config(theta_sun_deg=theta).to_c()
+    out = np.zeros((4, 8))
+    assert lib.photic_band_constants(C.byref(cfg), out.ctypes.data_as(C.POINTER(C.c_double))) == 0
+    np.testing.assert_array_equal(out, port.band_constants(theta_sun=theta))

@@ -1,0 +1,43 @@
+"""The C restatement against the reference compiled from its own sources,
+on fresh inputs (skipped where the reference sources are not present)."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.skipif(not O.reference_available(),
+                                reason="oracle/_ref not built (reference sources absent)")
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_invert_bit_exact(seed):
+    rrs, _ = O.generate_single(seed, 600)
+    a = O.invert_batch(rrs)
+    b = O.invert_batch(rrs, which="reference")
+    cols = list(range(0, 11)) + [11, 19, 27]
+    assert np.array_equal(a[:, cols], b[:, cols])
+
+
+def test_invert_edge_spectra_bit_exact():
+    rng = np.random.default_rng(3)
+    rrs = rng.uniform(1e-5, 0.05, size=(300, 4)).astype(np.float32)  # arbitrary, not physical
+    rrs[::10, 1] = 0.0
+    rrs[5::10, 0] = 1e-6
+    a = O.invert_batch(rrs)
+    b = O.invert_batch(rrs, which="reference")
+    cols = list(range(0, 11)) + [11, 19, 27]
+    assert np.array_equal(a[:, cols], b[:, cols], equal_nan=True)
+
+
+def test_joint_bit_exact():
+    offs, th, rrs, _ = O.generate_joint(11, 80)
+    a = O.joint_invert_batch(offs, th, rrs)
+    b = O.joint_invert_batch(offs, th, rrs, which="reference")
+    assert np.array_equal(a[:, :35], b[:, :35])
+
+
+def test_interp_1d_bit_exact():
+    X = np.array([443.0, 482.0, 561.0, 655.0])
+    Y = np.array([0.011, 0.013, 0.009, 0.001])
+    for x in [400.0, 440.0, 443.0, 443.001, 482.0, 490.0, 550.0, 640.0, 655.0, 700.0, 750.0]:
+        assert O.interp_1d(X, Y, x) == O.interp_1d(X, Y, x, which="reference")
