@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "photic_dfcost.cuh"
 #include "photic_fp64.cuh"
 #include "photic_kernels.h"
 
@@ -104,6 +105,22 @@ __global__ void generate_kernel(GenArgs a) {
 }
 
 template <int NB>
+__global__ void cost_kernel_df(const __grid_constant__ CostArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int nb = a.fp.n_bands;
+  float r[NB];
+#pragma unroll
+  for (int b = 0; b < NB; b++) r[b] = b < nb ? a.rrs[i * nb + b] : 0.0f;
+  PixelDF<NB> px;
+  pixel_setup_df<NB>(a.fp, a.ds, r, px);
+  df64 x[6];
+#pragma unroll
+  for (int k = 0; k < 6; k++) x[k] = df_from_double(a.params[i * 6 + k]);
+  a.cost[i] = df_to_double(cost_df<false, NB>(a.fp, a.ds, px, x, nullptr));
+}
+
+template <int NB>
 __global__ void cost_kernel(CostArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
@@ -138,8 +155,13 @@ cudaError_t launch_cost(const CostArgs &a, cudaStream_t s) {
   if (a.n <= 0) return cudaSuccess;
   const int block = 128;
   const int64_t grid = (a.n + block - 1) / block;
-  if (a.fp.n_bands == 4) cost_kernel<4><<<(unsigned)grid, block, 0, s>>>(a);
-  else cost_kernel<8><<<(unsigned)grid, block, 0, s>>>(a);
+  if (a.precision == PHOTIC_PREC_DF64) {
+    if (a.fp.n_bands == 4) cost_kernel_df<4><<<(unsigned)grid, block, 0, s>>>(a);
+    else cost_kernel_df<8><<<(unsigned)grid, block, 0, s>>>(a);
+  } else {
+    if (a.fp.n_bands == 4) cost_kernel<4><<<(unsigned)grid, block, 0, s>>>(a);
+    else cost_kernel<8><<<(unsigned)grid, block, 0, s>>>(a);
+  }
   return cudaGetLastError();
 }
 

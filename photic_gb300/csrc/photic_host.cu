@@ -153,6 +153,41 @@ void make_fit(const photic_config &cfg, FitParams &fp) {
   }
 }
 
+DfPair split(double d) {
+  DfPair p;
+  p.hi = (float)d;
+  p.lo = (float)(d - (double)p.hi);
+  return p;
+}
+
+// Double-float copies of the cost constants (PHOTIC_PREC_DF64).
+void make_df(const photic_config &cfg, const FitParams &fp, const SceneConsts &sc, int n_params,
+             DfScene &ds) {
+  memset(&ds, 0, sizeof ds);
+  for (int b = 0; b < cfg.n_bands; b++) {
+    ds.a0[b] = split(sc.a0[b]);
+    ds.a1[b] = split(sc.a1[b]);
+    ds.aw[b] = split(sc.aw[b]);
+    ds.bbw[b] = split(sc.bbw[b]);
+    ds.refl[b] = split(sc.refl[b]);
+    ds.eS[b] = split(sc.eS[b]);
+    ds.ln_ratio440[b] = split(log(sc.ratio440[b]));
+  }
+  ds.sec_sun = split(sc.sec_sun);
+  ds.sec_view = split(sc.sec_view);
+  for (int t = 0; t < kNRefTargets; t++) {
+    ds.plan_t[t] = split(fp.plan[t].t);
+    ds.plan_omt[t] = split(fp.plan[t].one_minus_t);
+  }
+  ds.x_start_coef = split(100.0 * 30.0 * fp.aw640);
+  for (int i = 0; i < 5; i++) {
+    ds.k_thr[i] = split(fp.kp.k_thr[i]);
+    ds.inv_t[i] = split(fp.kp.inv_t[i]);
+  }
+  ds.reqmin_n = split(cfg.reqmin * (double)n_params);
+  for (int k = 0; k < cfg.n_hstarts; k++) ds.hstarts[k] = split(cfg.hstarts[k]);
+}
+
 // Sticky per-device error word the kernels OR their error bits into.
 std::mutex g_dev_mu;
 std::vector<unsigned int *> g_dev_err;
@@ -275,7 +310,7 @@ int photic_invert_batch(const photic_config *cfg, const float *d_rrs, int64_t np
   if (!d_rrs || !out) return fail(PHOTIC_ERR_INVALID, "NULL input or output");
   if (pixel_stride < 1 || band_stride < 1)
     return fail(PHOTIC_ERR_INVALID, "strides must be >= 1");
-  if (cfg->precision != PHOTIC_PREC_FP64)
+  if (cfg->precision == PHOTIC_PREC_FP32)
     return fail(PHOTIC_ERR_UNSUPPORTED, "precision %d not built in this version", cfg->precision);
   cudaStream_t s = (cudaStream_t)stream;
   unsigned int *err = nullptr;
@@ -287,6 +322,7 @@ int photic_invert_batch(const photic_config *cfg, const float *d_rrs, int64_t np
   memset(&a, 0, sizeof a);
   make_fit(*cfg, a.fp);
   make_scene(*cfg, cfg->theta_sun_deg, a.sc);
+  make_df(*cfg, a.fp, a.sc, 6, a.ds);
   a.rrs = d_rrs;
   a.npix = npix;
   a.pixel_stride = pixel_stride;
@@ -301,7 +337,7 @@ int photic_invert_batch(const photic_config *cfg, const float *d_rrs, int64_t np
   const int block = cfg->block_threads ? cfg->block_threads : 128;
   int per_sm = cfg->blocks_per_sm;
   if (per_sm == 0) {
-    per_sm = invert_f64_blocks_per_sm(cfg->n_bands, block);
+    per_sm = invert_blocks_per_sm(a, cfg->precision, block);
     if (per_sm < 1) return fail(PHOTIC_ERR_CUDA, "kernel does not fit on the device");
   }
   int64_t grid = (int64_t)sms * per_sm;
@@ -314,7 +350,7 @@ int photic_invert_batch(const photic_config *cfg, const float *d_rrs, int64_t np
   e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
   a.queue = queue;
-  e = launch_invert_f64(a, block, (int)grid, s);
+  e = launch_invert(a, cfg->precision, block, (int)grid, s);
   cudaError_t e2 = cudaFreeAsync(queue, s);
   if (e != cudaSuccess) return cuda_fail(e, "invert kernel launch");
   if (e2 != cudaSuccess) return cuda_fail(e2, "cudaFreeAsync");
@@ -338,6 +374,8 @@ int photic_cost_batch(const photic_config *cfg, const float *d_rrs, const double
   memset(&a, 0, sizeof a);
   make_fit(*cfg, a.fp);
   make_scene(*cfg, cfg->theta_sun_deg, a.sc);
+  make_df(*cfg, a.fp, a.sc, 6, a.ds);
+  a.precision = cfg->precision;
   a.rrs = d_rrs;
   a.params = d_params;
   a.n = n;

@@ -18,6 +18,7 @@ enum : unsigned {
 struct InvertArgs {
   FitParams fp;
   SceneConsts sc;
+  DfScene ds;
   const float *rrs;
   int64_t npix, pixel_stride, band_stride;
   int32_t vec4;  // rrs is [npix][4], 16-byte aligned
@@ -28,9 +29,11 @@ struct InvertArgs {
   double early_exit;  // early-exit cost threshold (per-scene value * scenes)
 };
 
-size_t smem_bytes_f64(int block, int nb);
-cudaError_t launch_invert_f64(const InvertArgs &a, int block, int grid, cudaStream_t s);
-int invert_f64_blocks_per_sm(int nb, int block);  // resident blocks per SM (0 on error)
+size_t invert_smem_bytes(int block, int nb);
+cudaError_t launch_invert(const InvertArgs &a, int precision, int block, int grid,
+                          cudaStream_t s);
+// Resident blocks per SM of the kernel that launch_invert would use (0 on error).
+int invert_blocks_per_sm(const InvertArgs &a, int precision, int block);
 
 struct GenArgs {
   FitParams fp;
@@ -46,6 +49,8 @@ cudaError_t launch_generate(const GenArgs &a, cudaStream_t s);
 struct CostArgs {
   FitParams fp;
   SceneConsts sc;
+  DfScene ds;
+  int32_t precision;
   const float *rrs;
   const double *params;
   int64_t n;

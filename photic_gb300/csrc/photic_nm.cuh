@@ -4,14 +4,16 @@
 // around calls of the cost function.  On the GPU each lane runs its own
 // pixel, and lanes must reach the cost evaluation together to keep the
 // warp converged where the work is.  So the method is restated as a state
-// machine: advance() consumes the cost of the point it last asked for and
+// machine: step() consumes the cost of the point it last asked for and
 // runs the bookkeeping up to the next point it needs, which it leaves in
 // x[].  The sequence of points, comparisons and counters is the
 // reference's; only the control flow is turned inside out.
 //
 // Vertices and vertex costs live in shared memory ([slot][thread], so a
-// warp's accesses are conflict-free); the vectors indexed with
-// compile-time indices live in registers.
+// warp's accesses are conflict-free); vectors indexed only with
+// compile-time indices live in registers.  The arithmetic type comes from
+// the precision policy P (PrecF64: IEEE double in the reference's order;
+// PrecDF: double-float on the FP32 pipes).
 #pragma once
 #include <stdint.h>
 
@@ -28,60 +30,45 @@ enum NmPhase : int32_t {
   PH_PROBE_PLUS,      // local-minimum probe xmin[i] + del
   PH_PROBE_MINUS,     // local-minimum probe xmin[i] - del
   PH_FINAL,           // re-evaluation at the kept optimum
-  PH_DONE
 };
 
-// Arithmetic hooks of the machine: T is the vertex/cost type.
-template <class T>
-struct NmOps;
-
-template <>
-struct NmOps<double> {
-  static __device__ __forceinline__ double half() { return 0.5; }
-  static __device__ __forceinline__ double two() { return 2.0; }
-};
-
-template <int N, class T, int BS>
+template <int N, class P, int BS>
 struct NmLane {
-  // shared-memory views: v[(j * N + i) * BS + tid], f[j * BS + tid]
-  T *v, *f;
-  // registers
-  T x[N];                          // point to evaluate next
+  using T = typename P::T;
+  T *v, *f;  // shared: v[(j * N + i) * BS + tid], f[j * BS + tid]
+  T x[N];    // point to evaluate next
   T cen[N], refl[N], trial[N], xmin[N], start[N], step[N];
-  T ylo, fr, scale;
+  T ylo, fr, scale, var_limit;
   long long floor_lo;
   int32_t phase, jj, hi, lo, icount, numres, ifault, countdown;
   int32_t kcount, konvge;
-  T var_limit;
 
   __device__ __forceinline__ T &V(int j, int i) { return v[(j * N + i) * BS]; }
   __device__ __forceinline__ T &F(int j) { return f[j * BS]; }
 
-  template <class A>
-  static __device__ __forceinline__ T pick(const A &a, int k) {
+  static __device__ __forceinline__ T pick(const T (&a)[N], int k) {
     T r = a[0];
 #pragma unroll
     for (int i = 1; i < N; i++)
       if (i == k) r = a[i];
     return r;
   }
-  template <class A>
-  static __device__ __forceinline__ void put(A &a, int k, T val) {
+  static __device__ __forceinline__ void put(T (&a)[N], int k, T val) {
 #pragma unroll
     for (int i = 0; i < N; i++)
       if (i == k) a[i] = val;
   }
 
   // Begin a nelmin call from start[]/step[] (model/asa047.c:161-170).
-  __device__ __forceinline__ void begin(T reqmin, int32_t konvge_, int32_t kcount_) {
+  __device__ __forceinline__ void begin(T var_limit_, int32_t konvge_, int32_t kcount_) {
     konvge = konvge_;
     kcount = kcount_;
     countdown = konvge_;
     icount = 0;
     numres = 0;
     ifault = 0;
-    scale = T(1.0);
-    var_limit = reqmin * T((double)N);
+    scale = P::one();
+    var_limit = var_limit_;
     restart_simplex();
   }
 
@@ -100,7 +87,7 @@ struct NmLane {
 #pragma unroll
     for (int i = 0; i < N; i++) {
       T s = start[i];
-      if (i == j) s = start[i] + step[i] * scale;
+      if (i == j) s = P::add(start[i], P::mul(step[i], scale));
       x[i] = s;
       V(j, i) = s;
     }
@@ -114,7 +101,7 @@ struct NmLane {
 #pragma unroll
     for (int j = 1; j <= N; j++) {
       T fj = F(j);
-      if (fj < ylo) {
+      if (P::lt(fj, ylo)) {
         ylo = fj;
         lo = j;
       }
@@ -122,8 +109,7 @@ struct NmLane {
   }
 
   // Top of the inner loop (model/asa047.c:213-250): budget check, worst
-  // vertex, centroid of the others, reflection.  Returns false when the
-  // inner loop ends instead.
+  // vertex, centroid of the others, reflection.  false: the loop ends.
   __device__ __forceinline__ bool inner_top() {
     if (kcount <= icount) return false;
     T yhi = F(0);
@@ -131,39 +117,39 @@ struct NmLane {
 #pragma unroll
     for (int j = 1; j <= N; j++) {
       T fj = F(j);
-      if (yhi < fj) {
+      if (P::lt(yhi, fj)) {
         yhi = fj;
         hi = j;
       }
     }
 #pragma unroll
     for (int i = 0; i < N; i++) {
-      T z = T(0.0);
+      T z = P::zero();
 #pragma unroll
-      for (int j = 0; j <= N; j++) z = z + V(j, i);
-      z = z - V(hi, i);
-      cen[i] = z / T((double)N);
+      for (int j = 0; j <= N; j++) z = P::add(z, V(j, i));
+      z = P::sub(z, V(hi, i));
+      cen[i] = P::div_n(z, N);
     }
 #pragma unroll
     for (int i = 0; i < N; i++) {
-      refl[i] = cen[i] + (cen[i] - V(hi, i));
+      refl[i] = P::add(cen[i], P::sub(cen[i], V(hi, i)));
       x[i] = refl[i];
     }
     phase = PH_REFLECT;
     return true;
   }
 
-  __device__ __forceinline__ void replace_hi(const T *p, T y) {
+  __device__ __forceinline__ void replace_hi(const T (&p)[N], T y) {
 #pragma unroll
     for (int i = 0; i < N; i++) V(hi, i) = p[i];
     F(hi) = y;
   }
 
-  // End of an iteration (model/asa047.c:395-434).  Returns true when the
-  // variance test ends the inner loop.
+  // End of an iteration (model/asa047.c:395-434).  true: the variance test
+  // ends the inner loop.
   __device__ __forceinline__ bool iteration_end() {
     T fh = F(hi);
-    if (fh < ylo) {
+    if (P::lt(fh, ylo)) {
       ylo = fh;
       lo = hi;
     }
@@ -171,17 +157,204 @@ struct NmLane {
     if (countdown > 0) return false;
     if (icount <= kcount) {
       countdown = konvge;
-      T z = T(0.0);
+      T z = P::zero();
 #pragma unroll
-      for (int j = 0; j <= N; j++) z = z + F(j);
-      T mean = z / T((double)(N + 1));
-      z = T(0.0);
+      for (int j = 0; j <= N; j++) z = P::add(z, F(j));
+      T mean = P::div_n(z, N + 1);
+      z = P::zero();
 #pragma unroll
       for (int j = 0; j <= N; j++) {
-        T d = F(j) - mean;
-        z = z + d * d;
+        T d = P::sub(F(j), mean);
+        z = P::add(z, P::mul(d, d));
       }
-      if (z <= var_limit) return true;
+      if (P::le(z, var_limit)) return true;
+    }
+    return false;
+  }
+
+  // Consume the cost y of x[] and advance to the next point.  Returns true
+  // when the nelmin call has returned (xmin, F(lo), icount, numres, ifault
+  // hold its results); the caller then starts another call or finishes.
+  __device__ __forceinline__ bool step_machine(T y) {
+    enum { CS_NONE = -1, CS_READY, CS_TOP, CS_ITER_END, CS_END_INNER, CS_PROBE_PLUS,
+           CS_PROBE_END, CS_NM_DONE };
+    int cs = CS_NONE;
+    switch (phase) {
+      case PH_INIT_BASE:
+        F(N) = y;
+        icount++;
+        make_vertex(0);
+        break;
+      case PH_INIT_VERT:
+        F(jj) = y;
+        icount++;
+        if (jj + 1 < N) make_vertex(jj + 1);
+        else cs = CS_READY;
+        break;
+      case PH_REFLECT:
+        fr = y;
+        icount++;
+        if (P::lt(fr, ylo)) {
+#pragma unroll
+          for (int i = 0; i < N; i++) {
+            trial[i] = P::add(cen[i], P::mul2(P::sub(refl[i], cen[i])));
+            x[i] = trial[i];
+          }
+          phase = PH_EXPAND;
+        } else {
+          int worse = 0;
+#pragma unroll
+          for (int j = 0; j <= N; j++)
+            if (P::lt(fr, F(j))) worse++;
+          if (worse > 1) {
+            replace_hi(refl, fr);
+            cs = CS_ITER_END;
+          } else if (worse == 0) {
+#pragma unroll
+            for (int i = 0; i < N; i++) {
+              trial[i] = P::add(cen[i], P::half(P::sub(V(hi, i), cen[i])));
+              x[i] = trial[i];
+            }
+            phase = PH_CONTRACT_IN;
+          } else {
+#pragma unroll
+            for (int i = 0; i < N; i++) {
+              trial[i] = P::add(cen[i], P::half(P::sub(refl[i], cen[i])));
+              x[i] = trial[i];
+            }
+            phase = PH_CONTRACT_OUT;
+          }
+        }
+        break;
+      case PH_EXPAND:
+        icount++;
+        if (P::lt(fr, y)) replace_hi(refl, fr);
+        else replace_hi(trial, y);
+        cs = CS_ITER_END;
+        break;
+      case PH_CONTRACT_IN:
+        icount++;
+        if (P::lt(F(hi), y)) {
+          // shrink every vertex towards the best (model/asa047.c:331-351)
+#pragma unroll
+          for (int i = 0; i < N; i++) {
+            T s = P::half(P::add(V(0, i), V(lo, i)));
+            V(0, i) = s;
+            x[i] = s;
+          }
+          jj = 0;
+          phase = PH_SHRINK;
+        } else {
+          replace_hi(trial, y);
+          cs = CS_ITER_END;
+        }
+        break;
+      case PH_SHRINK:
+        F(jj) = y;
+        icount++;
+        if (jj < N) {
+          const int j = jj + 1;
+#pragma unroll
+          for (int i = 0; i < N; i++) {
+            T s = P::half(P::add(V(j, i), V(lo, i)));
+            V(j, i) = s;
+            x[i] = s;
+          }
+          jj = j;
+        } else {
+          cs = CS_READY;
+        }
+        break;
+      case PH_CONTRACT_OUT:
+        icount++;
+        if (P::le(y, fr)) replace_hi(trial, y);
+        else replace_hi(refl, fr);
+        cs = CS_ITER_END;
+        break;
+      case PH_PROBE_PLUS: {
+        icount++;
+        if (P::trunc10(y) < floor_lo) {
+          ifault = 2;
+          cs = CS_PROBE_END;
+        } else {
+          const T del = P::eps_step(pick(step, jj));
+          put(xmin, jj, P::sub(P::sub(pick(xmin, jj), del), del));
+#pragma unroll
+          for (int i = 0; i < N; i++) x[i] = xmin[i];
+          phase = PH_PROBE_MINUS;
+        }
+        break;
+      }
+      case PH_PROBE_MINUS: {
+        icount++;
+        if (P::trunc10(y) < floor_lo) {
+          ifault = 2;
+          cs = CS_PROBE_END;
+        } else {
+          const T del = P::eps_step(pick(step, jj));
+          put(xmin, jj, P::add(pick(xmin, jj), del));
+          jj++;
+          cs = (jj < N) ? CS_PROBE_PLUS : CS_PROBE_END;
+        }
+        break;
+      }
+      default:
+        break;
+    }
+    // Bookkeeping until the next point to evaluate.
+    while (cs != CS_NONE) {
+      switch (cs) {
+        case CS_READY:
+          find_lo();
+          cs = CS_TOP;
+          break;
+        case CS_TOP:
+          cs = inner_top() ? CS_NONE : CS_END_INNER;
+          break;
+        case CS_ITER_END:
+          cs = iteration_end() ? CS_END_INNER : CS_TOP;
+          break;
+        case CS_END_INNER:
+#pragma unroll
+          for (int i = 0; i < N; i++) xmin[i] = V(lo, i);
+          floor_lo = P::trunc10(F(lo));
+          if (kcount < icount) {
+            ifault = 2;
+            cs = CS_NM_DONE;
+          } else {
+            ifault = 0;
+            jj = 0;
+            cs = CS_PROBE_PLUS;
+          }
+          break;
+        case CS_PROBE_PLUS: {
+          const T del = P::eps_step(pick(step, jj));
+          put(xmin, jj, P::add(pick(xmin, jj), del));
+#pragma unroll
+          for (int i = 0; i < N; i++) x[i] = xmin[i];
+          phase = PH_PROBE_PLUS;
+          cs = CS_NONE;
+          break;
+        }
+        case CS_PROBE_END:
+          if (ifault == 0) {
+            cs = CS_NM_DONE;
+          } else {
+            // restart from the probe point with a 1e-6 simplex
+#pragma unroll
+            for (int i = 0; i < N; i++) start[i] = xmin[i];
+            scale = P::eps_scale();
+            numres++;
+            restart_simplex();
+            cs = CS_NONE;
+          }
+          break;
+        case CS_NM_DONE:
+          return true;
+        default:
+          cs = CS_NONE;
+          break;
+      }
     }
     return false;
   }

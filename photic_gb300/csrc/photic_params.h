@@ -40,6 +40,26 @@ struct KPenalty {
   double inv_t[5];    // 1.0 / (0.01 + target)
 };
 
+// A double split into two floats (hi = fl(d), lo = fl(d - hi)), the
+// host-side form of the device's double-float constants.
+struct DfPair {
+  float hi, lo;
+};
+
+// Double-float copies of the constants the cost needs (filled on the host
+// from the double-precision SceneConsts / FitParams).
+struct DfScene {
+  DfPair a0[kMaxBands], a1[kMaxBands], aw[kMaxBands], bbw[kMaxBands];
+  DfPair refl[kMaxBands], eS[kMaxBands];
+  DfPair ln_ratio440[kMaxBands];  // log(440 / lambda)
+  DfPair sec_sun, sec_view;
+  DfPair plan_t[kNRefTargets], plan_omt[kNRefTargets];
+  DfPair x_start_coef;            // 100 * 30 * a_w(640)
+  DfPair k_thr[5], inv_t[5];
+  DfPair reqmin_n;                // reqmin * n
+  DfPair hstarts[kMaxHStarts];
+};
+
 struct FitParams {
   int32_t n_bands;
   int32_t kcount, konvge;
