@@ -122,6 +122,30 @@ int photic_invert_batch(const photic_config *cfg, const float *d_rrs, int64_t np
                         int64_t pixel_stride, int64_t band_stride, const double *d_seeds,
                         const photic_outputs *out, void *stream);
 
+/* Size of the static scratch array behind photic_invert_batch_noalloc. */
+#define PHOTIC_NOALLOC_SCRATCH_BYTES 256
+
+/* photic_invert_batch for callers that cannot allocate device memory.  No
+ * counterpart in the reference.  Callers such as a serving process that
+ * hands all of HBM to its own pool allocator at start-up, or a host
+ * application that forbids allocation once its pipeline is running
+ * (cudaMalloc can block on the device and breaks its memory accounting),
+ * need an inversion that takes only the inputs and outputs they pass in.
+ * This call allocates nothing: its 16 bytes of scratch (work-queue head and
+ * error word) live in a static device array of PHOTIC_NOALLOC_SCRATCH_BYTES
+ * that every GPU loading the library holds until the process exits.  The
+ * first call on a device looks up that array's address (and lets CUDA load
+ * the library's kernels), so make it before any stream capture.  All calls
+ * share the one array and each clears it before its launch, so calls whose
+ * kernels overlap on the GPU (two streams at once) race: serialise them.
+ * Kernel-detected errors show in the per-pixel status (PHOTIC_PX_INVALID);
+ * photic_sync() does not see them.  Arguments and results are those of
+ * photic_invert_batch. */
+int photic_invert_batch_noalloc(const photic_config *cfg, const float *d_rrs, int64_t npix,
+                                int64_t pixel_stride, int64_t band_stride,
+                                const double *d_seeds, const photic_outputs *out,
+                                void *stream);
+
 /* Temporal joint fit: pixel p owns observations d_offsets[p] ..
  * d_offsets[p+1]-1 (CSR, int32, device); observation o has spectrum
  * d_rrs[o * n_bands .. +n_bands) and subsurface sun zenith

@@ -78,6 +78,9 @@ _SIGS = {
     "photic_invert_batch": (C.c_int, [C.POINTER(photic_config), C.c_void_p, C.c_int64,
                                       C.c_int64, C.c_int64, C.c_void_p,
                                       C.POINTER(photic_outputs), C.c_void_p]),
+    "photic_invert_batch_noalloc": (C.c_int, [C.POINTER(photic_config), C.c_void_p, C.c_int64,
+                                              C.c_int64, C.c_int64, C.c_void_p,
+                                              C.POINTER(photic_outputs), C.c_void_p]),
     "photic_joint_invert_batch": (C.c_int, [C.POINTER(photic_config), C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_int64, C.c_int64,
                                             C.POINTER(photic_outputs), C.c_void_p]),

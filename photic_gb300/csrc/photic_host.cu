@@ -450,3 +450,109 @@ int photic_sync(void *stream) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// photic_invert_batch_noalloc: the plain-method inversion for callers that
+// must not allocate device memory.
+//
+// Its only scratch -- the 8-byte work-queue head and a 4-byte error word --
+// lives in this file-scope array instead of a per-call allocation.  The
+// array is part of the library's device image: every GPU that loads the
+// library holds PHOTIC_NOALLOC_SCRATCH_BYTES of it until the process exits.
+// Host code cannot use the array's name as a device address, so the address
+// is looked up with cudaGetSymbolAddress once per device, on the first call
+// made with that device current.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) unsigned long long
+    g_noalloc_scratch[PHOTIC_NOALLOC_SCRATCH_BYTES / sizeof(unsigned long long)];
+
+namespace {
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned long long *g_noalloc_ptr[kNoAllocMaxDevices];
+int g_noalloc_sms[kNoAllocMaxDevices];
+
+// Device address of the scratch array and SM count of the current device.
+int noalloc_setup(unsigned long long **ptr, int *sms) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kNoAllocMaxDevices)
+    return fail(PHOTIC_ERR_UNSUPPORTED, "device %d beyond the %d supported", dev, kNoAllocMaxDevices);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    unsigned long long *p = nullptr;
+    e = cudaGetSymbolAddress((void **)&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(noalloc scratch)");
+    int n = 0;
+    e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+    g_noalloc_sms[dev] = n;
+    g_noalloc_ptr[dev] = p;
+  }
+  *ptr = g_noalloc_ptr[dev];
+  *sms = g_noalloc_sms[dev];
+  return PHOTIC_OK;
+}
+
+}  // namespace
+
+extern "C" int photic_invert_batch_noalloc(const photic_config *cfg, const float *d_rrs,
+                                           int64_t npix, int64_t pixel_stride,
+                                           int64_t band_stride, const double *d_seeds,
+                                           const photic_outputs *out, void *stream) {
+  int rc = photic_config_check(cfg);
+  if (rc) return rc;
+  if (npix < 0) return fail(PHOTIC_ERR_INVALID, "npix < 0");
+  if (npix == 0) return PHOTIC_OK;
+  if (!d_rrs || !out) return fail(PHOTIC_ERR_INVALID, "NULL input or output");
+  if (pixel_stride < 1 || band_stride < 1)
+    return fail(PHOTIC_ERR_INVALID, "strides must be >= 1");
+  if (cfg->precision == PHOTIC_PREC_FP32)
+    return fail(PHOTIC_ERR_UNSUPPORTED, "precision %d not built in this version", cfg->precision);
+  // queue head (8 bytes) + error word (4 bytes, padded to 8)
+  const size_t needed = 2 * sizeof(unsigned long long);
+  if (needed > (size_t)PHOTIC_NOALLOC_SCRATCH_BYTES)
+    return fail(PHOTIC_ERR_INVALID, "needs %zu bytes of scratch, the static array holds %d",
+                needed, PHOTIC_NOALLOC_SCRATCH_BYTES);
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned long long *scratch = nullptr;
+  int sms = 0;
+  rc = noalloc_setup(&scratch, &sms);
+  if (rc) return rc;
+
+  InvertArgs a;
+  memset(&a, 0, sizeof a);
+  make_fit(*cfg, a.fp);
+  make_scene(*cfg, cfg->theta_sun_deg, a.sc);
+  make_df(*cfg, a.fp, a.sc, 6, a.ds);
+  a.rrs = d_rrs;
+  a.npix = npix;
+  a.pixel_stride = pixel_stride;
+  a.band_stride = band_stride;
+  a.vec4 = (cfg->n_bands == 4 && pixel_stride == 4 && band_stride == 1 &&
+            ((uintptr_t)d_rrs & 15u) == 0);
+  a.seeds = d_seeds;
+  a.out = *out;
+  a.queue = scratch;
+  a.error = reinterpret_cast<unsigned int *>(scratch + 1);
+  a.early_exit = cfg->early_exit_per_scene * (double)(float)1;
+
+  const int block = cfg->block_threads ? cfg->block_threads : 128;
+  int per_sm = cfg->blocks_per_sm;
+  if (per_sm == 0) {
+    per_sm = invert_blocks_per_sm(a, cfg->precision, block);
+    if (per_sm < 1) return fail(PHOTIC_ERR_CUDA, "kernel does not fit on the device");
+  }
+  int64_t grid = (int64_t)sms * per_sm;
+  const int64_t need = (npix + block - 1) / block;
+  if (grid > need) grid = need;
+
+  // The previous call left its final queue position and error bits here.
+  cudaError_t e = cudaMemsetAsync(scratch, 0, needed, s);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(noalloc scratch)");
+  e = launch_invert(a, cfg->precision, block, (int)grid, s);
+  if (e != cudaSuccess) return cuda_fail(e, "invert kernel launch");
+  return PHOTIC_OK;
+}
