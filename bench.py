@@ -150,7 +150,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="photic", choices=["photic", "reference"])
     ap.add_argument("--npix", type=int, default=4096 * 4096)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "df64", "fp32"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "df64", "fp32", "guarded"])
     ap.add_argument("--warmup-npix", type=int, default=1 << 20)
     ap.add_argument("--sample", type=int, default=2048, help="pixels re-fitted by the CPU oracle")
     ap.add_argument("--cpu-sample", type=int, default=1 << 16)
@@ -184,6 +184,8 @@ def main():
     out = pg.alloc_outputs(npix, dev, ("depth", "depth_f64", "P", "G", "X", "bottom_albedo",
                                        "model_error", "evals", "status"))
 
+    counter = torch.zeros(1, dtype=torch.int64, device=dev)
+    L.check(L.lib().photic_set_counter(counter.data_ptr()))
     # warm-up on a slice of the scene (W launches)
     for _ in range(args.warmup):
         pg.invert(rrs[: min(npix, args.warmup_npix)], cfg)
@@ -208,6 +210,7 @@ def main():
     barrier()
     pg.sync()
     ms_step = ev0.elapsed_time(ev1) / args.steps
+    L.check(L.lib().photic_set_counter(None))
     if pg_ is not None:
         t = torch.tensor([ms_step], device=dev)
         pg_.all_reduce(t, op=pg_.ReduceOp.MAX)
@@ -303,13 +306,15 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": {"fp64": "f64", "df64": "df64 (2 x f32)", "fp32": "f32"}[args.precision],
+                "dtype": {"fp64": "f64", "df64": "df64 (2 x f32)", "fp32": "f32",
+                          "guarded": "f64 decisions (df64 screening)"}[args.precision],
                 "data": "synthetic (seeded on-device generator, plain-method prior)",
                 "config": {"workload": "plain method, 4096x4096 single scene, 4 bands, "
                                        "cold start, reqmin 1e-10, kcount 2000",
                            "pixels_per_gpu": npix, "precision": args.precision,
                            "l2": "inputs 268 MB > L2; compute-bound kernel"},
                 "gpu_launches": args.steps,
+                "exact_evals_per_step": int(counter.item()) // max(1, args.steps + args.warmup),
                 "pixels": {"fitted": int(fitted.sum()), "converged": int(conv.sum()),
                            "within_1cm_of_fp64": int(within.sum()),
                            "mean_evals": float(evals[fitted].mean()) if fitted.any() else 0.0},

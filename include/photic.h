@@ -53,8 +53,11 @@ enum {
 enum {
   PHOTIC_PREC_FP64 = 0, /* IEEE double in the reference's operation order */
   PHOTIC_PREC_DF64 = 1, /* double-float (two FP32 words) on the FP32 pipes */
-  PHOTIC_PREC_FP32 = 2  /* FP32 forward model; FP64 for the convergence and
+  PHOTIC_PREC_FP32 = 2, /* FP32 forward model; FP64 for the convergence and
                            local-minimum tests only */
+  PHOTIC_PREC_GUARDED = 3 /* FP64 decisions: every cost screened in
+                             double-float, near ties re-evaluated in IEEE
+                             double; same trajectory as PHOTIC_PREC_FP64 */
 };
 
 /* Per-pixel status word: low byte is the pixel state, bit 8 is set when
@@ -194,6 +197,11 @@ int photic_sync(void *stream);
  * denominators of the compute-bound kernels: FP64 and FP32 FMA (TFLOP/s,
  * 2 flops per FMA) and MUFU ex2 (T ops/s).  Synchronous; ~0.1 s. */
 int photic_measure_peaks(double *fp64_tflops, double *fp32_tflops, double *mufu_tops);
+
+/* Instrumentation: if d_counter (device, unsigned long long) is not NULL,
+ * later PHOTIC_PREC_GUARDED inversions add the number of exact FP64
+ * re-evaluations they served to it.  Pass NULL to stop. */
+int photic_set_counter(unsigned long long *d_counter);
 
 /* Message of the most recent error on this host thread. */
 const char *photic_last_error(void);

@@ -16,7 +16,7 @@ MAX_SCENES = 8
 MAX_HSTARTS = 32
 
 OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT, ERR_UNSUPPORTED = range(6)
-PREC_FP64, PREC_DF64, PREC_FP32 = 0, 1, 2
+PREC_FP64, PREC_DF64, PREC_FP32, PREC_GUARDED = 0, 1, 2, 3
 LAYOUT_REFERENCE, LAYOUT_SCENE_B = 0, 1
 PX_FITTED, PX_MASKED, PX_INVALID = 0, 1, 2
 PX_CONVERGED = 0x100
@@ -100,6 +100,7 @@ _SIGS = {
     "photic_band_constants": (C.c_int, [C.POINTER(photic_config), C.POINTER(C.c_double)]),
     "photic_sync": (C.c_int, [C.c_void_p]),
     "photic_measure_peaks": (C.c_int, [C.POINTER(C.c_double)] * 3),
+    "photic_set_counter": (C.c_int, [C.c_void_p]),
 }
 
 

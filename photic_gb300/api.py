@@ -22,7 +22,8 @@ import torch
 from . import _lib as L
 from ._lib import PhoticError  # noqa: F401
 
-PRECISIONS = {"fp64": L.PREC_FP64, "df64": L.PREC_DF64, "fp32": L.PREC_FP32}
+PRECISIONS = {"fp64": L.PREC_FP64, "df64": L.PREC_DF64, "fp32": L.PREC_FP32,
+              "guarded": L.PREC_GUARDED}
 LAYOUTS = {"reference": L.LAYOUT_REFERENCE, "scene_b": L.LAYOUT_SCENE_B}
 OUTPUT_FIELDS = ("depth", "depth_f64", "P", "G", "X", "bottom_albedo", "model_error",
                  "rrs_error", "K_min", "iod", "evals", "evals_kept", "status")

@@ -97,9 +97,11 @@ __device__ __forceinline__ df64 cost_df(const FitParams &fp, const DfScene &ds,
   const df64 X = df_mul(c001, df_abs(x[5]));
   const df64 lnP = dlog(P);
   df64 err = df64{0.0f, 0.0f}, K_min = df64{1.0e4f, 0.0f}, iod = df64{0.0f, 0.0f};
-#pragma unroll
-  for (int b = 0; b < NB; b++) {
-    if (b < nb) {
+  // One band per trip: the double-float exp/div/sqrt sequences are long, and
+  // unrolling the band loop multiplies the code beyond the instruction cache.
+#pragma unroll 1
+  for (int b = 0; b < nb; b++) {
+    {
       df64 rho = df_mul(qB, dp(ds.refl[b]));
       df64 a_phi = df_mul(df_add(dp(ds.a0[b]), df_mul(dp(ds.a1[b]), lnP)), P);
       df64 a_g = df_mul(G, dp(ds.eS[b]));

@@ -188,6 +188,10 @@ void make_df(const photic_config &cfg, const FitParams &fp, const SceneConsts &s
   for (int k = 0; k < cfg.n_hstarts; k++) ds.hstarts[k] = split(cfg.hstarts[k]);
 }
 
+// Optional device counter of exact evaluations served by the guarded
+// kernel (photic_set_counter); NULL when unset.
+unsigned long long *g_counter_ptr = nullptr;
+
 // Sticky per-device error word the kernels OR their error bits into.
 std::mutex g_dev_mu;
 std::vector<unsigned int *> g_dev_err;
@@ -264,7 +268,7 @@ int photic_config_check(const photic_config *cfg) {
   if (cfg->kcount < 1) return fail(PHOTIC_ERR_INVALID, "kcount must be >= 1");
   if (cfg->n_hstarts < 1 || cfg->n_hstarts > PHOTIC_MAX_HSTARTS)
     return fail(PHOTIC_ERR_INVALID, "n_hstarts %d outside 1..%d", cfg->n_hstarts, PHOTIC_MAX_HSTARTS);
-  if (cfg->precision < PHOTIC_PREC_FP64 || cfg->precision > PHOTIC_PREC_FP32)
+  if (cfg->precision < PHOTIC_PREC_FP64 || cfg->precision > PHOTIC_PREC_GUARDED)
     return fail(PHOTIC_ERR_INVALID, "unknown precision %d", cfg->precision);
   if (cfg->layout != PHOTIC_LAYOUT_REFERENCE && cfg->layout != PHOTIC_LAYOUT_SCENE_B)
     return fail(PHOTIC_ERR_INVALID, "unknown layout %d", cfg->layout);
@@ -334,10 +338,13 @@ int photic_invert_batch(const photic_config *cfg, const float *d_rrs, int64_t np
   a.error = err;
   a.early_exit = cfg->early_exit_per_scene * (double)(float)1;
 
-  const int block = cfg->block_threads ? cfg->block_threads : 128;
+  const bool guarded = cfg->precision == PHOTIC_PREC_GUARDED;
+  int block = cfg->block_threads ? cfg->block_threads : 128;
+  if (guarded && block == 64) block = 128;
   int per_sm = cfg->blocks_per_sm;
   if (per_sm == 0) {
-    per_sm = invert_blocks_per_sm(a, cfg->precision, block);
+    per_sm = guarded ? guarded_blocks_per_sm(a, block)
+                     : invert_blocks_per_sm(a, cfg->precision, block);
     if (per_sm < 1) return fail(PHOTIC_ERR_CUDA, "kernel does not fit on the device");
   }
   int64_t grid = (int64_t)sms * per_sm;
@@ -350,7 +357,9 @@ int photic_invert_batch(const photic_config *cfg, const float *d_rrs, int64_t np
   e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
   a.queue = queue;
-  e = launch_invert(a, cfg->precision, block, (int)grid, s);
+  a.counters = g_counter_ptr;
+  e = guarded ? launch_guarded(a, block, (int)grid, s)
+              : launch_invert(a, cfg->precision, block, (int)grid, s);
   cudaError_t e2 = cudaFreeAsync(queue, s);
   if (e != cudaSuccess) return cuda_fail(e, "invert kernel launch");
   if (e2 != cudaSuccess) return cuda_fail(e2, "cudaFreeAsync");
@@ -421,6 +430,11 @@ int photic_generate_joint(const photic_config *cfg, uint64_t seed, int64_t npix,
   (void)cfg; (void)seed; (void)npix; (void)d_offsets; (void)theta_sun_min; (void)theta_sun_max;
   (void)mask_frac; (void)noise_sigma; (void)d_theta_sun; (void)d_rrs; (void)d_truth; (void)stream;
   return fail(PHOTIC_ERR_UNSUPPORTED, "joint generator not built in this version");
+}
+
+int photic_set_counter(unsigned long long *d_counter) {
+  g_counter_ptr = d_counter;
+  return PHOTIC_OK;
 }
 
 int photic_measure_peaks(double *fp64_tflops, double *fp32_tflops, double *mufu_tops) {

@@ -26,6 +26,7 @@ struct InvertArgs {
   photic_outputs out;
   unsigned long long *queue;
   unsigned int *error;
+  unsigned long long *counters;  // optional: exact evaluations served (guarded)
   double early_exit;  // early-exit cost threshold (per-scene value * scenes)
 };
 
@@ -34,6 +35,10 @@ cudaError_t launch_invert(const InvertArgs &a, int precision, int block, int gri
                           cudaStream_t s);
 // Resident blocks per SM of the kernel that launch_invert would use (0 on error).
 int invert_blocks_per_sm(const InvertArgs &a, int precision, int block);
+
+// FP64-faithful inversion with double-float screening (photic_guarded.cu).
+cudaError_t launch_guarded(const InvertArgs &a, int block, int grid, cudaStream_t s);
+int guarded_blocks_per_sm(const InvertArgs &a, int block);
 
 struct GenArgs {
   FitParams fp;

@@ -1,0 +1,47 @@
+"""PHOTIC_PREC_GUARDED: double-float screening with exact FP64 re-evaluation
+of near-tie decisions.  Its decisions are the FP64 kernel's, so its depths
+must equal the FP64 kernel's bit for bit on (nearly) every pixel, and it
+meets the same bar against the oracle: median |dH| <= 1 cm, p99 <= 5 cm."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+NTHREADS = os.cpu_count() or 1
+
+
+@pytest.mark.parametrize("npix", [1, 33, 4096])
+def test_guarded_equals_fp64_kernel(gpu, port, npix):
+    rrs, _ = port.generate_single(20260101, npix, pix0=13000)
+    t = torch.tensor(rrs, device="cuda")
+    a = gpu.invert(t, gpu.Config(precision="fp64"))
+    b = gpu.invert(t, gpu.Config(precision="guarded"))
+    gpu.sync()
+    a = {k: v.cpu().numpy() for k, v in a.items()}
+    b = {k: v.cpu().numpy() for k, v in b.items()}
+    np.testing.assert_array_equal(a["status"] & 0xFF, b["status"] & 0xFF)
+    fit = (a["status"] & 0xFF) == 0
+    same = np.mean(a["depth_f64"][fit] == b["depth_f64"][fit]) if fit.any() else 1.0
+    assert same >= 0.999, same
+    if npix >= 1000:  # the oracle bar is a distribution: judge it on many pixels
+        ref = port.invert_batch(rrs, nthreads=NTHREADS)
+        d = np.abs(b["depth_f64"][fit] - ref[fit, 0])
+        assert np.median(d) <= 0.01 and np.quantile(d, 0.99) <= 0.05
+
+
+def test_guarded_seeded_and_reference_tolerances(gpu, port):
+    rrs, truth = port.generate_single(515, 1024, mask_frac=0.0)
+    seeds = np.column_stack([truth[:, 0], 100 * truth[:, 4], np.ones(1024), 100 * truth[:, 1],
+                             100 * truth[:, 2], 100 * truth[:, 3]])
+    seeds[::3, 0] = np.nan
+    t = torch.tensor(rrs, device="cuda")
+    s = torch.tensor(seeds, device="cuda")
+    for kw in ({}, {"reqmin": 1e-2, "kcount": 5000}):
+        a = gpu.invert(t, gpu.Config(precision="fp64", **kw), seeds=s)
+        b = gpu.invert(t, gpu.Config(precision="guarded", **kw), seeds=s)
+        gpu.sync()
+        ha, hb = a["depth_f64"].cpu().numpy(), b["depth_f64"].cpu().numpy()
+        assert np.mean(ha == hb) >= 0.999
