@@ -189,6 +189,62 @@ def generate_scene(npix: int, seed: int = 20260101, config: Optional[Config] = N
     return rrs, truth
 
 
+def joint_invert(offsets: torch.Tensor, theta_sun: torch.Tensor, rrs: torch.Tensor,
+                 config: Optional[Config] = None, *,
+                 out: Optional[Dict[str, torch.Tensor]] = None,
+                 fields: Sequence[str] = OUTPUT_FIELDS,
+                 stream: Optional[torch.cuda.Stream] = None) -> Dict[str, torch.Tensor]:
+    """Temporal joint fit (model/samodel.c:2463-2491 with n_scenes = k).
+
+    Pixel p owns observations offsets[p] .. offsets[p+1]-1 (int32 CSR);
+    observation o has spectrum rrs[o] (float32, [n_obs, n_bands]) and
+    subsurface sun zenith theta_sun[o] (float64, degrees).  Per-pixel
+    outputs are [npix]; P, G, X are per observation ([n_obs]).
+    ``config.layout`` selects shared (B, q) -- the reference's -- or
+    per-scene B ("scene_b")."""
+    cfg = config or Config()
+    _check_cuda(offsets, "offsets", torch.int32)
+    _check_cuda(theta_sun, "theta_sun", torch.float64)
+    _check_cuda(rrs, "rrs", torch.float32)
+    npix = offsets.numel() - 1
+    n_obs = rrs.shape[0]
+    if rrs.dim() != 2 or rrs.shape[1] != cfg.n_bands or theta_sun.numel() != n_obs:
+        raise ValueError("rrs must be [n_obs, n_bands] and theta_sun [n_obs]")
+    if out is None:
+        out = alloc_outputs(npix, rrs.device, fields, n_obs=n_obs)
+    c = cfg.to_c()
+    os_ = _outputs_struct(out)
+    L.check(L.lib().photic_joint_invert_batch(C.byref(c), _ptr(offsets), _ptr(theta_sun),
+                                              _ptr(rrs), npix, n_obs, C.byref(os_),
+                                              _stream_handle(stream)))
+    return out
+
+
+def generate_joint(npix: int, seed: int = 20260202, config: Optional[Config] = None, *,
+                   kmin: int = 2, kmax: int = 8, theta_sun_range=(25.0, 50.0),
+                   mask_frac: float = 0.0, noise_sigma: float = 2.0e-4, device="cuda",
+                   stream: Optional[torch.cuda.Stream] = None):
+    """Synthetic multi-scene stacks (temporal workload): per pixel k scenes
+    with k ~ U{kmin..kmax}, shared depth, per-scene P, G, X, B and sun
+    zenith.  Returns (offsets, theta_sun, rrs, truth)."""
+    cfg = config or Config()
+    h = _stream_handle(stream)
+    counts = torch.empty(npix, dtype=torch.int32, device=device)
+    L.check(L.lib().photic_joint_counts(seed, npix, kmin, kmax, _ptr(counts), h))
+    offsets = torch.zeros(npix + 1, dtype=torch.int32, device=device)
+    offsets[1:] = torch.cumsum(counts, 0, dtype=torch.int32)
+    n_obs = int(offsets[-1].item())
+    theta = torch.empty(n_obs, dtype=torch.float64, device=device)
+    rrs = torch.empty(n_obs, cfg.n_bands, dtype=torch.float32, device=device)
+    truth = torch.empty(n_obs, 5, dtype=torch.float64, device=device)
+    c = cfg.to_c()
+    L.check(L.lib().photic_generate_joint(C.byref(c), seed, npix, _ptr(offsets),
+                                          float(theta_sun_range[0]), float(theta_sun_range[1]),
+                                          mask_frac, noise_sigma, _ptr(theta), _ptr(rrs),
+                                          _ptr(truth), h))
+    return offsets, theta, rrs, truth
+
+
 def sync(stream: Optional[torch.cuda.Stream] = None) -> None:
     """Wait for ``stream`` and raise if the device recorded an error."""
     L.check(L.lib().photic_sync(_stream_handle(stream)))

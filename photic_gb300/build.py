@@ -20,7 +20,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libphotic_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["photic_host.cu", "photic_invert.cu", "photic_guarded.cu", "photic_aux.cu"]
+SOURCES = ["photic_host.cu", "photic_invert.cu", "photic_guarded.cu", "photic_joint.cu",
+           "photic_aux.cu"]
 
 
 def nvcc() -> str:

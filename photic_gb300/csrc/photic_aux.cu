@@ -104,6 +104,74 @@ __global__ void generate_kernel(GenArgs a) {
   }
 }
 
+__global__ void joint_counts_kernel(uint64_t seed, int64_t npix, int32_t kmin, int32_t kmax,
+                                    int32_t *counts) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npix) return;
+  double u[4];
+  draw4(seed, (uint64_t)p, 0u, 1u, u);
+  int k = kmin + (int)(u[0] * (double)(kmax - kmin + 1));
+  if (k > kmax) k = kmax;
+  counts[p] = k;
+}
+
+// Stack of k scenes over one pixel: shared depth, per-scene P, G, X, B and
+// sun zenith U(theta_min, theta_max), independent noise.  The first
+// observation carries the pixel's mask, as in the CPU generator.
+template <int NB>
+__global__ void generate_joint_kernel(const __grid_constant__ JointGenArgs a) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.npix) return;
+  const int nb = a.fp.n_bands;
+  const int o0 = a.offsets[p], k = a.offsets[p + 1] - o0;
+  double uH[4];
+  draw4(a.seed, (uint64_t)p, 1u, 1u, uH);
+  const double H = 0.5 + 24.5 * uH[0];
+  for (int s = 0; s < k; s++) {
+    const uint64_t obs = (uint64_t)(o0 + s);
+    double u0[4], u1[4];
+    draw4(a.seed, obs, 0u, 2u, u0);
+    draw4(a.seed, obs, 1u, 2u, u1);
+    const double P = log_uniform(u0[0], 0.005, 0.1);
+    const double G = log_uniform(u0[1], 0.005, 0.2);
+    const double X = log_uniform(u0[2], 0.001, 0.05);
+    const double B = 0.05 + 0.45 * u0[3];
+    const double th = a.theta_min + (a.theta_max - a.theta_min) * u1[0];
+    a.theta_sun[obs] = th;
+    SceneConsts sc = a.sc;
+    double t = th;
+    t *= 3.141592653589793 / 180.0;
+    sc.sec_sun = 1.0 / cos(t);
+    double r[NB];
+    synthesise<NB>(a.fp, sc, H, P, G, X, B, r);
+    for (int b = 0; b < nb; b += 2) {
+      double u[4];
+      draw4(a.seed, obs, 2u + (uint32_t)(b / 4), 2u, u);
+      const double rad = sqrt(-2.0 * log(u[b % 4]));
+      const double ang = 2.0 * kPi * u[(b % 4) + 1];
+      r[b] += a.noise_sigma * rad * cos(ang);
+      if (b + 1 < nb) r[b + 1] += a.noise_sigma * rad * sin(ang);
+    }
+    float *out = a.rrs + obs * nb;
+    for (int b = 0; b < nb; b++) out[b] = (float)r[b];
+    if (s == 0 && uH[1] < a.mask_frac) {
+      if (uH[2] < 0.5) {
+        for (int b = 0; b < nb; b++) out[b] = a.fp.nodata;
+      } else {
+        out[nb - 1] = -fabsf(out[nb - 1]) - 1.0e-3f;
+      }
+    }
+    if (a.truth) {
+      double *tr = a.truth + obs * 5;
+      tr[0] = H;
+      tr[1] = P;
+      tr[2] = G;
+      tr[3] = X;
+      tr[4] = B;
+    }
+  }
+}
+
 template <int NB>
 __global__ void cost_kernel_df(const __grid_constant__ CostArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -148,6 +216,22 @@ cudaError_t launch_generate(const GenArgs &a, cudaStream_t s) {
   const int64_t grid = (a.npix + block - 1) / block;
   if (a.fp.n_bands == 4) generate_kernel<4><<<(unsigned)grid, block, 0, s>>>(a);
   else generate_kernel<8><<<(unsigned)grid, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_joint_counts(uint64_t seed, int64_t npix, int32_t kmin, int32_t kmax,
+                                int32_t *counts, cudaStream_t s) {
+  if (npix <= 0) return cudaSuccess;
+  joint_counts_kernel<<<(unsigned)((npix + 255) / 256), 256, 0, s>>>(seed, npix, kmin, kmax,
+                                                                      counts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_generate_joint(const JointGenArgs &a, cudaStream_t s) {
+  if (a.npix <= 0) return cudaSuccess;
+  const unsigned g = (unsigned)((a.npix + 127) / 128);
+  if (a.fp.n_bands == 4) generate_joint_kernel<4><<<g, 128, 0, s>>>(a);
+  else generate_joint_kernel<8><<<g, 128, 0, s>>>(a);
   return cudaGetLastError();
 }
 

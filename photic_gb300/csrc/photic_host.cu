@@ -369,9 +369,51 @@ int photic_invert_batch(const photic_config *cfg, const float *d_rrs, int64_t np
 int photic_joint_invert_batch(const photic_config *cfg, const int32_t *d_offsets,
                               const double *d_theta_sun_deg, const float *d_rrs, int64_t npix,
                               int64_t n_obs, const photic_outputs *out, void *stream) {
-  (void)cfg; (void)d_offsets; (void)d_theta_sun_deg; (void)d_rrs; (void)npix; (void)n_obs;
-  (void)out; (void)stream;
-  return fail(PHOTIC_ERR_UNSUPPORTED, "joint fit not built in this version");
+  int rc = photic_config_check(cfg);
+  if (rc) return rc;
+  if (npix < 0 || n_obs < 0) return fail(PHOTIC_ERR_INVALID, "npix / n_obs < 0");
+  if (npix == 0) return PHOTIC_OK;
+  if (!d_offsets || !d_theta_sun_deg || !d_rrs || !out)
+    return fail(PHOTIC_ERR_INVALID, "NULL input or output");
+  if (npix > 0x7fffffffLL) return fail(PHOTIC_ERR_INVALID, "npix beyond 2^31-1");
+  if (cfg->precision != PHOTIC_PREC_FP64 && cfg->precision != PHOTIC_PREC_GUARDED)
+    return fail(PHOTIC_ERR_UNSUPPORTED, "the joint fit runs in FP64 only");
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned int *err = nullptr;
+  int sms = 0;
+  rc = device_state(&err, &sms);
+  if (rc) return rc;
+
+  JointArgs a;
+  memset(&a, 0, sizeof a);
+  make_fit(*cfg, a.fp);
+  make_scene(*cfg, cfg->theta_sun_deg, a.sc);
+  a.offsets = d_offsets;
+  a.theta_sun = d_theta_sun_deg;
+  a.rrs = d_rrs;
+  a.npix = npix;
+  a.out = *out;
+  a.error = err;
+
+  // workspace: counts, starts, fills (8 x i32 each), queues (8 x u64), list
+  const size_t head = 3 * 8 * sizeof(int32_t) + 8 * sizeof(unsigned long long);
+  const size_t bytes = head + (size_t)npix * sizeof(int32_t);
+  unsigned char *ws = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&ws, bytes, s);
+  if (e != cudaSuccess) return fail(PHOTIC_ERR_NOMEM, "joint workspace: %s", cudaGetErrorString(e));
+  e = cudaMemsetAsync(ws, 0, head, s);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  a.queues = reinterpret_cast<unsigned long long *>(ws);
+  a.bin_count = reinterpret_cast<int32_t *>(ws + 8 * sizeof(unsigned long long));
+  a.bin_start = a.bin_count + 8;
+  int32_t *fill = a.bin_count + 16;
+  a.list = reinterpret_cast<int32_t *>(ws + head);
+  const int per_sm = cfg->blocks_per_sm ? cfg->blocks_per_sm : 4;
+  e = launch_joint(a, fill, sms * per_sm, s);
+  cudaError_t e2 = cudaFreeAsync(ws, s);
+  if (e != cudaSuccess) return cuda_fail(e, "joint launch");
+  if (e2 != cudaSuccess) return cuda_fail(e2, "cudaFreeAsync");
+  return PHOTIC_OK;
 }
 
 int photic_cost_batch(const photic_config *cfg, const float *d_rrs, const double *d_params,
@@ -419,17 +461,38 @@ int photic_generate_scene(const photic_config *cfg, uint64_t seed, int64_t pix0,
 
 int photic_joint_counts(uint64_t seed, int64_t npix, int32_t kmin, int32_t kmax,
                         int32_t *d_counts, void *stream) {
-  (void)seed; (void)npix; (void)kmin; (void)kmax; (void)d_counts; (void)stream;
-  return fail(PHOTIC_ERR_UNSUPPORTED, "joint generator not built in this version");
+  if (npix < 0 || !d_counts || kmin < 1 || kmax > PHOTIC_MAX_SCENES || kmin > kmax)
+    return fail(PHOTIC_ERR_INVALID, "bad arguments (need 1 <= kmin <= kmax <= 8)");
+  cudaError_t e = launch_joint_counts(seed, npix, kmin, kmax, d_counts, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "joint counts launch");
+  return PHOTIC_OK;
 }
 
 int photic_generate_joint(const photic_config *cfg, uint64_t seed, int64_t npix,
                           const int32_t *d_offsets, double theta_sun_min, double theta_sun_max,
                           double mask_frac, double noise_sigma, double *d_theta_sun,
                           float *d_rrs, double *d_truth, void *stream) {
-  (void)cfg; (void)seed; (void)npix; (void)d_offsets; (void)theta_sun_min; (void)theta_sun_max;
-  (void)mask_frac; (void)noise_sigma; (void)d_theta_sun; (void)d_rrs; (void)d_truth; (void)stream;
-  return fail(PHOTIC_ERR_UNSUPPORTED, "joint generator not built in this version");
+  int rc = photic_config_check(cfg);
+  if (rc) return rc;
+  if (npix < 0 || !d_offsets || !d_theta_sun || !d_rrs)
+    return fail(PHOTIC_ERR_INVALID, "bad arguments");
+  JointGenArgs a;
+  memset(&a, 0, sizeof a);
+  make_fit(*cfg, a.fp);
+  make_scene(*cfg, cfg->theta_sun_deg, a.sc);
+  a.seed = seed;
+  a.npix = npix;
+  a.offsets = d_offsets;
+  a.theta_min = theta_sun_min;
+  a.theta_max = theta_sun_max;
+  a.mask_frac = mask_frac;
+  a.noise_sigma = noise_sigma;
+  a.theta_sun = d_theta_sun;
+  a.rrs = d_rrs;
+  a.truth = d_truth;
+  cudaError_t e = launch_generate_joint(a, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "joint generator launch");
+  return PHOTIC_OK;
 }
 
 int photic_set_counter(unsigned long long *d_counter) {

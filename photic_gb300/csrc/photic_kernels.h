@@ -64,6 +64,38 @@ struct CostArgs {
 };
 cudaError_t launch_cost(const CostArgs &a, cudaStream_t s);
 
+struct JointArgs {
+  FitParams fp;
+  SceneConsts sc;             // band constants; sun secant per observation
+  const int32_t *offsets;     // [npix + 1] CSR over observations
+  const double *theta_sun;    // [n_obs] subsurface sun zenith (deg)
+  const float *rrs;           // [n_obs][n_bands]
+  int64_t npix;
+  int32_t *list;              // [npix] pixel ids binned by scene count
+  int32_t *bin_start;         // [8]
+  int32_t *bin_count;         // [8]
+  unsigned long long *queues; // [8] work-queue heads
+  photic_outputs out;
+  unsigned int *error;
+};
+// Bins pixels by scene count and runs one persistent kernel per count.
+cudaError_t launch_joint(const JointArgs &a, int32_t *fill, int grid, cudaStream_t s);
+
+struct JointGenArgs {
+  FitParams fp;
+  SceneConsts sc;
+  uint64_t seed;
+  int64_t npix;
+  const int32_t *offsets;
+  double theta_min, theta_max, mask_frac, noise_sigma;
+  double *theta_sun;
+  float *rrs;
+  double *truth;
+};
+cudaError_t launch_joint_counts(uint64_t seed, int64_t npix, int32_t kmin, int32_t kmax,
+                                int32_t *counts, cudaStream_t s);
+cudaError_t launch_generate_joint(const JointGenArgs &a, cudaStream_t s);
+
 // Throughput probes (TFLOP/s of FP64 and FP32 FMA, Tops/s of MUFU ex2).
 cudaError_t measure_peaks(double *fp64_tflops, double *fp32_tflops, double *mufu_tops);
 

@@ -32,9 +32,19 @@ enum NmPhase : int32_t {
   PH_FINAL,           // re-evaluation at the kept optimum
 };
 
+// Loops over the simplex unroll fully for the small single-scene simplex
+// (n = 6) and stay rolled for the temporal fit (n up to 33).
+template <int N>
+struct NmUnroll {
+  static constexpr int kV = N <= 8 ? N + 1 : 1;  // loops over vertices
+  static constexpr int kC = N <= 8 ? N : 1;      // loops over coordinates
+};
+
 template <int N, class P, int BS>
 struct NmLane {
   using T = typename P::T;
+  static constexpr int UV = NmUnroll<N>::kV;
+  static constexpr int UC = NmUnroll<N>::kC;
   T *v, *f;  // shared: v[(j * N + i) * BS + tid], f[j * BS + tid]
   T x[N];    // point to evaluate next
   T cen[N], refl[N], trial[N], xmin[N], start[N], step[N];
@@ -48,13 +58,13 @@ struct NmLane {
 
   static __device__ __forceinline__ T pick(const T (&a)[N], int k) {
     T r = a[0];
-#pragma unroll
+#pragma unroll UC
     for (int i = 1; i < N; i++)
       if (i == k) r = a[i];
     return r;
   }
   static __device__ __forceinline__ void put(T (&a)[N], int k, T val) {
-#pragma unroll
+#pragma unroll UC
     for (int i = 0; i < N; i++)
       if (i == k) a[i] = val;
   }
@@ -73,7 +83,7 @@ struct NmLane {
   }
 
   __device__ __forceinline__ void restart_simplex() {
-#pragma unroll
+#pragma unroll UC
     for (int i = 0; i < N; i++) {
       x[i] = start[i];
       V(N, i) = start[i];
@@ -84,7 +94,7 @@ struct NmLane {
   // Vertex j: the start point moved by step[j] * scale along coordinate j
   // (model/asa047.c:181-194).
   __device__ __forceinline__ void make_vertex(int j) {
-#pragma unroll
+#pragma unroll UC
     for (int i = 0; i < N; i++) {
       T s = start[i];
       if (i == j) s = P::add(start[i], P::mul(step[i], scale));
@@ -98,7 +108,7 @@ struct NmLane {
   __device__ __forceinline__ void find_lo() {
     ylo = F(0);
     lo = 0;
-#pragma unroll
+#pragma unroll UV
     for (int j = 1; j <= N; j++) {
       T fj = F(j);
       if (P::lt(fj, ylo)) {
@@ -114,7 +124,7 @@ struct NmLane {
     if (kcount <= icount) return false;
     T yhi = F(0);
     hi = 0;
-#pragma unroll
+#pragma unroll UV
     for (int j = 1; j <= N; j++) {
       T fj = F(j);
       if (P::lt(yhi, fj)) {
@@ -122,15 +132,15 @@ struct NmLane {
         hi = j;
       }
     }
-#pragma unroll
+#pragma unroll UC
     for (int i = 0; i < N; i++) {
       T z = P::zero();
-#pragma unroll
+#pragma unroll UV
       for (int j = 0; j <= N; j++) z = P::add(z, V(j, i));
       z = P::sub(z, V(hi, i));
       cen[i] = P::div_n(z, N);
     }
-#pragma unroll
+#pragma unroll UC
     for (int i = 0; i < N; i++) {
       refl[i] = P::add(cen[i], P::sub(cen[i], V(hi, i)));
       x[i] = refl[i];
@@ -140,7 +150,7 @@ struct NmLane {
   }
 
   __device__ __forceinline__ void replace_hi(const T (&p)[N], T y) {
-#pragma unroll
+#pragma unroll UC
     for (int i = 0; i < N; i++) V(hi, i) = p[i];
     F(hi) = y;
   }
@@ -158,11 +168,11 @@ struct NmLane {
     if (icount <= kcount) {
       countdown = konvge;
       T z = P::zero();
-#pragma unroll
+#pragma unroll UV
       for (int j = 0; j <= N; j++) z = P::add(z, F(j));
       T mean = P::div_n(z, N + 1);
       z = P::zero();
-#pragma unroll
+#pragma unroll UV
       for (int j = 0; j <= N; j++) {
         T d = P::sub(F(j), mean);
         z = P::add(z, P::mul(d, d));
@@ -195,7 +205,7 @@ struct NmLane {
         fr = y;
         icount++;
         if (P::lt(fr, ylo)) {
-#pragma unroll
+#pragma unroll UC
           for (int i = 0; i < N; i++) {
             trial[i] = P::add(cen[i], P::mul2(P::sub(refl[i], cen[i])));
             x[i] = trial[i];
@@ -203,21 +213,21 @@ struct NmLane {
           phase = PH_EXPAND;
         } else {
           int worse = 0;
-#pragma unroll
+#pragma unroll UV
           for (int j = 0; j <= N; j++)
             if (P::lt(fr, F(j))) worse++;
           if (worse > 1) {
             replace_hi(refl, fr);
             cs = CS_ITER_END;
           } else if (worse == 0) {
-#pragma unroll
+#pragma unroll UC
             for (int i = 0; i < N; i++) {
               trial[i] = P::add(cen[i], P::half(P::sub(V(hi, i), cen[i])));
               x[i] = trial[i];
             }
             phase = PH_CONTRACT_IN;
           } else {
-#pragma unroll
+#pragma unroll UC
             for (int i = 0; i < N; i++) {
               trial[i] = P::add(cen[i], P::half(P::sub(refl[i], cen[i])));
               x[i] = trial[i];
@@ -236,7 +246,7 @@ struct NmLane {
         icount++;
         if (P::lt(F(hi), y)) {
           // shrink every vertex towards the best (model/asa047.c:331-351)
-#pragma unroll
+#pragma unroll UC
           for (int i = 0; i < N; i++) {
             T s = P::half(P::add(V(0, i), V(lo, i)));
             V(0, i) = s;
@@ -254,7 +264,7 @@ struct NmLane {
         icount++;
         if (jj < N) {
           const int j = jj + 1;
-#pragma unroll
+#pragma unroll UC
           for (int i = 0; i < N; i++) {
             T s = P::half(P::add(V(j, i), V(lo, i)));
             V(j, i) = s;
@@ -279,7 +289,7 @@ struct NmLane {
         } else {
           const T del = P::eps_step(pick(step, jj));
           put(xmin, jj, P::sub(P::sub(pick(xmin, jj), del), del));
-#pragma unroll
+#pragma unroll UC
           for (int i = 0; i < N; i++) x[i] = xmin[i];
           phase = PH_PROBE_MINUS;
         }
@@ -315,7 +325,7 @@ struct NmLane {
           cs = iteration_end() ? CS_END_INNER : CS_TOP;
           break;
         case CS_END_INNER:
-#pragma unroll
+#pragma unroll UC
           for (int i = 0; i < N; i++) xmin[i] = V(lo, i);
           floor_lo = P::trunc10(F(lo));
           if (kcount < icount) {
@@ -330,7 +340,7 @@ struct NmLane {
         case CS_PROBE_PLUS: {
           const T del = P::eps_step(pick(step, jj));
           put(xmin, jj, P::add(pick(xmin, jj), del));
-#pragma unroll
+#pragma unroll UC
           for (int i = 0; i < N; i++) x[i] = xmin[i];
           phase = PH_PROBE_PLUS;
           cs = CS_NONE;
@@ -341,7 +351,7 @@ struct NmLane {
             cs = CS_NM_DONE;
           } else {
             // restart from the probe point with a 1e-6 simplex
-#pragma unroll
+#pragma unroll UC
             for (int i = 0; i < N; i++) start[i] = xmin[i];
             scale = P::eps_scale();
             numres++;
