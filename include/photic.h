@@ -198,6 +198,50 @@ int photic_sync(void *stream);
  * 2 flops per FMA) and MUFU ex2 (T ops/s).  Synchronous; ~0.1 s. */
 int photic_measure_peaks(double *fp64_tflops, double *fp32_tflops, double *mufu_tops);
 
+/* BF16 GEMM on the tcgen05 tensor cores (FP32 accumulation in tensor
+ * memory): C[M x N] = A[M x K] * B[N x K]^T, A and B row-major BF16 with
+ * K contiguous (lda, ldb elements, multiples of 8; 16-byte aligned), C
+ * row-major FP32.  K must be a positive multiple of 16.  The building block
+ * of the surrogate network's training and inference (no counterpart in the
+ * reference). */
+int photic_gemm_bf16(const void *d_A, int32_t lda, const void *d_B, int32_t ldb, float *d_C,
+                     int32_t ldc, int32_t M, int32_t N, int32_t K, void *stream);
+/* The same with explicit core-matrix strides of the shared-memory operand
+ * layout (lbo: between core matrices along K, sbo: along M/N; bytes);
+ * photic_gemm_bf16 uses 128 / 1024.  For layout diagnostics. */
+int photic_gemm_bf16_strides(const void *d_A, int32_t lda, const void *d_B, int32_t ldb,
+                             float *d_C, int32_t ldc, int32_t M, int32_t N, int32_t K,
+                             int32_t lbo, int32_t sbo, void *stream);
+
+/* ---- Learned warm start (no counterpart in the reference) --------------
+ * An MLP 6 -> 128 -> 128 -> 128 -> 5 with SiLU maps the observed Rrs of the
+ * four bands and the subsurface sun / view zenith (degrees) to
+ * (ln P, ln G, ln X, B, H).  BF16 weights and activations, FP32
+ * accumulation, trained and run on the tcgen05 tensor cores.  Features are
+ * [R][6] floats, targets and predictions [R][5] floats. */
+typedef struct photic_surrogate photic_surrogate;
+int photic_surrogate_create(photic_surrogate **out, uint64_t seed);
+int photic_surrogate_destroy(photic_surrogate *s);
+int32_t photic_surrogate_num_params(void);
+/* Copy the FP32 master parameters out (write = 0) or in (write = 1). */
+int photic_surrogate_params(photic_surrogate *s, float *h_params, int32_t n, int32_t write);
+/* Gradient of the mean squared error on standardised targets (no update);
+ * d_grad [num_params]; d_loss (device float) is incremented by the loss. */
+int photic_surrogate_grads(photic_surrogate *s, const float *d_x, const float *d_t, int32_t R,
+                           float *d_grad, float *d_loss, void *stream);
+/* One Adam step (lr) on a batch of R rows. */
+int photic_surrogate_train_step(photic_surrogate *s, const float *d_x, const float *d_t,
+                                int32_t R, float lr, float *d_loss, void *stream);
+int photic_surrogate_infer(photic_surrogate *s, const float *d_x, int64_t R, float *d_y,
+                           void *stream);
+/* Start vectors for photic_invert_batch's d_seeds from the surrogate: pixels
+ * whose predicted parameters reproduce the measured spectrum to an RMS of
+ * resid_max or better get (H, 100B, 1, 100P, 100G, 100X); the others get NaN
+ * (cold start).  d_resid (optional, [npix] float) receives the RMS. */
+int photic_surrogate_seed(photic_surrogate *s, const photic_config *cfg, const float *d_rrs,
+                          int64_t npix, double resid_max, double *d_seeds, float *d_resid,
+                          void *stream);
+
 /* Instrumentation: if d_counter (device, unsigned long long) is not NULL,
  * later PHOTIC_PREC_GUARDED inversions add the number of exact FP64
  * re-evaluations they served to it.  Pass NULL to stop. */

@@ -101,6 +101,24 @@ _SIGS = {
     "photic_sync": (C.c_int, [C.c_void_p]),
     "photic_measure_peaks": (C.c_int, [C.POINTER(C.c_double)] * 3),
     "photic_set_counter": (C.c_int, [C.c_void_p]),
+    "photic_surrogate_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_uint64]),
+    "photic_surrogate_destroy": (C.c_int, [C.c_void_p]),
+    "photic_surrogate_num_params": (C.c_int32, []),
+    "photic_surrogate_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32]),
+    "photic_surrogate_grads": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                         C.c_void_p, C.c_void_p, C.c_void_p]),
+    "photic_surrogate_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                              C.c_float, C.c_void_p, C.c_void_p]),
+    "photic_surrogate_infer": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                         C.c_void_p]),
+    "photic_surrogate_seed": (C.c_int, [C.c_void_p, C.POINTER(photic_config), C.c_void_p,
+                                        C.c_int64, C.c_double, C.c_void_p, C.c_void_p,
+                                        C.c_void_p]),
+    "photic_gemm_bf16": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,
+                                   C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
+    "photic_gemm_bf16_strides": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
+                                           C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
+                                           C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
 }
 
 

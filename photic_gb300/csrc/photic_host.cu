@@ -495,6 +495,307 @@ int photic_generate_joint(const photic_config *cfg, uint64_t seed, int64_t npix,
   return PHOTIC_OK;
 }
 
+int photic_gemm_bf16_strides(const void *d_A, int32_t lda, const void *d_B, int32_t ldb,
+                             float *d_C, int32_t ldc, int32_t M, int32_t N, int32_t K,
+                             int32_t lbo, int32_t sbo, void *stream) {
+  if (!d_A || !d_B || !d_C || M < 0 || N < 0 || K < 16 || (K % 16) != 0)
+    return fail(PHOTIC_ERR_INVALID, "GEMM needs K a positive multiple of 16");
+  if ((lda % 8) || (ldb % 8) || lda < K || ldb < K || ldc < N ||
+      ((uintptr_t)d_A & 15u) || ((uintptr_t)d_B & 15u))
+    return fail(PHOTIC_ERR_INVALID, "GEMM operands need 16-byte aligned rows (ld % 8 == 0)");
+  unsigned int *err = nullptr;
+  int sms = 0;
+  int rc = device_state(&err, &sms);
+  if (rc) return rc;
+  GemmArgs g;
+  memset(&g, 0, sizeof g);
+  g.A = d_A;
+  g.B = d_B;
+  g.lda = lda;
+  g.ldb = ldb;
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.C = d_C;
+  g.ldc = ldc;
+  g.error = err;
+  g.lbo = lbo;
+  g.sbo = sbo;
+  g.epi = EPI_F32;
+  cudaError_t e = launch_gemm(g, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "GEMM launch");
+  return PHOTIC_OK;
+}
+
+int photic_gemm_bf16(const void *d_A, int32_t lda, const void *d_B, int32_t ldb, float *d_C,
+                     int32_t ldc, int32_t M, int32_t N, int32_t K, void *stream) {
+  return photic_gemm_bf16_strides(d_A, lda, d_B, ldb, d_C, ldc, M, N, K, 128, 1024, stream);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Surrogate network handle
+// ---------------------------------------------------------------------------
+struct photic_surrogate {
+  MlpState st;
+  void *block;  // one device allocation holding every buffer of st
+  int step;
+};
+
+namespace {
+
+// Workspace of a forward (inference) or forward+backward pass over Rpad rows.
+struct WorkAlloc {
+  void *mem = nullptr;
+  MlpWork w{};
+  cudaError_t alloc(int Rpad, bool train, cudaStream_t s) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+      size_t o = off;
+      off += (bytes + 255) & ~(size_t)255;
+      return o;
+    };
+    const size_t bfH = (size_t)Rpad * kMlpH * 2, fH = (size_t)Rpad * kMlpH * 4;
+    size_t oX0 = take((size_t)Rpad * kMlpIn * 2), oA1 = take(bfH), oA2 = take(bfH), oA3 = take(bfH);
+    size_t oY = take((size_t)Rpad * kMlpOut * 4);
+    size_t oZ1 = 0, oZ2 = 0, oZ3 = 0, odY = 0, odZ = 0, odZ2 = 0, oT1 = 0, oT2 = 0, oG4 = 0, oG = 0;
+    if (train) {
+      oZ1 = take(fH); oZ2 = take(fH); oZ3 = take(fH);
+      odY = take((size_t)Rpad * kMlpOut * 2); odZ = take(bfH); odZ2 = take(bfH);
+      oT1 = take(bfH); oT2 = take(bfH);
+      oG4 = take((size_t)kMlpH * kMlpOut * 4); oG = take((size_t)kMlpParams * 4);
+    }
+    cudaError_t e = cudaMallocAsync(&mem, off, s);
+    if (e != cudaSuccess) return e;
+    unsigned char *b = (unsigned char *)mem;
+    w.X0 = (__nv_bfloat16 *)(b + oX0);
+    w.A1 = (__nv_bfloat16 *)(b + oA1);
+    w.A2 = (__nv_bfloat16 *)(b + oA2);
+    w.A3 = (__nv_bfloat16 *)(b + oA3);
+    w.Y = (float *)(b + oY);
+    if (train) {
+      w.Z1 = (float *)(b + oZ1); w.Z2 = (float *)(b + oZ2); w.Z3 = (float *)(b + oZ3);
+      w.dY = (__nv_bfloat16 *)(b + odY); w.dZ = (__nv_bfloat16 *)(b + odZ);
+      w.dZ2 = (__nv_bfloat16 *)(b + odZ2); w.T1 = (__nv_bfloat16 *)(b + oT1);
+      w.T2 = (__nv_bfloat16 *)(b + oT2); w.G4t = (float *)(b + oG4); w.grad = (float *)(b + oG);
+    }
+    return cudaSuccess;
+  }
+  void release(cudaStream_t s) {
+    if (mem) cudaFreeAsync(mem, s);
+    mem = nullptr;
+  }
+};
+
+int pad128(int64_t R) { return (int)((R + 127) / 128 * 128); }
+
+}  // namespace
+
+extern "C" {
+
+int32_t photic_surrogate_num_params(void) { return kMlpParams; }
+
+int photic_surrogate_create(photic_surrogate **out, uint64_t seed) {
+  if (!out) return fail(PHOTIC_ERR_INVALID, "NULL handle");
+  *out = nullptr;
+  photic_surrogate *h = new photic_surrogate();
+  const size_t nP = kMlpParams * sizeof(float);
+  const size_t nW = (size_t)(kMlpH * kMlpIn + 2 * kMlpH * kMlpH + kMlpOut * kMlpH) * 2;
+  const size_t total = 3 * nP + 2 * nW + 4 * 16 * sizeof(float) + 1024;
+  cudaError_t e = cudaMalloc(&h->block, total);
+  if (e != cudaSuccess) {
+    delete h;
+    return fail(PHOTIC_ERR_NOMEM, "surrogate: %s", cudaGetErrorString(e));
+  }
+  unsigned char *b = (unsigned char *)h->block;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    unsigned char *p = b + off;
+    off += (bytes + 255) & ~(size_t)255;
+    return p;
+  };
+  MlpState &st = h->st;
+  st.P = (float *)take(nP);
+  st.M = (float *)take(nP);
+  st.V = (float *)take(nP);
+  st.W1b = (__nv_bfloat16 *)take((size_t)kMlpH * kMlpIn * 2);
+  st.W2b = (__nv_bfloat16 *)take((size_t)kMlpH * kMlpH * 2);
+  st.W3b = (__nv_bfloat16 *)take((size_t)kMlpH * kMlpH * 2);
+  st.W4b = (__nv_bfloat16 *)take((size_t)kMlpOut * kMlpH * 2);
+  st.W2t = (__nv_bfloat16 *)take((size_t)kMlpH * kMlpH * 2);
+  st.W3t = (__nv_bfloat16 *)take((size_t)kMlpH * kMlpH * 2);
+  st.W4t = (__nv_bfloat16 *)take((size_t)kMlpOut * kMlpH * 2);
+  st.in_mean = (float *)take(64);
+  st.in_std = (float *)take(64);
+  st.out_mean = (float *)take(64);
+  st.out_std = (float *)take(64);
+  // Initial weights: uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) from a
+  // splitmix64 stream; biases 0; padded output rows 0.
+  std::vector<float> P(kMlpParams, 0.0f);
+  uint64_t z = seed ^ 0x9E3779B97F4A7C15ull;
+  auto rnd = [&]() {
+    z += 0x9E3779B97F4A7C15ull;
+    uint64_t x = z;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    x ^= x >> 31;
+    return (double)(x >> 11) * (1.0 / 9007199254740992.0);
+  };
+  auto fill = [&](int off0, int rows, int cols, int fan_in, int valid_rows, int valid_cols) {
+    const double a = 1.0 / sqrt((double)fan_in);
+    for (int r = 0; r < rows; r++)
+      for (int c = 0; c < cols; c++)
+        P[off0 + r * cols + c] =
+            (r < valid_rows && c < valid_cols) ? (float)((2.0 * rnd() - 1.0) * a) : 0.0f;
+  };
+  fill(kOffW1, kMlpH, kMlpIn, 6, kMlpH, 6);
+  fill(kOffW2, kMlpH, kMlpH, kMlpH, kMlpH, kMlpH);
+  fill(kOffW3, kMlpH, kMlpH, kMlpH, kMlpH, kMlpH);
+  fill(kOffW4, kMlpOut, kMlpH, kMlpH, 5, kMlpH);
+  // Standardisation of inputs (Rrs of the 4 bands, sun and view zenith in
+  // degrees) and outputs (ln P, ln G, ln X, B, H) from the synthetic prior.
+  float in_mean[16] = {0.011f, 0.012f, 0.010f, 0.0035f, 35.0f, 0.0f};
+  float in_std[16] = {0.006f, 0.007f, 0.007f, 0.004f, 10.0f, 10.0f};
+  float out_mean[16] = {-3.80f, -3.45f, -4.95f, 0.275f, 12.75f};
+  float out_std[16] = {0.865f, 1.065f, 1.129f, 0.130f, 7.07f};
+  for (int i = 6; i < 16; i++) in_std[i] = 1.0f;
+  for (int i = 5; i < 16; i++) out_std[i] = 1.0f;
+  e = cudaMemcpy(st.P, P.data(), nP, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(st.M, 0, nP);
+  if (e == cudaSuccess) e = cudaMemset(st.V, 0, nP);
+  if (e == cudaSuccess) e = cudaMemcpy(st.in_mean, in_mean, 64, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(st.in_std, in_std, 64, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(st.out_mean, out_mean, 64, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(st.out_std, out_std, 64, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = mlp_refresh(st, 0);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    cudaFree(h->block);
+    delete h;
+    return cuda_fail(e, "surrogate init");
+  }
+  h->step = 0;
+  *out = h;
+  return PHOTIC_OK;
+}
+
+int photic_surrogate_destroy(photic_surrogate *s) {
+  if (!s) return PHOTIC_OK;
+  cudaFree(s->block);
+  delete s;
+  return PHOTIC_OK;
+}
+
+int photic_surrogate_params(photic_surrogate *s, float *h_params, int32_t n, int32_t write) {
+  if (!s || !h_params || n != kMlpParams) return fail(PHOTIC_ERR_INVALID, "bad arguments");
+  cudaError_t e = write ? cudaMemcpy(s->st.P, h_params, n * sizeof(float), cudaMemcpyHostToDevice)
+                        : cudaMemcpy(h_params, s->st.P, n * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && write) e = mlp_refresh(s->st, 0);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_fail(e, "surrogate params");
+  return PHOTIC_OK;
+}
+
+int photic_surrogate_grads(photic_surrogate *s, const float *d_x, const float *d_t, int32_t R,
+                           float *d_grad, float *d_loss, void *stream) {
+  if (!s || !d_x || !d_t || !d_grad || R <= 0) return fail(PHOTIC_ERR_INVALID, "bad arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned int *err = nullptr;
+  int sms = 0;
+  int rc = device_state(&err, &sms);
+  if (rc) return rc;
+  WorkAlloc wa;
+  const int Rpad = pad128(R);
+  cudaError_t e = wa.alloc(Rpad, true, st);
+  if (e != cudaSuccess) return fail(PHOTIC_ERR_NOMEM, "surrogate workspace");
+  e = mlp_backward(s->st, d_x, d_t, R, Rpad, wa.w, d_loss, err, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_grad, wa.w.grad, kMlpParams * sizeof(float), cudaMemcpyDeviceToDevice, st);
+  wa.release(st);
+  if (e != cudaSuccess) return cuda_fail(e, "surrogate gradients");
+  return PHOTIC_OK;
+}
+
+int photic_surrogate_train_step(photic_surrogate *s, const float *d_x, const float *d_t,
+                                int32_t R, float lr, float *d_loss, void *stream) {
+  if (!s || !d_x || !d_t || R <= 0) return fail(PHOTIC_ERR_INVALID, "bad arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned int *err = nullptr;
+  int sms = 0;
+  int rc = device_state(&err, &sms);
+  if (rc) return rc;
+  WorkAlloc wa;
+  const int Rpad = pad128(R);
+  cudaError_t e = wa.alloc(Rpad, true, st);
+  if (e != cudaSuccess) return fail(PHOTIC_ERR_NOMEM, "surrogate workspace");
+  e = mlp_backward(s->st, d_x, d_t, R, Rpad, wa.w, d_loss, err, st);
+  if (e == cudaSuccess) e = mlp_adam(s->st, wa.w, lr, ++s->step, st);
+  wa.release(st);
+  if (e != cudaSuccess) return cuda_fail(e, "surrogate train step");
+  return PHOTIC_OK;
+}
+
+int photic_surrogate_infer(photic_surrogate *s, const float *d_x, int64_t R, float *d_y,
+                           void *stream) {
+  if (!s || !d_x || !d_y || R < 0) return fail(PHOTIC_ERR_INVALID, "bad arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned int *err = nullptr;
+  int sms = 0;
+  int rc = device_state(&err, &sms);
+  if (rc) return rc;
+  const int64_t chunk = 1 << 20;
+  for (int64_t r0 = 0; r0 < R; r0 += chunk) {
+    const int n = (int)((R - r0) < chunk ? (R - r0) : chunk);
+    WorkAlloc wa;
+    const int Rpad = pad128(n);
+    cudaError_t e = wa.alloc(Rpad, false, st);
+    if (e != cudaSuccess) return fail(PHOTIC_ERR_NOMEM, "surrogate workspace");
+    e = mlp_forward(s->st, d_x + r0 * 6, n, Rpad, wa.w, err, st);
+    if (e == cudaSuccess) e = mlp_denorm(s->st, wa.w, n, d_y + r0 * 5, st);
+    wa.release(st);
+    if (e != cudaSuccess) return cuda_fail(e, "surrogate inference");
+  }
+  return PHOTIC_OK;
+}
+
+int photic_surrogate_seed(photic_surrogate *s, const photic_config *cfg, const float *d_rrs,
+                          int64_t npix, double resid_max, double *d_seeds, float *d_resid,
+                          void *stream) {
+  int rc = photic_config_check(cfg);
+  if (rc) return rc;
+  if (!s || !d_rrs || !d_seeds || npix < 0) return fail(PHOTIC_ERR_INVALID, "bad arguments");
+  if (npix == 0) return PHOTIC_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  float *x = nullptr, *y = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&x, (size_t)npix * 6 * sizeof(float), st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void **)&y, (size_t)npix * 5 * sizeof(float), st);
+  if (e != cudaSuccess) return fail(PHOTIC_ERR_NOMEM, "seed workspace");
+  e = mlp_features(d_rrs, npix, cfg->n_bands, (float)cfg->theta_sun_deg,
+                   (float)cfg->theta_view_deg, x, st);
+  if (e == cudaSuccess) {
+    rc = photic_surrogate_infer(s, x, npix, y, stream);
+    if (rc == PHOTIC_OK) {
+      SeedArgs a;
+      memset(&a, 0, sizeof a);
+      make_fit(*cfg, a.fp);
+      make_scene(*cfg, cfg->theta_sun_deg, a.sc);
+      a.rrs = d_rrs;
+      a.y = y;
+      a.npix = npix;
+      a.resid_max = resid_max;
+      a.seeds = d_seeds;
+      a.resid = d_resid;
+      e = mlp_seeds(a, st);
+    }
+  }
+  cudaFreeAsync(x, st);
+  cudaFreeAsync(y, st);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(e, "surrogate seeds");
+  return PHOTIC_OK;
+}
+
 int photic_set_counter(unsigned long long *d_counter) {
   g_counter_ptr = d_counter;
   return PHOTIC_OK;

@@ -1,6 +1,7 @@
 // photic_kernels.h -- launch arguments and launchers of the device code
 // (internal to the library; the public ABI is include/photic.h).
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -11,8 +12,9 @@ namespace photic {
 
 // Device error bits accumulated in the per-call error word.
 enum : unsigned {
-  PHOTIC_DEVERR_EVAL_CAP = 1u,   // a pixel exceeded the defensive evaluation cap
-  PHOTIC_DEVERR_BAD_SCENES = 2u  // a joint pixel had a scene count outside 1..8
+  PHOTIC_DEVERR_EVAL_CAP = 1u,     // a pixel exceeded the defensive evaluation cap
+  PHOTIC_DEVERR_BAD_SCENES = 2u,   // a joint pixel had a scene count outside 1..8
+  PHOTIC_DEVERR_MMA_TIMEOUT = 4u   // a tensor-core wait gave up
 };
 
 struct InvertArgs {
@@ -95,6 +97,68 @@ struct JointGenArgs {
 cudaError_t launch_joint_counts(uint64_t seed, int64_t npix, int32_t kmin, int32_t kmax,
                                 int32_t *counts, cudaStream_t s);
 cudaError_t launch_generate_joint(const JointGenArgs &a, cudaStream_t s);
+
+// BF16 TN GEMM on tcgen05 (photic_gemm.cu).
+enum { EPI_F32 = 0, EPI_BIAS_F32 = 1, EPI_BIAS_SILU = 2, EPI_DSILU = 3 };
+struct GemmArgs {
+  const void *A;   // __nv_bfloat16 [M][lda]
+  const void *B;   // __nv_bfloat16 [N][ldb]
+  int lda, ldb, M, N, K;
+  float *C;        // EPI_F32 / EPI_BIAS_F32 output [M][ldc]
+  int ldc;
+  void *O;         // __nv_bfloat16 output [M][ldo] (SILU / DSILU)
+  int ldo;
+  float *Z;        // pre-activation [M][ldz]: written by SILU, read by DSILU
+  int ldz;
+  const float *bias;
+  unsigned int *error;
+  int lbo, sbo;    // core-matrix strides of the shared-memory layout (bytes)
+  int epi;
+};
+cudaError_t launch_gemm(const GemmArgs &g, cudaStream_t s);
+
+// Surrogate MLP (photic_mlp.cu): 6 (padded 16) -> 128 -> 128 -> 128 -> 5
+// (padded 16).  FP32 master parameters, flat, in this order.
+constexpr int kMlpIn = 16, kMlpH = 128, kMlpOut = 16;
+constexpr int kOffW1 = 0;
+constexpr int kOffB1 = kOffW1 + kMlpH * kMlpIn;
+constexpr int kOffW2 = kOffB1 + kMlpH;
+constexpr int kOffB2 = kOffW2 + kMlpH * kMlpH;
+constexpr int kOffW3 = kOffB2 + kMlpH;
+constexpr int kOffB3 = kOffW3 + kMlpH * kMlpH;
+constexpr int kOffW4 = kOffB3 + kMlpH;
+constexpr int kOffB4 = kOffW4 + kMlpOut * kMlpH;
+constexpr int kMlpParams = kOffB4 + kMlpOut;
+
+struct MlpState {
+  float *P, *M, *V;  // parameters and Adam moments
+  __nv_bfloat16 *W1b, *W2b, *W3b, *W4b, *W2t, *W3t, *W4t;
+  float *in_mean, *in_std, *out_mean, *out_std;  // [16] each
+};
+struct MlpWork {
+  __nv_bfloat16 *X0, *A1, *A2, *A3, *dY, *dZ, *dZ2, *T1, *T2;
+  float *Z1, *Z2, *Z3, *Y, *G4t, *grad;
+};
+struct SeedArgs {
+  FitParams fp;
+  SceneConsts sc;
+  const float *rrs;
+  const float *y;     // [npix][5] surrogate outputs (ln P, ln G, ln X, B, H)
+  int64_t npix;
+  double resid_max;
+  double *seeds;      // [npix][6]
+  float *resid;       // optional [npix]
+};
+cudaError_t mlp_refresh(const MlpState &st, cudaStream_t s);
+cudaError_t mlp_forward(const MlpState &st, const float *x, int R, int Rpad, MlpWork &w,
+                        unsigned int *err, cudaStream_t s);
+cudaError_t mlp_backward(const MlpState &st, const float *x, const float *t, int R, int Rpad,
+                         MlpWork &w, float *loss, unsigned int *err, cudaStream_t s);
+cudaError_t mlp_adam(const MlpState &st, const MlpWork &w, float lr, int step, cudaStream_t s);
+cudaError_t mlp_denorm(const MlpState &st, const MlpWork &w, int R, float *y, cudaStream_t s);
+cudaError_t mlp_features(const float *rrs, int64_t npix, int nb, float th_sun, float th_view,
+                         float *x, cudaStream_t s);
+cudaError_t mlp_seeds(const SeedArgs &a, cudaStream_t s);
 
 // Throughput probes (TFLOP/s of FP64 and FP32 FMA, Tops/s of MUFU ex2).
 cudaError_t measure_peaks(double *fp64_tflops, double *fp32_tflops, double *mufu_tops);
