@@ -89,6 +89,8 @@ typedef struct photic_config {
   int32_t layout;                            /* PHOTIC_LAYOUT_* (joint fit) */
   int32_t block_threads;                     /* launch shape; 0 = tuned default */
   int32_t blocks_per_sm;                     /* 0 = tuned default */
+  double seed_step_scale;                    /* seeded starts: steps = this x the
+                                                cold start's relative steps (1) */
 } photic_config;
 
 /* Outputs, structure of arrays.  Every pointer may be NULL (not written).

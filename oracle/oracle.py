@@ -83,7 +83,7 @@ def port() -> _Lib:
         L.po_interp_1d.restype = C.c_double
         L.po_invert_batch.argtypes = [C.c_int, _dp, C.c_double, C.c_double, C.c_double, _fp,
                                       C.c_int64, C.c_float, C.c_double, C.c_int, C.c_int,
-                                      C.c_int, _dp, _dp, C.c_int, _dp]
+                                      C.c_int, _dp, _dp, C.c_double, C.c_int, _dp]
         L.po_joint_invert_batch.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _i32p, _dp,
                                             _fp, C.c_int64, C.c_float, C.c_int, C.c_double,
                                             C.c_int, C.c_int, C.c_int, _dp, C.c_int, _dp]
@@ -139,7 +139,7 @@ def reference() -> _Lib:
 
 def invert_batch(rrs, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0, h_tide=0.0,
                  nodata=-9999.0, reqmin=1e-10, konvge=100, kcount=2000, hstarts=None,
-                 seeds=None, nthreads=0, which="port"):
+                 seeds=None, seed_step_scale=1.0, nthreads=0, which="port"):
     """Invert [npix, n_bands] float32 spectra; returns [npix, NOUT] float64.
 
     ``which="reference"`` runs the reference's own samodel_optimise with the
@@ -165,8 +165,8 @@ def invert_batch(rrs, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0, h_tide=0.
     sd = _f64(seeds) if seeds is not None else None
     rc = L.po_invert_batch(nb, _ptr(wl, _dp), theta_sun, theta_view, h_tide, _ptr(rrs, _fp),
                            npix, nodata, reqmin, konvge, kcount,
-                           0 if hs is None else len(hs), _ptr(hs, _dp), _ptr(sd, _dp), nthreads,
-                           _ptr(out, _dp))
+                           0 if hs is None else len(hs), _ptr(hs, _dp), _ptr(sd, _dp),
+                           seed_step_scale, nthreads, _ptr(out, _dp))
     if rc:
         raise ValueError(f"po_invert_batch failed ({rc})")
     return out

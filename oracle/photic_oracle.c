@@ -550,6 +550,7 @@ typedef struct {
   int konvge, kcount;
   int n_hstarts;
   const double *hstarts;
+  double seed_step_scale;
 } po_fit;
 
 static void cold_start(const po_pixel *px, double H0, double *start, double *step) {
@@ -599,14 +600,16 @@ static void cold_start(const po_pixel *px, double H0, double *start, double *ste
   }
 }
 
-/* Steps of a seeded start: the same relative steps as the cold start. */
-static void seeded_start(const po_pixel *px, const double *seed, double *start, double *step) {
+/* Steps of a seeded start: the cold start's relative steps times a scale
+ * (1 reproduces the reference's hot-start steps, model/samodel.c:2286-2309). */
+static void seeded_start(const po_pixel *px, const double *seed, double scale, double *start,
+                         double *step) {
   int n = n_params_of(px), i;
   double rel_ref[6] = {1.25, 1.5, 0.5, 2.0, 2.0, 2.0};
   for (i = 0; i < n; i++) {
     double rel = (i < 6) ? rel_ref[i] : 2.0;
     start[i] = seed[i];
-    step[i] = rel * start[i];
+    step[i] = (rel * scale) * start[i];
   }
 }
 
@@ -623,7 +626,7 @@ static void fit_pixel(po_pixel *px, const po_fit *fit, const double *seed, doubl
   nst = seed ? 1 : fit->n_hstarts;
   for (k = 0; k < nst; k++) {
     if (seed)
-      seeded_start(px, seed, start, step);
+      seeded_start(px, seed, fit->seed_step_scale, start, step);
     else
       cold_start(px, fit->hstarts[k], start, step);
     po_nelmin(pixel_cost, px, n, start, xm, &y, fit->reqmin, step, fit->konvge, fit->kcount,
@@ -701,12 +704,13 @@ int po_nout(void) { return PO_NOUT; }
 int po_invert_batch(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
                     double h_tide, const float *rrs, int64_t npix, float nodata, double reqmin,
                     int konvge, int kcount, int n_hstarts, const double *hstarts,
-                    const double *seeds, int nthreads, double *out) {
+                    const double *seeds, double seed_step_scale, int nthreads, double *out) {
   po_scene sc;
   po_fit fit;
   int64_t p;
   if (n_bands < 2 || n_bands > PO_MAX_BANDS) return 1;
   scene_init(&sc, n_bands, wl, theta_sun_deg, theta_view_deg, h_tide);
+  fit.seed_step_scale = seed_step_scale;
   fit.reqmin = reqmin;
   fit.konvge = konvge;
   fit.kcount = kcount;
@@ -748,6 +752,7 @@ int po_joint_invert_batch(int n_bands, const double *wl, double theta_view_deg, 
   po_fit fit;
   int64_t p;
   if (n_bands < 2 || n_bands > PO_MAX_BANDS) return 1;
+  fit.seed_step_scale = 1.0;
   fit.reqmin = reqmin;
   fit.konvge = konvge;
   fit.kcount = kcount;

@@ -55,7 +55,7 @@ void po_nelmin_pixel(int n_bands, const double *wl, double theta_sun_deg, double
 int po_invert_batch(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
                     double h_tide, const float *rrs, int64_t npix, float nodata, double reqmin,
                     int konvge, int kcount, int n_hstarts, const double *hstarts,
-                    const double *seeds, int nthreads, double *out);
+                    const double *seeds, double seed_step_scale, int nthreads, double *out);
 int po_joint_invert_batch(int n_bands, const double *wl, double theta_view_deg, double h_tide,
                           const int32_t *scene_offsets, const double *theta_sun_deg,
                           const float *rrs, int64_t npix, float nodata, int layout,

@@ -40,6 +40,7 @@ class photic_config(C.Structure):
         ("layout", C.c_int32),
         ("block_threads", C.c_int32),
         ("blocks_per_sm", C.c_int32),
+        ("seed_step_scale", C.c_double),
     ]
 
 

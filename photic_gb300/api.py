@@ -50,6 +50,7 @@ class Config:
     layout: str = "reference"
     block_threads: int = 0
     blocks_per_sm: int = 0
+    seed_step_scale: float = 1.0
 
     @classmethod
     def reference_default(cls, **kw) -> "Config":
@@ -88,6 +89,7 @@ class Config:
         c.layout = LAYOUTS[self.layout]
         c.block_threads = int(self.block_threads)
         c.blocks_per_sm = int(self.blocks_per_sm)
+        c.seed_step_scale = float(self.seed_step_scale)
         return c
 
 

@@ -811,7 +811,7 @@ __global__ void __launch_bounds__(BS) guarded_kernel(const __grid_constant__ Inv
 #pragma unroll
               for (int i = 0; i < kN; i++) {
                 start[i] = sd[i];
-                step[i] = rel[i] * sd[i];
+                step[i] = (rel[i] * fp.seed_step_scale) * sd[i];
               }
             }
           }

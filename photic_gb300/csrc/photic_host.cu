@@ -135,6 +135,7 @@ void make_fit(const photic_config &cfg, FitParams &fp) {
   fp.nodata = cfg.nodata_value;
   fp.reqmin = cfg.reqmin;
   fp.early_exit_per_scene = cfg.early_exit_per_scene;
+  fp.seed_step_scale = cfg.seed_step_scale;
   fp.aw640 = table_at(tables::aw, 640.0);
   for (int k = 0; k < cfg.n_hstarts; k++) fp.hstarts[k] = cfg.hstarts[k];
   const double targets[kNRefTargets] = {440.0, 490.0, 550.0, 640.0, 750.0};
@@ -251,6 +252,7 @@ void photic_config_default(photic_config *cfg) {
   cfg->layout = PHOTIC_LAYOUT_REFERENCE;
   cfg->block_threads = 0;
   cfg->blocks_per_sm = 0;
+  cfg->seed_step_scale = 1.0;
 }
 
 int photic_config_check(const photic_config *cfg) {
@@ -277,6 +279,8 @@ int photic_config_check(const photic_config *cfg) {
     return fail(PHOTIC_ERR_INVALID, "block_threads must be 0, 64, 128 or 256");
   if (cfg->blocks_per_sm < 0 || cfg->blocks_per_sm > 32)
     return fail(PHOTIC_ERR_INVALID, "blocks_per_sm outside 0..32");
+  if (!(cfg->seed_step_scale > 0.0) || !isfinite(cfg->seed_step_scale))
+    return fail(PHOTIC_ERR_INVALID, "seed_step_scale must be a positive number");
   return PHOTIC_OK;
 }
 

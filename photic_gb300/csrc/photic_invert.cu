@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(BS) invert_kernel(const __grid_constant__ Inve
 #pragma unroll
               for (int i = 0; i < kN; i++) {
                 m.start[i] = P::from_double(sd[i]);
-                m.step[i] = P::from_double(rel[i] * sd[i]);
+                m.step[i] = P::from_double((rel[i] * fp.seed_step_scale) * sd[i]);
               }
             }
           }

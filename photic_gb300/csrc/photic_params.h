@@ -69,6 +69,7 @@ struct FitParams {
   double reqmin;
   double early_exit_per_scene;
   double aw640;
+  double seed_step_scale;
   double hstarts[kMaxHStarts];
   InterpPlan plan[kNRefTargets];
   KPenalty kp;
