@@ -108,6 +108,8 @@ typedef struct photic_outputs {
   int32_t *evals;        /* cost evaluations over all starts */
   int32_t *evals_kept;   /* evaluations of the kept start */
   int32_t *status;       /* PHOTIC_PX_* | PHOTIC_PX_CONVERGED | start << 16 */
+  double *params;        /* single-scene calls: [npix * 6] kept parameter vector
+                            (H, 100B, q, 100P, 100G, 100X) as nelmin returned it */
 } photic_outputs;
 
 /* Defaults: OLI-like bands 443/482/561/655 nm, sun 35 deg, nadir, the

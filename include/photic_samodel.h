@@ -1,0 +1,193 @@
+/*
+ * photic_samodel.h -- link-compatible drop-ins for photic's samodel entry
+ * points, backed by the GB300 kernels of libphotic_gb300.
+ *
+ * The reference declares these in model/samodel.h:8-29 over the types of
+ * model/common.h (geogrid :69-84, model_data :116-190, scene :194-216).  For
+ * a program built against the reference headers to relink against this
+ * library unchanged, the structs below repeat those layouts field for field
+ * (same order, same types; the reference's bool is an int, MAX_STRING_LEN
+ * 2048, MAX_GRIDS 265).  They carry photic_ names so this header never
+ * clashes with the reference's own.
+ *
+ * Semantics kept: the per-pixel fit of samodel_optimise (cold multi-start,
+ * or the single empirical depth start when empirical_depth_present), the
+ * cost of samodel_error and the forward model of samodel_Rrs, for one
+ * spatial region and the sand bottom; outputs are written where the
+ * reference writes them.  Not reproduced: the reference samodel()'s
+ * order-dependent shortcuts (lookup table of earlier fits, hot start from
+ * the previous pixel, model/samodel.c:980-1109), its depth-sigma Monte Carlo
+ * and its netCDF writes -- samodel() here fits every unmasked pixel with the
+ * plain method and fills the output grids in memory.  The functions return
+ * void like the reference; each clears photic_last_error() on entry, and a
+ * failure leaves the outputs untouched and its message there, so an empty
+ * message after the call means success.
+ *
+ * Rrs_measured is read at float precision (samodel() fills it from float
+ * grids).  samodel_optimise honours start_at_previous for one scene (one
+ * start at depth_prev, or h_empirical, with P, G, X from md->prev); a joint
+ * fit over n_scenes > 1 uses the cold multi-start and band constants from
+ * the wavelengths' tables, with each scene's theta_sun from md.
+ */
+#ifndef PHOTIC_SAMODEL_H
+#define PHOTIC_SAMODEL_H
+
+#include "photic.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PHOTIC_REF_MAX_STRING_LEN 2048
+#define PHOTIC_REF_MAX_GRIDS 265
+
+typedef struct photic_geogrid {
+  int nrows;
+  int ncols;
+  float cellsize;
+  float wlon;
+  float slat;
+  float elon;
+  float nlat;
+  float nodata_value;
+  float lambda;
+  float theta_v;
+  float theta_w;
+  float **array;
+} photic_geogrid;
+
+typedef struct photic_model_data {
+  int n_bottoms;
+  int n_scenes;
+  int n_regions;
+  int max_n_bands;
+  int max_n_regions;
+  int *n_bands;
+  int *n_raw_bands;
+  int origin;
+  int n_params;
+  double ***Rrs_measured;
+  double **wavelengths;
+  double **raw_wavelengths;
+  double ***bottom_reflectance;
+  double **a_0;
+  double **a_1;
+  double **a_w;
+  double **b_bw;
+  double a_w640;
+  double *H_tide;
+  double *theta_sun;
+  double *theta_view;
+  double *sec_theta_sun;
+  double *sec_theta_view;
+  double **Rrs440;
+  double **Rrs490;
+  double **Rrs550;
+  double **Rrs640;
+  double **Rrs750;
+  double **rrs_noise;
+  double h_empirical;
+  int bottom_type_indexes[12];
+  char B_type_name[12][PHOTIC_REF_MAX_STRING_LEN];
+  int empirical_depth_present;
+  int i;
+  int j;
+  int prev_i;
+  int prev_j;
+  int start_at_previous;
+  double *P;
+  double *G;
+  double *X;
+  double *B;
+  double *H;
+  double *D;
+  double *prev;
+  double ***Rrs_modelled;
+  double ***rrs_modelled;
+  double ***rrs_bottom;
+  double ***rrs_dp;
+  double **K;
+  double ***rho;
+  double depth;
+  double depth_prev;
+  double depth_sigma;
+  double Rrs_error;
+  double SAM_error;
+  double K_error;
+  double depth_error;
+  double bottom_error;
+  double model_error;
+  double K_min;
+  double K_min_prev;
+  double bottom_albedo;
+  double B_type_percent[12];
+  double index_optical_depth;
+  int bottom_type;
+  int converged;
+  int n_iterations;
+} photic_model_data;
+
+typedef struct photic_scene {
+  char scene_name[PHOTIC_REF_MAX_STRING_LEN];
+  int n_bands;
+  int nrows;
+  int ncols;
+  int band_indexes[PHOTIC_REF_MAX_GRIDS];
+  int wavelengths[PHOTIC_REF_MAX_GRIDS];
+  double theta_w;
+  double theta_v;
+  double H_tide;
+  double R_inf[PHOTIC_REF_MAX_GRIDS];
+  double R_sigma[PHOTIC_REF_MAX_GRIDS];
+  double K[PHOTIC_REF_MAX_GRIDS];
+  double K_sigma[PHOTIC_REF_MAX_GRIDS];
+  double ratio_min;
+  double ratio_max;
+  double slope_min;
+  double slope_max;
+  int pgx_present;
+  int ps_p;
+  int ps_g;
+  int ps_x;
+} photic_scene;
+
+/* model/samodel.h:8-19.  Fits every pixel that has data in all bands of all
+ * scenes (model/samodel.c:672-700); n_spatial <= 1 and n_bottoms == 1 are
+ * required (one region, sand); depth_sigma is set to 0.  Depth is written
+ * negative below the datum, as the reference does (model/samodel.c:1486). */
+void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scene_indexes,
+             int nscenes, int empirical_depth_present, photic_geogrid empirical_depths,
+             int n_smoothing_radius, int n_spatial, int n_bottoms, float **depth,
+             float **depth_sigma, float **model_error, float **bottom_albedo, float **bottom_sand,
+             float **bottom_seagrass, float **bottom_coral, float **K_min, float **bottom_type,
+             float **index_optical_depth, float pagesize, int background, int linewidth);
+
+/* model/samodel.h:21.  Reads the measured spectra and band constants of md
+ * (one region) and writes depth, P, G, X, bottom albedo, the errors, K_min,
+ * index of optical depth, n_iterations, converged and Rrs_modelled. */
+void samodel_optimise(photic_model_data *md);
+
+/* model/samodel.h:25.  Cost of params for md's first region; also writes
+ * md->Rrs_modelled[0][s][b], Rrs_error and model_error. */
+double samodel_error(double *params, photic_model_data *md);
+
+/* model/samodel.h:27-29.  Forward model of one band at the given water
+ * column, depth and bottom (q normalised, one bottom type); writes, as the
+ * reference does, md->Rrs_modelled, rrs_modelled, rrs_bottom, rrs_dp and rho
+ * at [k_region][k_scene][k_band] (each when allocated), md->K[k_scene][k_band],
+ * md->depth and md->bottom_albedo. */
+void samodel_Rrs(double P, double G, double X, double B[], double q[], double H, double Delta,
+                 photic_model_data *md, int k_scene, int k_band, int k_region);
+
+/* Forward model batch (samodel_Rrs over all bands of cfg): for n parameter
+ * rows of 7 doubles -- P, G, X, B, q, H, Delta -- and the spectrum-shape
+ * inputs Rrs(440) and Rrs(490) per row, writes Rrs [n * n_bands] and
+ * K [n * n_bands] (doubles; K may be NULL).  Device pointers. */
+int photic_forward_batch(const photic_config *cfg, const double *d_params,
+                         const double *d_rrs440, const double *d_rrs490, int64_t n,
+                         double *d_rrs, double *d_K, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

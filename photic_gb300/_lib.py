@@ -59,6 +59,7 @@ class photic_outputs(C.Structure):
         ("evals", C.c_void_p),
         ("evals_kept", C.c_void_p),
         ("status", C.c_void_p),
+        ("params", C.c_void_p),
     ]
 
 
@@ -100,6 +101,9 @@ _SIGS = {
                                       C.c_double]),
     "photic_band_constants": (C.c_int, [C.POINTER(photic_config), C.POINTER(C.c_double)]),
     "photic_sync": (C.c_int, [C.c_void_p]),
+    "photic_forward_batch": (C.c_int, [C.POINTER(photic_config), C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                                       C.c_void_p]),
     "photic_measure_peaks": (C.c_int, [C.POINTER(C.c_double)] * 3),
     "photic_set_counter": (C.c_int, [C.c_void_p]),
     "photic_surrogate_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_uint64]),

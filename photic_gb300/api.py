@@ -26,9 +26,9 @@ PRECISIONS = {"fp64": L.PREC_FP64, "df64": L.PREC_DF64, "fp32": L.PREC_FP32,
               "guarded": L.PREC_GUARDED}
 LAYOUTS = {"reference": L.LAYOUT_REFERENCE, "scene_b": L.LAYOUT_SCENE_B}
 OUTPUT_FIELDS = ("depth", "depth_f64", "P", "G", "X", "bottom_albedo", "model_error",
-                 "rrs_error", "K_min", "iod", "evals", "evals_kept", "status")
+                 "rrs_error", "K_min", "iod", "evals", "evals_kept", "status", "params")
 _DTYPES = {"depth_f64": torch.float64, "evals": torch.int32, "evals_kept": torch.int32,
-           "status": torch.int32}
+           "status": torch.int32, "params": torch.float64}
 
 
 @dataclass
@@ -119,6 +119,10 @@ def alloc_outputs(npix: int, device, fields: Sequence[str] = OUTPUT_FIELDS,
                   n_obs: Optional[int] = None) -> Dict[str, torch.Tensor]:
     out = {}
     for f in fields:
+        if f == "params":
+            if n_obs is None:
+                out[f] = torch.empty(npix, 6, dtype=torch.float64, device=device)
+            continue
         n = n_obs if (n_obs is not None and f in ("P", "G", "X")) else npix
         out[f] = torch.empty(n, dtype=_DTYPES.get(f, torch.float32), device=device)
     return out

@@ -5,7 +5,10 @@ translation units are compiled in parallel and linked with a static CUDA
 runtime, so the .so has no dependency beyond the driver.  Every unit is
 compiled with --fmad=false: no multiply-add pair is fused unless the
 source asks for it with an explicit fma, which keeps the double-precision
-path in the reference's rounding.
+path in the reference's rounding.  The host side gets -ffp-contract=off for
+the same reason: GCC on aarch64 fuses a*b+c by default, which moved the
+host-computed band constants and Rrs(440) off the reference's values by an
+ulp.
 """
 from __future__ import annotations
 
@@ -33,7 +36,7 @@ def nvcc() -> str:
 
 def flags(extra=()):
     return (ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
-                    "-Xcompiler", "-O2", "--expt-relaxed-constexpr"] + list(extra))
+                    "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"] + list(extra))
 
 
 def _compile(src: str, extra) -> str:

@@ -172,6 +172,54 @@ __global__ void generate_joint_kernel(const __grid_constant__ JointGenArgs a) {
   }
 }
 
+// Forward model of n parameter sets (P, G, X, B, q, H, Delta per row, 7
+// doubles) with caller-given Rrs(440)/Rrs(490).
+__global__ void forward_kernel(const __grid_constant__ ForwardArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const double *x = a.params + i * 7;
+  const double chi = a.rrs440[i] / a.rrs490[i];
+  double Y = 3.44 * (1.0 - 3.17 * exp(-2.01 * chi));
+  if (Y < 0.0) Y = 0.0;
+  if (Y > 2.5) Y = 2.5;
+  const double qB = x[4] * x[3];
+  for (int b = 0; b < a.fp.n_bands; b++) {
+    double K, parts[4];
+    const double r = forward_band_f64(a.sc, b, x[0], x[1], x[2], qB, x[5], x[6],
+                                      pow(a.sc.ratio440[b], Y), &K, parts);
+    a.rrs[i * a.fp.n_bands + b] = r;
+    if (a.K) a.K[i * a.fp.n_bands + b] = K;
+    if (a.parts)
+      for (int j = 0; j < 4; j++) a.parts[(i * a.fp.n_bands + b) * 4 + j] = parts[j];
+  }
+}
+
+// Start vectors of the reference's empirical-depth path (one start at the
+// pixel's empirical depth, model/samodel.c:2208-2231): the cold start of
+// model/samodel.c:2249-2353 with H replaced; NaN where no depth is given.
+template <int NB>
+__global__ void empirical_seeds_kernel(const __grid_constant__ EmpSeedArgs a) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.npix) return;
+  double *sd = a.seeds + p * 6;
+  const double h = a.h[p];
+  if (isnan(h)) {
+    sd[0] = h;
+    return;
+  }
+  const int nb = a.fp.n_bands;
+  double r[NB];
+#pragma unroll
+  for (int b = 0; b < NB; b++) r[b] = b < nb ? (double)a.rrs[p * nb + b] : 0.0;
+  PixelF64<NB> px;
+  pixel_setup_f64<NB>(a.fp, a.sc, r, px);
+  double start[6], step[6];
+  cold_start_f64<NB>(a.fp, px, start, step);
+  start[0] = h;
+#pragma unroll
+  for (int i = 0; i < 6; i++) sd[i] = start[i];
+}
+
 template <int NB>
 __global__ void cost_kernel_df(const __grid_constant__ CostArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -206,6 +254,14 @@ __global__ void cost_kernel(CostArgs a) {
   a.cost[i] = c;
   if (a.rrs_modelled)
     for (int b = 0; b < nb; b++) a.rrs_modelled[i * nb + b] = det.Rm[b];
+  if (a.details) {
+    double *d = a.details + i * 5;
+    d[0] = det.rrs_error;
+    d[1] = det.model_error;
+    d[2] = det.bottom_albedo;
+    d[3] = det.K_min;
+    d[4] = det.iod;
+  }
 }
 
 }  // namespace
@@ -232,6 +288,20 @@ cudaError_t launch_generate_joint(const JointGenArgs &a, cudaStream_t s) {
   const unsigned g = (unsigned)((a.npix + 127) / 128);
   if (a.fp.n_bands == 4) generate_joint_kernel<4><<<g, 128, 0, s>>>(a);
   else generate_joint_kernel<8><<<g, 128, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_forward(const ForwardArgs &a, cudaStream_t s) {
+  if (a.n <= 0) return cudaSuccess;
+  forward_kernel<<<(unsigned)((a.n + 127) / 128), 128, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_empirical_seeds(const EmpSeedArgs &a, cudaStream_t s) {
+  if (a.npix <= 0) return cudaSuccess;
+  const unsigned g = (unsigned)((a.npix + 127) / 128);
+  if (a.fp.n_bands == 4) empirical_seeds_kernel<4><<<g, 128, 0, s>>>(a);
+  else empirical_seeds_kernel<8><<<g, 128, 0, s>>>(a);
   return cudaGetLastError();
 }
 

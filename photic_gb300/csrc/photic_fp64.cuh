@@ -177,6 +177,40 @@ __device__ __forceinline__ void cold_start_f64(const FitParams &fp, const PixelF
   step[5] = 2.0 * start[5];
 }
 
+// samodel_Rrs (model/samodel.c:2846-2949) as the reference calls it: the
+// physical parameters as given (fabs only where the reference takes it),
+// Y from the caller's Rrs(440)/Rrs(490).  Returns Rrs; writes K.
+__device__ __forceinline__ double forward_band_f64(const SceneConsts &sc, int b, double P,
+                                                   double G, double X, double qB, double H,
+                                                   double Delta, double pw, double *K_out,
+                                                   double *parts = nullptr) {
+  const double rho = qB * sc.refl[b];
+  const double a_phi = (sc.a0[b] + sc.a1[b] * log(fabs(P))) * fabs(P);
+  const double a_g = fabs(G) * sc.eS[b];
+  const double a = sc.aw[b] + a_phi + a_g;
+  const double bb = sc.bbw[b] + X * pw;
+  const double u = bb / (a + bb);
+  double K = a + bb;
+  if (K < 0.0) K = 0.0;
+  if (K > 2.5) K = 2.5;
+  *K_out = K;
+  const double rrs_dp = (0.084 + 0.170 * u) * u;
+  const double DuC = 1.03 * sqrt(1.0 + 2.4 * u);
+  const double DuB = 1.04 * sqrt(1.0 + 5.4 * u);
+  double M = sc.sec_sun + DuC * sc.sec_view;
+  const double rrs_C = rrs_dp * (1.0 - exp(-M * K * H));
+  M = sc.sec_sun + DuB * sc.sec_view;
+  const double rrs_B = rho / kPi * exp(-M * K * H);
+  const double rrs = rrs_C + rrs_B;
+  if (parts) {  // the intermediates samodel_Rrs stores in model_data
+    parts[0] = rho;
+    parts[1] = rrs_dp;
+    parts[2] = rrs_B;
+    parts[3] = rrs;
+  }
+  return 0.5 * rrs / (1.0 - 1.5 * rrs) + Delta;
+}
+
 // (long)(10 * y) of the local-minimum test (model/asa047.c:438-470).  C
 // leaves the conversion of NaN or |v| >= 2^63 undefined; the x86-64
 // instruction returns LONG_MIN there, and that result is used here so the

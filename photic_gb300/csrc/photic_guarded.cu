@@ -948,6 +948,8 @@ __global__ void __launch_bounds__(BS) guarded_kernel(const __grid_constant__ Inv
       if (o.iod) o.iod[p] = (float)det.iod;
       if (o.evals) o.evals[p] = total;
       if (o.evals_kept) o.evals_kept[p] = kept_evals;
+      if (o.params)
+        for (int i = 0; i < kN; i++) o.params[p * kN + i] = xb[i];
       if (o.status)
         o.status[p] = PHOTIC_PX_FITTED | (kept_fault == 0 ? PHOTIC_PX_CONVERGED : 0) |
                       (kept_start << 16);

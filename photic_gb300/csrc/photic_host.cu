@@ -938,3 +938,590 @@ extern "C" int photic_invert_batch_noalloc(const photic_config *cfg, const float
   if (e != cudaSuccess) return cuda_fail(e, "invert kernel launch");
   return PHOTIC_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Link-compatible samodel entry points (include/photic_samodel.h).
+// ---------------------------------------------------------------------------
+#include "../../include/photic_samodel.h"
+
+namespace {
+
+// The reference's hard-coded nelmin tolerances (model/samodel.c:2142-2144).
+void reference_tolerances(photic_config &cfg) {
+  cfg.reqmin = 1.0e-2;
+  cfg.konvge = 100;
+  cfg.kcount = 5000;
+}
+
+// Configuration and band constants of scene s of a model_data, taking the
+// constants as the caller prepared them (model/samodel.c:521-618).
+int from_md(const photic_model_data *md, int s, photic_config &cfg, FitParams &fp,
+            SceneConsts &sc) {
+  if (!md || s < 0 || s >= md->n_scenes) return fail(PHOTIC_ERR_INVALID, "bad model_data");
+  photic_config_default(&cfg);
+  const int nb = md->n_bands[s];
+  if (nb < 2 || nb > PHOTIC_MAX_BANDS) return fail(PHOTIC_ERR_INVALID, "n_bands %d", nb);
+  cfg.n_bands = nb;
+  for (int b = 0; b < nb; b++) cfg.wavelengths[b] = md->wavelengths[s][b];
+  cfg.theta_sun_deg = md->theta_sun ? md->theta_sun[s] * (180.0 / kPiHost) : 0.0;
+  cfg.theta_view_deg = md->theta_view ? md->theta_view[s] * (180.0 / kPiHost) : 0.0;
+  cfg.h_tide = md->H_tide ? md->H_tide[s] : 0.0;
+  reference_tolerances(cfg);
+  if (md->empirical_depth_present) {
+    cfg.n_hstarts = 1;
+    cfg.hstarts[0] = md->h_empirical;
+  }
+  int rc = photic_config_check(&cfg);
+  if (rc) return rc;
+  make_fit(cfg, fp);
+  fp.aw640 = md->a_w640;
+  memset(&sc, 0, sizeof sc);
+  const int bt = md->bottom_type_indexes[0];
+  for (int b = 0; b < nb; b++) {
+    const double l = md->wavelengths[s][b];
+    sc.wl[b] = l;
+    sc.a0[b] = md->a_0[s][b];
+    sc.a1[b] = md->a_1[s][b];
+    sc.aw[b] = md->a_w[s][b];
+    sc.bbw[b] = md->b_bw[s][b];
+    sc.refl[b] = md->bottom_reflectance[bt][s][b];
+    sc.eS[b] = exp(-0.015 * (l - 440.0));
+    sc.ratio440[b] = 440.0 / l;
+  }
+  sc.sec_sun = md->sec_theta_sun[s];
+  sc.sec_view = md->sec_theta_view[s];
+  sc.h_tide = cfg.h_tide;
+  return PHOTIC_OK;
+}
+
+// Single-scene inversion with prepared constants (same kernel and launch
+// shape as photic_invert_batch).
+int invert_prepared(const photic_config &cfg, const FitParams &fp, const SceneConsts &sc,
+                    const float *d_rrs, int64_t npix, const double *d_seeds,
+                    const photic_outputs &out, cudaStream_t s) {
+  unsigned int *err = nullptr;
+  int sms = 0;
+  int rc = device_state(&err, &sms);
+  if (rc) return rc;
+  InvertArgs a;
+  memset(&a, 0, sizeof a);
+  a.fp = fp;
+  a.sc = sc;
+  make_df(cfg, a.fp, a.sc, 6, a.ds);
+  a.rrs = d_rrs;
+  a.npix = npix;
+  a.pixel_stride = cfg.n_bands;
+  a.band_stride = 1;
+  a.vec4 = cfg.n_bands == 4 && ((uintptr_t)d_rrs & 15u) == 0;
+  a.seeds = d_seeds;
+  a.out = out;
+  a.error = err;
+  a.early_exit = cfg.early_exit_per_scene * (double)(float)1;
+  a.no_mask = 1;  // the mask test belongs to samodel()'s pixel loop
+  const int block = 128;
+  int per_sm = invert_blocks_per_sm(a, PHOTIC_PREC_FP64, block);
+  if (per_sm < 1) return fail(PHOTIC_ERR_CUDA, "kernel does not fit on the device");
+  int64_t grid = (int64_t)sms * per_sm;
+  if (grid > (npix + block - 1) / block) grid = (npix + block - 1) / block;
+  unsigned long long *queue = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&queue, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return fail(PHOTIC_ERR_NOMEM, "queue head");
+  cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
+  a.queue = queue;
+  e = launch_invert(a, PHOTIC_PREC_FP64, block, (int)grid, s);
+  cudaFreeAsync(queue, s);
+  if (e != cudaSuccess) return cuda_fail(e, "invert launch");
+  return PHOTIC_OK;
+}
+
+// Cost with details at n parameter vectors, prepared constants.
+int cost_prepared(const photic_config &cfg, const FitParams &fp, const SceneConsts &sc,
+                  const float *d_rrs, const double *d_params, int64_t n, double *d_cost,
+                  double *d_rm, double *d_det, cudaStream_t s) {
+  CostArgs a;
+  memset(&a, 0, sizeof a);
+  a.fp = fp;
+  a.sc = sc;
+  make_df(cfg, a.fp, a.sc, 6, a.ds);
+  a.precision = PHOTIC_PREC_FP64;
+  a.rrs = d_rrs;
+  a.params = d_params;
+  a.n = n;
+  a.cost = d_cost;
+  a.rrs_modelled = d_rm;
+  a.details = d_det;
+  cudaError_t e = launch_cost(a, s);
+  if (e != cudaSuccess) return cuda_fail(e, "cost launch");
+  return PHOTIC_OK;
+}
+
+// Device scratch for the per-pixel drop-ins (one pixel at a time).
+struct PixelScratch {
+  unsigned char *mem = nullptr;
+  float *rrs;
+  double *params, *cost, *rm, *det, *depth64;
+  float *f[9];
+  int32_t *evals_kept, *status;
+  int alloc() {
+    const size_t bytes = 4096;
+    if (cudaMalloc((void **)&mem, bytes) != cudaSuccess)
+      return fail(PHOTIC_ERR_NOMEM, "drop-in scratch");
+    cudaMemset(mem, 0, bytes);
+    rrs = (float *)(mem);
+    params = (double *)(mem + 128);
+    cost = (double *)(mem + 256);
+    rm = (double *)(mem + 320);
+    det = (double *)(mem + 448);
+    depth64 = (double *)(mem + 512);
+    for (int i = 0; i < 9; i++) f[i] = (float *)(mem + 640 + 64 * i);
+    evals_kept = (int32_t *)(mem + 1280);
+    status = (int32_t *)(mem + 1344);
+    return PHOTIC_OK;
+  }
+  ~PixelScratch() {
+    if (mem) cudaFree(mem);
+  }
+};
+
+// Post-fit products of samodel_optimise (model/samodel.c:1994-2097) for
+// one region and one bottom type, from the kept vector and its details.
+void store_fit(photic_model_data *md, const double *best, const double *det, int s,
+               int evals_kept, int converged) {
+  md->depth = fabs(best[0]);
+  md->Rrs_error = det[0];
+  md->model_error = det[1];
+  md->bottom_albedo = det[2];
+  md->K_min = det[3];
+  md->index_optical_depth = det[4];
+  for (int k = 0; k < 12; k++) md->B_type_percent[k] = 0.0;
+  const int bt = md->bottom_type_indexes[0];
+  md->B_type_percent[bt] = 100.0 * fabs(best[2]) / fabs(best[2]);
+  md->bottom_type = 1 + bt;
+  md->P[s] = 0.01 * fabs(best[3]);
+  md->G[s] = 0.01 * fabs(best[4]);
+  md->X[s] = 0.01 * fabs(best[5]);
+  if (md->prev) {
+    md->prev[0] = fabs(best[3]);
+    md->prev[1] = fabs(best[4]);
+    md->prev[2] = fabs(best[5]);
+  }
+  md->n_iterations = evals_kept;
+  md->converged = converged;
+}
+
+bool f_close_ref(float a, float b) { return f_close(a, b, 1.0e-6f); }
+
+}  // namespace
+
+extern "C" {
+
+int photic_forward_batch(const photic_config *cfg, const double *d_params,
+                         const double *d_rrs440, const double *d_rrs490, int64_t n,
+                         double *d_rrs, double *d_K, void *stream) {
+  int rc = photic_config_check(cfg);
+  if (rc) return rc;
+  if (n < 0 || !d_params || !d_rrs440 || !d_rrs490 || !d_rrs)
+    return fail(PHOTIC_ERR_INVALID, "bad arguments");
+  ForwardArgs a;
+  memset(&a, 0, sizeof a);
+  make_fit(*cfg, a.fp);
+  make_scene(*cfg, cfg->theta_sun_deg, a.sc);
+  a.params = d_params;
+  a.rrs440 = d_rrs440;
+  a.rrs490 = d_rrs490;
+  a.n = n;
+  a.rrs = d_rrs;
+  a.K = d_K;
+  cudaError_t e = launch_forward(a, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "forward launch");
+  return PHOTIC_OK;
+}
+
+void samodel_optimise(photic_model_data *md) {
+  g_err.clear();
+  if (!md) {
+    fail(PHOTIC_ERR_INVALID, "NULL model_data");
+    return;
+  }
+  if (md->n_regions != 1 || md->n_bottoms != 1) {
+    fail(PHOTIC_ERR_UNSUPPORTED, "samodel_optimise: one region and one bottom type only");
+    return;
+  }
+  PixelScratch ps;
+  if (ps.alloc()) return;
+  const int ns = md->n_scenes;
+  photic_config cfg;
+  FitParams fp;
+  SceneConsts sc;
+  if (from_md(md, 0, cfg, fp, sc)) return;
+  const int nb = cfg.n_bands;
+  // Rrs at 440/490/550/640/750 nm per scene, stored as the reference does
+  // (model/samodel.c:1783-1799).
+  const double targets[5] = {440.0, 490.0, 550.0, 640.0, 750.0};
+  double **dst[5] = {md->Rrs440, md->Rrs490, md->Rrs550, md->Rrs640, md->Rrs750};
+  for (int s = 0; s < ns; s++)
+    for (int t = 0; t < 5; t++) {
+      double v = interp_apply(resolve_interp(md->wavelengths[s], md->n_bands[s], targets[t]),
+                              md->Rrs_measured[0][s]);
+      if (t == 0 && v < 0.0) v = 0.0001;
+      if (dst[t]) dst[t][0][s] = v;
+    }
+  if (ns == 1) {
+    float r[PHOTIC_MAX_BANDS];
+    for (int b = 0; b < nb; b++) r[b] = (float)md->Rrs_measured[0][0][b];
+    cudaMemcpy(ps.rrs, r, nb * sizeof(float), cudaMemcpyHostToDevice);
+    photic_outputs o;
+    memset(&o, 0, sizeof o);
+    o.params = ps.params;
+    o.evals_kept = ps.evals_kept;
+    o.status = ps.status;
+    // Hot start from the previous optimum (model/samodel.c:2234-2241,
+    // 2285-2305): one start whose steps are the cold-start ratios, i.e. a
+    // seed with step scale 1.
+    const double *d_seed = nullptr;
+    if (md->start_at_previous && md->prev) {
+      const double r490 = interp_apply(resolve_interp(md->wavelengths[0], nb, 490.0),
+                                       md->Rrs_measured[0][0]);
+      const double seed[6] = {md->empirical_depth_present ? md->h_empirical : md->depth_prev,
+                              100.0 * 4.0 * r490, 1.0, md->prev[0], md->prev[1], md->prev[2]};
+      cudaMemcpy(ps.depth64, seed, sizeof seed, cudaMemcpyHostToDevice);
+      d_seed = ps.depth64;
+      fp.seed_step_scale = 1.0;
+    }
+    if (invert_prepared(cfg, fp, sc, ps.rrs, 1, d_seed, o, 0)) return;
+    if (cost_prepared(cfg, fp, sc, ps.rrs, ps.params, 1, ps.cost, ps.rm, ps.det, 0)) return;
+    if (photic_sync(0)) return;
+    double best[6], det[5], rm[PHOTIC_MAX_BANDS];
+    int32_t ek = 0, st = 0;
+    cudaMemcpy(best, ps.params, sizeof best, cudaMemcpyDeviceToHost);
+    cudaMemcpy(det, ps.det, sizeof det, cudaMemcpyDeviceToHost);
+    cudaMemcpy(rm, ps.rm, nb * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaMemcpy(&ek, ps.evals_kept, sizeof ek, cudaMemcpyDeviceToHost);
+    cudaMemcpy(&st, ps.status, sizeof st, cudaMemcpyDeviceToHost);
+    if ((st & 0xFF) != PHOTIC_PX_FITTED) {
+      fail(PHOTIC_ERR_CUDA, "samodel_optimise: the fit did not complete");
+      return;
+    }
+    store_fit(md, best, det, 0, ek, (st & PHOTIC_PX_CONVERGED) != 0);
+    for (int b = 0; b < nb; b++) md->Rrs_modelled[0][0][b] = rm[b];
+    return;
+  }
+  // Temporal joint fit (n_scenes = k), reference layout.
+  if (ns > PHOTIC_MAX_SCENES) {
+    fail(PHOTIC_ERR_UNSUPPORTED, "at most %d scenes", PHOTIC_MAX_SCENES);
+    return;
+  }
+  std::vector<float> r((size_t)ns * nb);
+  std::vector<double> th(ns);
+  for (int s = 0; s < ns; s++) {
+    for (int b = 0; b < nb; b++) r[(size_t)s * nb + b] = (float)md->Rrs_measured[0][s][b];
+    th[s] = md->theta_sun[s] * (180.0 / kPiHost);
+  }
+  unsigned char *mem = nullptr;
+  if (cudaMalloc((void **)&mem, 8192) != cudaSuccess) {
+    fail(PHOTIC_ERR_NOMEM, "drop-in scratch");
+    return;
+  }
+  int32_t offs[2] = {0, ns};
+  int32_t *d_off = (int32_t *)mem;
+  double *d_th = (double *)(mem + 64);
+  float *d_r = (float *)(mem + 256);
+  double *d_depth = (double *)(mem + 1024);
+  float *d_P = (float *)(mem + 1088), *d_G = (float *)(mem + 1152), *d_X = (float *)(mem + 1216);
+  float *d_f = (float *)(mem + 1280);  // albedo, model, rrs error, K_min, iod
+  int32_t *d_i = (int32_t *)(mem + 1344);
+  cudaMemcpy(d_off, offs, sizeof offs, cudaMemcpyHostToDevice);
+  cudaMemcpy(d_th, th.data(), ns * sizeof(double), cudaMemcpyHostToDevice);
+  cudaMemcpy(d_r, r.data(), r.size() * sizeof(float), cudaMemcpyHostToDevice);
+  photic_outputs o;
+  memset(&o, 0, sizeof o);
+  o.depth_f64 = d_depth;
+  o.P = d_P;
+  o.G = d_G;
+  o.X = d_X;
+  o.bottom_albedo = d_f;
+  o.model_error = d_f + 1;
+  o.rrs_error = d_f + 2;
+  o.K_min = d_f + 3;
+  o.iod = d_f + 4;
+  o.evals_kept = d_i;
+  o.status = d_i + 1;
+  cfg.theta_sun_deg = th[0];
+  int rc = photic_joint_invert_batch(&cfg, d_off, d_th, d_r, 1, ns, &o, 0);
+  if (rc == PHOTIC_OK) rc = photic_sync(0);
+  if (rc == PHOTIC_OK) {
+    double H;
+    float P[PHOTIC_MAX_SCENES], G[PHOTIC_MAX_SCENES], X[PHOTIC_MAX_SCENES], f[5];
+    int32_t iv[2];
+    cudaMemcpy(&H, d_depth, sizeof H, cudaMemcpyDeviceToHost);
+    cudaMemcpy(P, d_P, ns * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaMemcpy(G, d_G, ns * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaMemcpy(X, d_X, ns * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaMemcpy(f, d_f, sizeof f, cudaMemcpyDeviceToHost);
+    cudaMemcpy(iv, d_i, sizeof iv, cudaMemcpyDeviceToHost);
+    md->depth = H;
+    md->bottom_albedo = f[0];
+    md->model_error = f[1];
+    md->Rrs_error = f[2];
+    md->K_min = f[3];
+    md->index_optical_depth = f[4];
+    for (int s = 0; s < ns; s++) {
+      md->P[s] = P[s];
+      md->G[s] = G[s];
+      md->X[s] = X[s];
+    }
+    for (int k = 0; k < 12; k++) md->B_type_percent[k] = 0.0;
+    md->B_type_percent[md->bottom_type_indexes[0]] = 100.0;
+    md->bottom_type = 1 + md->bottom_type_indexes[0];
+    md->n_iterations = iv[0];
+    md->converged = (iv[1] & PHOTIC_PX_CONVERGED) != 0;
+  }
+  cudaFree(mem);
+}
+
+double samodel_error(double *params, photic_model_data *md) {
+  g_err.clear();
+  if (!md || !params) {
+    fail(PHOTIC_ERR_INVALID, "NULL argument");
+    return NAN;
+  }
+  if (md->n_regions != 1 || md->n_bottoms != 1 || md->n_scenes != 1) {
+    fail(PHOTIC_ERR_UNSUPPORTED, "samodel_error: one region, one scene, one bottom type");
+    return NAN;
+  }
+  photic_config cfg;
+  FitParams fp;
+  SceneConsts sc;
+  if (from_md(md, 0, cfg, fp, sc)) return NAN;
+  PixelScratch ps;
+  if (ps.alloc()) return NAN;
+  const int nb = cfg.n_bands;
+  float r[PHOTIC_MAX_BANDS];
+  for (int b = 0; b < nb; b++) r[b] = (float)md->Rrs_measured[0][0][b];
+  cudaMemcpy(ps.rrs, r, nb * sizeof(float), cudaMemcpyHostToDevice);
+  cudaMemcpy(ps.params, params, 6 * sizeof(double), cudaMemcpyHostToDevice);
+  if (cost_prepared(cfg, fp, sc, ps.rrs, ps.params, 1, ps.cost, ps.rm, ps.det, 0)) return NAN;
+  if (photic_sync(0)) return NAN;
+  double c, det[5], rm[PHOTIC_MAX_BANDS];
+  cudaMemcpy(&c, ps.cost, sizeof c, cudaMemcpyDeviceToHost);
+  cudaMemcpy(det, ps.det, sizeof det, cudaMemcpyDeviceToHost);
+  cudaMemcpy(rm, ps.rm, nb * sizeof(double), cudaMemcpyDeviceToHost);
+  for (int b = 0; b < nb; b++) md->Rrs_modelled[0][0][b] = rm[b];
+  md->Rrs_error = det[0];
+  md->model_error = det[1];
+  md->bottom_albedo = det[2];
+  return c;
+}
+
+void samodel_Rrs(double P, double G, double X, double B[], double q[], double H, double Delta,
+                 photic_model_data *md, int k_scene, int k_band, int k_region) {
+  g_err.clear();
+  if (!md || !B || !q || md->n_bottoms != 1) {
+    fail(PHOTIC_ERR_UNSUPPORTED, "samodel_Rrs: one bottom type");
+    return;
+  }
+  photic_config cfg;
+  FitParams fp;
+  SceneConsts sc;
+  if (from_md(md, k_scene, cfg, fp, sc)) return;
+  if (k_band < 0 || k_band >= cfg.n_bands) {
+    fail(PHOTIC_ERR_INVALID, "k_band out of range");
+    return;
+  }
+  unsigned char *mem = nullptr;
+  if (cudaMalloc((void **)&mem, 1024) != cudaSuccess) {
+    fail(PHOTIC_ERR_NOMEM, "drop-in scratch");
+    return;
+  }
+  const double row[7] = {P, G, X, B[0], q[0], H, Delta};
+  const double r440 = md->Rrs440[k_region][k_scene], r490 = md->Rrs490[k_region][k_scene];
+  double *d_row = (double *)mem, *d_440 = d_row + 8, *d_490 = d_row + 9;
+  double *d_out = d_row + 16, *d_K = d_row + 32, *d_parts = d_row + 48;
+  cudaMemcpy(d_row, row, sizeof row, cudaMemcpyHostToDevice);
+  cudaMemcpy(d_440, &r440, sizeof r440, cudaMemcpyHostToDevice);
+  cudaMemcpy(d_490, &r490, sizeof r490, cudaMemcpyHostToDevice);
+  ForwardArgs a;
+  memset(&a, 0, sizeof a);
+  a.fp = fp;
+  a.sc = sc;
+  a.params = d_row;
+  a.rrs440 = d_440;
+  a.rrs490 = d_490;
+  a.n = 1;
+  a.rrs = d_out;
+  a.K = d_K;
+  a.parts = d_parts;
+  cudaError_t e = launch_forward(a, 0);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) {
+    double out[PHOTIC_MAX_BANDS], K[PHOTIC_MAX_BANDS], parts[4];
+    cudaMemcpy(out, d_out, cfg.n_bands * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaMemcpy(K, d_K, cfg.n_bands * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaMemcpy(parts, d_parts + 4 * k_band, sizeof parts, cudaMemcpyDeviceToHost);
+    md->Rrs_modelled[k_region][k_scene][k_band] = out[k_band];
+    md->K[k_scene][k_band] = K[k_band];
+    if (md->rho) md->rho[k_region][k_scene][k_band] = parts[0];
+    if (md->rrs_dp) md->rrs_dp[k_region][k_scene][k_band] = parts[1];
+    if (md->rrs_bottom) md->rrs_bottom[k_region][k_scene][k_band] = parts[2];
+    if (md->rrs_modelled) md->rrs_modelled[k_region][k_scene][k_band] = parts[3];
+    md->depth = H + sc.h_tide;       // the reference's side effects (:2873-2883)
+    md->bottom_albedo = q[0] * B[0];
+  } else {
+    cuda_fail(e, "samodel_Rrs");
+  }
+  cudaFree(mem);
+}
+
+void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scene_indexes,
+             int nscenes, int empirical_depth_present, photic_geogrid empirical_depths,
+             int n_smoothing_radius, int n_spatial, int n_bottoms, float **depth,
+             float **depth_sigma, float **model_error, float **bottom_albedo, float **bottom_sand,
+             float **bottom_seagrass, float **bottom_coral, float **K_min, float **bottom_type,
+             float **index_optical_depth, float pagesize, int background, int linewidth) {
+  g_err.clear();
+  (void)n_smoothing_radius;
+  (void)pagesize;
+  (void)background;
+  (void)linewidth;
+  if (!scene_data || !gridded_data || !scene_indexes || nscenes < 1 ||
+      nscenes > PHOTIC_MAX_SCENES) {
+    fail(PHOTIC_ERR_INVALID, "samodel: bad scenes");
+    return;
+  }
+  if (n_spatial > 1 || n_bottoms != 1) {
+    fail(PHOTIC_ERR_UNSUPPORTED, "samodel: n_spatial <= 1 and n_bottoms == 1 only");
+    return;
+  }
+  const photic_scene &s0 = scene_data[scene_indexes[0]];
+  const int nrows = s0.nrows, ncols = s0.ncols, nb = s0.n_bands;
+  photic_config cfg;
+  photic_config_default(&cfg);
+  cfg.n_bands = nb;
+  for (int b = 0; b < nb && b < PHOTIC_MAX_BANDS; b++) cfg.wavelengths[b] = s0.wavelengths[b];
+  cfg.theta_sun_deg = s0.theta_w;
+  cfg.theta_view_deg = s0.theta_v;
+  cfg.h_tide = s0.H_tide;
+  reference_tolerances(cfg);
+  if (photic_config_check(&cfg)) return;
+  for (int k = 1; k < nscenes; k++) {
+    const photic_scene &sk = scene_data[scene_indexes[k]];
+    if (sk.n_bands != nb || sk.nrows != nrows || sk.ncols != ncols) {
+      fail(PHOTIC_ERR_UNSUPPORTED, "samodel: scenes must share grid and bands");
+      return;
+    }
+  }
+  const int64_t npix = (int64_t)nrows * ncols;
+  const int64_t nobs = npix * nscenes;
+  // Gather the band grids into [pixel][scene][band] with one nodata marker.
+  std::vector<float> h_rrs((size_t)nobs * nb);
+  for (int k = 0; k < nscenes; k++) {
+    const photic_scene &sk = scene_data[scene_indexes[k]];
+    for (int b = 0; b < nb; b++) {
+      const photic_geogrid &g = gridded_data[sk.band_indexes[b]];
+      for (int i = 0; i < nrows; i++)
+        for (int j = 0; j < ncols; j++) {
+          float v = g.array[i][j];
+          if (f_close_ref(v, g.nodata_value)) v = cfg.nodata_value;
+          h_rrs[(((size_t)i * ncols + j) * nscenes + k) * nb + b] = v;
+        }
+    }
+  }
+  std::vector<double> h_emp;
+  if (empirical_depth_present && nscenes == 1) {
+    h_emp.assign((size_t)npix, NAN);
+    for (int i = 0; i < nrows; i++)
+      for (int j = 0; j < ncols; j++) {
+        const float e = empirical_depths.array[i][j];
+        if (!f_close_ref(e, empirical_depths.nodata_value))  // model/samodel.c:960-967
+          h_emp[(size_t)i * ncols + j] = e > -1.0f ? 1.0 : fabs((double)e);
+      }
+  }
+  // device buffers
+  float *d_rrs = nullptr;
+  double *d_depth = nullptr, *d_seeds = nullptr, *d_emp = nullptr, *d_th = nullptr;
+  float *d_f = nullptr;
+  int32_t *d_status = nullptr, *d_off = nullptr;
+  bool ok = cudaMalloc((void **)&d_rrs, h_rrs.size() * sizeof(float)) == cudaSuccess &&
+            cudaMalloc((void **)&d_depth, npix * sizeof(double)) == cudaSuccess &&
+            cudaMalloc((void **)&d_f, 4 * npix * sizeof(float)) == cudaSuccess &&
+            cudaMalloc((void **)&d_status, npix * sizeof(int32_t)) == cudaSuccess;
+  if (!ok) {
+    fail(PHOTIC_ERR_NOMEM, "samodel: device buffers");
+  } else {
+    cudaMemcpy(d_rrs, h_rrs.data(), h_rrs.size() * sizeof(float), cudaMemcpyHostToDevice);
+    photic_outputs o;
+    memset(&o, 0, sizeof o);
+    o.depth_f64 = d_depth;
+    o.rrs_error = d_f;
+    o.bottom_albedo = d_f + npix;
+    o.K_min = d_f + 2 * npix;
+    o.iod = d_f + 3 * npix;
+    o.status = d_status;
+    int rc;
+    if (nscenes == 1) {
+      if (!h_emp.empty()) {
+        cudaMalloc((void **)&d_emp, npix * sizeof(double));
+        cudaMalloc((void **)&d_seeds, npix * 6 * sizeof(double));
+        cudaMemcpy(d_emp, h_emp.data(), npix * sizeof(double), cudaMemcpyHostToDevice);
+        EmpSeedArgs ea;
+        memset(&ea, 0, sizeof ea);
+        make_fit(cfg, ea.fp);
+        make_scene(cfg, cfg.theta_sun_deg, ea.sc);
+        ea.rrs = d_rrs;
+        ea.h = d_emp;
+        ea.npix = npix;
+        ea.seeds = d_seeds;
+        launch_empirical_seeds(ea, 0);
+      }
+      rc = photic_invert_batch(&cfg, d_rrs, npix, nb, 1, d_seeds, &o, 0);
+    } else {
+      std::vector<int32_t> offs((size_t)npix + 1);
+      std::vector<double> th((size_t)nobs);
+      for (int64_t p = 0; p <= npix; p++) offs[p] = (int32_t)(p * nscenes);
+      for (int64_t p = 0; p < npix; p++)
+        for (int k = 0; k < nscenes; k++)
+          th[(size_t)(p * nscenes + k)] = scene_data[scene_indexes[k]].theta_w;
+      cudaMalloc((void **)&d_off, offs.size() * sizeof(int32_t));
+      cudaMalloc((void **)&d_th, th.size() * sizeof(double));
+      cudaMemcpy(d_off, offs.data(), offs.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+      cudaMemcpy(d_th, th.data(), th.size() * sizeof(double), cudaMemcpyHostToDevice);
+      rc = photic_joint_invert_batch(&cfg, d_off, d_th, d_rrs, npix, nobs, &o, 0);
+    }
+    if (rc == PHOTIC_OK) rc = photic_sync(0);
+    if (rc == PHOTIC_OK) {
+      std::vector<double> H((size_t)npix);
+      std::vector<float> f((size_t)4 * npix);
+      std::vector<int32_t> st((size_t)npix);
+      cudaMemcpy(H.data(), d_depth, npix * sizeof(double), cudaMemcpyDeviceToHost);
+      cudaMemcpy(f.data(), d_f, 4 * npix * sizeof(float), cudaMemcpyDeviceToHost);
+      cudaMemcpy(st.data(), d_status, npix * sizeof(int32_t), cudaMemcpyDeviceToHost);
+      // outputs as the reference's pixel loop leaves them (:820-831,
+      // :1120-1164), depth negative below the datum (:1486-1490)
+      for (int i = 0; i < nrows; i++)
+        for (int j = 0; j < ncols; j++) {
+          const size_t p = (size_t)i * ncols + j;
+          const bool fit = (st[p] & 0xFF) == PHOTIC_PX_FITTED;
+          depth[i][j] = fit ? (float)H[p] * -1.0f : 0.0f * -1.0f;
+          if (depth_sigma) depth_sigma[i][j] = 0.0f;
+          model_error[i][j] = fit ? f[p] : 0.0f;
+          bottom_albedo[i][j] = fit ? f[npix + p] : 0.0f;
+          bottom_sand[i][j] = fit ? 100.0f : -9999.0f;
+          bottom_seagrass[i][j] = fit ? 0.0f : -9999.0f;
+          bottom_coral[i][j] = fit ? 0.0f : -9999.0f;
+          K_min[i][j] = fit ? f[2 * npix + p] : 0.0f;
+          bottom_type[i][j] = fit ? 1.0f : -9999.0f;
+          index_optical_depth[i][j] = fit ? f[3 * npix + p] : 0.0f;
+        }
+    }
+  }
+  cudaFree(d_rrs);
+  cudaFree(d_depth);
+  cudaFree(d_f);
+  cudaFree(d_status);
+  if (d_emp) cudaFree(d_emp);
+  if (d_seeds) cudaFree(d_seeds);
+  if (d_off) cudaFree(d_off);
+  if (d_th) cudaFree(d_th);
+}
+
+}  // extern "C"

@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(BS) invert_kernel(const __grid_constant__ Inve
         for (int b = 0; b < NB; b++) r[b] = wchunk[(p - chunk_base) * NB + b];
 #pragma unroll
         for (int b = 0; b < NB; b++)
-          if (b < fp.n_bands && band_masked(r[b], fp.nodata)) masked = true;
+          if (b < fp.n_bands && !args.no_mask && band_masked(r[b], fp.nodata)) masked = true;
         if (masked) {
           write_masked(o, p);
         } else {
@@ -310,6 +310,8 @@ __global__ void __launch_bounds__(BS) invert_kernel(const __grid_constant__ Inve
         if (o.iod) o.iod[p] = (float)det.iod;
         if (o.evals) o.evals[p] = total;
         if (o.evals_kept) o.evals_kept[p] = kept_evals;
+        if (o.params)
+          for (int i = 0; i < kN; i++) o.params[p * kN + i] = P::to_double(m.x[i]);
         if (o.status)
           o.status[p] = PHOTIC_PX_FITTED | (kept_fault == 0 ? PHOTIC_PX_CONVERGED : 0) |
                         (kept_start << 16);

@@ -30,6 +30,7 @@ struct InvertArgs {
   unsigned int *error;
   unsigned long long *counters;  // optional: exact evaluations served (guarded)
   double early_exit;  // early-exit cost threshold (per-scene value * scenes)
+  int32_t no_mask;    // fit every pixel: samodel_optimise has no mask test
 };
 
 size_t invert_smem_bytes(int block, int nb);
@@ -63,6 +64,7 @@ struct CostArgs {
   int64_t n;
   double *cost;
   double *rrs_modelled;
+  double *details;  // optional [n][5]: Rrs error, model error, albedo, K_min, IOD
 };
 cudaError_t launch_cost(const CostArgs &a, cudaStream_t s);
 
@@ -159,6 +161,27 @@ cudaError_t mlp_denorm(const MlpState &st, const MlpWork &w, int R, float *y, cu
 cudaError_t mlp_features(const float *rrs, int64_t npix, int nb, float th_sun, float th_view,
                          float *x, cudaStream_t s);
 cudaError_t mlp_seeds(const SeedArgs &a, cudaStream_t s);
+
+struct ForwardArgs {
+  FitParams fp;
+  SceneConsts sc;
+  const double *params;  // [n][7]: P, G, X, B, q, H, Delta
+  const double *rrs440, *rrs490;
+  int64_t n;
+  double *rrs, *K;       // [n][n_bands]
+  double *parts;         // optional [n][n_bands][4]: rho, rrs_dp, rrs_bottom, rrs
+};
+cudaError_t launch_forward(const ForwardArgs &a, cudaStream_t s);
+
+struct EmpSeedArgs {
+  FitParams fp;
+  SceneConsts sc;
+  const float *rrs;      // [npix][n_bands]
+  const double *h;       // [npix] empirical depth, NaN = none
+  int64_t npix;
+  double *seeds;         // [npix][6]
+};
+cudaError_t launch_empirical_seeds(const EmpSeedArgs &a, cudaStream_t s);
 
 // Throughput probes (TFLOP/s of FP64 and FP32 FMA, Tops/s of MUFU ex2).
 cudaError_t measure_peaks(double *fp64_tflops, double *fp32_tflops, double *mufu_tops);

@@ -1,0 +1,132 @@
+"""GPU parity of the link-compatible drop-ins (samodel_optimise,
+samodel_error, samodel_Rrs, samodel) called from a C program the way the
+reference's own code calls them, against the oracle run with the reference's
+hard-coded nelmin tolerances (1e-2, 100, 5000; model/samodel.c:2142-2144).
+
+Bars follow the batch inversion tests: the cost and forward model agree to
+1e-13 relative (CUDA vs glibc last-ulp exp / log / pow), and fits agree
+pixel for pixel except where such a last-ulp difference decides a
+Nelder-Mead comparison (>= 97% identical depths, median |dH| <= 1 cm).
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from tests.test_dropin_layout import build_driver
+
+pytestmark = pytest.mark.gpu
+
+OLI = np.array([443.0, 482.0, 561.0, 655.0])
+TH_SUN, TH_VIEW = 35.0, 0.0
+
+
+def _write_input(path, rrs, params=None, nrows=0, ncols=0):
+    npix, nb = rrs.shape
+    if params is None:
+        params = np.zeros((npix, 6))
+    with open(path, "wb") as f:
+        np.array([nb, npix, nrows, ncols], dtype=np.int32).tofile(f)
+        OLI.astype(np.float64).tofile(f)
+        np.array([TH_SUN, TH_VIEW]).tofile(f)
+        np.ascontiguousarray(rrs, dtype=np.float32).tofile(f)
+        np.ascontiguousarray(params, dtype=np.float64).tofile(f)
+
+
+def _run(exe, mode, inp, out):
+    r = subprocess.run([exe, mode, inp, out], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, (mode, r.returncode, r.stderr[-2000:])
+
+
+@pytest.fixture(scope="module")
+def driver(tmp_path_factory, gpu):
+    return build_driver(tmp_path_factory.mktemp("dropin"))
+
+
+def test_samodel_error_and_rrs(driver, golden_dir, tmp_path):
+    g = np.load(os.path.join(golden_dir, "cost_nelmin.npz"))
+    inp, out = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    _write_input(inp, g["rrs"], g["params"])
+    _run(driver, "error", inp, out)
+    e = np.fromfile(out, dtype=np.float64).reshape(len(g["cost"]), 5)
+    np.testing.assert_allclose(e[:, 0], g["cost"], rtol=1e-13)
+    np.testing.assert_allclose(e[:, 1:], g["rrs_modelled"], rtol=1e-13)
+    _run(driver, "rrs", inp, out)
+    r = np.fromfile(out, dtype=np.float64).reshape(len(g["cost"]), 8)
+    np.testing.assert_allclose(r[:, :4], g["rrs_modelled"], rtol=1e-13)
+    np.testing.assert_allclose(r[:, 4:], g["K"], rtol=1e-13)
+
+
+def test_samodel_optimise_matches_oracle(driver, port, tmp_path):
+    rrs, _ = port.generate_single(20260301, 160, pix0=777, mask_frac=0.0)
+    inp, out = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    _write_input(inp, rrs)
+    _run(driver, "optimise", inp, out)
+    d = np.fromfile(out, dtype=np.float64).reshape(len(rrs), 18)[:, 4:]
+    ref = port.invert_batch(rrs, reqmin=None, nthreads=os.cpu_count() or 1)
+    # samodel_optimise fits every spectrum it is given (the mask test is
+    # samodel()'s); the oracle's batch masks negative bands, so compare the
+    # spectra it fits
+    assert np.isfinite(d[:, 0]).all()
+    fit = ref[:, 9] == 0
+    assert fit.mean() > 0.9
+    d, ref = d[fit], ref[fit]
+    dh = np.abs(d[:, 0] - ref[:, 0])
+    same = dh == 0.0
+    assert np.median(dh) <= 0.01 and same.mean() >= 0.97, (np.median(dh), same.mean())
+    # where the trajectories agree, every product agrees
+    cols = [(1, 11), (2, 19), (3, 27), (4, 1), (5, 2), (6, 3), (7, 4), (8, 5), (9, 6), (10, 8)]
+    for c, rc in cols:
+        np.testing.assert_allclose(d[same, c], ref[same, rc], rtol=1e-9, atol=1e-12,
+                                   err_msg=f"column {c}")
+    # 100 |q| / q_sum over the one bottom type: 100 up to its rounding
+    np.testing.assert_allclose(d[:, 12], 100.0, rtol=1e-15)
+    assert (d[:, 13] == 1).all()
+    r440 = np.array([port.interp_1d(OLI, rrs[i].astype(np.float64), 440.0)
+                     for i in range(len(rrs))])[fit]
+    np.testing.assert_array_equal(d[:, 11], np.where(r440 < 0, 1e-4, r440))
+
+
+def test_samodel_optimise_start_at_previous(driver, port, tmp_path):
+    rrs, _ = port.generate_single(20260302, 64, pix0=99, mask_frac=0.0)
+    inp, out = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    _write_input(inp, rrs)
+    _run(driver, "prev", inp, out)
+    d = np.fromfile(out, dtype=np.float64).reshape(len(rrs), 18)
+    used, res = d[1:, :4], d[1:, 4:]
+    # the oracle fits each pixel from the start the library was given:
+    # (depth_prev, 400 Rrs(490), 1, prev P, G, X), cold-start step ratios
+    r490 = np.array([port.interp_1d(OLI, rrs[i].astype(np.float64), 490.0)
+                     for i in range(1, len(rrs))])
+    seeds = np.stack([used[:, 0], 100.0 * 4.0 * r490, np.ones(len(r490)),
+                      used[:, 1], used[:, 2], used[:, 3]], axis=1)
+    ref = port.invert_batch(rrs[1:], reqmin=None, seeds=seeds, seed_step_scale=1.0)
+    fit = ref[:, 9] == 0
+    res, ref = res[fit], ref[fit]
+    dh = np.abs(res[:, 0] - ref[:, 0])
+    assert np.median(dh) <= 0.01 and np.mean(dh == 0.0) >= 0.95, (np.median(dh), np.mean(dh == 0))
+    np.testing.assert_array_equal(res[dh == 0, 9], ref[dh == 0, 6])
+
+
+def test_samodel_grid_matches_oracle(driver, port, tmp_path):
+    nrows, ncols = 24, 20
+    rrs, _ = port.generate_single(20260303, nrows * ncols, pix0=4242, mask_frac=0.15)
+    inp, out = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    _write_input(inp, rrs, nrows=nrows, ncols=ncols)
+    _run(driver, "grid", inp, out)
+    g = np.fromfile(out, dtype=np.float32).reshape(10, nrows * ncols)
+    ref = port.invert_batch(rrs, reqmin=None, nthreads=os.cpu_count() or 1)
+    fit = ref[:, 9] == 0
+    assert 0 < fit.sum() < len(fit)
+    # masked pixels keep the reference's defaults
+    assert (g[0, ~fit] == 0).all() and (g[4, ~fit] == -9999).all() and (g[8, ~fit] == -9999).all()
+    assert (g[4, fit] == 100).all() and (g[5, fit] == 0).all() and (g[8, fit] == 1).all()
+    # depth is written negative below the datum, in float
+    dh = np.abs(-g[0, fit] - ref[fit, 0].astype(np.float32))
+    assert np.median(dh) <= 0.01 and np.mean(dh == 0) >= 0.97, (np.median(dh), np.mean(dh == 0))
+    same = dh == 0
+    # the model-error grid holds the Rrs error (model/samodel.c:1120)
+    np.testing.assert_allclose(g[2, fit][same], ref[fit, 3][same].astype(np.float32), rtol=1e-6)
+    np.testing.assert_allclose(g[3, fit][same], ref[fit, 1][same].astype(np.float32), rtol=1e-6)
+    np.testing.assert_allclose(g[7, fit][same], ref[fit, 4][same].astype(np.float32), rtol=1e-6)
