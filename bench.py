@@ -161,6 +161,9 @@ def main():
     ap.add_argument("--train-forward", type=int, default=1 << 23)
     ap.add_argument("--train-inverted", type=int, default=1 << 20)
     ap.add_argument("--train-epochs", type=int, default=4)
+    ap.add_argument("--serve-requests", type=int, default=12,
+                    help="tile requests of the serving leg (0: skip)")
+    ap.add_argument("--serve-rate", type=float, default=50.0)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -307,9 +310,11 @@ def main():
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{n} pixels of the same generator, {dt:.1f} s on {threads} threads"}
 
-    warm = None
+    warm, net, serving = None, None, None
     if rank == 0 and args.warm_npix > 0:
-        warm = warm_start_leg(args, dev)
+        net, warm = warm_start_leg(args, dev)
+    if rank == 0 and args.serve_requests > 0:
+        serving = serving_leg(args, net)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
@@ -328,7 +333,7 @@ def main():
                            "within_1cm_of_fp64": int(within.sum()),
                            "mean_evals": float(evals[fitted].mean()) if fitted.any() else 0.0},
                 "oracle_sample": sample_stats, "roofline": roof, "cpu_baseline": cpu,
-                "warm_start": warm,
+                "warm_start": warm, "serving": serving,
                 "e2e": e2e, "clocks": clk}
         print(json.dumps(line))
     if pg_ is not None:
@@ -389,7 +394,7 @@ def warm_start_leg(args, dev):
     within = float(np.mean(d <= 0.01)) if m.any() else 1.0
     v_cold = float(cc.sum().item()) / t_cold
     v_warm = float(cw.sum().item()) * within / (t_warm + t_seed)
-    return {"workload": f"{n} pixels of the 8192x8192 plain-method scene",
+    return net, {"workload": f"{n} pixels of the 8192x8192 plain-method scene",
             "cold_px_s": v_cold, "warm_px_s": v_warm, "speedup": v_warm / v_cold,
             "seeded_share": float(seeded.float().mean().item()),
             "evals_per_pixel_cold": float(cold["evals"].float()[cc].mean().item()),
@@ -402,6 +407,25 @@ def warm_start_leg(args, dev):
                                         "median_abs_dH_m": float(np.median(d)) if m.any() else 0.0,
                                         "p99_abs_dH_m": float(np.quantile(d, 0.99)) if m.any() else 0.0,
                                         "frac_within_1cm": within}}
+
+
+def serving_leg(args, net):
+    """Tile requests (square, side logU(256, 4096), Poisson arrivals)
+    through the serving loop, plain cold start and, when a trained network
+    is at hand, warm start; same schedule for both."""
+    import torch
+    from photic_gb300 import serve as S
+    sched = lambda: S.poisson_schedule(args.serve_requests, rate=args.serve_rate)
+    out = {"schedule": {"requests": args.serve_requests, "rate_per_s": args.serve_rate,
+                        "side": "logU(256, 4096)", "seed": 20260404,
+                        "pixels": sum(r.npix for r in sched())}}
+    # the kernels and allocator are warm from the legs before
+    out["cold"] = S.serve(sched())
+    if net is not None:
+        out["warm"] = S.serve(sched(), surrogate=net)
+        out["warm_vs_cold_px_s"] = out["warm"]["px_s"] / out["cold"]["px_s"]
+    torch.cuda.empty_cache()
+    return out
 
 
 # Algorithmic double-precision operations of one cost evaluation at 4 bands

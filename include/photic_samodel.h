@@ -167,6 +167,13 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
  * index of optical depth, n_iterations, converged and Rrs_modelled. */
 void samodel_optimise(photic_model_data *md);
 
+/* model/samodel.h:23.  The fit of md's one scene, region and bottom type
+ * (cold multi-start, empirical depth or start_at_previous, as
+ * samodel_optimise): writes |best| into params[0..5] (H, 100 B, q, 100 P,
+ * 100 G, 100 X), md->n_iterations, converged and what the final cost leaves
+ * (Rrs_modelled, Rrs_error, model_error, bottom_albedo, depth). */
+void samodel_optimise_one_bottom_combination(photic_model_data *md, double *params);
+
 /* model/samodel.h:25.  Cost of params for md's first region; also writes
  * md->Rrs_modelled[0][s][b], Rrs_error and model_error. */
 double samodel_error(double *params, photic_model_data *md);

@@ -1109,6 +1109,51 @@ void store_fit(photic_model_data *md, const double *best, const double *det, int
   md->converged = converged;
 }
 
+// The single-scene fit of samodel_optimise_one_bottom_combination
+// (model/samodel.c:2119-2427) for md's one region and bottom type: the kept
+// vector (signed, as nelmin left it), the cost details and modelled Rrs at
+// it, the evaluations of the kept start and the pixel status.
+int fit_single(photic_model_data *md, const photic_config &cfg, FitParams fp,
+               const SceneConsts &sc, PixelScratch &ps, double best[6], double det[5],
+               double *rm, int32_t *ek, int32_t *st) {
+  const int nb = cfg.n_bands;
+  float r[PHOTIC_MAX_BANDS];
+  for (int b = 0; b < nb; b++) r[b] = (float)md->Rrs_measured[0][0][b];
+  cudaMemcpy(ps.rrs, r, nb * sizeof(float), cudaMemcpyHostToDevice);
+  photic_outputs o;
+  memset(&o, 0, sizeof o);
+  o.params = ps.params;
+  o.evals_kept = ps.evals_kept;
+  o.status = ps.status;
+  // Hot start from the previous optimum (model/samodel.c:2234-2241,
+  // 2285-2305): one start whose steps are the cold-start ratios, i.e. a
+  // seed with step scale 1.
+  const double *d_seed = nullptr;
+  if (md->start_at_previous && md->prev) {
+    const double r490 = interp_apply(resolve_interp(md->wavelengths[0], nb, 490.0),
+                                     md->Rrs_measured[0][0]);
+    const double seed[6] = {md->empirical_depth_present ? md->h_empirical : md->depth_prev,
+                            100.0 * 4.0 * r490, 1.0, md->prev[0], md->prev[1], md->prev[2]};
+    cudaMemcpy(ps.depth64, seed, sizeof seed, cudaMemcpyHostToDevice);
+    d_seed = ps.depth64;
+    fp.seed_step_scale = 1.0;
+  }
+  int rc = invert_prepared(cfg, fp, sc, ps.rrs, 1, d_seed, o, 0);
+  if (rc) return rc;
+  rc = cost_prepared(cfg, fp, sc, ps.rrs, ps.params, 1, ps.cost, ps.rm, ps.det, 0);
+  if (rc) return rc;
+  rc = photic_sync(0);
+  if (rc) return rc;
+  cudaMemcpy(best, ps.params, 6 * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaMemcpy(det, ps.det, 5 * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaMemcpy(rm, ps.rm, nb * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaMemcpy(ek, ps.evals_kept, sizeof *ek, cudaMemcpyDeviceToHost);
+  cudaMemcpy(st, ps.status, sizeof *st, cudaMemcpyDeviceToHost);
+  if ((*st & 0xFF) != PHOTIC_PX_FITTED)
+    return fail(PHOTIC_ERR_CUDA, "the fit did not complete");
+  return PHOTIC_OK;
+}
+
 bool f_close_ref(float a, float b) { return f_close(a, b, 1.0e-6f); }
 
 }  // namespace
@@ -1167,41 +1212,9 @@ void samodel_optimise(photic_model_data *md) {
       if (dst[t]) dst[t][0][s] = v;
     }
   if (ns == 1) {
-    float r[PHOTIC_MAX_BANDS];
-    for (int b = 0; b < nb; b++) r[b] = (float)md->Rrs_measured[0][0][b];
-    cudaMemcpy(ps.rrs, r, nb * sizeof(float), cudaMemcpyHostToDevice);
-    photic_outputs o;
-    memset(&o, 0, sizeof o);
-    o.params = ps.params;
-    o.evals_kept = ps.evals_kept;
-    o.status = ps.status;
-    // Hot start from the previous optimum (model/samodel.c:2234-2241,
-    // 2285-2305): one start whose steps are the cold-start ratios, i.e. a
-    // seed with step scale 1.
-    const double *d_seed = nullptr;
-    if (md->start_at_previous && md->prev) {
-      const double r490 = interp_apply(resolve_interp(md->wavelengths[0], nb, 490.0),
-                                       md->Rrs_measured[0][0]);
-      const double seed[6] = {md->empirical_depth_present ? md->h_empirical : md->depth_prev,
-                              100.0 * 4.0 * r490, 1.0, md->prev[0], md->prev[1], md->prev[2]};
-      cudaMemcpy(ps.depth64, seed, sizeof seed, cudaMemcpyHostToDevice);
-      d_seed = ps.depth64;
-      fp.seed_step_scale = 1.0;
-    }
-    if (invert_prepared(cfg, fp, sc, ps.rrs, 1, d_seed, o, 0)) return;
-    if (cost_prepared(cfg, fp, sc, ps.rrs, ps.params, 1, ps.cost, ps.rm, ps.det, 0)) return;
-    if (photic_sync(0)) return;
     double best[6], det[5], rm[PHOTIC_MAX_BANDS];
     int32_t ek = 0, st = 0;
-    cudaMemcpy(best, ps.params, sizeof best, cudaMemcpyDeviceToHost);
-    cudaMemcpy(det, ps.det, sizeof det, cudaMemcpyDeviceToHost);
-    cudaMemcpy(rm, ps.rm, nb * sizeof(double), cudaMemcpyDeviceToHost);
-    cudaMemcpy(&ek, ps.evals_kept, sizeof ek, cudaMemcpyDeviceToHost);
-    cudaMemcpy(&st, ps.status, sizeof st, cudaMemcpyDeviceToHost);
-    if ((st & 0xFF) != PHOTIC_PX_FITTED) {
-      fail(PHOTIC_ERR_CUDA, "samodel_optimise: the fit did not complete");
-      return;
-    }
+    if (fit_single(md, cfg, fp, sc, ps, best, det, rm, &ek, &st)) return;
     store_fit(md, best, det, 0, ek, (st & PHOTIC_PX_CONVERGED) != 0);
     for (int b = 0; b < nb; b++) md->Rrs_modelled[0][0][b] = rm[b];
     return;
@@ -1277,6 +1290,37 @@ void samodel_optimise(photic_model_data *md) {
     md->converged = (iv[1] & PHOTIC_PX_CONVERGED) != 0;
   }
   cudaFree(mem);
+}
+
+void samodel_optimise_one_bottom_combination(photic_model_data *md, double *params) {
+  g_err.clear();
+  if (!md || !params) {
+    fail(PHOTIC_ERR_INVALID, "NULL argument");
+    return;
+  }
+  if (md->n_regions != 1 || md->n_bottoms != 1 || md->n_scenes != 1) {
+    fail(PHOTIC_ERR_UNSUPPORTED,
+         "samodel_optimise_one_bottom_combination: one region, scene and bottom type");
+    return;
+  }
+  photic_config cfg;
+  FitParams fp;
+  SceneConsts sc;
+  if (from_md(md, 0, cfg, fp, sc)) return;
+  PixelScratch ps;
+  if (ps.alloc()) return;
+  double best[6], det[5], rm[PHOTIC_MAX_BANDS];
+  int32_t ek = 0, st = 0;
+  if (fit_single(md, cfg, fp, sc, ps, best, det, rm, &ek, &st)) return;
+  for (int i = 0; i < 6; i++) params[i] = fabs(best[i]);  // model/samodel.c:2415-2417
+  md->n_iterations = ek;
+  md->converged = (st & PHOTIC_PX_CONVERGED) != 0;
+  // what the final samodel_error(best) leaves in md (model/samodel.c:2413)
+  for (int b = 0; b < cfg.n_bands; b++) md->Rrs_modelled[0][0][b] = rm[b];
+  md->Rrs_error = det[0];
+  md->model_error = det[1];
+  md->bottom_albedo = det[2];
+  md->depth = fabs(best[0]) + cfg.h_tide;
 }
 
 double samodel_error(double *params, photic_model_data *md) {

@@ -15,6 +15,9 @@
  *                   converged, Rrs440, B_type_percent[0], bottom_type
  *        prev     : as optimise, but each pixel after the first starts at
  *                   the previous pixel's optimum (start_at_previous)
+ *        combo    : samodel_optimise_one_bottom_combination; OUT = double
+ *                   [npix][8] (|best| H, 100 B, q, 100 P, 100 G, 100 X,
+ *                   n_iterations, converged)
  *        error    : OUT = double [npix][1 + n_bands] (cost, Rrs_modelled)
  *        rrs      : OUT = double [npix][2 * n_bands] (Rrs_modelled, K) at
  *                   the model inputs samodel_error derives from params
@@ -202,6 +205,12 @@ int main(int argc, char **argv) {
                               md->B_type_percent[0], md->bottom_type};
       fwrite(row, sizeof row, 1, o);
       md->depth_prev = md->depth;
+    } else if (!strcmp(mode, "combo")) {
+      double x[8];
+      samodel_optimise_one_bottom_combination(md, x);
+      x[6] = md->n_iterations;
+      x[7] = md->converged;
+      fwrite(x, sizeof x, 1, o);
     } else if (!strcmp(mode, "error")) {
       double x[6];
       memcpy(x, params + (size_t)p * 6, sizeof x);

@@ -88,6 +88,25 @@ def test_samodel_optimise_matches_oracle(driver, port, tmp_path):
     np.testing.assert_array_equal(d[:, 11], np.where(r440 < 0, 1e-4, r440))
 
 
+def test_one_bottom_combination(driver, port, tmp_path):
+    rrs, _ = port.generate_single(20260304, 96, pix0=31337, mask_frac=0.0)
+    inp, out = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    _write_input(inp, rrs)
+    _run(driver, "combo", inp, out)
+    d = np.fromfile(out, dtype=np.float64).reshape(len(rrs), 8)
+    ref = port.invert_batch(rrs, reqmin=None, nthreads=os.cpu_count() or 1)
+    fit = ref[:, 9] == 0
+    d, ref = d[fit], ref[fit]
+    same = d[:, 0] == ref[:, 0]
+    assert same.mean() >= 0.95, same.mean()
+    # P, G, X are stored as 0.01 |best| by samodel_optimise
+    for c, rc in ((3, 11), (4, 19), (5, 27)):
+        np.testing.assert_allclose(0.01 * d[same, c], ref[same, rc], rtol=1e-9)
+    assert np.mean(d[same, 6] == ref[same, 6]) >= 0.9
+    np.testing.assert_array_equal(d[same, 7], ref[same, 8])
+    assert (d[:, :6] >= 0).all()
+
+
 def test_samodel_optimise_start_at_previous(driver, port, tmp_path):
     rrs, _ = port.generate_single(20260302, 64, pix0=99, mask_frac=0.0)
     inp, out = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
