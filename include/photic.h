@@ -193,6 +193,20 @@ double photic_interp_1d(const double *X, const double *Y, int32_t n, double x);
  * a_w(640). */
 int photic_band_constants(const photic_config *cfg, double *out);
 
+/* Launch-shape autotuner (new; no reference counterpart).  Times the
+ * inversion (kind PHOTIC_TUNE_INVERT: block_threads 64/128/256 x blocks per
+ * SM 0 (occupancy limit)/2/3/4) or the temporal joint fit (PHOTIC_TUNE_JOINT:
+ * blocks per SM 2/3/4/6/8) on a seeded synthetic sample of sample_npix
+ * pixels of cfg's workload, each candidate once untimed and once timed with
+ * CUDA events, and writes the fastest into cfg->block_threads and
+ * cfg->blocks_per_sm.  results (optional, max_results rows of 3 doubles)
+ * receives (block_threads, blocks_per_sm, ms) per candidate.  Fits are
+ * independent of the launch shape, so any choice gives the same outputs.
+ * Synchronous on the legacy default stream. */
+enum { PHOTIC_TUNE_INVERT = 0, PHOTIC_TUNE_JOINT = 1 };
+int photic_autotune(photic_config *cfg, int32_t kind, int64_t sample_npix, double *results,
+                    int32_t max_results, int32_t *n_results);
+
 /* Waits for the stream, then reports any error recorded by the device
  * (bounded-wait timeouts, invalid inputs) since the previous call. */
 int photic_sync(void *stream);

@@ -174,7 +174,7 @@ def invert_batch(rrs, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0, h_tide=0.
 
 def joint_invert_batch(scene_offsets, theta_sun, rrs, *, wl=OLI_BANDS, theta_view=0.0,
                        h_tide=0.0, nodata=-9999.0, layout=0, reqmin=1e-10, konvge=100,
-                       kcount=2000, nthreads=0, which="port"):
+                       kcount=2000, hstarts=None, nthreads=0, which="port"):
     offs = np.ascontiguousarray(scene_offsets, dtype=np.int32)
     th = _f64(theta_sun)
     rrs = _f32(rrs)
@@ -191,9 +191,11 @@ def joint_invert_batch(scene_offsets, theta_sun, rrs, *, wl=OLI_BANDS, theta_vie
                                         kcount, nthreads, _ptr(out, _dp))
         return out
     L = port().lib
+    hs = _f64(hstarts) if hstarts is not None else None
     rc = L.po_joint_invert_batch(rrs.shape[1], _ptr(wl, _dp), theta_view, h_tide,
                                  offs.ctypes.data_as(_i32p), _ptr(th, _dp), _ptr(rrs, _fp),
-                                 npix, nodata, layout, reqmin, konvge, kcount, 0, None,
+                                 npix, nodata, layout, reqmin, konvge, kcount,
+                                 0 if hs is None else len(hs), _ptr(hs, _dp),
                                  nthreads, _ptr(out, _dp))
     if rc:
         raise ValueError(f"po_joint_invert_batch failed ({rc})")

@@ -4,5 +4,5 @@ the reference's modified AS 47 Nelder-Mead -- behind a C ABI
 (include/photic.h) and this thin Python host layer over it.
 """
 from . import api  # noqa: F401
-from .api import (Config, PhoticError, alloc_outputs, cost, generate_joint,  # noqa: F401
-                  generate_scene, invert, joint_invert, sync, version)
+from .api import (Config, JointGraph, PhoticError, alloc_outputs, cost,  # noqa: F401
+                  generate_joint, generate_scene, invert, joint_invert, sync, version)

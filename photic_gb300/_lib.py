@@ -18,6 +18,7 @@ MAX_HSTARTS = 32
 OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT, ERR_UNSUPPORTED = range(6)
 PREC_FP64, PREC_DF64, PREC_FP32, PREC_GUARDED = 0, 1, 2, 3
 LAYOUT_REFERENCE, LAYOUT_SCENE_B = 0, 1
+TUNE_INVERT, TUNE_JOINT = 0, 1
 PX_FITTED, PX_MASKED, PX_INVALID = 0, 1, 2
 PX_CONVERGED = 0x100
 
@@ -105,6 +106,8 @@ _SIGS = {
                                        C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
                                        C.c_void_p]),
     "photic_measure_peaks": (C.c_int, [C.POINTER(C.c_double)] * 3),
+    "photic_autotune": (C.c_int, [C.POINTER(photic_config), C.c_int32, C.c_int64,
+                                  C.POINTER(C.c_double), C.c_int32, C.POINTER(C.c_int32)]),
     "photic_set_counter": (C.c_int, [C.c_void_p]),
     "photic_surrogate_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_uint64]),
     "photic_surrogate_destroy": (C.c_int, [C.c_void_p]),

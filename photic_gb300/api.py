@@ -254,3 +254,50 @@ def generate_joint(npix: int, seed: int = 20260202, config: Optional[Config] = N
 def sync(stream: Optional[torch.cuda.Stream] = None) -> None:
     """Wait for ``stream`` and raise if the device recorded an error."""
     L.check(L.lib().photic_sync(_stream_handle(stream)))
+
+
+class JointGraph:
+    """The temporal joint fit captured once as a CUDA graph for a fixed
+    pixel count and observation count.  One replay runs the binning by
+    scene count, the eight per-k kernels (parallel branches of the graph)
+    and the workspace allocation, whatever the per-pixel counts in the
+    offsets are.  Inputs live in the static tensors ``offsets``,
+    ``theta_sun`` and ``rrs``; :meth:`run` copies new ones in (optional)
+    and replays; outputs are the static tensors of ``out``.
+
+    The library's per-device state is set up by an eager call before the
+    capture, so the capture itself makes no synchronous allocation."""
+
+    def __init__(self, npix: int, n_obs: int, config: Optional[Config] = None, *,
+                 fields: Sequence[str] = OUTPUT_FIELDS, device=None):
+        self.cfg = config or Config()
+        dev = device or torch.device("cuda", torch.cuda.current_device())
+        self.offsets = torch.zeros(npix + 1, dtype=torch.int32, device=dev)
+        self.theta_sun = torch.full((n_obs,), 35.0, dtype=torch.float64, device=dev)
+        self.rrs = torch.full((n_obs, self.cfg.n_bands), 0.01, dtype=torch.float32, device=dev)
+        # a valid CSR layout for the warm-up: pixel p owns observation p
+        # while there are observations
+        self.offsets[1:] = torch.clamp(torch.arange(1, npix + 1, device=dev), max=n_obs).int()
+        self.out = alloc_outputs(npix, dev, fields, n_obs=n_obs)
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            joint_invert(self.offsets, self.theta_sun, self.rrs, self.cfg, out=self.out,
+                         stream=side)
+        sync(side)
+        torch.cuda.current_stream(dev).wait_stream(side)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            joint_invert(self.offsets, self.theta_sun, self.rrs, self.cfg, out=self.out)
+
+    def run(self, offsets: Optional[torch.Tensor] = None,
+            theta_sun: Optional[torch.Tensor] = None,
+            rrs: Optional[torch.Tensor] = None) -> Dict[str, torch.Tensor]:
+        if offsets is not None:
+            self.offsets.copy_(offsets)
+        if theta_sun is not None:
+            self.theta_sun.copy_(theta_sun)
+        if rrs is not None:
+            self.rrs.copy_(rrs)
+        self.graph.replay()
+        return self.out

@@ -224,6 +224,38 @@ int device_state(unsigned int **err, int *sms) {
   return PHOTIC_OK;
 }
 
+// Per-device fork set of the joint launch (created on first use, kept for
+// the life of the process); its mutex orders concurrent joint launches.
+struct ForkSlot {
+  JointFork f;
+  bool ready = false;
+  std::mutex mu;
+};
+std::mutex g_fork_mu;
+std::vector<ForkSlot *> g_fork;
+
+int joint_fork(ForkSlot **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  std::lock_guard<std::mutex> lk(g_fork_mu);
+  if ((int)g_fork.size() <= dev) g_fork.resize(dev + 1, nullptr);
+  if (!g_fork[dev]) g_fork[dev] = new ForkSlot();
+  ForkSlot *fs = g_fork[dev];
+  if (!fs->ready) {
+    for (int k = 0; k < 8; k++) {
+      e = cudaStreamCreateWithFlags(&fs->f.side[k], cudaStreamNonBlocking);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fs->f.join[k], cudaEventDisableTiming);
+      if (e != cudaSuccess) return cuda_fail(e, "joint fork streams");
+    }
+    e = cudaEventCreateWithFlags(&fs->f.fork, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(e, "joint fork event");
+    fs->ready = true;
+  }
+  *out = fs;
+  return PHOTIC_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -412,8 +444,17 @@ int photic_joint_invert_batch(const photic_config *cfg, const int32_t *d_offsets
   a.bin_start = a.bin_count + 8;
   int32_t *fill = a.bin_count + 16;
   a.list = reinterpret_cast<int32_t *>(ws + head);
-  const int per_sm = cfg->blocks_per_sm ? cfg->blocks_per_sm : 4;
-  e = launch_joint(a, fill, sms * per_sm, s);
+  const int per_sm = cfg->blocks_per_sm;
+  ForkSlot *fs = nullptr;
+  rc = joint_fork(&fs);
+  if (rc) {
+    cudaFreeAsync(ws, s);
+    return rc;
+  }
+  {
+    std::lock_guard<std::mutex> lk(fs->mu);
+    e = launch_joint(a, fill, sms, per_sm, s, &fs->f);
+  }
   cudaError_t e2 = cudaFreeAsync(ws, s);
   if (e != cudaSuccess) return cuda_fail(e, "joint launch");
   if (e2 != cudaSuccess) return cuda_fail(e2, "cudaFreeAsync");
@@ -1569,3 +1610,122 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Launch-shape autotuner.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct TuneBuffers {
+  std::vector<void *> ptrs;
+  void *get(size_t bytes) {
+    void *p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+    ptrs.push_back(p);
+    return p;
+  }
+  ~TuneBuffers() {
+    for (void *p : ptrs) cudaFree(p);
+  }
+};
+
+}  // namespace
+
+extern "C" int photic_autotune(photic_config *cfg, int32_t kind, int64_t sample_npix,
+                               double *results, int32_t max_results, int32_t *n_results) {
+  g_err.clear();
+  int rc = photic_config_check(cfg);
+  if (rc) return rc;
+  if ((kind != PHOTIC_TUNE_INVERT && kind != PHOTIC_TUNE_JOINT) || sample_npix < 1 ||
+      sample_npix > (1LL << 26) || (max_results > 0 && !results))
+    return fail(PHOTIC_ERR_INVALID, "bad autotune arguments");
+  const int nb = cfg->n_bands;
+  TuneBuffers buf;
+  photic_outputs o;
+  memset(&o, 0, sizeof o);
+  float *rrs = nullptr;
+  int32_t *offs = nullptr;
+  double *theta = nullptr;
+  int64_t n_obs = sample_npix;
+  const uint64_t seed = 0x7475e5eedULL;
+  if (kind == PHOTIC_TUNE_INVERT) {
+    rrs = (float *)buf.get((size_t)sample_npix * nb * sizeof(float));
+    if (!rrs) return fail(PHOTIC_ERR_NOMEM, "autotune sample");
+    rc = photic_generate_scene(cfg, seed, 0, sample_npix, 0.15, 2.0e-4, rrs, nullptr, nullptr);
+    if (rc) return rc;
+  } else {
+    offs = (int32_t *)buf.get((size_t)(sample_npix + 1) * sizeof(int32_t));
+    if (!offs) return fail(PHOTIC_ERR_NOMEM, "autotune sample");
+    rc = photic_joint_counts(seed, sample_npix, 2, PHOTIC_MAX_SCENES, offs + 1, nullptr);
+    if (rc) return rc;
+    std::vector<int32_t> h((size_t)sample_npix + 1, 0);
+    cudaMemcpy(h.data() + 1, offs + 1, sample_npix * sizeof(int32_t), cudaMemcpyDeviceToHost);
+    for (int64_t p = 1; p <= sample_npix; p++) h[p] += h[p - 1];
+    n_obs = h[sample_npix];
+    cudaMemcpy(offs, h.data(), h.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+    theta = (double *)buf.get((size_t)n_obs * sizeof(double));
+    rrs = (float *)buf.get((size_t)n_obs * nb * sizeof(float));
+    if (!theta || !rrs) return fail(PHOTIC_ERR_NOMEM, "autotune sample");
+    rc = photic_generate_joint(cfg, seed, sample_npix, offs, 25.0, 50.0, 0.0, 2.0e-4, theta, rrs,
+                               nullptr, nullptr);
+    if (rc) return rc;
+  }
+  o.depth = (float *)buf.get((size_t)sample_npix * sizeof(float));
+  o.status = (int32_t *)buf.get((size_t)sample_npix * sizeof(int32_t));
+  if (!o.depth || !o.status) return fail(PHOTIC_ERR_NOMEM, "autotune outputs");
+  if (kind == PHOTIC_TUNE_JOINT) {
+    o.P = (float *)buf.get((size_t)n_obs * sizeof(float));
+    if (!o.P) return fail(PHOTIC_ERR_NOMEM, "autotune outputs");
+  }
+
+  // candidates: thread-per-pixel blocks of 64/128/256 (the joint kernel's
+  // block is fixed at 128) x blocks per SM (0 = occupancy limit)
+  const int blocks_inv[3] = {64, 128, 256};
+  const int per_sm_inv[4] = {0, 2, 3, 4};
+  const int per_sm_joint[5] = {2, 3, 4, 6, 8};
+  std::vector<std::pair<int, int>> cand;
+  if (kind == PHOTIC_TUNE_INVERT) {
+    for (int b : blocks_inv)
+      for (int s : per_sm_inv) cand.push_back({b, s});
+  } else {
+    for (int s : per_sm_joint) cand.push_back({128, s});
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best_ms = 0.0f;
+  int best = -1, nres = 0;
+  for (size_t c = 0; c < cand.size(); c++) {
+    photic_config t = *cfg;
+    t.block_threads = cand[c].first;
+    t.blocks_per_sm = cand[c].second;
+    float ms = 0.0f;
+    for (int rep = 0; rep < 2 && rc == PHOTIC_OK; rep++) {  // first run untimed
+      cudaEventRecord(e0, 0);
+      rc = kind == PHOTIC_TUNE_INVERT
+               ? photic_invert_batch(&t, rrs, sample_npix, nb, 1, nullptr, &o, nullptr)
+               : photic_joint_invert_batch(&t, offs, theta, rrs, sample_npix, n_obs, &o, nullptr);
+      cudaEventRecord(e1, 0);
+      if (rc == PHOTIC_OK) rc = photic_sync(nullptr);
+      cudaEventElapsedTime(&ms, e0, e1);
+    }
+    if (rc) break;
+    if (nres < max_results) {
+      results[3 * nres + 0] = cand[c].first;
+      results[3 * nres + 1] = cand[c].second;
+      results[3 * nres + 2] = ms;
+      nres++;
+    }
+    if (best < 0 || ms < best_ms) {
+      best = (int)c;
+      best_ms = ms;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (n_results) *n_results = nres;
+  if (rc) return rc;
+  cfg->block_threads = kind == PHOTIC_TUNE_INVERT ? cand[best].first : 0;
+  cfg->blocks_per_sm = cand[best].second;
+  return PHOTIC_OK;
+}

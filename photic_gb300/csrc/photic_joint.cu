@@ -371,22 +371,41 @@ cudaError_t launch_k(const JointArgs &a, int grid, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// The per-k kernels, largest k (longest fits) first.  With a fork set each
+// goes to its own stream after the binning and joins back into s, so the
+// kernels run side by side and one kernel's ragged tail is filled by the
+// others' blocks; inside a stream capture the fork becomes parallel branches
+// of the graph.  Without one they run in order on s.
 template <int LAYOUT, int NB>
-cudaError_t launch_all_k(const JointArgs &a, int grid, cudaStream_t s) {
+cudaError_t launch_all_k(const JointArgs &a, int sms, int per_sm, cudaStream_t s,
+                         const JointFork *f) {
+  const int grid = sms * (per_sm > 0 ? per_sm : 4);
+  typedef cudaError_t (*Launch)(const JointArgs &, int, cudaStream_t);
+  const Launch fn[kMaxScenes] = {launch_k<LAYOUT, 1, NB>, launch_k<LAYOUT, 2, NB>,
+                                 launch_k<LAYOUT, 3, NB>, launch_k<LAYOUT, 4, NB>,
+                                 launch_k<LAYOUT, 5, NB>, launch_k<LAYOUT, 6, NB>,
+                                 launch_k<LAYOUT, 7, NB>, launch_k<LAYOUT, 8, NB>};
   cudaError_t e;
-  if ((e = launch_k<LAYOUT, 1, NB>(a, grid, s)) != cudaSuccess) return e;
-  if ((e = launch_k<LAYOUT, 2, NB>(a, grid, s)) != cudaSuccess) return e;
-  if ((e = launch_k<LAYOUT, 3, NB>(a, grid, s)) != cudaSuccess) return e;
-  if ((e = launch_k<LAYOUT, 4, NB>(a, grid, s)) != cudaSuccess) return e;
-  if ((e = launch_k<LAYOUT, 5, NB>(a, grid, s)) != cudaSuccess) return e;
-  if ((e = launch_k<LAYOUT, 6, NB>(a, grid, s)) != cudaSuccess) return e;
-  if ((e = launch_k<LAYOUT, 7, NB>(a, grid, s)) != cudaSuccess) return e;
-  return launch_k<LAYOUT, 8, NB>(a, grid, s);
+  if (f && (e = cudaEventRecord(f->fork, s)) != cudaSuccess) return e;
+  for (int k = kMaxScenes; k >= 1; k--) {
+    cudaStream_t t = f ? f->side[k - 1] : s;
+    if (f && (e = cudaStreamWaitEvent(t, f->fork, 0)) != cudaSuccess) return e;
+    // up to four bands: a group of lanes per pixel (photic_joint_group.cu);
+    // more bands: one thread per pixel
+    e = NB <= 4 ? launch_joint_group(a, k, per_sm, sms, t) : fn[k - 1](a, grid, t);
+    if (e != cudaSuccess) return e;
+    if (f) {
+      if ((e = cudaEventRecord(f->join[k - 1], t)) != cudaSuccess) return e;
+      if ((e = cudaStreamWaitEvent(s, f->join[k - 1], 0)) != cudaSuccess) return e;
+    }
+  }
+  return cudaSuccess;
 }
 
 }  // namespace
 
-cudaError_t launch_joint(const JointArgs &a, int32_t *fill, int grid, cudaStream_t s) {
+cudaError_t launch_joint(const JointArgs &a, int32_t *fill, int sms, int per_sm, cudaStream_t s,
+                         const JointFork *f) {
   const int block = 256;
   const unsigned g = (unsigned)((a.npix + block - 1) / block);
   if (a.npix > 0) {
@@ -397,11 +416,11 @@ cudaError_t launch_joint(const JointArgs &a, int32_t *fill, int grid, cudaStream
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if (a.fp.n_bands <= 4) {
-    return a.fp.layout == PHOTIC_LAYOUT_REFERENCE ? launch_all_k<PHOTIC_LAYOUT_REFERENCE, 4>(a, grid, s)
-                                                  : launch_all_k<PHOTIC_LAYOUT_SCENE_B, 4>(a, grid, s);
+    return a.fp.layout == PHOTIC_LAYOUT_REFERENCE ? launch_all_k<PHOTIC_LAYOUT_REFERENCE, 4>(a, sms, per_sm, s, f)
+                                                  : launch_all_k<PHOTIC_LAYOUT_SCENE_B, 4>(a, sms, per_sm, s, f);
   }
-  return a.fp.layout == PHOTIC_LAYOUT_REFERENCE ? launch_all_k<PHOTIC_LAYOUT_REFERENCE, 8>(a, grid, s)
-                                                : launch_all_k<PHOTIC_LAYOUT_SCENE_B, 8>(a, grid, s);
+  return a.fp.layout == PHOTIC_LAYOUT_REFERENCE ? launch_all_k<PHOTIC_LAYOUT_REFERENCE, 8>(a, sms, per_sm, s, f)
+                                                : launch_all_k<PHOTIC_LAYOUT_SCENE_B, 8>(a, sms, per_sm, s, f);
 }
 
 }  // namespace photic

@@ -83,7 +83,18 @@ struct JointArgs {
   unsigned int *error;
 };
 // Bins pixels by scene count and runs one persistent kernel per count.
-cudaError_t launch_joint(const JointArgs &a, int32_t *fill, int grid, cudaStream_t s);
+// Streams and events for running the per-k joint kernels side by side.
+struct JointFork {
+  cudaStream_t side[8];
+  cudaEvent_t fork;
+  cudaEvent_t join[8];
+};
+// per_sm: blocks per SM of each per-k kernel (0: the kernel's occupancy
+// limit for the lane-group kernels, 4 for the thread-per-pixel ones).
+cudaError_t launch_joint(const JointArgs &a, int32_t *fill, int sms, int per_sm, cudaStream_t s,
+                         const JointFork *f);
+// One per-k lane-group kernel (photic_joint_group.cu), n_bands <= 4.
+cudaError_t launch_joint_group(const JointArgs &a, int k, int per_sm, int sms, cudaStream_t s);
 
 struct JointGenArgs {
   FitParams fp;
