@@ -275,7 +275,10 @@ def main():
     flops_per_eval = FLOPS_PER_EVAL_F64
     achieved = total_evals * flops_per_eval / (ms_step * 1e-3) / 1e12
     roof = {"bound": "fp64-pipe", "achieved": achieved, "peak": float(p64[0]),
-            "unit": "TFLOP/s", "frac": achieved / float(p64[0]), "traffic": None,
+            "unit": "TFLOP/s", "frac": achieved / float(p64[0]),
+            "traffic": TRAFFIC_BYTES_PER_PIXEL * npix,
+            "traffic_note": "DRAM bytes per launch, scaled by pixels from an ncu capture of "
+                            "a 65536-pixel launch of the same kernel",
             "peak_source": "measured by photic_measure_peaks (DFMA chains) in this run",
             "evals_per_s": total_evals / (ms_step * 1e-3),
             "flops_per_eval": flops_per_eval}
@@ -501,6 +504,10 @@ def serving_leg(args, net):
 # (adds, multiplies, divides, square roots; exp/log counted as one each):
 # 43 per band (photic_fp64.cuh cost_f64) + 9 in the tail.
 FLOPS_PER_EVAL_F64 = 4 * 43 + 9
+
+# dram__bytes_read.sum + dram__bytes_write.sum of the FP64 inversion kernel
+# over a 65 536-pixel launch (1.902080 MB + 0.158464 MB), per pixel.
+TRAFFIC_BYTES_PER_PIXEL = (1.902080e6 + 0.158464e6) / 65536
 
 if __name__ == "__main__":
     main()
