@@ -156,11 +156,15 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=1 << 16)
     ap.add_argument("--ref-sample", type=int, default=1 << 16)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--warm-npix", type=int, default=1 << 20,
+    ap.add_argument("--warm-npix", type=int, default=1 << 22,
                     help="pixels of the 8192x8192 scene for the warm-start comparison (0: skip)")
     ap.add_argument("--train-forward", type=int, default=1 << 23)
     ap.add_argument("--train-inverted", type=int, default=1 << 20)
     ap.add_argument("--train-epochs", type=int, default=4)
+    ap.add_argument("--polish-iters", type=int, default=15,
+                    help="Levenberg-Marquardt steps on each surrogate seed (0: raw prediction)")
+    ap.add_argument("--seed-step-scale", type=float, default=0.1,
+                    help="initial simplex of a seeded fit, relative to the cold-start steps")
     ap.add_argument("--joint-npix", type=int, default=1 << 16,
                     help="pixels of the 4096x4096 temporal grid for the joint-fit leg (0: skip)")
     ap.add_argument("--serve-requests", type=int, default=12,
@@ -382,10 +386,17 @@ def warm_start_leg(args, dev):
         torch.cuda.synchronize()
         return r, ev0.elapsed_time(ev1) * 1e-3
 
+    wcfg = pg.Config(seed_step_scale=args.seed_step_scale)
     pg.invert(rrs[:4096], cfg, fields=fields)  # warm the kernels
     cold, t_cold = timed(lambda: pg.invert(rrs, cfg, fields=fields))
-    (seeds, res), t_seed = timed(lambda: net.seeds(rrs, cfg))
-    warm, t_warm = timed(lambda: pg.invert(rrs, cfg, seeds=seeds, fields=fields))
+    # the raw network prediction as seed, for comparison
+    (seeds0, _), t_seed0 = timed(lambda: net.seeds(rrs, cfg))
+    warm0, t_warm0 = timed(lambda: pg.invert(rrs, wcfg, seeds=seeds0, fields=fields))
+    (seeds, res, order), t_seed = timed(
+        lambda: (*net.seeds(rrs, cfg, polish_iters=args.polish_iters), None))
+    order, t_order = timed(lambda: pg.fallbacks_first(seeds))
+    t_seed += t_order
+    warm, t_warm = timed(lambda: pg.invert(rrs, wcfg, seeds=seeds, order=order, fields=fields))
     pg.sync()
 
     def conv(o):
@@ -396,14 +407,21 @@ def warm_start_leg(args, dev):
     # parity of the warm path: the oracle started from the same seeds
     idx = torch.arange(0, n, max(1, n // 1024), device=dev)
     sd_np = seeds[idx].cpu().numpy()
-    ref = O.invert_batch(rrs[idx].cpu().numpy(), seeds=sd_np, nthreads=os.cpu_count() or 1)
+    ref = O.invert_batch(rrs[idx].cpu().numpy(), seeds=sd_np, seed_step_scale=args.seed_step_scale,
+                         nthreads=os.cpu_count() or 1)
     m = (ref[:, 9] == 0) & cw[idx].cpu().numpy()
     d = np.abs(warm["depth_f64"][idx].cpu().numpy()[m] - ref[m, 0])
     within = float(np.mean(d <= 0.01)) if m.any() else 1.0
     v_cold = float(cc.sum().item()) / t_cold
     v_warm = float(cw.sum().item()) * within / (t_warm + t_seed)
+    v_warm0 = float(conv(warm0).sum().item()) / (t_warm0 + t_seed0)
+    seeded0 = ~torch.isnan(seeds0[:, 0]) & ((cold["status"] & 0xFF) == 0)
     return net, {"workload": f"{n} pixels of the 8192x8192 plain-method scene",
             "cold_px_s": v_cold, "warm_px_s": v_warm, "speedup": v_warm / v_cold,
+            "seed": f"network prediction + {args.polish_iters} Levenberg-Marquardt steps, "
+                    f"simplex scale {args.seed_step_scale}; cold-start fallbacks queued first",
+            "unpolished": {"warm_px_s": v_warm0, "speedup": v_warm0 / v_cold,
+                           "seeded_share": float(seeded0.float().mean().item())},
             "seeded_share": float(seeded.float().mean().item()),
             "evals_per_pixel_cold": float(cold["evals"].float()[cc].mean().item()),
             "evals_per_pixel_warm": float(warm["evals"].float()[cw].mean().item()),

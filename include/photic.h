@@ -129,6 +129,16 @@ int photic_invert_batch(const photic_config *cfg, const float *d_rrs, int64_t np
                         int64_t pixel_stride, int64_t band_stride, const double *d_seeds,
                         const photic_outputs *out, void *stream);
 
+/* photic_invert_batch with the pixels taken from the work queue in the order
+ * d_order gives (device int32 [npix], a permutation of 0..npix-1; NULL: in
+ * index order).  Results are written at each pixel's own index.  Taking the
+ * fits expected to be longest first (e.g. the cold-start fallbacks of a
+ * seeded batch) shortens the kernel's tail.  Not in guarded precision. */
+int photic_invert_batch_ordered(const photic_config *cfg, const float *d_rrs, int64_t npix,
+                                int64_t pixel_stride, int64_t band_stride,
+                                const double *d_seeds, const int32_t *d_order,
+                                const photic_outputs *out, void *stream);
+
 /* Size of the static scratch array behind photic_invert_batch_noalloc. */
 #define PHOTIC_NOALLOC_SCRATCH_BYTES 256
 
@@ -259,6 +269,15 @@ int photic_surrogate_infer(photic_surrogate *s, const float *d_x, int64_t R, flo
 int photic_surrogate_seed(photic_surrogate *s, const photic_config *cfg, const float *d_rrs,
                           int64_t npix, double resid_max, double *d_seeds, float *d_resid,
                           void *stream);
+/* As photic_surrogate_seed, with polish_iters (0..100) Levenberg-Marquardt
+ * steps on each prediction before the residual test: single-precision
+ * forward model, misfit in units of the noise sigma (resid_max / 3) plus a
+ * weak pull towards the prediction, which picks the nearest point of the
+ * underdetermined solution set.  The polished vector only seeds nelmin. */
+int photic_surrogate_seed_polished(photic_surrogate *s, const photic_config *cfg,
+                                   const float *d_rrs, int64_t npix, double resid_max,
+                                   int32_t polish_iters, double *d_seeds, float *d_resid,
+                                   void *stream);
 
 /* Instrumentation: if d_counter (device, unsigned long long) is not NULL,
  * later PHOTIC_PREC_GUARDED inversions add the number of exact FP64

@@ -81,6 +81,9 @@ _SIGS = {
     "photic_invert_batch": (C.c_int, [C.POINTER(photic_config), C.c_void_p, C.c_int64,
                                       C.c_int64, C.c_int64, C.c_void_p,
                                       C.POINTER(photic_outputs), C.c_void_p]),
+    "photic_invert_batch_ordered": (C.c_int, [C.POINTER(photic_config), C.c_void_p, C.c_int64,
+                                              C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
+                                              C.POINTER(photic_outputs), C.c_void_p]),
     "photic_invert_batch_noalloc": (C.c_int, [C.POINTER(photic_config), C.c_void_p, C.c_int64,
                                               C.c_int64, C.c_int64, C.c_void_p,
                                               C.POINTER(photic_outputs), C.c_void_p]),
@@ -122,6 +125,9 @@ _SIGS = {
     "photic_surrogate_seed": (C.c_int, [C.c_void_p, C.POINTER(photic_config), C.c_void_p,
                                         C.c_int64, C.c_double, C.c_void_p, C.c_void_p,
                                         C.c_void_p]),
+    "photic_surrogate_seed_polished": (C.c_int, [C.c_void_p, C.POINTER(photic_config),
+                                                 C.c_void_p, C.c_int64, C.c_double, C.c_int32,
+                                                 C.c_void_p, C.c_void_p, C.c_void_p]),
     "photic_gemm_bf16": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,
                                    C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
     "photic_gemm_bf16_strides": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,

@@ -135,16 +135,25 @@ def _outputs_struct(out: Dict[str, torch.Tensor]) -> L.photic_outputs:
     return s
 
 
+def fallbacks_first(seeds: torch.Tensor) -> torch.Tensor:
+    """A pixel order for :func:`invert` that takes the cold-start fallbacks
+    of a seeded batch (NaN seeds, several times longer to fit) first."""
+    return torch.argsort((~torch.isnan(seeds[:, 0])).to(torch.int8), stable=True).to(torch.int32)
+
+
 def invert(rrs: torch.Tensor, config: Optional[Config] = None, *,
-           seeds: Optional[torch.Tensor] = None, out: Optional[Dict[str, torch.Tensor]] = None,
+           seeds: Optional[torch.Tensor] = None, order: Optional[torch.Tensor] = None,
+           out: Optional[Dict[str, torch.Tensor]] = None,
            fields: Sequence[str] = OUTPUT_FIELDS,
            stream: Optional[torch.cuda.Stream] = None) -> Dict[str, torch.Tensor]:
     """Fit every pixel of ``rrs`` ([npix, n_bands] float32, CUDA).
 
     ``seeds`` ([npix, 6] float64) starts a pixel's single fit from the given
     vector (H, 100B, q, 100P, 100G, 100X); NaN in column 0 keeps that pixel
-    on the cold multi-start.  Asynchronous on ``stream``; call :func:`sync`
-    to surface device-side errors.
+    on the cold multi-start.  ``order`` (int32 permutation of the pixels)
+    is the order the work queue hands them out in; results stay at each
+    pixel's index.  Asynchronous on ``stream``; call :func:`sync` to surface
+    device-side errors.
     """
     cfg = config or Config()
     _check_cuda(rrs, "rrs", torch.float32)
@@ -155,12 +164,17 @@ def invert(rrs: torch.Tensor, config: Optional[Config] = None, *,
         _check_cuda(seeds, "seeds", torch.float64)
         if tuple(seeds.shape) != (npix, 6):
             raise ValueError("seeds must be [npix, 6]")
+    if order is not None:
+        _check_cuda(order, "order", torch.int32)
+        if order.numel() != npix:
+            raise ValueError("order must hold one entry per pixel")
     if out is None:
         out = alloc_outputs(npix, rrs.device, fields)
     c = cfg.to_c()
     os_ = _outputs_struct(out)
-    L.check(L.lib().photic_invert_batch(C.byref(c), _ptr(rrs), npix, cfg.n_bands, 1,
-                                        _ptr(seeds), C.byref(os_), _stream_handle(stream)))
+    L.check(L.lib().photic_invert_batch_ordered(C.byref(c), _ptr(rrs), npix, cfg.n_bands, 1,
+                                                _ptr(seeds), _ptr(order), C.byref(os_),
+                                                _stream_handle(stream)))
     return out
 
 

@@ -772,6 +772,8 @@ __global__ void __launch_bounds__(BS) guarded_kernel(const __grid_constant__ Inv
           if (o.evals) o.evals[p] = 0;
           if (o.evals_kept) o.evals_kept[p] = 0;
           if (o.status) o.status[p] = PHOTIC_PX_MASKED;
+          if (o.params)
+            for (int i = 0; i < kN; i++) o.params[p * kN + i] = 0.0;
         } else {
           // FP64 pixel constants (shared, for exact evaluations) and the
           // double-float ones (registers, for screening)

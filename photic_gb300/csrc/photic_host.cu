@@ -343,6 +343,14 @@ int photic_band_constants(const photic_config *cfg, double *out) {
 int photic_invert_batch(const photic_config *cfg, const float *d_rrs, int64_t npix,
                         int64_t pixel_stride, int64_t band_stride, const double *d_seeds,
                         const photic_outputs *out, void *stream) {
+  return photic_invert_batch_ordered(cfg, d_rrs, npix, pixel_stride, band_stride, d_seeds,
+                                     nullptr, out, stream);
+}
+
+int photic_invert_batch_ordered(const photic_config *cfg, const float *d_rrs, int64_t npix,
+                                int64_t pixel_stride, int64_t band_stride,
+                                const double *d_seeds, const int32_t *d_order,
+                                const photic_outputs *out, void *stream) {
   int rc = photic_config_check(cfg);
   if (rc) return rc;
   if (npix < 0) return fail(PHOTIC_ERR_INVALID, "npix < 0");
@@ -352,6 +360,9 @@ int photic_invert_batch(const photic_config *cfg, const float *d_rrs, int64_t np
     return fail(PHOTIC_ERR_INVALID, "strides must be >= 1");
   if (cfg->precision == PHOTIC_PREC_FP32)
     return fail(PHOTIC_ERR_UNSUPPORTED, "precision %d not built in this version", cfg->precision);
+  if (d_order && cfg->precision == PHOTIC_PREC_GUARDED)
+    return fail(PHOTIC_ERR_UNSUPPORTED, "a pixel order is not supported in guarded precision");
+  if (d_order && npix > 0x7fffffffLL) return fail(PHOTIC_ERR_INVALID, "npix beyond 2^31-1");
   cudaStream_t s = (cudaStream_t)stream;
   unsigned int *err = nullptr;
   int sms = 0;
@@ -370,6 +381,7 @@ int photic_invert_batch(const photic_config *cfg, const float *d_rrs, int64_t np
   a.vec4 = (cfg->n_bands == 4 && pixel_stride == 4 && band_stride == 1 &&
             ((uintptr_t)d_rrs & 15u) == 0);
   a.seeds = d_seeds;
+  a.order = d_order;
   a.out = *out;
   a.error = err;
   a.early_exit = cfg->early_exit_per_scene * (double)(float)1;
@@ -807,9 +819,18 @@ int photic_surrogate_infer(photic_surrogate *s, const float *d_x, int64_t R, flo
 int photic_surrogate_seed(photic_surrogate *s, const photic_config *cfg, const float *d_rrs,
                           int64_t npix, double resid_max, double *d_seeds, float *d_resid,
                           void *stream) {
+  return photic_surrogate_seed_polished(s, cfg, d_rrs, npix, resid_max, 0, d_seeds, d_resid,
+                                        stream);
+}
+
+int photic_surrogate_seed_polished(photic_surrogate *s, const photic_config *cfg,
+                                   const float *d_rrs, int64_t npix, double resid_max,
+                                   int32_t polish_iters, double *d_seeds, float *d_resid,
+                                   void *stream) {
   int rc = photic_config_check(cfg);
   if (rc) return rc;
-  if (!s || !d_rrs || !d_seeds || npix < 0) return fail(PHOTIC_ERR_INVALID, "bad arguments");
+  if (!s || !d_rrs || !d_seeds || npix < 0 || polish_iters < 0 || polish_iters > 100)
+    return fail(PHOTIC_ERR_INVALID, "bad arguments");
   if (npix == 0) return PHOTIC_OK;
   cudaStream_t st = (cudaStream_t)stream;
   float *x = nullptr, *y = nullptr;
@@ -829,6 +850,17 @@ int photic_surrogate_seed(photic_surrogate *s, const photic_config *cfg, const f
       a.y = y;
       a.npix = npix;
       a.resid_max = resid_max;
+      a.polish_iters = polish_iters;
+      for (int b = 0; b < 8; b++) {
+        a.sf.refl[b] = (float)a.sc.refl[b];
+        a.sf.aw[b] = (float)a.sc.aw[b];
+        a.sf.a0[b] = (float)a.sc.a0[b];
+        a.sf.a1[b] = (float)a.sc.a1[b];
+        a.sf.eS[b] = (float)a.sc.eS[b];
+        a.sf.bbw[b] = (float)a.sc.bbw[b];
+      }
+      a.sf.sec_sun = (float)a.sc.sec_sun;
+      a.sf.sec_view = (float)a.sc.sec_view;
       a.seeds = d_seeds;
       a.resid = d_resid;
       e = mlp_seeds(a, st);

@@ -172,6 +172,8 @@ __device__ __forceinline__ void write_masked(const photic_outputs &o, int64_t p)
   if (o.evals) o.evals[p] = 0;
   if (o.evals_kept) o.evals_kept[p] = 0;
   if (o.status) o.status[p] = PHOTIC_PX_MASKED;
+  if (o.params)
+    for (int i = 0; i < 6; i++) o.params[p * 6 + i] = 0.0;
 }
 
 template <class P, int NB, int BS>
@@ -221,8 +223,9 @@ __global__ void __launch_bounds__(BS) invert_kernel(const __grid_constant__ Inve
         chunk_next = chunk_base;
         chunk_end = min(chunk_base + 32, args.npix);
         __syncwarp();
-        const int64_t p = chunk_base + lane;
-        if (p < args.npix) {
+        const int64_t q = chunk_base + lane;
+        if (q < args.npix) {
+          const int64_t p = args.order ? (int64_t)args.order[q] : q;
           if (NB == 4 && args.vec4) {
             const float4 v4 = __ldg(reinterpret_cast<const float4 *>(args.rrs) + p);
             wchunk[lane * NB + 0] = v4.x;
@@ -245,10 +248,11 @@ __global__ void __launch_bounds__(BS) invert_kernel(const __grid_constant__ Inve
       const unsigned taken = __ballot_sync(kFull, mine);
       bool masked = false;
       if (mine) {
-        const int64_t p = chunk_next + rank;
+        const int64_t q = chunk_next + rank;  // queue position -> pixel
+        const int64_t p = args.order ? (int64_t)args.order[q] : q;
         float r[NB];
 #pragma unroll
-        for (int b = 0; b < NB; b++) r[b] = wchunk[(p - chunk_base) * NB + b];
+        for (int b = 0; b < NB; b++) r[b] = wchunk[(q - chunk_base) * NB + b];
 #pragma unroll
         for (int b = 0; b < NB; b++)
           if (b < fp.n_bands && !args.no_mask && band_masked(r[b], fp.nodata)) masked = true;

@@ -31,6 +31,7 @@ struct InvertArgs {
   unsigned long long *counters;  // optional: exact evaluations served (guarded)
   double early_exit;  // early-exit cost threshold (per-scene value * scenes)
   int32_t no_mask;    // fit every pixel: samodel_optimise has no mask test
+  const int32_t *order;  // optional queue position -> pixel (e.g. long fits first)
 };
 
 size_t invert_smem_bytes(int block, int nb);
@@ -152,13 +153,21 @@ struct MlpWork {
   __nv_bfloat16 *X0, *A1, *A2, *A3, *dY, *dZ, *dZ2, *T1, *T2;
   float *Z1, *Z2, *Z3, *Y, *G4t, *grad;
 };
+// Band constants in single precision, for the seed polish.
+struct SceneF32 {
+  float refl[8], aw[8], a0[8], a1[8], eS[8], bbw[8];
+  float sec_sun, sec_view;
+};
+
 struct SeedArgs {
   FitParams fp;
   SceneConsts sc;
+  SceneF32 sf;
   const float *rrs;
   const float *y;     // [npix][5] surrogate outputs (ln P, ln G, ln X, B, H)
   int64_t npix;
   double resid_max;
+  int32_t polish_iters;  // Levenberg-Marquardt steps on the seed (0: none)
   double *seeds;      // [npix][6]
   float *resid;       // optional [npix]
 };

@@ -145,9 +145,173 @@ __global__ void denorm_kernel(const float *Y, int R, const float *out_mean, cons
   for (int o = 0; o < 5; o++) y[(size_t)r * 5 + o] = Y[(size_t)r * kMlpOut + o] * out_std[o] + out_mean[o];
 }
 
-// Seeds for nelmin from the surrogate's prediction, and the fallback test:
-// the seed's modelled spectrum must match the measured one to within
-// resid_max (RMS over bands), otherwise the pixel keeps the cold start.
+// Forward model of one band in single precision for the seed polish
+// (the seed only has to land near a minimum; nelmin then runs in FP64):
+// z = (ln P, ln G, ln X, B, H), one bottom type with q = 1.  The band
+// constants come as floats (SceneF32), so the loop has no double
+// conversions.
+__device__ __forceinline__ float forward_band_f32(const SceneF32 &sf, int b, const float (&z)[5],
+                                                  float pw) {
+  const float P = __expf(z[0]), G = __expf(z[1]), X = __expf(z[2]);
+  const float B = fabsf(z[3]), H = fabsf(z[4]);
+  const float rho = B * sf.refl[b];
+  const float a = sf.aw[b] + (sf.a0[b] + sf.a1[b] * z[0]) * P + G * sf.eS[b];
+  const float bb = sf.bbw[b] + X * pw;
+  const float u = bb / (a + bb);
+  const float K = fminf(fmaxf(a + bb, 0.0f), 2.5f);
+  const float rdp = (0.084f + 0.170f * u) * u;
+  const float duc = 1.03f * sqrtf(1.0f + 2.4f * u);
+  const float dub = 1.04f * sqrtf(1.0f + 5.4f * u);
+  const float rc = rdp * (1.0f - __expf(-(sf.sec_sun + duc * sf.sec_view) * K * H));
+  const float rb = rho * 0.3183098862f * __expf(-(sf.sec_sun + dub * sf.sec_view) * K * H);
+  const float r = rc + rb;
+  return 0.5f * r / (1.0f - 1.5f * r);
+}
+
+// Sum of squares of the polish residuals: the spectral misfit in units of
+// the noise sigma, plus a weak pull towards the network's prediction z0
+// that picks one point of the (underdetermined) solution set.
+template <int NB>
+__device__ __forceinline__ float polish_cost(const SceneF32 &sf, int nb, const float (&z)[5],
+                                             const float (&z0)[5], const float (&pw)[NB],
+                                             const float (&rs)[NB], float inv_sigma,
+                                             float w, float (&e)[NB + 5]) {
+  float s = 0.0f;
+#pragma unroll
+  for (int b = 0; b < NB; b++) {
+    e[b] = 0.0f;
+    if (b < nb) e[b] = (forward_band_f32(sf, b, z, pw[b]) - rs[b]) * inv_sigma;
+    s += e[b] * e[b];
+  }
+#pragma unroll
+  for (int i = 0; i < 5; i++) {
+    e[NB + i] = w * (z[i] - z0[i]);
+    s += e[NB + i] * e[NB + i];
+  }
+  return s;
+}
+
+// Levenberg-Marquardt on the 5 seed parameters, all in FP32: forward-
+// difference Jacobian, normal equations scaled to a unit diagonal (which
+// takes the parameters' disparate units out of the conditioning), damping
+// lambda on the scaled system (Marquardt's lambda * diag), Cholesky solve;
+// lambda divided by 4 on an accepted step and multiplied by 4 on a
+// rejected one.  Returns the final spectral misfit (sum of squares over
+// the bands, in units of sigma^2).
+template <int NB>
+__device__ __forceinline__ float polish_seed(const SceneF32 &sf, int nb, const float (&pw)[NB],
+                             const float (&rs)[NB], float inv_sigma, int iters, float (&z)[5]) {
+  constexpr int M = NB + 5;
+  const float w = 0.05f;
+  float z0[5], e[M], et[M], J[M][5];
+#pragma unroll
+  for (int i = 0; i < 5; i++) z0[i] = z[i];
+  float S = polish_cost<NB>(sf, nb, z, z0, pw, rs, inv_sigma, w, e);
+  float lambda = 1.0e-3f;
+  bool need_j = true;
+  for (int it = 0; it < iters; it++) {
+    if (need_j) {
+#pragma unroll
+      for (int i = 0; i < 5; i++) {
+        const float h = 1.0e-3f * fmaxf(1.0f, fabsf(z[i]));
+        float zi[5];
+#pragma unroll
+        for (int k = 0; k < 5; k++) zi[k] = z[k];
+        zi[i] += h;
+        polish_cost<NB>(sf, nb, zi, z0, pw, rs, inv_sigma, w, et);
+        const float inv_h = 1.0f / h;
+#pragma unroll
+        for (int m = 0; m < M; m++) J[m][i] = (et[m] - e[m]) * inv_h;
+      }
+      need_j = false;
+    }
+    float A[5][5], g[5], sc[5];
+#pragma unroll
+    for (int i = 0; i < 5; i++) {
+      float gs = 0.0f;
+#pragma unroll
+      for (int m = 0; m < M; m++) gs += J[m][i] * e[m];
+      g[i] = gs;
+#pragma unroll
+      for (int k = 0; k <= i; k++) {
+        float s = 0.0f;
+#pragma unroll
+        for (int m = 0; m < M; m++) s += J[m][i] * J[m][k];
+        A[i][k] = s;
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 5; i++) sc[i] = rsqrtf(A[i][i] + 1.0e-30f);
+#pragma unroll
+    for (int i = 0; i < 5; i++) {
+      g[i] *= sc[i];
+#pragma unroll
+      for (int k = 0; k <= i; k++) A[i][k] *= sc[i] * sc[k];
+      A[i][i] += lambda;
+    }
+    // Cholesky of the scaled, damped matrix (lower triangle in place)
+    bool ok = true;
+#pragma unroll
+    for (int i = 0; i < 5; i++) {
+#pragma unroll
+      for (int k = 0; k <= i; k++) {
+        float s = A[i][k];
+#pragma unroll
+        for (int m = 0; m < k; m++) s -= A[i][m] * A[k][m];
+        if (i == k) {
+          if (!(s > 0.0f)) ok = false;
+          A[i][i] = sqrtf(fmaxf(s, 1.0e-30f));
+        } else {
+          A[i][k] = s / A[k][k];
+        }
+      }
+    }
+    if (!ok) {
+      lambda *= 4.0f;
+      continue;
+    }
+    float y[5], d[5];
+#pragma unroll
+    for (int i = 0; i < 5; i++) {
+      float s = -g[i];
+#pragma unroll
+      for (int m = 0; m < i; m++) s -= A[i][m] * y[m];
+      y[i] = s / A[i][i];
+    }
+#pragma unroll
+    for (int i = 4; i >= 0; i--) {
+      float s = y[i];
+#pragma unroll
+      for (int m = i + 1; m < 5; m++) s -= A[m][i] * d[m];
+      d[i] = s / A[i][i];
+    }
+    float zt[5];
+#pragma unroll
+    for (int i = 0; i < 5; i++) zt[i] = z[i] + d[i] * sc[i];
+    const float St = polish_cost<NB>(sf, nb, zt, z0, pw, rs, inv_sigma, w, et);
+    if (St < S) {
+      S = St;
+#pragma unroll
+      for (int i = 0; i < 5; i++) z[i] = zt[i];
+#pragma unroll
+      for (int m = 0; m < M; m++) e[m] = et[m];
+      lambda *= 0.25f;
+      need_j = true;
+    } else {
+      lambda *= 4.0f;
+    }
+  }
+  float fit = 0.0f;
+#pragma unroll
+  for (int b = 0; b < NB; b++) fit += e[b] * e[b];
+  return fit;
+}
+
+// Seeds for nelmin from the surrogate's prediction (optionally polished
+// by a few Levenberg-Marquardt steps on the spectral misfit), and the
+// fallback test: the seed's modelled spectrum must match the measured one
+// to within resid_max (RMS over bands), otherwise the pixel keeps the cold
+// start.
 template <int NB>
 __global__ void seeds_kernel(const __grid_constant__ SeedArgs a) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -155,11 +319,6 @@ __global__ void seeds_kernel(const __grid_constant__ SeedArgs a) {
   const int nb = a.fp.n_bands;
   const float *yp = a.y + p * 5;
   double *sd = a.seeds + p * 6;
-  const double P = exp((double)yp[0]), G = exp((double)yp[1]), X = exp((double)yp[2]);
-  double B = (double)yp[3], H = (double)yp[4];
-  if (B < 0.001) B = 0.001;
-  if (H < 0.1) H = 0.1;
-  double x[6] = {H, 100.0 * B, 1.0, 100.0 * P, 100.0 * G, 100.0 * X};
   double r[NB];
   bool bad = false;
 #pragma unroll
@@ -167,10 +326,43 @@ __global__ void seeds_kernel(const __grid_constant__ SeedArgs a) {
     r[b] = b < nb ? (double)a.rrs[p * nb + b] : 0.0;
     if (b < nb && !(r[b] >= 0.0)) bad = true;
   }
+  PixelF64<NB> px;
+  if (!bad) pixel_setup_f64<NB>(a.fp, a.sc, r, px);
+  float z[5] = {yp[0], yp[1], yp[2], fmaxf(yp[3], 0.001f), fmaxf(yp[4], 0.1f)};
+  if (!bad && a.polish_iters > 0 && isfinite(z[0] + z[1] + z[2] + z[3] + z[4])) {
+    // up to three attempts: the prediction, then its depth scaled by 0.4
+    // and by 2.5 (the depth is the least determined parameter); the first
+    // that fits the spectrum to 0.8 resid_max wins, else the best fit
+    float pw[NB], rs[NB];
+#pragma unroll
+    for (int b = 0; b < NB; b++) {
+      pw[b] = (float)px.pw[b];
+      rs[b] = (float)r[b];
+    }
+    const float inv_sigma = (float)(3.0 / a.resid_max);
+    const float accept = 0.64f * 9.0f * (float)nb;  // (0.8 resid_max / sigma)^2 * bands
+    const float hs[3] = {1.0f, 0.4f, 2.5f};
+    float best[5] = {z[0], z[1], z[2], z[3], z[4]}, best_fit = 3.0e38f;
+    for (int k = 0; k < 3; k++) {
+      float zk[5] = {z[0], z[1], z[2], z[3], fmaxf(z[4] * hs[k], 0.1f)};
+      const float f = polish_seed<NB>(a.sf, nb, pw, rs, inv_sigma, a.polish_iters, zk);
+      if (f < best_fit) {
+        best_fit = f;
+#pragma unroll
+        for (int i = 0; i < 5; i++) best[i] = zk[i];
+      }
+      if (best_fit <= accept) break;
+    }
+#pragma unroll
+    for (int i = 0; i < 5; i++) z[i] = best[i];
+  }
+  const double P = exp((double)z[0]), G = exp((double)z[1]), X = exp((double)z[2]);
+  double B = fabs((double)z[3]), H = fabs((double)z[4]);
+  if (B < 0.001) B = 0.001;
+  if (H < 0.1) H = 0.1;
+  double x[6] = {H, 100.0 * B, 1.0, 100.0 * P, 100.0 * G, 100.0 * X};
   double resid = 1.0e30;
   if (!bad) {
-    PixelF64<NB> px;
-    pixel_setup_f64<NB>(a.fp, a.sc, r, px);
     CostDetailsF64 det;
     cost_f64<true, NB>(a.fp, a.sc, px, x, &det);
     double s2 = 0.0;

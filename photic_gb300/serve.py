@@ -26,6 +26,7 @@ sees its batch complete.
 """
 from __future__ import annotations
 
+import dataclasses
 import math
 import time
 from collections import deque
@@ -193,13 +194,16 @@ class GpuTileExecutor:
     BYTES_PER_PIXEL = 144
 
     def __init__(self, config=None, surrogate=None, mask_frac: float = 0.15,
-                 device=None, n_streams: int = 2):
+                 device=None, n_streams: int = 2, polish_iters: int = 15,
+                 seed_step_scale: float = 0.1):
         import torch
         from . import api
         self.torch = torch
         self.api = api
         self.cfg = config or api.Config()
         self.net = surrogate
+        self.polish_iters = polish_iters
+        self.wcfg = dataclasses.replace(self.cfg, seed_step_scale=seed_step_scale)
         self.mask_frac = mask_frac
         self.device = device or torch.device("cuda", torch.cuda.current_device())
         self.streams = [torch.cuda.Stream(self.device) for _ in range(max(1, n_streams))]
@@ -231,10 +235,12 @@ class GpuTileExecutor:
                 torch.cat([r.state["rrs"] for r in reqs])
             for r in reqs:
                 r.state["rrs"].record_stream(s)
-            seeds = None
+            seeds = order = None
             if self.net is not None:
-                seeds, _ = self.net.seeds(rrs, self.cfg)
-            out = self.api.invert(rrs, self.cfg, seeds=seeds, fields=("depth", "status"),
+                seeds, _ = self.net.seeds(rrs, self.cfg, polish_iters=self.polish_iters)
+                order = self.api.fallbacks_first(seeds)
+            out = self.api.invert(rrs, self.wcfg if seeds is not None else self.cfg,
+                                  seeds=seeds, order=order, fields=("depth", "status"),
                                   stream=s)
             st = out["status"]
             fitted = (st & 0xFF) == 0
@@ -253,7 +259,7 @@ class GpuTileExecutor:
             ev.record(s)
         # keep the batch's device tensors alive until the event completes
         return {"event": ev, "stream": s, "depth": depth_h, "counts": counts_h, "offs": offs,
-                "keep": (rrs, seeds, out, counts)}
+                "keep": (rrs, seeds, order, out, counts)}
 
     def done(self, tok) -> bool:
         return tok["event"].query()

@@ -74,17 +74,19 @@ class Surrogate:
         return y
 
     def seeds(self, rrs: torch.Tensor, config: Optional[Config] = None,
-              resid_max: float = 3.0 * NOISE_SIGMA):
+              resid_max: float = 3.0 * NOISE_SIGMA, polish_iters: int = 0):
         """Start vectors [npix, 6] (NaN in column 0 = cold start) and the
-        seed's spectral RMS residual [npix]."""
+        seed's spectral RMS residual [npix].  ``polish_iters`` > 0 refines
+        each prediction with that many Levenberg-Marquardt steps on the
+        spectral misfit before the residual test."""
         cfg = config or Config()
         npix = rrs.shape[0]
         sd = torch.empty(npix, 6, dtype=torch.float64, device=rrs.device)
         res = torch.empty(npix, dtype=torch.float32, device=rrs.device)
         c = cfg.to_c()
-        L.check(L.lib().photic_surrogate_seed(self.h, C.byref(c), rrs.data_ptr(), npix,
-                                              resid_max, sd.data_ptr(), res.data_ptr(),
-                                              _stream_handle(None)))
+        L.check(L.lib().photic_surrogate_seed_polished(
+            self.h, C.byref(c), rrs.data_ptr(), npix, resid_max, int(polish_iters),
+            sd.data_ptr(), res.data_ptr(), _stream_handle(None)))
         return sd, res
 
 

@@ -147,3 +147,16 @@ def test_invert_empty_and_seeded(gpu, port):
     fit = (o["status"].cpu().numpy() & 0xFF) == 0
     med, p99, same = _stats(h, ref[:, 0], fit)
     assert med <= 0.01 and p99 <= 0.05, (med, p99, same)
+
+
+def test_invert_order_is_a_permutation_of_work(gpu):
+    """A queue order changes only which lane fits which pixel: every
+    pixel's outputs stay bit for bit, at its own index."""
+    rrs, _ = gpu.generate_scene(20000, seed=314, pix0=777)
+    fields = ("depth_f64", "evals", "status", "params")
+    a = gpu.invert(rrs, fields=fields)
+    order = torch.randperm(20000, device="cuda", generator=torch.Generator("cuda").manual_seed(1))
+    b = gpu.invert(rrs, order=order.to(torch.int32), fields=fields)
+    gpu.sync()
+    for f in fields:
+        assert torch.equal(torch.nan_to_num(a[f]), torch.nan_to_num(b[f])), f

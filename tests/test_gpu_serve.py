@@ -14,7 +14,8 @@ def _direct(pg, r, cfg, net=None):
                                with_truth=False)
     seeds = None
     if net is not None:
-        seeds, _ = net.seeds(rrs, cfg)
+        seeds, _ = net.seeds(rrs, cfg, polish_iters=15)
+        cfg = pg.Config(seed_step_scale=0.1)
     out = pg.invert(rrs, cfg, seeds=seeds, fields=("depth", "status"))
     pg.sync()
     return out["depth"].cpu().numpy(), out["status"].cpu().numpy()

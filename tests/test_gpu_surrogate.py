@@ -79,3 +79,26 @@ def test_training_reduces_loss_and_warm_start(surr, gpu, port):
     ec = out_c["evals"].cpu().numpy()[fit].mean()
     print(f"evals/pixel warm {ew:.0f} cold {ec:.0f} (warm share {warm.mean():.2f})")
     assert ew < ec
+
+    # polished seeds: a few Levenberg-Marquardt steps move the prediction
+    # onto the measured spectrum, so more pixels pass the residual test and
+    # the seeded fits need fewer evaluations; parity against the oracle
+    # started from the same seeds with the same initial simplex
+    seeds_p, res_p = net.seeds(rrs, polish_iters=15)
+    cfg_p = gpu.Config(seed_step_scale=0.1)
+    out_p = gpu.invert(rrs, cfg_p, seeds=seeds_p)
+    gpu.sync()
+    sp_np = seeds_p.cpu().numpy()
+    warm_p = fit & ~np.isnan(sp_np[:, 0])
+    r0, r1 = res.cpu().numpy()[fit], res_p.cpu().numpy()[fit]
+    print(f"seeded share raw {warm.mean():.2f} polished {warm_p.mean():.2f}; "
+          f"median residual {np.median(r0):.2e} -> {np.median(r1):.2e}")
+    assert warm_p.mean() > warm.mean() and np.median(r1) < np.median(r0)
+    ref_p = port.invert_batch(rrs.cpu().numpy(), seeds=sp_np, seed_step_scale=0.1,
+                              nthreads=NTHREADS)
+    fp_ = (out_p["status"].cpu().numpy() & 0xFF) == 0
+    d = np.abs(out_p["depth_f64"].cpu().numpy()[fp_] - ref_p[fp_, 0])
+    assert np.median(d) <= 0.01 and np.quantile(d, 0.99) <= 0.05
+    ep = out_p["evals"].cpu().numpy()[fit].mean()
+    print(f"evals/pixel polished {ep:.0f}")
+    assert ep < ew
