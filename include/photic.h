@@ -203,6 +203,24 @@ double photic_interp_1d(const double *X, const double *Y, int32_t n, double x);
  * a_w(640). */
 int photic_band_constants(const photic_config *cfg, double *out);
 
+/* Depth uncertainty, the reference's ad hoc estimate (model/samodel.c:
+ * 1368-1479): for each 0.25 m interval up to the deepest fitted depth (whole
+ * metres, at most 30 m), n_samples pixels of the interval are drawn (up to
+ * sqrt(npix) uniform probes each), every band moved by n * r_sigma[b] with
+ * one n uniform in [-1, 1] per sample, and refitted with cfg; the interval's
+ * sigma is the population standard deviation of the non-zero refitted
+ * depths, and every pixel gets the sigma of the interval (d, d + 0.25]
+ * holding its depth (0 elsewhere).  d_depth: [npix] fitted depths, positive,
+ * 0 where not fitted; r_sigma: host [n_bands].  Draws come from Philox keyed
+ * by seed (reproducible) instead of rand(); the refits are independent cold
+ * starts instead of the reference's chain of hot starts.  Optional outputs:
+ * d_table [120] sigmas, d_sample_pixel [120 * n_samples] (-1 = none found),
+ * d_sample_depth [120 * n_samples]. */
+int photic_depth_sigma(const photic_config *cfg, const float *d_rrs, int64_t npix,
+                       const float *d_depth, const double *r_sigma, int32_t n_samples,
+                       uint64_t seed, float *d_depth_sigma, double *d_table,
+                       int32_t *d_sample_pixel, double *d_sample_depth, void *stream);
+
 /* Launch-shape autotuner (new; no reference counterpart).  Times the
  * inversion (kind PHOTIC_TUNE_INVERT: block_threads 64/128/256 x blocks per
  * SM 0 (occupancy limit)/2/3/4) or the temporal joint fit (PHOTIC_TUNE_JOINT:

@@ -16,9 +16,9 @@
  * spatial region and the sand bottom; outputs are written where the
  * reference writes them.  Not reproduced: the reference samodel()'s
  * order-dependent shortcuts (lookup table of earlier fits, hot start from
- * the previous pixel, model/samodel.c:980-1109), its depth-sigma Monte Carlo
- * and its netCDF writes -- samodel() here fits every unmasked pixel with the
- * plain method and fills the output grids in memory.  The functions return
+ * the previous pixel, model/samodel.c:980-1109) and its netCDF writes --
+ * samodel() here fits every unmasked pixel with the plain method and fills
+ * the output grids in memory.  The functions return
  * void like the reference; each clears photic_last_error() on entry, and a
  * failure leaves the outputs untouched and its message there, so an empty
  * message after the call means success.
@@ -153,8 +153,11 @@ typedef struct photic_scene {
 
 /* model/samodel.h:8-19.  Fits every pixel that has data in all bands of all
  * scenes (model/samodel.c:672-700); n_spatial <= 1 and n_bottoms == 1 are
- * required (one region, sand); depth_sigma is set to 0.  Depth is written
- * negative below the datum, as the reference does (model/samodel.c:1486). */
+ * required (one region, sand).  depth_sigma (one scene) is the reference's
+ * Monte Carlo estimate computed by photic_depth_sigma with the scene's
+ * R_sigma, 128 samples per 0.25 m interval and a fixed seed; 0 for more
+ * scenes.  Depth is written negative below the datum, as the reference does
+ * (model/samodel.c:1486). */
 void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scene_indexes,
              int nscenes, int empirical_depth_present, photic_geogrid empirical_depths,
              int n_smoothing_radius, int n_spatial, int n_bottoms, float **depth,

@@ -101,6 +101,9 @@ def port() -> _Lib:
         L.po_band_constants.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _dp]
         L.po_interp_1d.argtypes = [_dp, _dp, C.c_int, C.c_double]
         L.po_philox4x32.argtypes = [C.c_uint32] * 6 + [C.POINTER(C.c_uint32)]
+        L.po_depth_sigma.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _fp, C.c_int64, _fp,
+                                     _dp, C.c_int, C.c_uint64, C.c_double, C.c_int, C.c_int,
+                                     C.c_int, _dp, _i32p, _dp, _dp, _fp]
     return _port
 
 
@@ -293,3 +296,30 @@ def philox4x32(c, k):
     out = (C.c_uint32 * 4)()
     port().lib.po_philox4x32(*(list(c) + list(k)), out)
     return list(out)
+
+
+def depth_sigma(rrs, depth, r_sigma, *, n_samples=128, seed=1, wl=OLI_BANDS, theta_sun=35.0,
+                theta_view=0.0, reqmin=1e-10, konvge=100, kcount=2000, sample_depth=None,
+                nthreads=0):
+    """Depth uncertainty (model/samodel.c:1368-1479) with Philox draws; returns
+    (depth_sigma [npix] f32, table [120], sample_pixel [120*n], sample_depth)."""
+    rrs = _f32(rrs)
+    npix, nb = rrs.shape
+    dep = np.ascontiguousarray(depth, dtype=np.float32)
+    rs = _f64(r_sigma)
+    wl = _f64(wl)
+    ns = 120 * n_samples
+    spix = np.zeros(ns, dtype=np.int32)
+    sdep = np.zeros(ns)
+    table = np.zeros(120)
+    sig = np.zeros(npix, dtype=np.float32)
+    sin = _f64(sample_depth) if sample_depth is not None else None
+    rc = port().lib.po_depth_sigma(nb, _ptr(wl, _dp), theta_sun, theta_view, _ptr(rrs, _fp),
+                                   npix, dep.ctypes.data_as(_fp), _ptr(rs, _dp), n_samples,
+                                   seed, reqmin, konvge, kcount, nthreads, _ptr(sin, _dp),
+                                   spix.ctypes.data_as(_i32p), _ptr(sdep, _dp), _ptr(table, _dp),
+                                   sig.ctypes.data_as(_fp))
+    if rc:
+        raise ValueError("po_depth_sigma failed")
+    return sig, table, spix, sdep
+

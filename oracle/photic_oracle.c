@@ -1008,3 +1008,129 @@ void po_generate_joint(uint64_t seed, int64_t npix, int n_bands, const double *w
     }
   }
 }
+
+/* ---- depth uncertainty (model/samodel.c:1368-1479) ------------------------
+ * The reference's estimate with its random draws replaced by Philox draws
+ * keyed by seed (the GPU uses the same stream): sample g = k * n_samples + s
+ * of interval k probes pixel (w0 * npix) >> 32 of counter (g, trial, 0xD5),
+ * and moves every band by n * r_sigma[b], n = +/- u1 (sign from u0) of
+ * counter (g, 0xFFFFFFFF, 0xD6).  Refits are independent cold starts.
+ * With sample_depth_in the refits are skipped and those depths are used. */
+#define PO_DS_MAX 120
+
+static int po_approx_f(float a, float b, float eps) {
+  float d = fabsf(a - b);
+  return d <= ((fabsf(a) < fabsf(b) ? fabsf(b) : fabsf(a)) * eps);
+}
+
+int po_depth_sigma(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
+                   const float *rrs, int64_t npix, const float *depth, const double *r_sigma,
+                   int n_samples, uint64_t seed, double reqmin, int konvge, int kcount,
+                   int nthreads, const double *sample_depth_in, int32_t *sample_pixel,
+                   double *sample_depth, double *table, float *depth_sigma) {
+  const double interval = 0.25;
+  const int64_t ns = (int64_t)PO_DS_MAX * n_samples;
+  float mx = 0.0f;
+  int64_t p, g;
+  int k, n_int, n_trials = (int)sqrt((double)npix);
+  double m;
+  float *srrs;
+  for (p = 0; p < npix; p++) {
+    float v = depth[p];
+    if (!(v > 0.0f) || po_approx_f(v, 0.0f, 1.0e-4f)) continue;
+    if (v > mx) mx = v;
+  }
+  m = interval * (double)((int)mx / interval);
+  if (m > 30.0) m = 30.0;
+  n_int = (int)(m / interval);
+  if (n_int > PO_DS_MAX) n_int = PO_DS_MAX;
+  srrs = (float *)malloc((size_t)ns * n_bands * sizeof(float));
+  if (!srrs) return 1;
+  for (g = 0; g < ns; g++) {
+    int64_t found = -1;
+    int t2, b;
+    k = (int)(g / n_samples);
+    if (k < n_int) {
+      double d = k * interval;
+      for (t2 = 0; t2 < n_trials && found < 0; t2++) {
+        uint32_t w[4];
+        int64_t q;
+        po_philox4x32((uint32_t)g, (uint32_t)(g >> 32), (uint32_t)t2, 0xD5u, (uint32_t)seed,
+                      (uint32_t)(seed >> 32), w);
+        q = (int64_t)(((uint64_t)w[0] * (uint64_t)npix) >> 32);
+        if (depth[q] > d && depth[q] < d + interval) found = q;
+      }
+    }
+    sample_pixel[g] = (int32_t)found;
+    if (found < 0) {
+      for (b = 0; b < n_bands; b++) srrs[g * n_bands + b] = -9999.0f;
+    } else {
+      uint32_t w[4];
+      double u0, u1;
+      float n;
+      po_philox4x32((uint32_t)g, (uint32_t)(g >> 32), 0xFFFFFFFFu, 0xD6u, (uint32_t)seed,
+                    (uint32_t)(seed >> 32), w);
+      u0 = ((double)w[0] + 0.5) * 2.3283064365386963e-10;
+      u1 = ((double)w[1] + 0.5) * 2.3283064365386963e-10;
+      n = u0 < 0.5 ? (float)u1 : -1.0f * (float)u1; /* frand2(1.0), model/common.c:220 */
+      for (b = 0; b < n_bands; b++) {
+        double v = (double)rrs[found * n_bands + b];
+        if (!po_approx_f(n, 0.0f, 1.0e-6f)) v += (double)n * r_sigma[b];
+        srrs[g * n_bands + b] = (float)v;
+      }
+    }
+  }
+  if (sample_depth_in) {
+    memcpy(sample_depth, sample_depth_in, (size_t)ns * sizeof(double));
+  } else {
+    double *out = (double *)malloc((size_t)ns * PO_NOUT * sizeof(double));
+    if (!out) {
+      free(srrs);
+      return 1;
+    }
+    if (po_invert_batch(n_bands, wl, theta_sun_deg, theta_view_deg, 0.0, srrs, ns, -9999.0f,
+                        reqmin, konvge, kcount, 0, NULL, NULL, 1.0, nthreads, out)) {
+      free(out);
+      free(srrs);
+      return 1;
+    }
+    for (g = 0; g < ns; g++) sample_depth[g] = out[g * PO_NOUT + 0];
+    free(out);
+  }
+  free(srrs);
+  /* vec_mean2_double / vec_stddev_double (model/common.c:877-940) */
+  for (k = 0; k < PO_DS_MAX; k++) {
+    double sigma = 0.0;
+    if (k < n_int) {
+      const double *v = sample_depth + (int64_t)k * n_samples;
+      double total = 0.0, mean, sumdev = 0.0;
+      int s, count = 0;
+      for (s = 0; s < n_samples; s++)
+        if (!po_approx_f((float)v[s], 0.0f, 1.0e-4f)) {
+          total += v[s];
+          count++;
+        }
+      if (count > 0) {
+        mean = (double)(float)(total / (double)count);
+        for (s = 0; s < n_samples; s++)
+          if (!po_approx_f((float)v[s], 0.0f, 1.0e-4f)) sumdev += pow(v[s] - mean, 2);
+        sigma = sqrt(sumdev / (double)count);
+      }
+    }
+    table[k] = sigma;
+  }
+  for (p = 0; p < npix; p++) {
+    float s = 0.0f, dp = depth[p];
+    if (dp > 0.0f) {
+      double d = 0.0;
+      for (k = 0; k < n_int; k++, d += interval)
+        if (dp > d && dp <= d + interval) {
+          s = (float)table[k];
+          break;
+        }
+    }
+    depth_sigma[p] = s;
+  }
+  return 0;
+}
+

@@ -72,6 +72,11 @@ void po_generate_joint(uint64_t seed, int64_t npix, int n_bands, const double *w
                        double *truth_out);
 void po_philox4x32(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
                    uint32_t *out4);
+int po_depth_sigma(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
+                   const float *rrs, int64_t npix, const float *depth, const double *r_sigma,
+                   int n_samples, uint64_t seed, double reqmin, int konvge, int kcount,
+                   int nthreads, const double *sample_depth_in, int32_t *sample_pixel,
+                   double *sample_depth, double *table, float *depth_sigma);
 
 #ifdef __cplusplus
 }

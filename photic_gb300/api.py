@@ -178,6 +178,36 @@ def invert(rrs: torch.Tensor, config: Optional[Config] = None, *,
     return out
 
 
+def depth_sigma(rrs: torch.Tensor, depth: torch.Tensor, r_sigma: Sequence[float],
+                config: Optional[Config] = None, *, n_samples: int = 128, seed: int = 1,
+                stream: Optional[torch.cuda.Stream] = None) -> Dict[str, torch.Tensor]:
+    """The reference's depth uncertainty (model/samodel.c:1368-1479) on the
+    GPU: per 0.25 m depth interval, ``n_samples`` pixels of the interval are
+    refitted with their spectra moved by n * ``r_sigma`` (n uniform in
+    [-1, 1]); each pixel gets its interval's standard deviation of refitted
+    depths.  ``depth`` ([npix] float32, positive, 0 = not fitted) is the
+    scene's fit.  Returns sigma [npix], table [120], sample_pixel and
+    sample_depth [120 * n_samples]."""
+    cfg = config or Config()
+    _check_cuda(rrs, "rrs", torch.float32)
+    _check_cuda(depth, "depth", torch.float32)
+    npix = rrs.shape[0]
+    if depth.numel() != npix or len(r_sigma) != cfg.n_bands:
+        raise ValueError("depth must be [npix] and r_sigma one value per band")
+    dev = rrs.device
+    out = {"sigma": torch.empty(npix, dtype=torch.float32, device=dev),
+           "table": torch.empty(120, dtype=torch.float64, device=dev),
+           "sample_pixel": torch.empty(120 * n_samples, dtype=torch.int32, device=dev),
+           "sample_depth": torch.empty(120 * n_samples, dtype=torch.float64, device=dev)}
+    rs = (C.c_double * cfg.n_bands)(*[float(v) for v in r_sigma])
+    c = cfg.to_c()
+    L.check(L.lib().photic_depth_sigma(C.byref(c), _ptr(rrs), npix, _ptr(depth), rs,
+                                       int(n_samples), int(seed), _ptr(out["sigma"]),
+                                       _ptr(out["table"]), _ptr(out["sample_pixel"]),
+                                       _ptr(out["sample_depth"]), _stream_handle(stream)))
+    return out
+
+
 def cost(rrs: torch.Tensor, params: torch.Tensor, config: Optional[Config] = None, *,
          stream: Optional[torch.cuda.Stream] = None):
     """samodel_error of [n, 6] parameter vectors against [n, n_bands]

@@ -264,6 +264,124 @@ __global__ void cost_kernel(CostArgs a) {
   }
 }
 
+// ---- depth uncertainty (model/samodel.c:1368-1479) -------------------
+// The reference's ad hoc depth error: for each 0.25 m depth interval up to
+// the deepest fitted depth (whole metres, at most 30 m), refit 128 pixels
+// drawn at random from that interval with every band moved by the same
+// random multiple n in [-1, 1] of the scene's deep-water sigma, and give
+// every pixel of the interval the standard deviation of the refitted depths.
+// Draws come from Philox (seeded, reproducible) instead of rand().
+
+__device__ __forceinline__ bool approx_f(float a, float b, float eps) {
+  const float d = fabsf(a - b);
+  return d <= (fabsf(a) < fabsf(b) ? fabsf(b) : fabsf(a)) * eps;
+}
+
+// Deepest fitted depth as float bits (non-negative floats order as ints).
+__global__ void ds_max_kernel(const float *depth, int64_t npix, unsigned int *max_bits) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float v = 0.0f;
+  if (p < npix) {
+    v = depth[p];
+    if (!(v > 0.0f) || approx_f(v, 0.0f, 1.0e-4f)) v = 0.0f;  // array_max2 skips 0
+  }
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0 && v > 0.0f) atomicMax(max_bits, __float_as_uint(v));
+}
+
+__device__ __forceinline__ int ds_intervals(const unsigned int *max_bits, double interval) {
+  const float mx = __uint_as_float(*max_bits);
+  double m = interval * (double)((int)mx / interval);  // model/samodel.c:1384
+  if (m > 30.0) m = 30.0;
+  int n = (int)(m / interval);
+  return n < kDsMaxIntervals ? n : kDsMaxIntervals;
+}
+
+// One thread per (interval, sample): find a pixel of the interval by up to
+// n_trials uniform probes, draw n, write the perturbed spectrum (or a
+// nodata spectrum when none was found).
+__global__ void ds_select_kernel(const __grid_constant__ DepthSigmaArgs a) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= (int64_t)kDsMaxIntervals * a.n_samples) return;
+  const int k = (int)(g / a.n_samples);
+  const int nb = a.n_bands;
+  const int n_int = ds_intervals(a.max_bits, a.interval);
+  const double d = k * a.interval;
+  int64_t found = -1;
+  if (k < n_int) {
+    for (int t = 0; t < a.n_trials && found < 0; t++) {
+      uint32_t c[4] = {(uint32_t)g, (uint32_t)(g >> 32), (uint32_t)t, 0xD5u};
+      philox(c, (uint32_t)a.seed, (uint32_t)(a.seed >> 32));
+      const int64_t p = (int64_t)(((uint64_t)c[0] * (uint64_t)a.npix) >> 32);
+      const float dp = a.depth[p];
+      if (dp > d && dp < d + a.interval) found = p;
+    }
+  }
+  a.sample_pixel[g] = (int32_t)found;
+  float *out = a.sample_rrs + g * nb;
+  if (found < 0) {
+    for (int b = 0; b < nb; b++) out[b] = a.nodata;
+    return;
+  }
+  uint32_t c[4] = {(uint32_t)g, (uint32_t)(g >> 32), 0xFFFFFFFFu, 0xD6u};
+  philox(c, (uint32_t)a.seed, (uint32_t)(a.seed >> 32));
+  const double u0 = ((double)c[0] + 0.5) * 2.3283064365386963e-10;
+  const double u1 = ((double)c[1] + 0.5) * 2.3283064365386963e-10;
+  const float n = u0 < 0.5 ? (float)u1 : -1.0f * (float)u1;  // frand2(1.0)
+  for (int b = 0; b < nb; b++) {
+    const float refl = a.rrs[found * nb + b];
+    double v = (double)refl;
+    if (!approx_f(n, 0.0f, 1.0e-6f)) v += (double)n * a.r_sigma[b];
+    out[b] = (float)v;
+  }
+}
+
+// One thread per interval: mean (rounded to float, as vec_mean2_double
+// returns it) and population standard deviation of the non-zero refitted
+// depths (model/common.c:877-940).
+__global__ void ds_table_kernel(const __grid_constant__ DepthSigmaArgs a) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= kDsMaxIntervals) return;
+  const int n_int = ds_intervals(a.max_bits, a.interval);
+  double sigma = 0.0;
+  if (k < n_int) {
+    const double *v = a.sample_depth + (int64_t)k * a.n_samples;
+    double total = 0.0;
+    int count = 0;
+    for (int s = 0; s < a.n_samples; s++)
+      if (!approx_f((float)v[s], 0.0f, 1.0e-4f)) {
+        total += v[s];
+        count++;
+      }
+    if (count > 0) {
+      const double mean = (double)(float)(total / (double)count);
+      double sumdev = 0.0;
+      for (int s = 0; s < a.n_samples; s++)
+        if (!approx_f((float)v[s], 0.0f, 1.0e-4f)) sumdev += pow(v[s] - mean, 2.0);
+      sigma = sqrt(sumdev / (double)count);
+    }
+  }
+  a.table[k] = sigma;
+}
+
+// Per pixel: the sigma of the interval (d, d + interval] holding its depth.
+__global__ void ds_map_kernel(const __grid_constant__ DepthSigmaArgs a) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.npix) return;
+  const int n_int = ds_intervals(a.max_bits, a.interval);
+  const float dp = a.depth[p];
+  float s = 0.0f;
+  if (dp > 0.0f) {
+    double d = 0.0;
+    for (int k = 0; k < n_int; k++, d += a.interval)
+      if (dp > d && dp <= d + a.interval) {
+        s = (float)a.table[k];
+        break;
+      }
+  }
+  a.depth_sigma[p] = s;
+}
+
 }  // namespace
 
 cudaError_t launch_generate(const GenArgs &a, cudaStream_t s) {
@@ -391,6 +509,20 @@ cudaError_t measure_peaks(double *fp64_tflops, double *fp32_tflops, double *mufu
   e = cudaGetLastError();
   cudaFree(buf);
   return e;
+}
+
+cudaError_t launch_depth_sigma_select(const DepthSigmaArgs &a, cudaStream_t s) {
+  const unsigned g = (unsigned)((a.npix + 255) / 256);
+  if (a.npix > 0) ds_max_kernel<<<g, 256, 0, s>>>(a.depth, a.npix, a.max_bits);
+  const int64_t n = (int64_t)kDsMaxIntervals * a.n_samples;
+  ds_select_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_depth_sigma_finish(const DepthSigmaArgs &a, cudaStream_t s) {
+  ds_table_kernel<<<1, kDsMaxIntervals, 0, s>>>(a);
+  if (a.npix > 0) ds_map_kernel<<<(unsigned)((a.npix + 255) / 256), 256, 0, s>>>(a);
+  return cudaGetLastError();
 }
 
 }  // namespace photic

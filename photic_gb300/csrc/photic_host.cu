@@ -1612,14 +1612,37 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
       cudaMemcpy(H.data(), d_depth, npix * sizeof(double), cudaMemcpyDeviceToHost);
       cudaMemcpy(f.data(), d_f, 4 * npix * sizeof(float), cudaMemcpyDeviceToHost);
       cudaMemcpy(st.data(), d_status, npix * sizeof(int32_t), cudaMemcpyDeviceToHost);
+      // depth uncertainty of the fitted grid (:1368-1479), one scene
+      std::vector<float> sig((size_t)npix, 0.0f);
+      if (depth_sigma && nscenes == 1) {
+        std::vector<float> hpos((size_t)npix);
+        for (int64_t p = 0; p < npix; p++)
+          hpos[p] = (st[p] & 0xFF) == PHOTIC_PX_FITTED ? (float)H[p] : 0.0f;
+        float *d_hpos = nullptr, *d_sig = nullptr;
+        if (cudaMalloc((void **)&d_hpos, npix * sizeof(float)) == cudaSuccess &&
+            cudaMalloc((void **)&d_sig, npix * sizeof(float)) == cudaSuccess) {
+          cudaMemcpy(d_hpos, hpos.data(), npix * sizeof(float), cudaMemcpyHostToDevice);
+          double rs[PHOTIC_MAX_BANDS];
+          for (int b = 0; b < nb; b++) rs[b] = s0.R_sigma[b];
+          rc = photic_depth_sigma(&cfg, d_rrs, npix, d_hpos, rs, 128, 1, d_sig, nullptr,
+                                  nullptr, nullptr, nullptr);
+          if (rc == PHOTIC_OK) rc = photic_sync(nullptr);
+          if (rc == PHOTIC_OK)
+            cudaMemcpy(sig.data(), d_sig, npix * sizeof(float), cudaMemcpyDeviceToHost);
+        } else {
+          rc = fail(PHOTIC_ERR_NOMEM, "samodel: depth-sigma buffers");
+        }
+        cudaFree(d_hpos);
+        cudaFree(d_sig);
+      }
       // outputs as the reference's pixel loop leaves them (:820-831,
       // :1120-1164), depth negative below the datum (:1486-1490)
-      for (int i = 0; i < nrows; i++)
+      for (int i = 0; i < nrows && rc == PHOTIC_OK; i++)
         for (int j = 0; j < ncols; j++) {
           const size_t p = (size_t)i * ncols + j;
           const bool fit = (st[p] & 0xFF) == PHOTIC_PX_FITTED;
           depth[i][j] = fit ? (float)H[p] * -1.0f : 0.0f * -1.0f;
-          if (depth_sigma) depth_sigma[i][j] = 0.0f;
+          if (depth_sigma) depth_sigma[i][j] = sig[p];
           model_error[i][j] = fit ? f[p] : 0.0f;
           bottom_albedo[i][j] = fit ? f[npix + p] : 0.0f;
           bottom_sand[i][j] = fit ? 100.0f : -9999.0f;
@@ -1759,5 +1782,62 @@ extern "C" int photic_autotune(photic_config *cfg, int32_t kind, int64_t sample_
   if (rc) return rc;
   cfg->block_threads = kind == PHOTIC_TUNE_INVERT ? cand[best].first : 0;
   cfg->blocks_per_sm = cand[best].second;
+  return PHOTIC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Depth uncertainty (model/samodel.c:1368-1479).
+// ---------------------------------------------------------------------------
+extern "C" int photic_depth_sigma(const photic_config *cfg, const float *d_rrs, int64_t npix,
+                                  const float *d_depth, const double *r_sigma, int32_t n_samples,
+                                  uint64_t seed, float *d_depth_sigma, double *d_table,
+                                  int32_t *d_sample_pixel, double *d_sample_depth, void *stream) {
+  int rc = photic_config_check(cfg);
+  if (rc) return rc;
+  if (npix < 0 || (npix > 0 && (!d_rrs || !d_depth)) || !r_sigma || !d_depth_sigma ||
+      n_samples < 1 || n_samples > 4096 || npix > 0xffffffffLL)
+    return fail(PHOTIC_ERR_INVALID, "bad arguments");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nb = cfg->n_bands;
+  const int64_t ns = (int64_t)kDsMaxIntervals * n_samples;
+  // scratch: max bits, sample pixels, sample spectra, sample depths, table
+  const size_t off_pix = 256, off_rrs = off_pix + ((ns * 4 + 255) / 256) * 256;
+  const size_t off_dep = off_rrs + ((ns * nb * 4 + 255) / 256) * 256;
+  const size_t off_tab = off_dep + ((ns * 8 + 255) / 256) * 256;
+  const size_t bytes = off_tab + kDsMaxIntervals * 8;
+  unsigned char *ws = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&ws, bytes, s);
+  if (e != cudaSuccess) return fail(PHOTIC_ERR_NOMEM, "depth-sigma workspace");
+  cudaMemsetAsync(ws, 0, 256, s);
+  DepthSigmaArgs a;
+  memset(&a, 0, sizeof a);
+  a.rrs = d_rrs;
+  a.depth = d_depth;
+  a.npix = npix;
+  a.n_bands = nb;
+  a.n_samples = n_samples;
+  a.n_trials = (int)sqrt((double)npix);  // (int) sqrt(nrows * ncols)
+  a.interval = 0.25;
+  for (int b = 0; b < nb; b++) a.r_sigma[b] = r_sigma[b];
+  a.nodata = cfg->nodata_value;
+  a.seed = seed;
+  a.max_bits = (unsigned int *)ws;
+  a.sample_pixel = d_sample_pixel ? d_sample_pixel : (int32_t *)(ws + off_pix);
+  a.sample_rrs = (float *)(ws + off_rrs);
+  double *sdep = d_sample_depth ? d_sample_depth : (double *)(ws + off_dep);
+  a.sample_depth = sdep;
+  a.table = d_table ? d_table : (double *)(ws + off_tab);
+  a.depth_sigma = d_depth_sigma;
+  e = launch_depth_sigma_select(a, s);
+  if (e == cudaSuccess) {
+    photic_outputs o;
+    memset(&o, 0, sizeof o);
+    o.depth_f64 = sdep;
+    rc = photic_invert_batch(cfg, a.sample_rrs, ns, nb, 1, nullptr, &o, stream);
+    if (rc == PHOTIC_OK) e = launch_depth_sigma_finish(a, s);
+  }
+  cudaFreeAsync(ws, s);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(e, "depth-sigma kernels");
   return PHOTIC_OK;
 }

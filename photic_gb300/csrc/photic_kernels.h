@@ -203,6 +203,27 @@ struct EmpSeedArgs {
 };
 cudaError_t launch_empirical_seeds(const EmpSeedArgs &a, cudaStream_t s);
 
+// Depth uncertainty by re-inversion of perturbed samples (photic_aux.cu).
+constexpr int kDsMaxIntervals = 120;  // 30 m in 0.25 m steps
+struct DepthSigmaArgs {
+  const float *rrs;          // [npix][n_bands] scene spectra
+  const float *depth;        // [npix] fitted depths (positive, 0 = not fitted)
+  int64_t npix;
+  int n_bands, n_samples, n_trials;
+  double interval;           // 0.25 m
+  double r_sigma[8];         // deep-water sigma per band
+  float nodata;
+  uint64_t seed;
+  unsigned int *max_bits;    // scratch: deepest depth (float bits), zeroed
+  int32_t *sample_pixel;     // [kDsMaxIntervals * n_samples], -1 = none
+  float *sample_rrs;         // [kDsMaxIntervals * n_samples][n_bands]
+  const double *sample_depth;  // refitted depths of the samples
+  double *table;             // [kDsMaxIntervals]
+  float *depth_sigma;        // [npix]
+};
+cudaError_t launch_depth_sigma_select(const DepthSigmaArgs &a, cudaStream_t s);
+cudaError_t launch_depth_sigma_finish(const DepthSigmaArgs &a, cudaStream_t s);
+
 // Throughput probes (TFLOP/s of FP64 and FP32 FMA, Tops/s of MUFU ex2).
 cudaError_t measure_peaks(double *fp64_tflops, double *fp32_tflops, double *mufu_tops);
 

@@ -145,6 +145,14 @@ def test_samodel_grid_matches_oracle(driver, port, tmp_path):
     dh = np.abs(-g[0, fit] - ref[fit, 0].astype(np.float32))
     assert np.median(dh) <= 0.01 and np.mean(dh == 0) >= 0.97, (np.median(dh), np.mean(dh == 0))
     same = dh == 0
+    # depth sigma (model/samodel.c:1368-1479): the oracle's estimate from
+    # the same depth grid, draws and tolerances (R_sigma 0 in this scene)
+    depth_pos = np.where(fit, -g[0], 0.0).astype(np.float32)
+    sig_ref, _, _, _ = port.depth_sigma(rrs, depth_pos, [0.0] * 4, n_samples=128, seed=1,
+                                        reqmin=1e-2, konvge=100, kcount=5000,
+                                        nthreads=os.cpu_count() or 1)
+    assert (g[1] > 0).any()
+    assert np.mean(np.isclose(g[1], sig_ref, rtol=1e-5, atol=0)) >= 0.8
     # the model-error grid holds the Rrs error (model/samodel.c:1120)
     np.testing.assert_allclose(g[2, fit][same], ref[fit, 3][same].astype(np.float32), rtol=1e-6)
     np.testing.assert_allclose(g[3, fit][same], ref[fit, 1][same].astype(np.float32), rtol=1e-6)
