@@ -387,7 +387,11 @@ def warm_start_leg(args, dev):
         return r, ev0.elapsed_time(ev1) * 1e-3
 
     wcfg = pg.Config(seed_step_scale=args.seed_step_scale)
-    pg.invert(rrs[:4096], cfg, fields=fields)  # warm the kernels
+    # warm the kernels (and the lazily loaded library code of each step)
+    pg.invert(rrs[:4096], cfg, fields=fields)
+    s_w, _ = net.seeds(rrs[:4096], cfg, polish_iters=args.polish_iters)
+    pg.invert(rrs[:4096], wcfg, seeds=s_w, order=pg.fallbacks_first(s_w), fields=fields)
+    torch.cuda.synchronize()
     cold, t_cold = timed(lambda: pg.invert(rrs, cfg, fields=fields))
     # the raw network prediction as seed, for comparison
     (seeds0, _), t_seed0 = timed(lambda: net.seeds(rrs, cfg))

@@ -4,7 +4,10 @@
 // the building block of the surrogate MLP (photic_mlp.cu): forward layers
 // (bias + SiLU), input gradients (times SiLU') and weight gradients.
 //
-// One CTA (4 warps) owns a 128 x BN output tile.  K is consumed in chunks
+// One CTA (4 warps) owns a 128 x BN output tile (or, split-K, one slice of
+// K of it: the weight-gradient products have 128 x 128 outputs and K = the
+// batch, so their K is spread over CTAs and the partial sums are added in a
+// fixed order by a second kernel).  K is consumed in chunks
 // of 64: all threads stage the A and B chunks into shared memory in the
 // canonical no-swizzle core-matrix layout (16-byte vector loads), one
 // thread issues four K=16 MMAs and commits them to an mbarrier, everyone
@@ -71,8 +74,12 @@ __global__ void __launch_bounds__(128) tn_gemm_kernel(const __grid_constant__ Ge
   const uint32_t idesc = tc::make_idesc_bf16(kBM, mma_n);
 
   bool ok = true;
+  // split-K: CTA z takes chunks [c0, c1) of K and writes a partial sum
   const int nchunks = (g.K + kBK - 1) / kBK;
-  for (int kc = 0; kc < nchunks && ok; kc++) {
+  const int per = g.ksplit > 1 ? (nchunks + g.ksplit - 1) / g.ksplit : nchunks;
+  const int c0 = (int)blockIdx.z * per;
+  const int c1 = min(nchunks, c0 + per);
+  for (int kc = c0; kc < c1 && ok; kc++) {
     const int k0 = kc * kBK;
     stage(gA, g.lda, g.M, m0, kBM, k0, g.K, sA);
     stage(gB, g.ldb, g.N, n0, kBN, k0, g.K, sB);
@@ -86,33 +93,43 @@ __global__ void __launch_bounds__(128) tn_gemm_kernel(const __grid_constant__ Ge
         if (k0 + kk * 16 < g.K) {
           const uint64_t ad = tc::make_desc(a0 + kk * 256, g.lbo, g.sbo);
           const uint64_t bd = tc::make_desc(b0 + kk * 256, g.lbo, g.sbo);
-          tc::mma_bf16(tmem, ad, bd, idesc, (kc > 0 || kk > 0) ? 1u : 0u);
+          tc::mma_bf16(tmem, ad, bd, idesc, (kc > c0 || kk > 0) ? 1u : 0u);
         }
       }
       tc::mma_commit(&mbar);
     }
-    if (!tc::mbar_wait(&mbar, (uint32_t)(kc & 1), kWaitLimit)) {
+    if (!tc::mbar_wait(&mbar, (uint32_t)((kc - c0) & 1), kWaitLimit)) {
       ok = false;
       if (threadIdx.x == 0) atomicOr(g.error, PHOTIC_DEVERR_MMA_TIMEOUT);
       // give the tensor core a second bounded chance to finish before the
       // shared memory and TMEM go away
-      tc::mbar_wait(&mbar, (uint32_t)(kc & 1), kWaitLimit);
+      tc::mbar_wait(&mbar, (uint32_t)((kc - c0) & 1), kWaitLimit);
     }
     tc::fence_after_sync();
     __syncthreads();
   }
 
-  if (ok) {
+  if (ok && c1 <= c0) {
+    // an empty split contributes zeros
     const int row = m0 + warp * 32 + lane;
-    for (int c0 = 0; c0 < mma_n; c0 += 16) {
+    if (row < g.M)
+      for (int j = 0; j < ncols; j++)
+        g.partial[((size_t)blockIdx.z * g.M + row) * g.N + n0 + j] = 0.0f;
+  } else if (ok) {
+    const int row = m0 + warp * 32 + lane;
+    for (int cc = 0; cc < mma_n; cc += 16) {
       float v[16];
-      tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cc, v);
       if (row < g.M) {
 #pragma unroll
         for (int j = 0; j < 16; j++) {
-          const int col = n0 + c0 + j;
-          if (c0 + j >= ncols) break;
+          const int col = n0 + cc + j;
+          if (cc + j >= ncols) break;
           float acc = v[j];
+          if (g.partial) {
+            g.partial[((size_t)blockIdx.z * g.M + row) * g.N + col] = acc;
+            continue;
+          }
           switch (g.epi) {
             case EPI_F32:
               g.C[(size_t)row * g.ldc + col] = acc;
@@ -143,6 +160,18 @@ __global__ void __launch_bounds__(128) tn_gemm_kernel(const __grid_constant__ Ge
   if (warp == 0) tc::tmem_free(tmem, kTmemCols);
 }
 
+// C = sum over splits of the partial products, in split order (the sum is
+// the same on every run).
+__global__ void splitk_reduce_kernel(const float *partial, int S, int M, int N, float *C,
+                                     int ldc) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)M * N) return;
+  const int r = (int)(i / N), c = (int)(i % N);
+  float s = 0.0f;
+  for (int z = 0; z < S; z++) s += partial[(size_t)z * M * N + i];
+  C[(size_t)r * ldc + c] = s;
+}
+
 }  // namespace
 
 // Dynamic shared memory is sized to keep at most two CTAs per SM, so the
@@ -155,8 +184,24 @@ cudaError_t launch_gemm(const GemmArgs &g, cudaStream_t s) {
   cudaError_t e = cudaFuncSetAttribute(tn_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return e;
-  dim3 grid((unsigned)((g.M + kBM - 1) / kBM), (unsigned)((g.N + kBN - 1) / kBN));
-  tn_gemm_kernel<<<grid, 128, smem, s>>>(g);
+  const int nchunks = (g.K + kBK - 1) / kBK;
+  GemmArgs a = g;
+  int S = 1;
+  if (g.ksplit > 1 && g.partial && g.epi == EPI_F32 && nchunks > 1) {
+    const int per = (nchunks + g.ksplit - 1) / g.ksplit;
+    S = (nchunks + per - 1) / per;
+    a.ksplit = S;
+  } else {
+    a.ksplit = 1;
+    a.partial = nullptr;
+  }
+  dim3 grid((unsigned)((g.M + kBM - 1) / kBM), (unsigned)((g.N + kBN - 1) / kBN), (unsigned)S);
+  tn_gemm_kernel<<<grid, 128, smem, s>>>(a);
+  if (S > 1) {
+    const int64_t n = (int64_t)g.M * g.N;
+    splitk_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a.partial, S, g.M, g.N, g.C,
+                                                                     g.ldc);
+  }
   return cudaGetLastError();
 }
 

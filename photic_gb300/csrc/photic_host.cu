@@ -616,12 +616,14 @@ struct WorkAlloc {
     const size_t bfH = (size_t)Rpad * kMlpH * 2, fH = (size_t)Rpad * kMlpH * 4;
     size_t oX0 = take((size_t)Rpad * kMlpIn * 2), oA1 = take(bfH), oA2 = take(bfH), oA3 = take(bfH);
     size_t oY = take((size_t)Rpad * kMlpOut * 4);
-    size_t oZ1 = 0, oZ2 = 0, oZ3 = 0, odY = 0, odZ = 0, odZ2 = 0, oT1 = 0, oT2 = 0, oG4 = 0, oG = 0;
+    size_t oZ1 = 0, oZ2 = 0, oZ3 = 0, odY = 0, odZ = 0, odZ2 = 0, oT1 = 0, oT2 = 0, oG4 = 0, oG = 0,
+           oSK = 0;
     if (train) {
       oZ1 = take(fH); oZ2 = take(fH); oZ3 = take(fH);
       odY = take((size_t)Rpad * kMlpOut * 2); odZ = take(bfH); odZ2 = take(bfH);
       oT1 = take(bfH); oT2 = take(bfH);
       oG4 = take((size_t)kMlpH * kMlpOut * 4); oG = take((size_t)kMlpParams * 4);
+      oSK = take((size_t)kMlpSplitK * kMlpH * kMlpH * 4);
     }
     cudaError_t e = cudaMallocAsync(&mem, off, s);
     if (e != cudaSuccess) return e;
@@ -636,6 +638,7 @@ struct WorkAlloc {
       w.dY = (__nv_bfloat16 *)(b + odY); w.dZ = (__nv_bfloat16 *)(b + odZ);
       w.dZ2 = (__nv_bfloat16 *)(b + odZ2); w.T1 = (__nv_bfloat16 *)(b + oT1);
       w.T2 = (__nv_bfloat16 *)(b + oT2); w.G4t = (float *)(b + oG4); w.grad = (float *)(b + oG);
+      w.splitk = (float *)(b + oSK);
     }
     return cudaSuccess;
   }

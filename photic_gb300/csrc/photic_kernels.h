@@ -128,6 +128,8 @@ struct GemmArgs {
   unsigned int *error;
   int lbo, sbo;    // core-matrix strides of the shared-memory layout (bytes)
   int epi;
+  int ksplit;      // > 1: split K over this many CTAs (EPI_F32 only) ...
+  float *partial;  // ... with partial sums in [ksplit][M][N] scratch
 };
 cudaError_t launch_gemm(const GemmArgs &g, cudaStream_t s);
 
@@ -149,9 +151,11 @@ struct MlpState {
   __nv_bfloat16 *W1b, *W2b, *W3b, *W4b, *W2t, *W3t, *W4t;
   float *in_mean, *in_std, *out_mean, *out_std;  // [16] each
 };
+constexpr int kMlpSplitK = 64;  // K splits of the weight-gradient products
 struct MlpWork {
   __nv_bfloat16 *X0, *A1, *A2, *A3, *dY, *dZ, *dZ2, *T1, *T2;
   float *Z1, *Z2, *Z3, *Y, *G4t, *grad;
+  float *splitk;  // [kMlpSplitK][128][128] partial sums (training)
 };
 // Band constants in single precision, for the seed polish.
 struct SceneF32 {

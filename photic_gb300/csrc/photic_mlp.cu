@@ -396,8 +396,10 @@ __global__ void features_from_rrs_kernel(const float *rrs, int64_t npix, int nb,
 
 static int gemm(const void *A, int lda, const void *B, int ldb, int M, int N, int K, int epi,
                 float *C, int ldc, void *O, int ldo, float *Z, int ldz, const float *bias,
-                unsigned int *err, cudaStream_t s) {
+                unsigned int *err, cudaStream_t s, float *splitk = nullptr) {
   GemmArgs g{};
+  g.ksplit = splitk ? kMlpSplitK : 1;
+  g.partial = splitk;
   g.A = A;
   g.B = B;
   g.lda = lda;
@@ -460,7 +462,7 @@ cudaError_t mlp_backward(const MlpState &st, const float *x, const float *t, int
   tr(w.A3, Rpad, kMlpH, Rpad, w.T1, s);
   tr(w.dY, Rpad, kMlpOut, Rpad, w.T2, s);
   bad |= gemm(w.T1, Rpad, w.T2, Rpad, kMlpH, kMlpOut, Rpad, EPI_F32, w.G4t, kMlpOut, nullptr, 0,
-              nullptr, 0, nullptr, err, s);
+              nullptr, 0, nullptr, err, s, w.splitk);
   transpose_f32_kernel<<<(kMlpH * kMlpOut + 255) / 256, 256, 0, s>>>(w.G4t, kMlpH, kMlpOut,
                                                                      g + kOffW4);
   colsum_kernel<<<kMlpOut, 256, 0, s>>>(w.dY, Rpad, kMlpOut, g + kOffB4);
@@ -471,7 +473,7 @@ cudaError_t mlp_backward(const MlpState &st, const float *x, const float *t, int
   tr(w.dZ, Rpad, kMlpH, Rpad, w.T2, s);
   tr(w.A2, Rpad, kMlpH, Rpad, w.T1, s);
   bad |= gemm(w.T2, Rpad, w.T1, Rpad, kMlpH, kMlpH, Rpad, EPI_F32, g + kOffW3, kMlpH, nullptr, 0,
-              nullptr, 0, nullptr, err, s);
+              nullptr, 0, nullptr, err, s, w.splitk);
   colsum_kernel<<<kMlpH, 256, 0, s>>>(w.dZ, Rpad, kMlpH, g + kOffB3);
   bad |= gemm(w.dZ, kMlpH, st.W3t, kMlpH, Rpad, kMlpH, kMlpH, EPI_DSILU, nullptr, 0, w.dZ2,
               kMlpH, w.Z2, kMlpH, nullptr, err, s);
@@ -479,7 +481,7 @@ cudaError_t mlp_backward(const MlpState &st, const float *x, const float *t, int
   tr(w.dZ2, Rpad, kMlpH, Rpad, w.T2, s);
   tr(w.A1, Rpad, kMlpH, Rpad, w.T1, s);
   bad |= gemm(w.T2, Rpad, w.T1, Rpad, kMlpH, kMlpH, Rpad, EPI_F32, g + kOffW2, kMlpH, nullptr, 0,
-              nullptr, 0, nullptr, err, s);
+              nullptr, 0, nullptr, err, s, w.splitk);
   colsum_kernel<<<kMlpH, 256, 0, s>>>(w.dZ2, Rpad, kMlpH, g + kOffB2);
   bad |= gemm(w.dZ2, kMlpH, st.W2t, kMlpH, Rpad, kMlpH, kMlpH, EPI_DSILU, nullptr, 0, w.dZ,
               kMlpH, w.Z1, kMlpH, nullptr, err, s);
@@ -487,7 +489,7 @@ cudaError_t mlp_backward(const MlpState &st, const float *x, const float *t, int
   tr(w.dZ, Rpad, kMlpH, Rpad, w.T2, s);
   tr(w.X0, Rpad, kMlpIn, Rpad, w.T1, s);
   bad |= gemm(w.T2, Rpad, w.T1, Rpad, kMlpH, kMlpIn, Rpad, EPI_F32, g + kOffW1, kMlpIn, nullptr,
-              0, nullptr, 0, nullptr, err, s);
+              0, nullptr, 0, nullptr, err, s, w.splitk);
   colsum_kernel<<<kMlpH, 256, 0, s>>>(w.dZ, Rpad, kMlpH, g + kOffB1);
   if (bad) return cudaErrorLaunchFailure;
   return cudaGetLastError();
