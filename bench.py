@@ -161,7 +161,7 @@ def main():
     ap.add_argument("--train-forward", type=int, default=1 << 23)
     ap.add_argument("--train-inverted", type=int, default=1 << 20)
     ap.add_argument("--train-epochs", type=int, default=4)
-    ap.add_argument("--polish-iters", type=int, default=15,
+    ap.add_argument("--polish-iters", type=int, default=25,
                     help="Levenberg-Marquardt steps on each surrogate seed (0: raw prediction)")
     ap.add_argument("--seed-step-scale", type=float, default=0.1,
                     help="initial simplex of a seeded fit, relative to the cold-start steps")

@@ -170,7 +170,10 @@ __device__ __forceinline__ float forward_band_f32(const SceneF32 &sf, int b, con
 
 // Sum of squares of the polish residuals: the spectral misfit in units of
 // the noise sigma, plus a weak pull towards the network's prediction z0
-// that picks one point of the (underdetermined) solution set.
+// that picks one point of the (underdetermined) solution set.  The pull is
+// kept small (weight 0.003): the closer the seed lies to the measured
+// spectrum, the sooner the plain-tolerance fit from it converges (most
+// seeded fits then end after their first convergence test).
 template <int NB>
 __device__ __forceinline__ float polish_cost(const SceneF32 &sf, int nb, const float (&z)[5],
                                              const float (&z0)[5], const float (&pw)[NB],
@@ -202,7 +205,7 @@ template <int NB>
 __device__ __forceinline__ float polish_seed(const SceneF32 &sf, int nb, const float (&pw)[NB],
                              const float (&rs)[NB], float inv_sigma, int iters, float (&z)[5]) {
   constexpr int M = NB + 5;
-  const float w = 0.05f;
+  const float w = 0.003f;
   float z0[5], e[M], et[M], J[M][5];
 #pragma unroll
   for (int i = 0; i < 5; i++) z0[i] = z[i];

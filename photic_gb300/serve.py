@@ -194,7 +194,7 @@ class GpuTileExecutor:
     BYTES_PER_PIXEL = 144
 
     def __init__(self, config=None, surrogate=None, mask_frac: float = 0.15,
-                 device=None, n_streams: int = 2, polish_iters: int = 15,
+                 device=None, n_streams: int = 2, polish_iters: int = 25,
                  seed_step_scale: float = 0.1):
         import torch
         from . import api
