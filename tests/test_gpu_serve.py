@@ -9,13 +9,13 @@ import torch
 pytestmark = pytest.mark.gpu
 
 
-def _direct(pg, r, cfg, net=None):
+def _direct(pg, r, cfg, net=None, polish_iters=0, seed_step_scale=1.0):
     rrs, _ = pg.generate_scene(r.npix, seed=r.seed, config=cfg, mask_frac=0.15,
                                with_truth=False)
     seeds = None
     if net is not None:
-        seeds, _ = net.seeds(rrs, cfg, polish_iters=15)
-        cfg = pg.Config(seed_step_scale=0.1)
+        seeds, _ = net.seeds(rrs, cfg, polish_iters=polish_iters)
+        cfg = pg.Config(seed_step_scale=seed_step_scale)
     out = pg.invert(rrs, cfg, seeds=seeds, fields=("depth", "status"))
     pg.sync()
     return out["depth"].cpu().numpy(), out["status"].cpu().numpy()
@@ -41,7 +41,7 @@ def test_serving_matches_direct(gpu, warm):
     assert len(done) == 10 and not sch.rejected
     assert sch.n_batches >= 2
     for r in done:
-        d, st = _direct(pg, r, cfg, net)
+        d, st = _direct(pg, r, cfg, net, ex.polish_iters, ex.wcfg.seed_step_scale)
         np.testing.assert_array_equal(r.state["depth"].numpy(), d)
         conv = ((st & 0xFF) == 0) & ((st >> 8) & 1).astype(bool)
         assert r.converged == int(conv.sum())
