@@ -177,7 +177,7 @@ int photic_joint_invert_batch(const photic_config *cfg, const int32_t *d_offsets
 int photic_cost_batch(const photic_config *cfg, const float *d_rrs, const double *d_params,
                       int64_t n, double *d_cost, double *d_rrs_modelled, void *stream);
 
-/* Synthetic scene of the plain-method workload (see photic_generate.cu):
+/* Synthetic scene of the plain-method workload (photic_aux.cu):
  * writes [npix * n_bands] floats and, if d_truth != NULL, [npix * 5]
  * doubles (H, P, G, X, B). Pixels pix0 .. pix0+npix-1 of the scene. */
 int photic_generate_scene(const photic_config *cfg, uint64_t seed, int64_t pix0, int64_t npix,

@@ -133,17 +133,13 @@ __device__ __forceinline__ df64 cost_df(const FitParams &fp, const DfScene &ds,
   const df64 E = df_div(df_mul_f(df_sqrt(df_div_f(err, (float)nb)), 100.0f), px.mean);
   df64 Ke = df64{0.0f, 0.0f};
   {
-    const KPenalty &kp = fp.kp;
     int c = -1;
-    const double Hd = (double)H.hi;
     // thresholds compared in double-float
     if (df_lt(H, df64{1.0f, 0.0f}) && df_lt(K_min, dp(ds.k_thr[0]))) c = 0;
     else if (df_lt(H, df64{2.0f, 0.0f}) && df_lt(K_min, dp(ds.k_thr[1]))) c = 1;
     else if (df_lt(H, df64{3.0f, 0.0f}) && df_lt(K_min, dp(ds.k_thr[2]))) c = 2;
     else if (df_lt(H, df64{4.0f, 0.0f}) && df_lt(K_min, dp(ds.k_thr[3]))) c = 3;
     else if (df_lt(H, df64{5.0f, 0.0f}) && df_lt(K_min, dp(ds.k_thr[4]))) c = 4;
-    (void)kp;
-    (void)Hd;
     if (c >= 0) {
       DfPair it = ds.inv_t[0];
 #pragma unroll
