@@ -101,6 +101,9 @@ def port() -> _Lib:
         L.po_band_constants.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _dp]
         L.po_interp_1d.argtypes = [_dp, _dp, C.c_int, C.c_double]
         L.po_philox4x32.argtypes = [C.c_uint32] * 6 + [C.POINTER(C.c_uint32)]
+        L.po_region_invert_batch.argtypes = [C.c_int, _dp, C.c_double, C.c_double, C.c_double,
+                                             _fp, C.c_int, C.c_int, C.c_float, C.c_double,
+                                             C.c_int, C.c_int, C.c_int, _dp]
         L.po_depth_sigma.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _fp, C.c_int64, _fp,
                                      _dp, C.c_int, C.c_uint64, C.c_double, C.c_int, C.c_int,
                                      C.c_int, _dp, _i32p, _dp, _dp, _fp]
@@ -322,4 +325,29 @@ def depth_sigma(rrs, depth, r_sigma, *, n_samples=128, seed=1, wl=OLI_BANDS, the
     if rc:
         raise ValueError("po_depth_sigma failed")
     return sig, table, spix, sdep
+
+
+def region_invert_batch(grid, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0, h_tide=0.0,
+                        nodata=-9999.0, reqmin=1e-10, konvge=100, kcount=2000, nthreads=0,
+                        which="port"):
+    """Spatial-region fit (3 x 3 neighbourhood per pixel) of a [nrows, ncols,
+    n_bands] float32 grid; returns [nrows*ncols, NOUT] (o[38] regions,
+    o[39] origin)."""
+    g = np.ascontiguousarray(grid, dtype=np.float32)
+    nrows, ncols, nb = g.shape
+    wl = _f64(wl)
+    out = np.zeros((nrows * ncols, NOUT), dtype=np.float64)
+    if which == "reference":
+        f = reference().lib.photic_ref_region_invert_batch
+        f.argtypes = [C.c_int, _dp, C.c_double, C.c_double, C.c_double, _fp, C.c_int, C.c_int,
+                      C.c_float, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, _dp]
+        rc = f(nb, _ptr(wl, _dp), theta_sun, theta_view, h_tide, g.ctypes.data_as(_fp), nrows,
+               ncols, nodata, 2, 1, reqmin, konvge, kcount, nthreads, _ptr(out, _dp))
+    else:
+        rc = port().lib.po_region_invert_batch(nb, _ptr(wl, _dp), theta_sun, theta_view, h_tide,
+                                               g.ctypes.data_as(_fp), nrows, ncols, nodata,
+                                               reqmin, konvge, kcount, nthreads, _ptr(out, _dp))
+    if rc:
+        raise ValueError("region_invert_batch failed")
+    return out
 

@@ -1134,3 +1134,295 @@ int po_depth_sigma(int n_bands, const double *wl, double theta_sun_deg, double t
   return 0;
 }
 
+/* ---- spatial regions (n_spatial = 2; model/samodel.c:2957-3027) ----------
+ * Each pixel is fitted together with its 3 x 3 neighbourhood (indexes
+ * clamped at the grid's edges, neighbours with a nodata band left out;
+ * smoothing radius 1): one depth, albedo and q per region, one P, G, X for
+ * the scene, and the cost's depth- and bottom-continuity terms
+ * (model/samodel.c:2594-2692).  One scene, one bottom type. */
+#define PO_MAX_REGIONS 9
+
+typedef struct {
+  int R, origin, n_bands;
+  const po_scene *sc;
+  double rrs[PO_MAX_REGIONS][PO_MAX_BANDS];
+  double r440[PO_MAX_REGIONS], r490[PO_MAX_REGIONS], r550[PO_MAX_REGIONS];
+  double r640[PO_MAX_REGIONS], r750[PO_MAX_REGIONS];
+  double K[PO_MAX_BANDS]; /* md->K[scene][band]: the last region's */
+  double rrs_mod[PO_MAX_REGIONS][PO_MAX_BANDS], rrs_bot[PO_MAX_REGIONS][PO_MAX_BANDS];
+  double bottom_albedo, rrs_error, model_error;
+} po_rpixel;
+
+/* samodel_error with R regions, one scene, one bottom type; parameters
+ * [H_0..H_R-1 | 100 B_0.. | q_0.. | 100 P, 100 G, 100 X]. */
+static double region_cost(const double *x, void *ctx) {
+  po_rpixel *px = (po_rpixel *)ctx;
+  const po_scene *sc = px->sc;
+  const int R = px->R, off = 3 * R;
+  double err = 0.0, tot = 0.0, rrs_error, depth_mean, th, error_depth, n_out, bottom_mean,
+         bottom_total, error_bottom, H, K_error, K_min = 1.0e4, model;
+  int r, b, nobs = 0;
+  for (r = 0; r < R; r++) {
+    double Hr = fabs(x[r]), P = 0.01 * fabs(x[off]), G = 0.01 * fabs(x[off + 1]),
+           X = 0.01 * fabs(x[off + 2]), B = 0.01 * fabs(x[R + r]), q = fabs(x[2 * R + r]),
+           q_sum = 0.0;
+    q_sum += q;
+    q /= q_sum;
+    for (b = 0; b < px->n_bands; b++) {
+      double rho = 0.0, albedo = 0.0, Rm, d;
+      albedo += q * B;
+      rho += q * B * sc->refl[0][b];
+      px->bottom_albedo = albedo;
+      Rm = hope_band(sc, b, P, G, X, rho, Hr, 0.0, px->r440[r], px->r490[r], &px->K[b],
+                     &px->rrs_bot[r][b], &px->rrs_mod[r][b]);
+      d = Rm - px->rrs[r][b];
+      err += pow(d, 2.0);
+      tot += px->rrs[r][b];
+      nobs++;
+    }
+  }
+  rrs_error = 100.0 * sqrt(err / (double)nobs) / (tot / (double)nobs);
+  px->rrs_error = rrs_error;
+  /* depth continuity, model/samodel.c:2594-2629 */
+  depth_mean = 0.0;
+  for (r = 0; r < R; r++) depth_mean += fabs(x[r]);
+  depth_mean /= (double)R;
+  if (depth_mean < 4.0) th = 0.4;
+  else if (depth_mean < 8.0) th = 0.2;
+  else if (depth_mean < 12.0) th = 0.1;
+  else th = 0.05;
+  error_depth = 0.0;
+  n_out = 0.0;
+  for (r = 0; r < R; r++)
+    if (fabs(x[r]) < (1.0 - th) * depth_mean || fabs(x[r]) > (1.0 + th) * depth_mean) {
+      error_depth += pow(fabs(x[r]) - depth_mean, 2.0);
+      n_out += 1.0;
+    }
+  if (n_out > 0.5) error_depth = 100.0 * sqrt(error_depth / n_out) / depth_mean;
+  /* bottom continuity, model/samodel.c:2633-2692 (one bottom type) */
+  if (depth_mean < 5.0) th = 0.25;
+  else if (depth_mean < 10.0) th = 0.1;
+  else if (depth_mean < 15.0) th = 0.05;
+  else th = 0.01;
+  error_bottom = 0.0;
+  n_out = 0.0;
+  bottom_total = 0.0;
+  bottom_mean = 0.0;
+  for (r = 0; r < R; r++) {
+    double q_sum = 0.0;
+    q_sum += fabs(x[2 * R + r]);
+    bottom_mean += fabs(x[R + r]) * fabs(x[2 * R + r]) / q_sum;
+  }
+  bottom_mean /= (double)R;
+  bottom_total += bottom_mean;
+  for (r = 0; r < R; r++) {
+    double q_sum = 0.0, bottom;
+    q_sum += fabs(x[2 * R + r]);
+    bottom = fabs(x[R + r]) * fabs(x[2 * R + r]) / q_sum;
+    if (bottom < (1.0 - th) * bottom_mean || bottom > (1.0 + th) * bottom_mean) {
+      error_bottom += pow(bottom - bottom_mean, 2.0);
+      n_out += 1.0;
+    }
+  }
+  if (n_out > 0.5) {
+    bottom_mean = bottom_total / ((double)1);
+    error_bottom = 100.0 * sqrt(error_bottom / n_out) / bottom_mean;
+  }
+  /* K penalties on the origin's depth and the scene's K (the last region's
+   * bands), model/samodel.c:2696-2732 */
+  {
+    const double mean_c = 0.275, min_c = 0.185;
+    H = fabs(x[px->origin]);
+    K_error = 0.0;
+    K_min = 1.0e4;
+    for (b = 0; b < px->n_bands; b++)
+      if (!f_close((float)px->K[b], 0.0f, 1.0e-6f) && px->K[b] < K_min) K_min = px->K[b];
+    if (H < 1.0 && K_min < mean_c) {
+      K_error += 100.0 * pow(1.0 / (0.01 + K_min) - 1.0 / (0.01 + min_c), 2);
+    } else if (H < 2.0 && K_min < 0.5 * (1.5 * min_c + 0.5 * mean_c)) {
+      K_error += 100.0 * pow(1.0 / (0.01 + K_min) - 1.0 / (0.01 + 0.5 * (1.5 * min_c + 0.5 * mean_c)), 2);
+    } else if (H < 3.0 && K_min < 0.5 * (1.25 * min_c + 0.75 * mean_c)) {
+      K_error += 100.0 * pow(1.0 / (0.01 + K_min) - 1.0 / (0.01 + 0.5 * (1.25 * min_c + 0.75 * mean_c)), 2);
+    } else if (H < 4.0 && K_min < 0.5 * (1.5 * min_c + 0.5 * mean_c)) {
+      K_error += 100.0 * pow(1.0 / (0.01 + K_min) - 1.0 / (0.01 + 0.5 * (1.5 * min_c + 0.5 * mean_c)), 2);
+    } else if (H < 5.0 && K_min < 0.5 * (1.75 * min_c + 0.25 * mean_c)) {
+      K_error += 100.0 * pow(1.0 / (0.01 + K_min) - 1.0 / (0.01 + 0.5 * (1.75 * min_c + 0.25 * mean_c)), 2);
+    }
+    if (K_min > 0.7) K_error += 100.0 * pow(4.0 * (K_min - 0.7), 2);
+  }
+  model = 80.0 * rrs_error + 15.0 * error_depth + 10.0 * error_bottom + 15.0 * K_error;
+  model /= 80.0 + 15.0 + 10.0 + 15.0;
+  px->model_error = model;
+  return model;
+}
+
+/* Cold start for R regions (model/samodel.c:2249-2353). */
+static void region_cold_start(const po_rpixel *px, double H0, double *start, double *step) {
+  const int R = px->R, off = 3 * R;
+  double m490 = 0.0, m550 = 0.0, m640 = 0.0;
+  int r;
+  for (r = 0; r < R; r++) {
+    start[r] = H0;
+    step[r] = 1.25 * start[r];
+  }
+  for (r = 0; r < R; r++) m490 += px->r490[r];
+  m490 /= (double)R * 1;
+  for (r = 0; r < R; r++) {
+    start[R + r] = 100.0 * 4.0 * m490;
+    step[R + r] = 1.5 * start[R + r];
+  }
+  for (r = 0; r < R; r++) {
+    start[2 * R + r] = 1.0;
+    step[2 * R + r] = 0.5 * start[2 * R + r];
+  }
+  m490 = 0.0;
+  for (r = 0; r < R; r++) {
+    m490 += px->r490[r];
+    m550 += px->r550[r];
+    m640 += px->r640[r];
+  }
+  m490 /= (double)R;
+  m550 /= (double)R;
+  m640 /= (double)R;
+  start[off] = 100.0 * 0.072 * pow(m490 / m550, -1.7);
+  start[off + 1] = 1.5 * start[off];
+  start[off + 2] = 100.0 * 30.0 * px->sc->aw640 * m640;
+  step[off] = 2.0 * start[off];
+  step[off + 1] = 2.0 * start[off + 1];
+  step[off + 2] = 2.0 * start[off + 2];
+}
+
+static void region_fit(po_rpixel *px, const po_fit *fit, double *o) {
+  const int R = px->R, n = 3 * R + 3;
+  double start[PO_MAX_PARAMS], step[PO_MAX_PARAMS], xm[PO_MAX_PARAMS], best[PO_MAX_PARAMS];
+  double lowest = 1.0e4, y = 0.0;
+  int icount = 0, numres = 0, ifault = 0, k, r, b;
+  long total = 0;
+  int kept_evals = 0, kept_res = 0, kept_start = 0, kept_fault = 0, converged = 0;
+  for (r = 0; r < R; r++) { /* model/samodel.c:1785-1799 */
+    const double *wl = px->sc->wl;
+    px->r440[r] = po_interp_1d(wl, px->rrs[r], px->n_bands, 440.0);
+    px->r490[r] = po_interp_1d(wl, px->rrs[r], px->n_bands, 490.0);
+    px->r550[r] = po_interp_1d(wl, px->rrs[r], px->n_bands, 550.0);
+    px->r640[r] = po_interp_1d(wl, px->rrs[r], px->n_bands, 640.0);
+    px->r750[r] = po_interp_1d(wl, px->rrs[r], px->n_bands, 750.0);
+    if (px->r440[r] < 0.0) px->r440[r] = 0.0001;
+  }
+  memset(best, 0, sizeof best);
+  for (k = 0; k < fit->n_hstarts; k++) {
+    region_cold_start(px, fit->hstarts[k], start, step);
+    po_nelmin(region_cost, px, n, start, xm, &y, fit->reqmin, step, fit->konvge, fit->kcount,
+              &icount, &numres, &ifault);
+    total += icount;
+    if (y < lowest) {
+      lowest = y;
+      memcpy(best, xm, n * sizeof(double));
+      kept_evals = icount;
+      kept_res = numres;
+      kept_start = k;
+      kept_fault = ifault;
+      converged = (ifault == 0);
+      if (lowest < 2.5 * ((float)1)) break; /* model/samodel.c:2404 */
+    }
+  }
+  region_cost(best, px);
+  {
+    double K_min = 1.0e10, iod = 0.0, nobs = 0.0, depth = 0.0, ow = sqrt((double)R);
+    int found = 0;
+    for (b = 0; b < px->n_bands; b++)
+      if (!f_close((float)px->K[b], (float)0.0, 1.0e-4f) && px->K[b] < K_min) {
+        K_min = px->K[b];
+        found = 1;
+      }
+    if (!found) K_min = 0.0;
+    for (r = 0; r < R; r++) { /* origin-weighted depth, model/samodel.c:1999-2017 */
+      double H = fabs(best[r]);
+      if (r == px->origin) depth += ow * H;
+      else depth += H;
+    }
+    depth /= ow + ((double)R) - 1.0;
+    for (r = 0; r < R; r++)
+      for (b = 0; b < px->n_bands; b++) {
+        iod += px->rrs_bot[r][b] / px->rrs_mod[r][b];
+        nobs += 1.0;
+      }
+    iod = 100.0 * iod / nobs;
+    o[0] = depth;
+    o[1] = px->bottom_albedo;
+    o[2] = px->model_error;
+    o[3] = px->rrs_error;
+    o[4] = K_min;
+    o[5] = iod;
+  }
+  o[6] = (double)kept_evals;
+  o[7] = (double)total;
+  o[8] = converged ? 1.0 : 0.0;
+  o[9] = 0.0;
+  o[10] = 1.0;
+  o[11] = 0.01 * fabs(best[3 * R]);
+  o[19] = 0.01 * fabs(best[3 * R + 1]);
+  o[27] = 0.01 * fabs(best[3 * R + 2]);
+  o[35] = (double)kept_res;
+  o[36] = (double)kept_start;
+  o[37] = (double)kept_fault;
+  o[38] = (double)R;
+  o[39] = (double)px->origin;
+}
+
+int po_region_invert_batch(int n_bands, const double *wl, double theta_sun_deg,
+                           double theta_view_deg, double h_tide, const float *grid, int nrows,
+                           int ncols, float nodata, double reqmin, int konvge, int kcount,
+                           int nthreads, double *out) {
+  po_scene sc;
+  po_fit fit;
+  int64_t p, npix = (int64_t)nrows * ncols;
+  if (n_bands < 2 || n_bands > PO_MAX_BANDS) return 1;
+  scene_init(&sc, n_bands, wl, theta_sun_deg, theta_view_deg, h_tide);
+  fit.seed_step_scale = 1.0;
+  fit.reqmin = reqmin;
+  fit.konvge = konvge;
+  fit.kcount = kcount;
+  fit.n_hstarts = 8;
+  fit.hstarts = po_default_hstarts;
+#if _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 4)
+#endif
+  for (p = 0; p < npix; p++) {
+    const int i = (int)(p / ncols), j = (int)(p % ncols);
+    double *o = out + p * PO_NOUT;
+    po_rpixel px;
+    int ii, jj, b;
+    memset(o, 0, PO_NOUT * sizeof(double));
+    if (masked(grid + p * n_bands, n_bands, nodata)) {
+      o[9] = 1.0;
+      continue;
+    }
+    memset(&px, 0, sizeof px);
+    px.sc = &sc;
+    px.n_bands = n_bands;
+    /* extract_Rrs_data, model/samodel.c:2957-3027 */
+    for (ii = -1; ii <= 1; ii++) {
+      const int iii = i + ii < 0 ? 0 : (i + ii > nrows - 1 ? nrows - 1 : i + ii);
+      for (jj = -1; jj <= 1; jj++) {
+        const int jjj = j + jj < 0 ? 0 : (j + jj > ncols - 1 ? ncols - 1 : j + jj);
+        const float *q = grid + ((int64_t)iii * ncols + jjj) * n_bands;
+        int nodata_region = 0;
+        for (b = 0; b < n_bands; b++) {
+          if (!f_close(q[b], nodata, 1.0e-6f)) {
+            px.rrs[px.R][b] = q[b];
+          } else {
+            nodata_region = 1;
+            break;
+          }
+        }
+        if (i == iii && j == jjj) px.origin = px.R;
+        if (!nodata_region) px.R++;
+      }
+    }
+    if (px.R == 0) continue;
+    region_fit(&px, &fit, o);
+  }
+  return 0;
+}
+

@@ -72,6 +72,10 @@ void po_generate_joint(uint64_t seed, int64_t npix, int n_bands, const double *w
                        double *truth_out);
 void po_philox4x32(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
                    uint32_t *out4);
+int po_region_invert_batch(int n_bands, const double *wl, double theta_sun_deg,
+                           double theta_view_deg, double h_tide, const float *grid, int nrows,
+                           int ncols, float nodata, double reqmin, int konvge, int kcount,
+                           int nthreads, double *out);
 int po_depth_sigma(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
                    const float *rrs, int64_t npix, const float *depth, const double *r_sigma,
                    int n_samples, uint64_t seed, double reqmin, int konvge, int kcount,

@@ -80,18 +80,19 @@ static double *bottom_table(int k) {
   }
 }
 
-static model_data *md_new(void) {
+/* model_data for up to R spatial regions (R = 1: one pixel). */
+static model_data *md_new_r(int R) {
   model_data *md = (model_data *)calloc(1, sizeof(model_data));
   int S = REF_MAX_SCENES, B = REF_MAX_BANDS;
-  md->max_n_regions = 1;
+  md->max_n_regions = R;
   md->n_bands = (int *)calloc(S, sizeof(int));
   md->n_raw_bands = (int *)calloc(S, sizeof(int));
-  allocate_double_array_3d(&md->Rrs_measured, 1, S, B);
-  allocate_double_array_3d(&md->Rrs_modelled, 1, S, B);
-  allocate_double_array_3d(&md->rrs_modelled, 1, S, B);
-  allocate_double_array_3d(&md->rrs_bottom, 1, S, B);
-  allocate_double_array_3d(&md->rrs_dp, 1, S, B);
-  allocate_double_array_3d(&md->rho, 1, S, B);
+  allocate_double_array_3d(&md->Rrs_measured, R, S, B);
+  allocate_double_array_3d(&md->Rrs_modelled, R, S, B);
+  allocate_double_array_3d(&md->rrs_modelled, R, S, B);
+  allocate_double_array_3d(&md->rrs_bottom, R, S, B);
+  allocate_double_array_3d(&md->rrs_dp, R, S, B);
+  allocate_double_array_3d(&md->rho, R, S, B);
   allocate_double_array_2d(&md->wavelengths, S, B);
   allocate_double_array_2d(&md->raw_wavelengths, S, B);
   allocate_double_array_2d(&md->a_0, S, B);
@@ -101,11 +102,11 @@ static model_data *md_new(void) {
   allocate_double_array_2d(&md->K, S, B);
   allocate_double_array_2d(&md->rrs_noise, S, B);
   allocate_double_array_3d(&md->bottom_reflectance, REF_N_BOTTOM_TABLE, S, B);
-  allocate_double_array_2d(&md->Rrs440, 1, S);
-  allocate_double_array_2d(&md->Rrs490, 1, S);
-  allocate_double_array_2d(&md->Rrs550, 1, S);
-  allocate_double_array_2d(&md->Rrs640, 1, S);
-  allocate_double_array_2d(&md->Rrs750, 1, S);
+  allocate_double_array_2d(&md->Rrs440, R, S);
+  allocate_double_array_2d(&md->Rrs490, R, S);
+  allocate_double_array_2d(&md->Rrs550, R, S);
+  allocate_double_array_2d(&md->Rrs640, R, S);
+  allocate_double_array_2d(&md->Rrs750, R, S);
   md->theta_view = (double *)calloc(S, sizeof(double));
   md->theta_sun = (double *)calloc(S, sizeof(double));
   md->sec_theta_view = (double *)calloc(S, sizeof(double));
@@ -120,14 +121,16 @@ static model_data *md_new(void) {
   return md;
 }
 
+static model_data *md_new(void) { return md_new_r(1); }
+
 static void md_free(model_data *md) {
-  int S = REF_MAX_SCENES;
-  free_double_array_3d(md->Rrs_measured, 1, S);
-  free_double_array_3d(md->Rrs_modelled, 1, S);
-  free_double_array_3d(md->rrs_modelled, 1, S);
-  free_double_array_3d(md->rrs_bottom, 1, S);
-  free_double_array_3d(md->rrs_dp, 1, S);
-  free_double_array_3d(md->rho, 1, S);
+  int S = REF_MAX_SCENES, R = md->max_n_regions;
+  free_double_array_3d(md->Rrs_measured, R, S);
+  free_double_array_3d(md->Rrs_modelled, R, S);
+  free_double_array_3d(md->rrs_modelled, R, S);
+  free_double_array_3d(md->rrs_bottom, R, S);
+  free_double_array_3d(md->rrs_dp, R, S);
+  free_double_array_3d(md->rho, R, S);
   free_double_array_2d(md->wavelengths, S);
   free_double_array_2d(md->raw_wavelengths, S);
   free_double_array_2d(md->a_0, S);
@@ -137,11 +140,11 @@ static void md_free(model_data *md) {
   free_double_array_2d(md->K, S);
   free_double_array_2d(md->rrs_noise, S);
   free_double_array_3d(md->bottom_reflectance, REF_N_BOTTOM_TABLE, S);
-  free_double_array_2d(md->Rrs440, 1);
-  free_double_array_2d(md->Rrs490, 1);
-  free_double_array_2d(md->Rrs550, 1);
-  free_double_array_2d(md->Rrs640, 1);
-  free_double_array_2d(md->Rrs750, 1);
+  free_double_array_2d(md->Rrs440, R);
+  free_double_array_2d(md->Rrs490, R);
+  free_double_array_2d(md->Rrs550, R);
+  free_double_array_2d(md->Rrs640, R);
+  free_double_array_2d(md->Rrs750, R);
   free(md->n_bands); free(md->n_raw_bands);
   free(md->theta_view); free(md->theta_sun); free(md->sec_theta_view); free(md->sec_theta_sun);
   free(md->H_tide); free(md->P); free(md->G); free(md->X); free(md->D); free(md->prev);
@@ -322,6 +325,82 @@ int photic_ref_joint_invert_batch(int n_bands, const double *wl, double theta_vi
     }
     md_free(md);
   }
+  return 0;
+}
+
+/* Spatial-region fit (n_spatial = 2: the 3 x 3 neighbourhood of each pixel,
+ * edges clamped, neighbours with nodata left out; model/samodel.c:2957-3027)
+ * through the reference's own extract_Rrs_data and samodel_optimise, one
+ * scene, smoothing radius 1.  grid is [nrows][ncols][n_bands] float; out is
+ * [npix][REF_NOUT] with o[38] = regions, o[39] = origin region. */
+int photic_ref_region_invert_batch(int n_bands, const double *wl, double theta_sun_deg,
+                                   double theta_view_deg, double h_tide, const float *grid,
+                                   int nrows, int ncols, float nodata, int n_spatial,
+                                   int use_override, double reqmin, int konvge, int kcount,
+                                   int nthreads, double *out) {
+  geogrid *gd;
+  scene *sc;
+  int b, R;
+  if (n_bands < 2 || n_bands > REF_MAX_BANDS || n_spatial < 1 || n_spatial > 2) return 1;
+  R = (2 * n_spatial - 1) * (2 * n_spatial - 1);
+  gd = (geogrid *)calloc(n_bands, sizeof(geogrid));
+  sc = (scene *)calloc(1, sizeof(scene));
+  sc->n_bands = n_bands;
+  sc->nrows = nrows;
+  sc->ncols = ncols;
+  for (b = 0; b < n_bands; b++) {
+    int i, j;
+    sc->band_indexes[b] = b;
+    gd[b].nrows = nrows;
+    gd[b].ncols = ncols;
+    gd[b].nodata_value = nodata;
+    allocate_float_array_2d(&gd[b].array, nrows, ncols);
+    for (i = 0; i < nrows; i++)
+      for (j = 0; j < ncols; j++) gd[b].array[i][j] = grid[((size_t)i * ncols + j) * n_bands + b];
+  }
+#if _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel
+#endif
+  {
+    model_data *md = md_new_r(R);
+    int scene_index = 0;
+    long long p, npix = (long long)nrows * ncols;
+    md_set_scene(md, 0, n_bands, wl, theta_sun_deg, theta_view_deg, h_tide);
+#if _OPENMP
+#pragma omp for schedule(dynamic, 4)
+#endif
+    for (p = 0; p < npix; p++) {
+      int i = (int)(p / ncols), j = (int)(p % ncols), r, bb;
+      double *o = out + p * REF_NOUT;
+      memset(o, 0, REF_NOUT * sizeof(double));
+      if (pixel_masked(grid + p * n_bands, n_bands, nodata)) {
+        o[9] = 1.0;
+        continue;
+      }
+      md_reset_pixel(md, 1, n_bands);
+      for (r = 0; r < R; r++) /* the loop's defaults, model/samodel.c:921-932 */
+        for (bb = 0; bb < n_bands; bb++) {
+          md->Rrs_measured[r][0][bb] = 0.0;
+          md->Rrs_modelled[r][0][bb] = 0.0;
+          md->rrs_modelled[r][0][bb] = 0.0;
+          md->rrs_bottom[r][0][bb] = 0.0;
+          md->rrs_dp[r][0][bb] = 0.0;
+          md->rho[r][0][bb] = 0.0;
+        }
+      extract_Rrs_data(i, j, sc, gd, &scene_index, 1, n_spatial, 1, nrows, ncols, md, 0.0);
+      if (md->n_regions == 0) continue;
+      set_tol(use_override, reqmin, konvge, kcount);
+      samodel_optimise(md);
+      store_result(md, o, g_tol.evals);
+      o[38] = (double)md->n_regions;
+      o[39] = (double)md->origin;
+    }
+    md_free(md);
+  }
+  for (b = 0; b < n_bands; b++) free_float_array_2d(gd[b].array, nrows);
+  free(gd);
+  free(sc);
   return 0;
 }
 

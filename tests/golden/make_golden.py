@@ -69,6 +69,18 @@ def cost_and_nelmin():
                         band_constants=bc)
 
 
+def regions():
+    # spatial-region fit (3 x 3 neighbourhoods) of a small grid with masked
+    # pixels, edges and a reduced evaluation budget
+    nr, nc = 14, 12
+    rrs, _ = O.generate_single(20260606, nr * nc, pix0=0, mask_frac=0.15)
+    grid = rrs.reshape(nr, nc, rrs.shape[1])
+    ref = O.region_invert_batch(grid, kcount=400, which="reference", nthreads=os.cpu_count())
+    cols = KEEP + [38, 39]
+    np.savez_compressed(os.path.join(OUT, "regions.npz"), grid=grid, ref=ref[:, cols],
+                        cols=np.array(cols), kcount=np.array(400))
+
+
 if __name__ == "__main__":
     O.build(ref=True)
     if not O.reference_available():
@@ -76,6 +88,7 @@ if __name__ == "__main__":
     single()
     joint()
     cost_and_nelmin()
+    regions()
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)), "bytes")

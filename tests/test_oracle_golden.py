@@ -85,3 +85,11 @@ def test_philox_known_answer(port):
                                                      0x9b00dbd8]
     assert port.philox4x32([0xffffffff] * 4, [0xffffffff] * 2) == [0x408f276d, 0x41c83b0e,
                                                                   0xa20bc7c6, 0x6d5451fd]
+
+
+def test_regions_golden(port, golden_dir):
+    """Spatial-region fit (3 x 3 neighbourhoods) against the reference's own
+    extract_Rrs_data + samodel_optimise."""
+    g = np.load(os.path.join(golden_dir, "regions.npz"))
+    out = port.region_invert_batch(g["grid"], kcount=int(g["kcount"]), nthreads=4)
+    np.testing.assert_array_equal(out[:, g["cols"]], g["ref"])

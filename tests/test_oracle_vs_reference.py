@@ -41,3 +41,16 @@ def test_interp_1d_bit_exact():
     Y = np.array([0.011, 0.013, 0.009, 0.001])
     for x in [400.0, 440.0, 443.0, 443.001, 482.0, 490.0, 550.0, 640.0, 655.0, 700.0, 750.0]:
         assert O.interp_1d(X, Y, x) == O.interp_1d(X, Y, x, which="reference")
+
+
+def test_regions_bit_exact():
+    """The spatial-region restatement against the compiled reference."""
+    if not O.reference_available():
+        pytest.skip("reference library not built")
+    rrs, _ = O.generate_single(31, 9 * 31, pix0=100, mask_frac=0.2)
+    grid = rrs.reshape(9, 31, 4)
+    cols = [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 19, 27, 38, 39]
+    a = O.region_invert_batch(grid, reqmin=1e-2, konvge=100, kcount=5000, nthreads=8)
+    b = O.region_invert_batch(grid, reqmin=1e-2, konvge=100, kcount=5000, nthreads=8,
+                              which="reference")
+    np.testing.assert_array_equal(a[:, cols], b[:, cols])
