@@ -203,6 +203,18 @@ double photic_interp_1d(const double *X, const double *Y, int32_t n, double x);
  * a_w(640). */
 int photic_band_constants(const photic_config *cfg, double *out);
 
+/* Spatial-region fit (model/samodel.c:2957-3027 with n_spatial = 2): every
+ * pixel of the [nrows][ncols][n_bands] grid (device, float) is fitted with
+ * its 3 x 3 neighbourhood -- indexes clamped at the edges, neighbours with a
+ * nodata band left out, the centre's slot the origin -- one depth, albedo and
+ * q per region, shared P, G, X, and the cost's depth- and bottom-continuity
+ * terms; depth is the origin-weighted mean (model/samodel.c:1999-2017).
+ * Outputs per pixel; status carries the region count in bits 24-27.  One
+ * scene, one bottom type, up to 4 bands, n_spatial = 2 only. */
+int photic_region_invert_batch(const photic_config *cfg, const float *d_grid, int32_t nrows,
+                               int32_t ncols, int32_t n_spatial, const photic_outputs *out,
+                               void *stream);
+
 /* Depth uncertainty, the reference's ad hoc estimate (model/samodel.c:
  * 1368-1479): for each 0.25 m interval up to the deepest fitted depth (whole
  * metres, at most 30 m), n_samples pixels of the interval are drawn (up to

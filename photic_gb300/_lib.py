@@ -109,6 +109,9 @@ _SIGS = {
                                        C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
                                        C.c_void_p]),
     "photic_measure_peaks": (C.c_int, [C.POINTER(C.c_double)] * 3),
+    "photic_region_invert_batch": (C.c_int, [C.POINTER(photic_config), C.c_void_p, C.c_int32,
+                                             C.c_int32, C.c_int32, C.POINTER(photic_outputs),
+                                             C.c_void_p]),
     "photic_depth_sigma": (C.c_int, [C.POINTER(photic_config), C.c_void_p, C.c_int64, C.c_void_p,
                                      C.POINTER(C.c_double), C.c_int32, C.c_uint64, C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -178,6 +178,28 @@ def invert(rrs: torch.Tensor, config: Optional[Config] = None, *,
     return out
 
 
+def region_invert(grid: torch.Tensor, config: Optional[Config] = None, *,
+                  fields: Sequence[str] = OUTPUT_FIELDS,
+                  stream: Optional[torch.cuda.Stream] = None) -> Dict[str, torch.Tensor]:
+    """Spatial-region fit (model/samodel.c:2957-3027, n_spatial = 2) of a
+    [nrows, ncols, n_bands] float32 grid: every pixel with its 3 x 3
+    neighbourhood, one depth / albedo / q per region, shared P, G, X,
+    depth- and bottom-continuity terms; depth is the origin-weighted mean.
+    Outputs are per pixel ([nrows * ncols]); bits 24-27 of status hold the
+    region count."""
+    cfg = config or Config()
+    _check_cuda(grid, "grid", torch.float32)
+    if grid.dim() != 3 or grid.shape[2] != cfg.n_bands:
+        raise ValueError(f"grid must be [nrows, ncols, {cfg.n_bands}]")
+    nrows, ncols = int(grid.shape[0]), int(grid.shape[1])
+    out = alloc_outputs(nrows * ncols, grid.device, [f for f in fields if f != "params"])
+    c = cfg.to_c()
+    os_ = _outputs_struct(out)
+    L.check(L.lib().photic_region_invert_batch(C.byref(c), _ptr(grid), nrows, ncols, 2,
+                                               C.byref(os_), _stream_handle(stream)))
+    return out
+
+
 def depth_sigma(rrs: torch.Tensor, depth: torch.Tensor, r_sigma: Sequence[float],
                 config: Optional[Config] = None, *, n_samples: int = 128, seed: int = 1,
                 stream: Optional[torch.cuda.Stream] = None) -> Dict[str, torch.Tensor]:

@@ -1844,3 +1844,42 @@ extern "C" int photic_depth_sigma(const photic_config *cfg, const float *d_rrs, 
   if (e != cudaSuccess) return cuda_fail(e, "depth-sigma kernels");
   return PHOTIC_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Spatial-region fit (model/samodel.c:2957-3027 with n_spatial = 2).
+// ---------------------------------------------------------------------------
+extern "C" int photic_region_invert_batch(const photic_config *cfg, const float *d_grid,
+                                          int32_t nrows, int32_t ncols, int32_t n_spatial,
+                                          const photic_outputs *out, void *stream) {
+  int rc = photic_config_check(cfg);
+  if (rc) return rc;
+  if (n_spatial != 2) return fail(PHOTIC_ERR_UNSUPPORTED, "n_spatial must be 2 (3 x 3 regions)");
+  if (cfg->n_bands > 4) return fail(PHOTIC_ERR_UNSUPPORTED, "the region fit takes up to 4 bands");
+  if (nrows < 0 || ncols < 0 || !out || ((int64_t)nrows * ncols > 0 && !d_grid))
+    return fail(PHOTIC_ERR_INVALID, "bad arguments");
+  if ((int64_t)nrows * ncols == 0) return PHOTIC_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned int *err = nullptr;
+  int sms = 0;
+  rc = device_state(&err, &sms);
+  if (rc) return rc;
+  RegionArgs a;
+  memset(&a, 0, sizeof a);
+  make_fit(*cfg, a.fp);
+  make_scene(*cfg, cfg->theta_sun_deg, a.sc);
+  a.grid = d_grid;
+  a.nrows = nrows;
+  a.ncols = ncols;
+  a.out = *out;
+  a.error = err;
+  unsigned long long *queue = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&queue, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return fail(PHOTIC_ERR_NOMEM, "queue head");
+  cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
+  a.queue = queue;
+  e = launch_region(a, sms, cfg->blocks_per_sm, s);
+  cudaFreeAsync(queue, s);
+  if (e != cudaSuccess) return cuda_fail(e, "region launch");
+  return PHOTIC_OK;
+}
+

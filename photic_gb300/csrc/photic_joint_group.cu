@@ -30,6 +30,7 @@
 #include "photic_fp64.cuh"
 #include "photic_kernels.h"
 #include "photic_nm.cuh"
+#include "photic_nmgroup.cuh"
 
 namespace photic {
 
@@ -60,348 +61,6 @@ struct JG {
 // Per-group view of the shared memory.
 struct GSmem {
   double *V, *F, *X, *dd, *kk, *io, *misc;
-};
-
-// Group-distributed Nelder-Mead: the state machine of NmLane with the
-// coordinate loops cut to the lane's own coordinates.
-template <int N, int C, int G, int CG>
-struct NmGroup {
-  double *V, *Fv, *X;  // shared: V[j * CG + i], this lane's costs Fv[j * G], X[i]
-  int gl;              // lane within the group
-  unsigned gmask;      // the group's lanes
-  double cen[C], refl[C], trial[C], xmin[C], start[C], step[C];
-  double ylo, fr, scale, var_limit;
-  long long floor_lo;
-  int32_t phase, jj, hi, lo, icount, numres, ifault, countdown, kcount, konvge;
-
-  __device__ __forceinline__ int coord(int t) const { return gl + t * G; }
-  __device__ __forceinline__ bool own(int t) const { return coord(t) < N; }
-  // The slot holding coordinate i on this lane, -1 if another lane owns it.
-  // (Matching i against coord(t) slot by slot instead lost the match on
-  // the second slot in the compiled kernel: the stepped vertex of the last
-  // coordinate came out unstepped.)
-  __device__ __forceinline__ int slot_of(int i) const { return (i % G) == gl ? i / G : -1; }
-  __device__ __forceinline__ double &Vv(int j, int i) { return V[j * CG + i]; }
-  __device__ __forceinline__ double &F(int j) { return Fv[j * G]; }
-
-  // Every slot gets a defined value, also those of coordinates the lane
-  // does not own (they are computed on but never stored).
-  __device__ __forceinline__ void clear() {
-#pragma unroll
-    for (int t = 0; t < C; t++) {
-      cen[t] = 0.0;
-      refl[t] = 0.0;
-      trial[t] = 0.0;
-      xmin[t] = 0.0;
-      start[t] = 0.0;
-      step[t] = 0.0;
-    }
-    ylo = fr = 0.0;
-    scale = 1.0;
-    floor_lo = 0;
-    phase = jj = hi = lo = icount = numres = ifault = countdown = 0;
-  }
-
-  __device__ __forceinline__ void begin(double var_limit_, int32_t konvge_, int32_t kcount_) {
-    konvge = konvge_;
-    kcount = kcount_;
-    countdown = konvge_;
-    icount = 0;
-    numres = 0;
-    ifault = 0;
-    scale = 1.0;
-    var_limit = var_limit_;
-    restart_simplex();
-  }
-
-  __device__ __forceinline__ void restart_simplex() {
-#pragma unroll
-    for (int t = 0; t < C; t++)
-      if (own(t)) {
-        X[coord(t)] = start[t];
-        Vv(N, coord(t)) = start[t];
-      }
-    phase = PH_INIT_BASE;
-  }
-
-  __device__ __forceinline__ void make_vertex(int j) {
-    const int ts = slot_of(j);
-#pragma unroll
-    for (int t = 0; t < C; t++)
-      if (own(t)) {
-        const int i = coord(t);
-        double s = start[t];
-        if (t == ts) s = start[t] + step[t] * scale;
-        X[i] = s;
-        Vv(j, i) = s;
-      }
-    jj = j;
-    phase = PH_INIT_VERT;
-  }
-
-  __device__ __forceinline__ void find_lo() {
-    ylo = F(0);
-    lo = 0;
-    for (int j = 1; j <= N; j++) {
-      const double fj = F(j);
-      if (fj < ylo) {
-        ylo = fj;
-        lo = j;
-      }
-    }
-  }
-
-  __device__ __forceinline__ bool inner_top() {
-    if (kcount <= icount) return false;
-    double yhi = F(0);
-    hi = 0;
-    for (int j = 1; j <= N; j++) {
-      const double fj = F(j);
-      if (yhi < fj) {
-        yhi = fj;
-        hi = j;
-      }
-    }
-#pragma unroll
-    for (int t = 0; t < C; t++)
-      if (own(t)) {
-        const int i = coord(t);
-        double z = 0.0;
-        for (int j = 0; j <= N; j++) z = z + Vv(j, i);
-        z = z - Vv(hi, i);
-        cen[t] = z / (double)N;
-        refl[t] = cen[t] + (cen[t] - Vv(hi, i));
-        X[i] = refl[t];
-      }
-    phase = PH_REFLECT;
-    return true;
-  }
-
-  // Each lane keeps its own copy of the vertex costs (the same values in
-  // every lane of the group), so no lane ever reads a cost another lane is
-  // writing, whatever the lanes' relative progress.
-  __device__ __forceinline__ void replace_hi(const double (&p)[C], double y) {
-#pragma unroll
-    for (int t = 0; t < C; t++)
-      if (own(t)) Vv(hi, coord(t)) = p[t];
-    F(hi) = y;
-  }
-
-  __device__ __forceinline__ bool iteration_end() {
-    const double fh = F(hi);
-    if (fh < ylo) {
-      ylo = fh;
-      lo = hi;
-    }
-    countdown--;
-    if (countdown > 0) return false;
-    if (icount <= kcount) {
-      countdown = konvge;
-      double z = 0.0;
-      for (int j = 0; j <= N; j++) z = z + F(j);
-      const double mean = z / (double)(N + 1);
-      z = 0.0;
-      for (int j = 0; j <= N; j++) {
-        const double d = F(j) - mean;
-        z = z + d * d;
-      }
-      if (z <= var_limit) return true;
-    }
-    return false;
-  }
-
-  __device__ __forceinline__ void set_x_from(const double (&p)[C]) {
-#pragma unroll
-    for (int t = 0; t < C; t++)
-      if (own(t)) X[coord(t)] = p[t];
-  }
-
-  // xmin[jj] += sgn * del on the lane that owns coordinate jj.
-  __device__ __forceinline__ void probe_move(int sgn_twice) {
-    const int ts = slot_of(jj);
-#pragma unroll
-    for (int t = 0; t < C; t++)
-      if (t == ts) {
-        const double del = step[t] * 1.0e-6;
-        if (sgn_twice > 0) xmin[t] = xmin[t] + del;
-        else if (sgn_twice < 0) xmin[t] = (xmin[t] - del) - del;
-        else xmin[t] = xmin[t] + del;  // back to the centre after the minus probe
-      }
-  }
-
-  __device__ __forceinline__ bool step_machine(double y) {
-    enum { CS_NONE = -1, CS_READY, CS_TOP, CS_ITER_END, CS_END_INNER, CS_PROBE_PLUS,
-           CS_PROBE_END, CS_NM_DONE };
-    int cs = CS_NONE;
-    switch (phase) {
-      case PH_INIT_BASE:
-        F(N) = y;
-        icount++;
-        make_vertex(0);
-        break;
-      case PH_INIT_VERT:
-        F(jj) = y;
-        icount++;
-        if (jj + 1 < N) make_vertex(jj + 1);
-        else cs = CS_READY;
-        break;
-      case PH_REFLECT:
-        fr = y;
-        icount++;
-        if (fr < ylo) {
-#pragma unroll
-          for (int t = 0; t < C; t++) trial[t] = cen[t] + 2.0 * (refl[t] - cen[t]);
-          set_x_from(trial);
-          phase = PH_EXPAND;
-        } else {
-          int worse = 0;
-          for (int j = 0; j <= N; j++)
-            if (fr < F(j)) worse++;
-          if (worse > 1) {
-            replace_hi(refl, fr);
-            cs = CS_ITER_END;
-          } else if (worse == 0) {
-#pragma unroll
-            for (int t = 0; t < C; t++)
-              if (own(t)) trial[t] = cen[t] + (Vv(hi, coord(t)) - cen[t]) * 0.5;
-            set_x_from(trial);
-            phase = PH_CONTRACT_IN;
-          } else {
-#pragma unroll
-            for (int t = 0; t < C; t++) trial[t] = cen[t] + (refl[t] - cen[t]) * 0.5;
-            set_x_from(trial);
-            phase = PH_CONTRACT_OUT;
-          }
-        }
-        break;
-      case PH_EXPAND:
-        icount++;
-        if (fr < y) replace_hi(refl, fr);
-        else replace_hi(trial, y);
-        cs = CS_ITER_END;
-        break;
-      case PH_CONTRACT_IN: {
-        icount++;
-        const bool shrink = F(hi) < y;
-        if (shrink) {
-#pragma unroll
-          for (int t = 0; t < C; t++)
-            if (own(t)) {
-              const int i = coord(t);
-              const double s = (Vv(0, i) + Vv(lo, i)) * 0.5;
-              Vv(0, i) = s;
-              X[i] = s;
-            }
-          jj = 0;
-          phase = PH_SHRINK;
-        } else {
-          replace_hi(trial, y);
-          cs = CS_ITER_END;
-        }
-        break;
-      }
-      case PH_SHRINK:
-        F(jj) = y;
-        icount++;
-        if (jj < N) {
-          const int j = jj + 1;
-#pragma unroll
-          for (int t = 0; t < C; t++)
-            if (own(t)) {
-              const int i = coord(t);
-              const double s = (Vv(j, i) + Vv(lo, i)) * 0.5;
-              Vv(j, i) = s;
-              X[i] = s;
-            }
-          jj = j;
-        } else {
-          cs = CS_READY;
-        }
-        break;
-      case PH_CONTRACT_OUT:
-        icount++;
-        if (y <= fr) replace_hi(trial, y);
-        else replace_hi(refl, fr);
-        cs = CS_ITER_END;
-        break;
-      case PH_PROBE_PLUS:
-        icount++;
-        if (trunc10(y) < floor_lo) {
-          ifault = 2;
-          cs = CS_PROBE_END;
-        } else {
-          probe_move(-1);
-          set_x_from(xmin);
-          phase = PH_PROBE_MINUS;
-        }
-        break;
-      case PH_PROBE_MINUS:
-        icount++;
-        if (trunc10(y) < floor_lo) {
-          ifault = 2;
-          cs = CS_PROBE_END;
-        } else {
-          probe_move(0);
-          jj++;
-          cs = (jj < N) ? CS_PROBE_PLUS : CS_PROBE_END;
-        }
-        break;
-      default:
-        break;
-    }
-    while (cs != CS_NONE) {
-      switch (cs) {
-        case CS_READY:
-          find_lo();
-          cs = CS_TOP;
-          break;
-        case CS_TOP:
-          cs = inner_top() ? CS_NONE : CS_END_INNER;
-          break;
-        case CS_ITER_END:
-          cs = iteration_end() ? CS_END_INNER : CS_TOP;
-          break;
-        case CS_END_INNER:
-#pragma unroll
-          for (int t = 0; t < C; t++)
-            if (own(t)) xmin[t] = Vv(lo, coord(t));
-          floor_lo = trunc10(F(lo));
-          if (kcount < icount) {
-            ifault = 2;
-            cs = CS_NM_DONE;
-          } else {
-            ifault = 0;
-            jj = 0;
-            cs = CS_PROBE_PLUS;
-          }
-          break;
-        case CS_PROBE_PLUS:
-          probe_move(+1);
-          set_x_from(xmin);
-          phase = PH_PROBE_PLUS;
-          cs = CS_NONE;
-          break;
-        case CS_PROBE_END:
-          if (ifault == 0) {
-            cs = CS_NM_DONE;
-          } else {
-#pragma unroll
-            for (int t = 0; t < C; t++) start[t] = xmin[t];
-            scale = 1.0e-6;
-            numres++;
-            restart_simplex();
-            cs = CS_NONE;
-          }
-          break;
-        case CS_NM_DONE:
-          return true;
-        default:
-          cs = CS_NONE;
-          break;
-      }
-    }
-    return false;
-  }
 };
 
 // Rrs(490), Rrs(550), Rrs(640) of scene s of the pixel whose observations

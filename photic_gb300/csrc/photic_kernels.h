@@ -207,6 +207,19 @@ struct EmpSeedArgs {
 };
 cudaError_t launch_empirical_seeds(const EmpSeedArgs &a, cudaStream_t s);
 
+// Spatial-region fit, 3 x 3 neighbourhoods (photic_region.cu).
+struct RegionArgs {
+  FitParams fp;
+  SceneConsts sc;
+  const float *grid;            // [nrows][ncols][n_bands]
+  int nrows, ncols;
+  unsigned long long *queue;    // work-queue head (zeroed)
+  photic_outputs out;           // per pixel; status carries the region count << 24
+  unsigned int *error;
+};
+size_t region_smem_bytes();
+cudaError_t launch_region(const RegionArgs &a, int sms, int per_sm, cudaStream_t s);
+
 // Depth uncertainty by re-inversion of perturbed samples (photic_aux.cu).
 constexpr int kDsMaxIntervals = 120;  // 30 m in 0.25 m steps
 struct DepthSigmaArgs {
