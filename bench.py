@@ -167,6 +167,8 @@ def main():
                     help="initial simplex of a seeded fit, relative to the cold-start steps")
     ap.add_argument("--joint-npix", type=int, default=1 << 16,
                     help="pixels of the 4096x4096 temporal grid for the joint-fit leg (0: skip)")
+    ap.add_argument("--region-side", type=int, default=96,
+                    help="side of the square grid for the spatial-region leg (0: skip)")
     ap.add_argument("--serve-requests", type=int, default=12,
                     help="tile requests of the serving leg (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=50.0)
@@ -322,6 +324,9 @@ def main():
     temporal = None
     if rank == 0 and args.joint_npix > 0:
         temporal = temporal_leg(args, dev)
+    regions = None
+    if rank == 0 and args.region_side > 0:
+        regions = region_leg(args, dev)
     warm, net, serving = None, None, None
     if rank == 0 and args.warm_npix > 0:
         net, warm = warm_start_leg(args, dev)
@@ -346,6 +351,7 @@ def main():
                            "mean_evals": float(evals[fitted].mean()) if fitted.any() else 0.0},
                 "oracle_sample": sample_stats, "roofline": roof, "cpu_baseline": cpu,
                 "warm_start": warm, "serving": serving, "temporal": temporal,
+                "regions": regions,
                 "e2e": e2e, "clocks": clk}
         print(json.dumps(line))
     if pg_ is not None:
@@ -501,6 +507,50 @@ def temporal_leg(args, dev):
         del g, out
     torch.cuda.empty_cache()
     return res
+
+
+def region_leg(args, dev):
+    """Spatial-region fit (3 x 3 neighbourhoods) of a square grid of the
+    plain-method generator: converged pixels/s, parity against the FP64
+    oracle on a corner block, and the oracle's own rate beside it."""
+    import torch
+    import photic_gb300 as pg
+    from oracle import oracle as O
+    n = args.region_side
+    rrs, _ = pg.generate_scene(n * n, seed=SEED + 5, device=dev)
+    grid = rrs.reshape(n, n, 4).contiguous()
+    cfg = pg.Config()
+    pg.region_invert(grid[:8, :8].contiguous(), cfg, fields=("depth_f64", "status"))
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record()
+    out = pg.region_invert(grid, cfg, fields=("depth_f64", "status", "evals"))
+    ev1.record()
+    torch.cuda.synchronize()
+    pg.sync()
+    t = ev0.elapsed_time(ev1) * 1e-3
+    st = out["status"]
+    conv = ((st & 0xFF) == 0) & ((st >> 8) & 1).bool()
+    # parity on a 16 x 16 corner block fitted on its own (its edge pixels
+    # see a clamped neighbourhood, as on the GPU for the same block)
+    k = min(16, n)
+    blk = grid[:k, :k].contiguous()
+    g_blk = pg.region_invert(blk, cfg, fields=("depth_f64", "status"))
+    pg.sync()
+    t0 = time.perf_counter()
+    ref = O.region_invert_batch(blk.cpu().numpy(), nthreads=os.cpu_count() or 1)
+    t_cpu = time.perf_counter() - t0
+    fit = (g_blk["status"].cpu().numpy() & 0xFF) == 0
+    d = np.abs(g_blk["depth_f64"].cpu().numpy()[fit] - ref[fit, 0])
+    within = float(np.mean(d <= 0.01)) if fit.any() else 1.0
+    return {"workload": f"{n}x{n} grid, 3x3 regions per pixel (n = 3R + 3 <= 30 unknowns)",
+            "converged_px_s_within_1cm": float(conv.sum().item()) * within / t, "seconds": t,
+            "converged_share": float(conv.float().mean().item()),
+            "mean_evals": float(out["evals"].float().mean().item()),
+            "oracle_sample": {"pixels": int(fit.sum()), "frac_within_1cm": within,
+                              "median_abs_dH_m": float(np.median(d)) if fit.any() else 0.0},
+            "cpu_oracle_px_s": k * k / t_cpu, "cpu_threads": os.cpu_count() or 1}
 
 
 def serving_leg(args, net):
