@@ -185,17 +185,14 @@ def main():
     import photic_gb300 as pg
     from photic_gb300 import _lib as L
 
+    from photic_gb300 import replicas
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    pg_ = None
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=dev)
-        pg_ = dist
+    pg_ = replicas.init("nccl", dev)
     stream = torch.cuda.current_stream()
     cfg = pg.Config(precision=args.precision)
     npix = args.npix
-    pix0 = rank * npix
+    pix0 = replicas.shard_start(rank, npix)
     rrs, truth = pg.generate_scene(npix, seed=SEED, config=cfg, pix0=pix0, device=dev)
     out = pg.alloc_outputs(npix, dev, ("depth", "depth_f64", "P", "G", "X", "bottom_albedo",
                                        "model_error", "evals", "status"))
@@ -227,10 +224,7 @@ def main():
     pg.sync()
     ms_step = ev0.elapsed_time(ev1) / args.steps
     L.check(L.lib().photic_set_counter(None))
-    if pg_ is not None:
-        t = torch.tensor([ms_step], device=dev)
-        pg_.all_reduce(t, op=pg_.ReduceOp.MAX)
-        ms_step = float(t.item())
+    ms_step = replicas.max_over_ranks(ms_step, pg_, dev)
 
     status = out["status"].cpu().numpy()
     fitted = (status & 0xFF) == 0
@@ -263,10 +257,7 @@ def main():
                         "p99_abs_dH_m": float(np.quantile(d, 0.99)),
                         "frac_within_1cm": sample_frac}
     good = float(np.sum(within)) * sample_frac
-    if pg_ is not None:
-        t = torch.tensor([good], device=dev, dtype=torch.float64)
-        pg_.all_reduce(t)
-        good = float(t.item())
+    good = replicas.sum_over_ranks(good, pg_, dev)
     value = good / (ms_step * 1e-3)
 
     # Roofline of the inversion kernel: FP64 pipe.
