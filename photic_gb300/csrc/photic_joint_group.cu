@@ -54,13 +54,13 @@ struct JG {
   // doubles of shared memory per group: vertices, per-lane vertex costs,
   // the evaluation point, band terms (squared residual, K, bottom share)
   // and the final cost details
-  static constexpr int kSmem = (N + 1) * CG + NF * G + CG + 3 * G + 8;
+  static constexpr int kSmem = (N + 1) * CG + NF * G + CG + 3 * G + 8 + 16;
   static constexpr int kGroups = kBlock / G;
 };
 
 // Per-group view of the shared memory.
 struct GSmem {
-  double *V, *F, *X, *dd, *kk, *io, *misc;
+  double *V, *F, *X, *dd, *kk, *io, *misc, *kmin, *kpen;
 };
 
 // Rrs(490), Rrs(550), Rrs(640) of scene s of the pixel whose observations
@@ -157,6 +157,8 @@ __global__ void __launch_bounds__(kBlock) joint_group_kernel(const __grid_consta
     g.kk = g.dd + G;
     g.io = g.kk + G;
     g.misc = g.io + G;
+    g.kmin = g.misc + 8;
+    g.kpen = g.kmin + 8;
   }
   NmGroup<N, C, G, CG> m;
   m.V = g.V;
@@ -312,23 +314,34 @@ __global__ void __launch_bounds__(kBlock) joint_group_kernel(const __grid_consta
       if (final_eval) g.io[gl] = rrs_B / rrs;
     }
     __syncwarp();
+    // each scene's K_min and K penalty on lane s (model/samodel.c:2696-2725);
+    // only the sums that fix the rounding stay on the head lane
+    if (has && gl < K) {
+      const double H = fabs(g.X[0]);
+      double km = 1.0e4;
+      for (int b = 0; b < nb; b++) {
+        const double Kb = g.kk[gl * 4 + b];
+        if (__double2float_rn(Kb) != 0.0f && Kb < km) km = Kb;
+      }
+      g.kmin[gl] = km;
+      g.kpen[gl] = k_penalty_f64(fp.kp, H, km);
+    }
+    __syncwarp();
     double y = 0.0;
     if (has && gl == 0) {
-      const double H = fabs(g.X[0]);
-      double err = 0.0, Ke = 0.0, km = 1.0e4, Kall = 1.0e4, iod = 0.0;
-      for (int s = 0; s < K; s++) {
-        km = 1.0e4;
-        for (int b = 0; b < nb; b++) {
-          const double Kb = g.kk[s * 4 + b];
-          err = err + g.dd[s * 4 + b];
-          if (__double2float_rn(Kb) != 0.0f && Kb < km) km = Kb;
-          if (final_eval) {
+      double err = 0.0, Ke = 0.0, Kall = 1.0e4, iod = 0.0;
+      for (int tau = 0; tau < K * 4; tau++)
+        if ((tau & 3) < nb) err = err + g.dd[tau];
+      for (int s = 0; s < K; s++) Ke = Ke + g.kpen[s];
+      if (final_eval) {
+        for (int s = 0; s < K; s++)
+          for (int b = 0; b < nb; b++) {
+            const double Kb = g.kk[s * 4 + b];
             iod = iod + g.io[s * 4 + b];
             if (__double2float_rn(Kb) != 0.0f && Kb < Kall) Kall = Kb;
           }
-        }
-        Ke = Ke + k_penalty_f64(fp.kp, H, km);
       }
+      const double km = g.kmin[K - 1];
       const double E = 100.0 * sqrt(err / (double)(K * nb)) / mean;
       if (km > 0.7) {  // the last scene's K_min (model/samodel.c:2726-2732)
         const double dk = 4.0 * (km - 0.7);
