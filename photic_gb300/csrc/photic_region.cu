@@ -31,8 +31,8 @@ constexpr int kMaxR = 9, kMaxN = 3 * kMaxR + 3, kTerms = 64;
 constexpr int kNF = kMaxN + 2;
 // doubles of shared memory per warp: vertices (n+1) x 32, per-lane vertex
 // costs, the evaluation point, band terms (residual^2, K, bottom share),
-// per-region Rrs(490/550/640), final details
-constexpr int kSmem = (kMaxN + 1) * 32 + kNF * 32 + 32 + 3 * kTerms + 3 * 16 + 8;
+// per-region Rrs(490/550/640), final details and per-region bottom shares
+constexpr int kSmem = (kMaxN + 1) * 32 + kNF * 32 + 32 + 3 * kTerms + 3 * 16 + 8 + 16;
 
 // The 3 x 3 neighbourhood of pixel (i, j): region pixel indexes in the
 // reference's order, their count and the origin's slot.
@@ -251,6 +251,13 @@ __global__ void __launch_bounds__(kBlock) region_kernel(const __grid_constant__ 
         kk[tau] = Kb;
         if (final_eval) io[tau] = rrs_B / rrs;
       }
+      // each region's bottom share |100 B| |q| / q_sum on its own lane (the
+      // division is the costly part of the bottom-continuity term)
+      if (lane < R) {
+        double qs = 0.0;
+        qs += fabs(X[2 * R + lane]);
+        misc[8 + lane] = fabs(X[R + lane]) * fabs(X[2 * R + lane]) / qs;
+      }
       __syncwarp();
       // ---- the cost on the head lane (model/samodel.c:2432-2759)
       double y = 0.0;
@@ -277,17 +284,11 @@ __global__ void __launch_bounds__(kBlock) region_kernel(const __grid_constant__ 
         th = dmean < 5.0 ? 0.25 : dmean < 10.0 ? 0.1 : dmean < 15.0 ? 0.05 : 0.01;
         double Eb = 0.0, bmean = 0.0, btotal = 0.0;
         nout = 0.0;
-        for (int r = 0; r < R; r++) {
-          double qs = 0.0;
-          qs += fabs(X[2 * R + r]);
-          bmean += fabs(X[R + r]) * fabs(X[2 * R + r]) / qs;
-        }
+        for (int r = 0; r < R; r++) bmean += misc[8 + r];
         bmean /= (double)R;
         btotal += bmean;
         for (int r = 0; r < R; r++) {
-          double qs = 0.0;
-          qs += fabs(X[2 * R + r]);
-          const double bt = fabs(X[R + r]) * fabs(X[2 * R + r]) / qs;
+          const double bt = misc[8 + r];
           if (bt < (1.0 - th) * bmean || bt > (1.0 + th) * bmean) {
             const double dv = bt - bmean;
             Eb += dv * dv;
