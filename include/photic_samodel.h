@@ -152,11 +152,14 @@ typedef struct photic_scene {
 } photic_scene;
 
 /* model/samodel.h:8-19.  Fits every pixel that has data in all bands of all
- * scenes (model/samodel.c:672-700); n_spatial <= 1 and n_bottoms == 1 are
- * required (one region, sand).  depth_sigma (one scene) is the reference's
+ * scenes (model/samodel.c:672-700); n_bottoms == 1 (sand) is required;
+ * n_spatial <= 1 fits each pixel alone, n_spatial == 2 (one scene, no
+ * empirical depths) fits it with its 3 x 3 neighbourhood
+ * (photic_region_invert_batch, model/samodel.c:2957-3027); smoothing radius
+ * 1 (none) only.  depth_sigma (one scene) is the reference's
  * Monte Carlo estimate computed by photic_depth_sigma with the scene's
  * R_sigma, 128 samples per 0.25 m interval and a fixed seed; 0 for more
- * scenes.  Depth is written negative below the datum, as the reference does
+ * scenes or n_spatial == 2.  Depth is written negative below the datum, as the reference does
  * (model/samodel.c:1486). */
 void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scene_indexes,
              int nscenes, int empirical_depth_present, photic_geogrid empirical_depths,

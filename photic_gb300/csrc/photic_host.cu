@@ -1499,7 +1499,6 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
              float **bottom_seagrass, float **bottom_coral, float **K_min, float **bottom_type,
              float **index_optical_depth, float pagesize, int background, int linewidth) {
   g_err.clear();
-  (void)n_smoothing_radius;
   (void)pagesize;
   (void)background;
   (void)linewidth;
@@ -1508,10 +1507,17 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
     fail(PHOTIC_ERR_INVALID, "samodel: bad scenes");
     return;
   }
-  if (n_spatial > 1 || n_bottoms != 1) {
-    fail(PHOTIC_ERR_UNSUPPORTED, "samodel: n_spatial <= 1 and n_bottoms == 1 only");
+  if (n_spatial > 2 || n_bottoms != 1 ||
+      (n_spatial == 2 && (nscenes != 1 || empirical_depth_present))) {
+    fail(PHOTIC_ERR_UNSUPPORTED,
+         "samodel: n_bottoms == 1, and n_spatial == 2 only for one scene without empirical depths");
     return;
   }
+  if (n_smoothing_radius > 1) {
+    fail(PHOTIC_ERR_UNSUPPORTED, "samodel: spectral smoothing (radius > 1) is not built");
+    return;
+  }
+  const bool regions = n_spatial == 2;
   const photic_scene &s0 = scene_data[scene_indexes[0]];
   const int nrows = s0.nrows, ncols = s0.ncols, nb = s0.n_bands;
   photic_config cfg;
@@ -1593,7 +1599,10 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
         ea.seeds = d_seeds;
         launch_empirical_seeds(ea, 0);
       }
-      rc = photic_invert_batch(&cfg, d_rrs, npix, nb, 1, d_seeds, &o, 0);
+      // one scene: [pixel][band] is the [nrows][ncols][band] grid the
+      // region fit takes (model/samodel.c:2957-3027 for n_spatial = 2)
+      rc = regions ? photic_region_invert_batch(&cfg, d_rrs, nrows, ncols, 2, &o, 0)
+                   : photic_invert_batch(&cfg, d_rrs, npix, nb, 1, d_seeds, &o, 0);
     } else {
       std::vector<int32_t> offs((size_t)npix + 1);
       std::vector<double> th((size_t)nobs);
@@ -1617,7 +1626,7 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
       cudaMemcpy(st.data(), d_status, npix * sizeof(int32_t), cudaMemcpyDeviceToHost);
       // depth uncertainty of the fitted grid (:1368-1479), one scene
       std::vector<float> sig((size_t)npix, 0.0f);
-      if (depth_sigma && nscenes == 1) {
+      if (depth_sigma && nscenes == 1 && !regions) {
         std::vector<float> hpos((size_t)npix);
         for (int64_t p = 0; p < npix; p++)
           hpos[p] = (st[p] & 0xFF) == PHOTIC_PX_FITTED ? (float)H[p] : 0.0f;

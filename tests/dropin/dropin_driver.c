@@ -21,7 +21,8 @@
  *        error    : OUT = double [npix][1 + n_bands] (cost, Rrs_modelled)
  *        rrs      : OUT = double [npix][2 * n_bands] (Rrs_modelled, K) at
  *                   the model inputs samodel_error derives from params
- *        grid     : samodel() over an nrows x ncols grid; OUT = float
+ *        grid     : samodel() over an nrows x ncols grid (grid2: with
+ *                   n_spatial = 2, 3 x 3 regions per pixel); OUT = float
  *                   [10][nrows][ncols] (depth, depth sigma, model error,
  *                   albedo, sand, seagrass, coral, K_min, type, IOD) */
 #include <math.h>
@@ -153,7 +154,8 @@ int main(int argc, char **argv) {
   FILE *o = fopen(argv[3], "wb");
   if (!o) return 1;
 
-  if (!strcmp(mode, "grid")) {
+  if (!strcmp(mode, "grid") || !strcmp(mode, "grid2")) {
+    const int n_spatial = !strcmp(mode, "grid2") ? 2 : 0;
     if (nrows * ncols != npix) return 1;
     photic_scene *sc = xcalloc(1, sizeof *sc);
     photic_geogrid *grids = xcalloc((size_t)nb, sizeof *grids);
@@ -178,8 +180,8 @@ int main(int argc, char **argv) {
     float **g[10];
     for (int k = 0; k < 10; k++) g[k] = fgrid(nrows, ncols);
     int idx = 0;
-    samodel(sc, grids, &idx, 1, 0, none, 0, 0, 1, g[0], g[1], g[2], g[3], g[4], g[5], g[6], g[7],
-            g[8], g[9], 0.0f, 0, 0);
+    samodel(sc, grids, &idx, 1, 0, none, 1, n_spatial, 1, g[0], g[1], g[2], g[3], g[4], g[5],
+            g[6], g[7], g[8], g[9], 0.0f, 0, 0);
     if (photic_last_error()[0]) {
       fprintf(stderr, "samodel: %s\n", photic_last_error());
       return 4;

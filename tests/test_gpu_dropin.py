@@ -157,3 +157,21 @@ def test_samodel_grid_matches_oracle(driver, port, tmp_path):
     np.testing.assert_allclose(g[2, fit][same], ref[fit, 3][same].astype(np.float32), rtol=1e-6)
     np.testing.assert_allclose(g[3, fit][same], ref[fit, 1][same].astype(np.float32), rtol=1e-6)
     np.testing.assert_allclose(g[7, fit][same], ref[fit, 4][same].astype(np.float32), rtol=1e-6)
+
+
+def test_samodel_grid_regions_matches_oracle(driver, port, tmp_path):
+    """samodel() with n_spatial = 2: every pixel fitted with its 3 x 3
+    neighbourhood, against the oracle pinned to the reference's own
+    extract_Rrs_data + samodel_optimise (reference tolerances)."""
+    nrows, ncols = 14, 11
+    rrs, _ = port.generate_single(20260808, nrows * ncols, pix0=77, mask_frac=0.15)
+    inp, out = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    _write_input(inp, rrs, nrows=nrows, ncols=ncols)
+    _run(driver, "grid2", inp, out)
+    g = np.fromfile(out, dtype=np.float32).reshape(10, nrows * ncols)
+    ref = port.region_invert_batch(rrs.reshape(nrows, ncols, 4), reqmin=1e-2, konvge=100,
+                                   kcount=5000, nthreads=os.cpu_count() or 1)
+    fit = ref[:, 9] == 0
+    assert (g[4, ~fit] == -9999).all() and (g[4, fit] == 100).all()
+    dh = np.abs(-g[0, fit] - ref[fit, 0].astype(np.float32))
+    assert np.median(dh) <= 0.01 and np.mean(dh == 0) >= 0.95, (np.median(dh), np.mean(dh == 0))
