@@ -26,7 +26,7 @@ def test_guarded_equals_fp64_kernel(gpu, port, npix):
     fit = (a["status"] & 0xFF) == 0
     same = np.mean(a["depth_f64"][fit] == b["depth_f64"][fit]) if fit.any() else 1.0
     assert same >= 0.999, same
-    if npix >= 1000:  # the oracle bar is a distribution: judge it on many pixels
+    if npix >= 1000:  # the oracle bar is a distribution: assess it on many pixels
         ref = port.invert_batch(rrs, nthreads=NTHREADS)
         d = np.abs(b["depth_f64"][fit] - ref[fit, 0])
         assert np.median(d) <= 0.01 and np.quantile(d, 0.99) <= 0.05

@@ -160,3 +160,18 @@ def test_invert_order_is_a_permutation_of_work(gpu):
     gpu.sync()
     for f in fields:
         assert torch.equal(torch.nan_to_num(a[f]), torch.nan_to_num(b[f])), f
+
+
+def test_empty_inputs_are_no_ops(gpu):
+    """Zero pixels: every batched entry point returns without launching."""
+    cfg = gpu.Config()
+    e = torch.empty(0, 4, dtype=torch.float32, device="cuda")
+    out = gpu.invert(e, cfg)
+    assert all(v.numel() == 0 for v in out.values())
+    offs = torch.zeros(1, dtype=torch.int32, device="cuda")
+    th = torch.empty(0, dtype=torch.float64, device="cuda")
+    gpu.joint_invert(offs, th, e, cfg)
+    gpu.region_invert(torch.empty(0, 5, 4, dtype=torch.float32, device="cuda"), cfg)
+    c, rm = gpu.cost(e, torch.empty(0, 6, dtype=torch.float64, device="cuda"), cfg)
+    assert c.numel() == 0
+    gpu.sync()
