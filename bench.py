@@ -165,7 +165,7 @@ def main():
                     help="Levenberg-Marquardt steps on each surrogate seed (0: raw prediction)")
     ap.add_argument("--seed-step-scale", type=float, default=0.1,
                     help="initial simplex of a seeded fit, relative to the cold-start steps")
-    ap.add_argument("--joint-npix", type=int, default=1 << 16,
+    ap.add_argument("--joint-npix", type=int, default=1 << 18,
                     help="pixels of the 4096x4096 temporal grid for the joint-fit leg (0: skip)")
     ap.add_argument("--region-side", type=int, default=96,
                     help="side of the square grid for the spatial-region leg (0: skip)")
