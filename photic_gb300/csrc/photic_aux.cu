@@ -179,7 +179,7 @@ __global__ void forward_kernel(const __grid_constant__ ForwardArgs a) {
   if (i >= a.n) return;
   const double *x = a.params + i * 7;
   const double chi = a.rrs440[i] / a.rrs490[i];
-  double Y = 3.44 * (1.0 - 3.17 * exp(-2.01 * chi));
+  double Y = 3.44 * (1.0 - 3.17 * fm::exp_t(-2.01 * chi));
   if (Y < 0.0) Y = 0.0;
   if (Y > 2.5) Y = 2.5;
   const double qB = x[4] * x[3];

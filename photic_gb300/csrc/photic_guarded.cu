@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(BS) guarded_kernel(const __grid_constant__ Inv
 #pragma unroll
             for (int j = 0; j <= kN; j++) z = z + V(j, i);
             z = z - V(hi, i);
-            cen[i] = z / (double)kN;
+            cen[i] = fm::div_by(z, (double)kN, 1.0 / (double)kN);
           }
 #pragma unroll
           for (int i = 0; i < kN; i++) refl[i] = cen[i] + (cen[i] - V(hi, i));
@@ -529,7 +529,7 @@ __global__ void __launch_bounds__(BS) guarded_kernel(const __grid_constant__ Inv
           } else {
             double zz = 0.0;
             for (int j = 0; j <= kN; j++) zz = zz + S.fex[j][tid];
-            double xm = zz / (double)(kN + 1);
+            double xm = fm::div_by(zz, (double)(kN + 1), 1.0 / (double)(kN + 1));
             zz = 0.0;
             for (int j = 0; j <= kN; j++) {
               double d = S.fex[j][tid] - xm;

@@ -477,7 +477,9 @@ int photic_cost_batch(const photic_config *cfg, const float *d_rrs, const double
                       int64_t n, double *d_cost, double *d_rrs_modelled, void *stream) {
   int rc = photic_config_check(cfg);
   if (rc) return rc;
-  if (n < 0 || !d_rrs || !d_params || !d_cost) return fail(PHOTIC_ERR_INVALID, "bad arguments");
+  if (n < 0 || (n > 0 && (!d_rrs || !d_params || !d_cost)))
+    return fail(PHOTIC_ERR_INVALID, "bad arguments");
+  if (n == 0) return PHOTIC_OK;
   CostArgs a;
   memset(&a, 0, sizeof a);
   make_fit(*cfg, a.fp);
@@ -832,7 +834,8 @@ int photic_surrogate_seed_polished(photic_surrogate *s, const photic_config *cfg
                                    void *stream) {
   int rc = photic_config_check(cfg);
   if (rc) return rc;
-  if (!s || !d_rrs || !d_seeds || npix < 0 || polish_iters < 0 || polish_iters > 100)
+  if (!s || npix < 0 || (npix > 0 && (!d_rrs || !d_seeds)) || polish_iters < 0 ||
+      polish_iters > 100)
     return fail(PHOTIC_ERR_INVALID, "bad arguments");
   if (npix == 0) return PHOTIC_OK;
   cudaStream_t st = (cudaStream_t)stream;
@@ -1241,8 +1244,9 @@ int photic_forward_batch(const photic_config *cfg, const double *d_params,
                          double *d_rrs, double *d_K, void *stream) {
   int rc = photic_config_check(cfg);
   if (rc) return rc;
-  if (n < 0 || !d_params || !d_rrs440 || !d_rrs490 || !d_rrs)
+  if (n < 0 || (n > 0 && (!d_params || !d_rrs440 || !d_rrs490 || !d_rrs)))
     return fail(PHOTIC_ERR_INVALID, "bad arguments");
+  if (n == 0) return PHOTIC_OK;
   ForwardArgs a;
   memset(&a, 0, sizeof a);
   make_fit(*cfg, a.fp);
@@ -1806,7 +1810,7 @@ extern "C" int photic_depth_sigma(const photic_config *cfg, const float *d_rrs, 
                                   int32_t *d_sample_pixel, double *d_sample_depth, void *stream) {
   int rc = photic_config_check(cfg);
   if (rc) return rc;
-  if (npix < 0 || (npix > 0 && (!d_rrs || !d_depth)) || !r_sigma || !d_depth_sigma ||
+  if (npix < 0 || (npix > 0 && (!d_rrs || !d_depth || !d_depth_sigma)) || !r_sigma ||
       n_samples < 1 || n_samples > 4096 || npix > 0xffffffffLL)
     return fail(PHOTIC_ERR_INVALID, "bad arguments");
   cudaStream_t s = (cudaStream_t)stream;

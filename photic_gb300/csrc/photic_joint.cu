@@ -35,7 +35,7 @@ struct PrecJ {
   static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
   static __device__ __forceinline__ T mul2(T a) { return 2.0 * a; }
   static __device__ __forceinline__ T half(T a) { return a * 0.5; }
-  static __device__ __forceinline__ T div_n(T a, int n) { return a / (double)n; }
+  static __device__ __forceinline__ T div_n(T a, int n) { return fm::div_by(a, (double)n, 1.0 / (double)n); }
   static __device__ __forceinline__ bool lt(T a, T b) { return a < b; }
   static __device__ __forceinline__ bool le(T a, T b) { return a <= b; }
   static __device__ __forceinline__ T eps_step(T s) { return s * 1.0e-6; }
@@ -78,7 +78,7 @@ __device__ __forceinline__ void jsetup(const JointArgs &a, int64_t o0, JPixel<K,
     px.r640[s] = interp_plan<NB>(fp.plan[3], px.rrs[s]);
     if (r440 < 0.0) r440 = 0.0001;
     const double chi = r440 / px.r490[s];
-    double Y = 3.44 * (1.0 - 3.17 * exp(-2.01 * chi));
+    double Y = 3.44 * (1.0 - 3.17 * fm::exp_t(-2.01 * chi));
     if (Y < 0.0) Y = 0.0;
     if (Y > 2.5) Y = 2.5;
 #pragma unroll
@@ -112,7 +112,7 @@ __device__ __forceinline__ double jcost(const JointArgs &a, const JPixel<K, NB> 
     if (LAYOUT == PHOTIC_LAYOUT_REFERENCE) {
       const double B = 0.01 * fabs(x[1]);
       const double qa = fabs(x[2]);
-      qB = (qa / qa) * B;
+      qB = fm::self_ratio(qa) * B;
       P = 0.01 * fabs(x[3 + 3 * s]);
       G = 0.01 * fabs(x[4 + 3 * s]);
       X = 0.01 * fabs(x[5 + 3 * s]);
@@ -140,9 +140,9 @@ __device__ __forceinline__ double jcost(const JointArgs &a, const JPixel<K, NB> 
         const double DuC = 1.03 * sqrt(1.0 + 2.4 * u);
         const double DuB = 1.04 * sqrt(1.0 + 5.4 * u);
         double M = px.sec_sun[s] + DuC * sc.sec_view;
-        const double rrs_C = rrs_dp * (1.0 - exp(-M * Kb * H));
+        const double rrs_C = rrs_dp * (1.0 - fm::exp_t(-M * Kb * H));
         M = px.sec_sun[s] + DuB * sc.sec_view;
-        const double rrs_B = rho / kPi * exp(-M * Kb * H);
+        const double rrs_B = fm::div_by(rho, kPi, fm::kInvPi) * fm::exp_t(-M * Kb * H);
         const double rrs = rrs_C + rrs_B;
         const double Rm = 0.5 * rrs / (1.0 - 1.5 * rrs);
         const double d = Rm - px.rrs[s][b];
@@ -156,7 +156,7 @@ __device__ __forceinline__ double jcost(const JointArgs &a, const JPixel<K, NB> 
     }
     kmin[s] = km;
   }
-  const double E = 100.0 * sqrt(err / (double)(K * nb)) / px.mean;
+  const double E = 100.0 * sqrt(fm::div_count(err, K * nb)) / px.mean;
   double Ke = 0.0;
   for (int s = 0; s < K; s++) Ke = Ke + k_penalty_f64(fp.kp, H, kmin[s]);
   if (kmin[K - 1] > 0.7) {
@@ -164,7 +164,7 @@ __device__ __forceinline__ double jcost(const JointArgs &a, const JPixel<K, NB> 
     Ke = Ke + 100.0 * (d * d);
   }
   double model = 80.0 * E + 15.0 * Ke;
-  model = model / 120.0;
+  model = fm::div_by(model, 120.0, fm::kInv120);
   if (kDetails) {
     det->rrs_error = E;
     det->model_error = model;

@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(kBlock) joint_group_kernel(const __grid_consta
       const double r490 = interp_plan<4>(fp.plan[1], r4);
       if (r440 < 0.0) r440 = 0.0001;
       const double chi = r440 / r490;
-      double Y = 3.44 * (1.0 - 3.17 * exp(-2.01 * chi));
+      double Y = 3.44 * (1.0 - 3.17 * fm::exp_t(-2.01 * chi));
       if (Y < 0.0) Y = 0.0;
       if (Y > 2.5) Y = 2.5;
       my_pw = pow(sc.ratio440[bb], Y);
@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(kBlock) joint_group_kernel(const __grid_consta
       if (LAYOUT == PHOTIC_LAYOUT_REFERENCE) {
         const double B = 0.01 * fabs(x[1]);
         const double qa = fabs(x[2]);
-        qB = (qa / qa) * B;
+        qB = fm::self_ratio(qa) * B;
       } else {
         qB = 1.0 * (0.01 * fabs(x[cB]));
       }
@@ -303,9 +303,9 @@ __global__ void __launch_bounds__(kBlock) joint_group_kernel(const __grid_consta
       const double DuC = 1.03 * sqrt(1.0 + 2.4 * u);
       const double DuB = 1.04 * sqrt(1.0 + 5.4 * u);
       double M = my_sec + DuC * sc.sec_view;
-      const double rrs_C = rrs_dp * (1.0 - exp(-M * Kb * H));
+      const double rrs_C = rrs_dp * (1.0 - fm::exp_t(-M * Kb * H));
       M = my_sec + DuB * sc.sec_view;
-      const double rrs_B = rho / kPi * exp(-M * Kb * H);
+      const double rrs_B = fm::div_by(rho, kPi, fm::kInvPi) * fm::exp_t(-M * Kb * H);
       const double rrs = rrs_C + rrs_B;
       const double Rm = 0.5 * rrs / (1.0 - 1.5 * rrs);
       const double d = Rm - my_rrs;
@@ -342,20 +342,20 @@ __global__ void __launch_bounds__(kBlock) joint_group_kernel(const __grid_consta
           }
       }
       const double km = g.kmin[K - 1];
-      const double E = 100.0 * sqrt(err / (double)(K * nb)) / mean;
+      const double E = 100.0 * sqrt(fm::div_count(err, K * nb)) / mean;
       if (km > 0.7) {  // the last scene's K_min (model/samodel.c:2726-2732)
         const double dk = 4.0 * (km - 0.7);
         Ke = Ke + 100.0 * (dk * dk);
       }
       double model = 80.0 * E + 15.0 * Ke;
-      model = model / 120.0;
+      model = fm::div_by(model, 120.0, fm::kInv120);
       y = model;
       if (final_eval) {
         double qB;
         if (LAYOUT == PHOTIC_LAYOUT_REFERENCE) {
           const double B = 0.01 * fabs(g.X[1]);
           const double qa = fabs(g.X[2]);
-          qB = (qa / qa) * B;
+          qB = fm::self_ratio(qa) * B;
         } else {
           qB = 1.0 * (0.01 * fabs(g.X[1 + 4 * (K - 1)]));
         }

@@ -24,6 +24,7 @@ struct NmGroup {
   unsigned gmask;      // the group's lanes
   double cen[C], refl[C], trial[C], xmin[C], start[C], step[C];
   double ylo, fr, scale, var_limit;
+  double inv_n, inv_n1;  // RN(1 / n), RN(1 / (n + 1)) for the centroid and the variance test
   long long floor_lo;
   int32_t phase, jj, hi, lo, icount, numres, ifault, countdown, kcount, konvge;
 
@@ -51,6 +52,7 @@ struct NmGroup {
       step[t] = 0.0;
     }
     ylo = fr = 0.0;
+    inv_n = inv_n1 = 1.0;
     scale = 1.0;
     floor_lo = 0;
     phase = jj = hi = lo = icount = numres = ifault = countdown = 0;
@@ -65,6 +67,8 @@ struct NmGroup {
     ifault = 0;
     scale = 1.0;
     var_limit = var_limit_;
+    inv_n = 1.0 / (double)dim();
+    inv_n1 = 1.0 / (double)(dim() + 1);
     restart_simplex();
   }
 
@@ -123,7 +127,7 @@ struct NmGroup {
         double z = 0.0;
         for (int j = 0; j <= dim(); j++) z = z + Vv(j, i);
         z = z - Vv(hi, i);
-        cen[t] = z / (double)dim();
+        cen[t] = fm::div_by(z, (double)dim(), inv_n);
         refl[t] = cen[t] + (cen[t] - Vv(hi, i));
         X[i] = refl[t];
       }
@@ -153,7 +157,7 @@ struct NmGroup {
       countdown = konvge;
       double z = 0.0;
       for (int j = 0; j <= dim(); j++) z = z + F(j);
-      const double mean = z / (double)(dim() + 1);
+      const double mean = fm::div_by(z, (double)(dim() + 1), inv_n1);
       z = 0.0;
       for (int j = 0; j <= dim(); j++) {
         const double d = F(j) - mean;

@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(kBlock) region_kernel(const __grid_constant__ 
         const double r490 = interp_plan<4>(fp.plan[1], r4);
         if (r440 < 0.0) r440 = 0.0001;
         const double chi = r440 / r490;
-        double Y = 3.44 * (1.0 - 3.17 * exp(-2.01 * chi));
+        double Y = 3.44 * (1.0 - 3.17 * fm::exp_t(-2.01 * chi));
         if (Y < 0.0) Y = 0.0;
         if (Y > 2.5) Y = 2.5;
         my_rrs[h] = r4[b];
@@ -241,9 +241,9 @@ __global__ void __launch_bounds__(kBlock) region_kernel(const __grid_constant__ 
         const double DuC = 1.03 * sqrt(1.0 + 2.4 * u);
         const double DuB = 1.04 * sqrt(1.0 + 5.4 * u);
         double M = sc.sec_sun + DuC * sc.sec_view;
-        const double rrs_C = rrs_dp * (1.0 - exp(-M * Kb * H));
+        const double rrs_C = rrs_dp * (1.0 - fm::exp_t(-M * Kb * H));
         M = sc.sec_sun + DuB * sc.sec_view;
-        const double rrs_B = rho / kPi * exp(-M * Kb * H);
+        const double rrs_B = fm::div_by(rho, kPi, fm::kInvPi) * fm::exp_t(-M * Kb * H);
         const double rrs = rrs_C + rrs_B;
         const double Rm = 0.5 * rrs / (1.0 - 1.5 * rrs);
         const double d = Rm - my_rrs[h];
@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(kBlock) region_kernel(const __grid_constant__ 
       if (lane == 0) {
         double err = 0.0;
         for (int tau = 0; tau < nterm; tau++) err = err + dd[tau];
-        const double E = 100.0 * sqrt(err / (double)nterm) / mean;
+        const double E = 100.0 * sqrt(fm::div_count(err, nterm)) / mean;
         // depth continuity
         double dmean = 0.0;
         for (int r = 0; r < R; r++) dmean += fabs(X[r]);
@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(kBlock) region_kernel(const __grid_constant__ 
           Ke = Ke + 100.0 * (dk * dk);
         }
         double model = 80.0 * E + 15.0 * Ed + 10.0 * Eb + 15.0 * Ke;
-        model = model / 120.0;
+        model = fm::div_by(model, 120.0, fm::kInv120);
         y = model;
         if (final_eval) {
           double iod = 0.0, Kall = 1.0e4;
