@@ -171,28 +171,6 @@ PHOTIC_FM_HD double self_ratio(double q) {
 constexpr double kInvPi = 1.0 / 3.141592653589793;
 constexpr double kInv120 = 1.0 / 120.0;
 
-// IEEE 754 comparisons on the bit patterns, executed on the integer pipes
-// (a double compare or a double-to-float conversion occupies the FP64 pipe
-// as long as a DADD does).  NaN compares false, -0 equals +0.
-PHOTIC_FM_HD int64_t order_key(int64_t ix) {
-  const int64_t m = ix & 0x7fffffffffffffffLL;
-  return ix < 0 ? -m : m;
-}
-PHOTIC_FM_HD bool lt(double a, double b) {
-  const int64_t ia = bits(a), ib = bits(b);
-  return order_key(ia) < order_key(ib) && (ia & 0x7fffffffffffffffLL) <= 0x7ff0000000000000LL &&
-         (ib & 0x7fffffffffffffffLL) <= 0x7ff0000000000000LL;
-}
-PHOTIC_FM_HD bool le(double a, double b) {
-  const int64_t ia = bits(a), ib = bits(b);
-  return order_key(ia) <= order_key(ib) && (ia & 0x7fffffffffffffffLL) <= 0x7ff0000000000000LL &&
-         (ib & 0x7fffffffffffffffLL) <= 0x7ff0000000000000LL;
-}
-// (float)x != 0.0f with round-to-nearest: x is NaN or |x| > 2^-150.
-PHOTIC_FM_HD bool f32_nonzero(double x) {
-  return (bits(x) & 0x7fffffffffffffffLL) > 0x3690000000000000LL;
-}
-
 // a / n for a count n > 0: a power of two scales exactly (the product and
 // the quotient are the same correctly rounded value), any other count is
 // divided.

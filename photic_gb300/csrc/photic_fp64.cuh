@@ -82,11 +82,11 @@ __device__ __forceinline__ void pixel_setup_f64(const FitParams &fp, const Scene
 __device__ __forceinline__ double k_penalty_f64(const KPenalty &kp, double H, double K_min) {
   double e = 0.0;
   int c = -1;
-  if (fm::lt(H, 1.0) && fm::lt(K_min, kp.k_thr[0])) c = 0;
-  else if (fm::lt(H, 2.0) && fm::lt(K_min, kp.k_thr[1])) c = 1;
-  else if (fm::lt(H, 3.0) && fm::lt(K_min, kp.k_thr[2])) c = 2;
-  else if (fm::lt(H, 4.0) && fm::lt(K_min, kp.k_thr[3])) c = 3;
-  else if (fm::lt(H, 5.0) && fm::lt(K_min, kp.k_thr[4])) c = 4;
+  if (H < 1.0 && K_min < kp.k_thr[0]) c = 0;
+  else if (H < 2.0 && K_min < kp.k_thr[1]) c = 1;
+  else if (H < 3.0 && K_min < kp.k_thr[2]) c = 2;
+  else if (H < 4.0 && K_min < kp.k_thr[3]) c = 3;
+  else if (H < 5.0 && K_min < kp.k_thr[4]) c = 4;
   if (c >= 0) {
     double d = 1.0 / (0.01 + K_min) - kp.inv_t[c];
     e = e + 100.0 * (d * d);
@@ -128,8 +128,8 @@ __device__ __forceinline__ double cost_f64(const FitParams &fp, const SceneConst
       double bb = sc.bbw[b] + X * px.pw[b];
       double u = bb / (a + bb);
       double K = a + bb;
-      if (fm::lt(K, 0.0)) K = 0.0;
-      if (fm::lt(2.5, K)) K = 2.5;
+      if (K < 0.0) K = 0.0;
+      if (K > 2.5) K = 2.5;
       double rrs_dp = (0.084 + 0.170 * u) * u;
       double DuC = 1.03 * sqrt(1.0 + 2.4 * u);
       double DuB = 1.04 * sqrt(1.0 + 5.4 * u);
@@ -141,7 +141,7 @@ __device__ __forceinline__ double cost_f64(const FitParams &fp, const SceneConst
       double Rm = 0.5 * rrs / (1.0 - 1.5 * rrs);
       double d = Rm - px.rrs[b];
       err = err + d * d;
-      if (fm::f32_nonzero(K) && fm::lt(K, K_min)) K_min = K;
+      if (__double2float_rn(K) != 0.0f && K < K_min) K_min = K;
       if (kDetails) {
         iod = iod + rrs_B / rrs;
         det->Rm[b] = Rm;
@@ -150,7 +150,7 @@ __device__ __forceinline__ double cost_f64(const FitParams &fp, const SceneConst
   }
   const double E = 100.0 * sqrt(fm::div_count(err, nb)) / px.mean;
   double Ke = k_penalty_f64(fp.kp, H, K_min);
-  if (fm::lt(0.7, K_min)) {
+  if (K_min > 0.7) {
     double d = 4.0 * (K_min - 0.7);
     Ke = Ke + 100.0 * (d * d);
   }
@@ -198,8 +198,8 @@ __device__ __forceinline__ double forward_band_f64(const SceneConsts &sc, int b,
   const double bb = sc.bbw[b] + X * pw;
   const double u = bb / (a + bb);
   double K = a + bb;
-  if (fm::lt(K, 0.0)) K = 0.0;
-  if (fm::lt(2.5, K)) K = 2.5;
+  if (K < 0.0) K = 0.0;
+  if (K > 2.5) K = 2.5;
   *K_out = K;
   const double rrs_dp = (0.084 + 0.170 * u) * u;
   const double DuC = 1.03 * sqrt(1.0 + 2.4 * u);

@@ -51,8 +51,8 @@ struct PrecF64 {
   static __device__ __forceinline__ T half(T a) { return a * 0.5; }
   // z / n for the simplex size n, a compile-time constant here
   static __device__ __forceinline__ T div_n(T a, int n) { return fm::div_by(a, (double)n, 1.0 / (double)n); }
-  static __device__ __forceinline__ bool lt(T a, T b) { return fm::lt(a, b); }
-  static __device__ __forceinline__ bool le(T a, T b) { return fm::le(a, b); }
+  static __device__ __forceinline__ bool lt(T a, T b) { return a < b; }
+  static __device__ __forceinline__ bool le(T a, T b) { return a <= b; }
   static __device__ __forceinline__ T eps_step(T s) { return s * 1.0e-6; }
   static __device__ __forceinline__ T eps_scale() { return 1.0e-6; }
   static __device__ __forceinline__ long long trunc10(T y) { return photic::trunc10(y); }

@@ -36,8 +36,8 @@ struct PrecJ {
   static __device__ __forceinline__ T mul2(T a) { return 2.0 * a; }
   static __device__ __forceinline__ T half(T a) { return a * 0.5; }
   static __device__ __forceinline__ T div_n(T a, int n) { return fm::div_by(a, (double)n, 1.0 / (double)n); }
-  static __device__ __forceinline__ bool lt(T a, T b) { return fm::lt(a, b); }
-  static __device__ __forceinline__ bool le(T a, T b) { return fm::le(a, b); }
+  static __device__ __forceinline__ bool lt(T a, T b) { return a < b; }
+  static __device__ __forceinline__ bool le(T a, T b) { return a <= b; }
   static __device__ __forceinline__ T eps_step(T s) { return s * 1.0e-6; }
   static __device__ __forceinline__ T eps_scale() { return 1.0e-6; }
   static __device__ __forceinline__ long long trunc10(T y) { return photic::trunc10(y); }
@@ -134,8 +134,8 @@ __device__ __forceinline__ double jcost(const JointArgs &a, const JPixel<K, NB> 
         const double bb = sc.bbw[b] + X * px.pw[s][b];
         const double u = bb / (aa + bb);
         double Kb = aa + bb;
-        if (fm::lt(Kb, 0.0)) Kb = 0.0;
-        if (fm::lt(2.5, Kb)) Kb = 2.5;
+        if (Kb < 0.0) Kb = 0.0;
+        if (Kb > 2.5) Kb = 2.5;
         const double rrs_dp = (0.084 + 0.170 * u) * u;
         const double DuC = 1.03 * sqrt(1.0 + 2.4 * u);
         const double DuB = 1.04 * sqrt(1.0 + 5.4 * u);
@@ -147,10 +147,10 @@ __device__ __forceinline__ double jcost(const JointArgs &a, const JPixel<K, NB> 
         const double Rm = 0.5 * rrs / (1.0 - 1.5 * rrs);
         const double d = Rm - px.rrs[s][b];
         err = err + d * d;
-        if (fm::f32_nonzero(Kb) && fm::lt(Kb, km)) km = Kb;
+        if (__double2float_rn(Kb) != 0.0f && Kb < km) km = Kb;
         if (kDetails) {
           iod = iod + rrs_B / rrs;
-          if (fm::f32_nonzero(Kb) && fm::lt(Kb, Kall)) Kall = Kb;
+          if (__double2float_rn(Kb) != 0.0f && Kb < Kall) Kall = Kb;
         }
       }
     }

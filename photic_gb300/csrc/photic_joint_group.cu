@@ -297,8 +297,8 @@ __global__ void __launch_bounds__(kBlock) joint_group_kernel(const __grid_consta
       const double bbk = sc.bbw[bb] + Xx * my_pw;
       const double u = bbk / (aa + bbk);
       double Kb = aa + bbk;
-      if (fm::lt(Kb, 0.0)) Kb = 0.0;
-      if (fm::lt(2.5, Kb)) Kb = 2.5;
+      if (Kb < 0.0) Kb = 0.0;
+      if (Kb > 2.5) Kb = 2.5;
       const double rrs_dp = (0.084 + 0.170 * u) * u;
       const double DuC = 1.03 * sqrt(1.0 + 2.4 * u);
       const double DuB = 1.04 * sqrt(1.0 + 5.4 * u);
@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(kBlock) joint_group_kernel(const __grid_consta
       double km = 1.0e4;
       for (int b = 0; b < nb; b++) {
         const double Kb = g.kk[gl * 4 + b];
-        if (fm::f32_nonzero(Kb) && fm::lt(Kb, km)) km = Kb;
+        if (__double2float_rn(Kb) != 0.0f && Kb < km) km = Kb;
       }
       g.kmin[gl] = km;
       g.kpen[gl] = k_penalty_f64(fp.kp, H, km);
@@ -338,12 +338,12 @@ __global__ void __launch_bounds__(kBlock) joint_group_kernel(const __grid_consta
           for (int b = 0; b < nb; b++) {
             const double Kb = g.kk[s * 4 + b];
             iod = iod + g.io[s * 4 + b];
-            if (fm::f32_nonzero(Kb) && fm::lt(Kb, Kall)) Kall = Kb;
+            if (__double2float_rn(Kb) != 0.0f && Kb < Kall) Kall = Kb;
           }
       }
       const double km = g.kmin[K - 1];
       const double E = 100.0 * sqrt(fm::div_count(err, K * nb)) / mean;
-      if (fm::lt(0.7, km)) {  // the last scene's K_min (model/samodel.c:2726-2732)
+      if (km > 0.7) {  // the last scene's K_min (model/samodel.c:2726-2732)
         const double dk = 4.0 * (km - 0.7);
         Ke = Ke + 100.0 * (dk * dk);
       }

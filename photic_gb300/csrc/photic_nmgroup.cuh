@@ -102,7 +102,7 @@ struct NmGroup {
     lo = 0;
     for (int j = 1; j <= dim(); j++) {
       const double fj = F(j);
-      if (fm::lt(fj, ylo)) {
+      if (fj < ylo) {
         ylo = fj;
         lo = j;
       }
@@ -115,7 +115,7 @@ struct NmGroup {
     hi = 0;
     for (int j = 1; j <= dim(); j++) {
       const double fj = F(j);
-      if (fm::lt(yhi, fj)) {
+      if (yhi < fj) {
         yhi = fj;
         hi = j;
       }
@@ -147,7 +147,7 @@ struct NmGroup {
 
   __device__ __forceinline__ bool iteration_end() {
     const double fh = F(hi);
-    if (fm::lt(fh, ylo)) {
+    if (fh < ylo) {
       ylo = fh;
       lo = hi;
     }
@@ -163,7 +163,7 @@ struct NmGroup {
         const double d = F(j) - mean;
         z = z + d * d;
       }
-      if (fm::le(z, var_limit)) return true;
+      if (z <= var_limit) return true;
     }
     return false;
   }
@@ -206,7 +206,7 @@ struct NmGroup {
       case PH_REFLECT:
         fr = y;
         icount++;
-        if (fm::lt(fr, ylo)) {
+        if (fr < ylo) {
 #pragma unroll
           for (int t = 0; t < C; t++) trial[t] = cen[t] + 2.0 * (refl[t] - cen[t]);
           set_x_from(trial);
@@ -214,7 +214,7 @@ struct NmGroup {
         } else {
           int worse = 0;
           for (int j = 0; j <= dim(); j++)
-            if (fm::lt(fr, F(j))) worse++;
+            if (fr < F(j)) worse++;
           if (worse > 1) {
             replace_hi(refl, fr);
             cs = CS_ITER_END;
@@ -234,13 +234,13 @@ struct NmGroup {
         break;
       case PH_EXPAND:
         icount++;
-        if (fm::lt(fr, y)) replace_hi(refl, fr);
+        if (fr < y) replace_hi(refl, fr);
         else replace_hi(trial, y);
         cs = CS_ITER_END;
         break;
       case PH_CONTRACT_IN: {
         icount++;
-        const bool shrink = fm::lt(F(hi), y);
+        const bool shrink = F(hi) < y;
         if (shrink) {
 #pragma unroll
           for (int t = 0; t < C; t++)
@@ -278,7 +278,7 @@ struct NmGroup {
         break;
       case PH_CONTRACT_OUT:
         icount++;
-        if (fm::le(y, fr)) replace_hi(trial, y);
+        if (y <= fr) replace_hi(trial, y);
         else replace_hi(refl, fr);
         cs = CS_ITER_END;
         break;

@@ -235,8 +235,8 @@ __global__ void __launch_bounds__(kBlock) region_kernel(const __grid_constant__ 
         const double bbk = sc.bbw[b] + Xx * my_pw[h];
         const double u = bbk / (aa + bbk);
         double Kb = aa + bbk;
-        if (fm::lt(Kb, 0.0)) Kb = 0.0;
-        if (fm::lt(2.5, Kb)) Kb = 2.5;
+        if (Kb < 0.0) Kb = 0.0;
+        if (Kb > 2.5) Kb = 2.5;
         const double rrs_dp = (0.084 + 0.170 * u) * u;
         const double DuC = 1.03 * sqrt(1.0 + 2.4 * u);
         const double DuB = 1.04 * sqrt(1.0 + 5.4 * u);
@@ -303,10 +303,10 @@ __global__ void __launch_bounds__(kBlock) region_kernel(const __grid_constant__ 
         double km = 1.0e4;
         for (int b = 0; b < nb; b++) {
           const double Kb = kk[(R - 1) * nb + b];
-          if (fm::f32_nonzero(Kb) && fm::lt(Kb, km)) km = Kb;
+          if (__double2float_rn(Kb) != 0.0f && Kb < km) km = Kb;
         }
         double Ke = k_penalty_f64(fp.kp, fabs(X[origin]), km);
-        if (fm::lt(0.7, km)) {
+        if (km > 0.7) {
           const double dk = 4.0 * (km - 0.7);
           Ke = Ke + 100.0 * (dk * dk);
         }
@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(kBlock) region_kernel(const __grid_constant__ 
           for (int tau = 0; tau < nterm; tau++) iod = iod + io[tau];
           for (int b = 0; b < nb; b++) {
             const double Kb = kk[(R - 1) * nb + b];
-            if (fm::f32_nonzero(Kb) && fm::lt(Kb, Kall)) Kall = Kb;
+            if (__double2float_rn(Kb) != 0.0f && Kb < Kall) Kall = Kb;
           }
           double q = fabs(X[3 * R - 1]), qs = 0.0;
           qs += q;
