@@ -569,8 +569,10 @@ def serving_leg(args, net):
 FLOPS_PER_EVAL_F64 = 4 * 43 + 9
 
 # dram__bytes_read.sum + dram__bytes_write.sum of the FP64 inversion kernel
-# over a 65 536-pixel launch (1.902080 MB + 0.158464 MB), per pixel.
-TRAFFIC_BYTES_PER_PIXEL = (1.902080e6 + 0.158464e6) / 65536
+# over a 65 536-pixel launch (26.730240 MB + 19.621888 MB), per pixel: 16 B
+# of spectra and the outputs, the rest the threads' local-memory stack frames
+# leaving L2.  Under 1 GB/s at the kernel's rate.
+TRAFFIC_BYTES_PER_PIXEL = (26.730240e6 + 19.621888e6) / 65536
 
 if __name__ == "__main__":
     main()
