@@ -46,7 +46,8 @@ enum {
   PHOTIC_ERR_CUDA = 2,        /* a CUDA call failed (message: photic_last_error) */
   PHOTIC_ERR_NOMEM = 3,       /* device allocation failed */
   PHOTIC_ERR_TIMEOUT = 4,     /* a bounded device wait gave up */
-  PHOTIC_ERR_UNSUPPORTED = 5  /* configuration outside what the kernels implement */
+  PHOTIC_ERR_UNSUPPORTED = 5, /* configuration outside what the kernels implement */
+  PHOTIC_ERR_IO = 6           /* a file is missing, unreadable or not in the expected format */
 };
 
 /* Arithmetic of the cost evaluations. */

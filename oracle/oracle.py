@@ -351,3 +351,74 @@ def region_invert_batch(grid, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0, h
         raise ValueError("region_invert_batch failed")
     return out
 
+
+
+# --------------------------------------------------------------------------
+# netCDF short packing (model/nc.c:251-320): the port's restatement and the
+# reference's own write_nc / read_nc through the in-memory netCDF stand-in.
+# --------------------------------------------------------------------------
+_i16p = C.POINTER(C.c_int16)
+
+
+def nc_compress(grid, spval, which="port"):
+    """compress_2d over a row-major grid: (packed int16, add_offset,
+    scale_factor, missing_value); with which="reference" the values the
+    reference's write_nc put in its file."""
+    g = _f32(grid)
+    packed = np.zeros(g.shape, dtype=np.int16)
+    off, sc, sp = C.c_float(), C.c_float(), C.c_float()
+    mv = C.c_int16()
+    if which == "port":
+        L = port().lib
+        L.po_nc_compress(_ptr(g, _fp), C.c_int64(g.size), C.c_double(spval), _ptr(packed, _i16p),
+                         C.byref(off), C.byref(sc), C.byref(mv))
+        return packed, off.value, sc.value, mv.value
+    L = reference().lib
+    nrows, ncols = g.shape
+    lons = np.arange(ncols, dtype=np.float32)
+    lats = np.arange(nrows, dtype=np.float32)
+    rc = L.photic_ref_nc_write(_ptr(g, _fp), C.c_int(ncols), C.c_int(nrows), _ptr(lons, _fp),
+                               _ptr(lats, _fp), C.c_double(spval), _ptr(packed, _i16p),
+                               C.byref(off), C.byref(sc), C.byref(mv), C.byref(sp))
+    if rc:
+        raise RuntimeError(f"reference write_nc harness failed ({rc})")
+    return packed, off.value, sc.value, mv.value
+
+
+def nc_decompress(packed, add_offset, scale_factor, missing_value=-32768, spval=-9999.0,
+                  which="port", has_missing=True, has_spval=True):
+    """decompress_2d of a row-major packed grid; with which="reference" the
+    grid (and spval) the reference's read_nc returns for a file holding it,
+    with or without the missing_value / decompressed_missing_value
+    attributes."""
+    p = np.ascontiguousarray(packed, dtype=np.int16)
+    out = np.zeros(p.shape, dtype=np.float32)
+    if which == "port":
+        mv = missing_value if has_missing else -32768
+        sp = float(np.float32(spval)) if has_spval else 0.0
+        port().lib.po_nc_decompress(_ptr(p, _i16p), C.c_int64(p.size), C.c_float(add_offset),
+                                    C.c_float(scale_factor), C.c_int16(mv), C.c_double(sp),
+                                    _ptr(out, _fp))
+        return out, sp
+    L = reference().lib
+    nrows, ncols = p.shape
+    lons = np.arange(ncols, dtype=np.float32)
+    lats = np.arange(nrows, dtype=np.float32)
+    spo = C.c_double()
+    rc = L.photic_ref_nc_read(_ptr(p, _i16p), C.c_int(ncols), C.c_int(nrows), _ptr(lons, _fp),
+                              _ptr(lats, _fp), C.c_float(add_offset), C.c_float(scale_factor),
+                              C.c_int(int(has_missing)), C.c_int16(missing_value),
+                              C.c_int(int(has_spval)), C.c_float(spval), _ptr(out, _fp),
+                              C.byref(spo))
+    if rc:
+        raise RuntimeError(f"reference read_nc harness failed ({rc})")
+    return out, spo.value
+
+
+def nc_reference_layout(grid, spval=-9999.0):
+    """The dimensions, variables and attributes (in call order) of the file
+    the reference's write_nc writes for a grid."""
+    nc_compress(grid, spval, which="reference")
+    buf = C.create_string_buffer(1 << 16)
+    reference().lib.photic_ref_nc_layout(buf, C.c_int(len(buf)))
+    return buf.value.decode().splitlines()

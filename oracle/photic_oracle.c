@@ -17,6 +17,7 @@
  */
 #include "photic_oracle.h"
 
+#include <float.h>
 #include <limits.h>
 #include <math.h>
 #include <stdlib.h>
@@ -1426,3 +1427,57 @@ int po_region_invert_batch(int n_bands, const double *wl, double theta_sun_deg,
   return 0;
 }
 
+
+/* ------------------------------------------------------------------------
+ * netCDF short packing of a float grid (model/nc.c:14-336).
+ *
+ * decompress_2d (model/nc.c:251-266): a packed value equal to the file's
+ * missing_value becomes (float) spval, every other c becomes
+ * (float) c * scale_factor + add_offset, a float product and a float sum.
+ *
+ * compress_2d (model/nc.c:271-320): the minimum and maximum are taken in
+ * one pass with `if (g < grmin) ... else if (g > grmax)` from
+ * grmin = FLT_MAX, grmax = FLT_MIN (model/nc.c:285-297), so a value that is
+ * a new running minimum is never compared with the maximum, and grmax never
+ * drops below FLT_MIN; cells equal to (float) spval are skipped.  Each cell
+ * becomes (short) rint((g - grmin) / scale) with scale =
+ * (grmax - grmin) / (float) SHRT_MAX in float arithmetic (model/nc.c:301-318).
+ * The double -> short conversion of a value outside the range of int (or
+ * NaN, e.g. 0/0 when every cell is equal) is undefined in C; it is pinned
+ * here to the x86-64 result: the truncating conversion to a 32-bit int
+ * (INT_MIN when out of range or NaN), then its low 16 bits.
+ * ------------------------------------------------------------------------ */
+static int16_t nc_to_short_x86(double v) {
+  int32_t i;
+  if (v >= -2147483648.0 && v < 2147483648.0) i = (int32_t)v;
+  else i = INT32_MIN;
+  return (int16_t)(uint16_t)((uint32_t)i & 0xFFFFu);
+}
+
+void po_nc_decompress(const int16_t *packed, int64_t n, float add_offset, float scale_factor,
+                      int16_t missing_value, double spval, float *grid) {
+  for (int64_t k = 0; k < n; k++) {
+    if (packed[k] == missing_value) grid[k] = (float)spval;
+    else grid[k] = ((float)packed[k]) * scale_factor + add_offset;
+  }
+}
+
+void po_nc_compress(const float *grid, int64_t n, double spval, int16_t *packed,
+                    float *add_offset, float *scale_factor, int16_t *missing_value) {
+  const float fspv = (float)spval;
+  float grmin = FLT_MAX, grmax = FLT_MIN, scale;
+  *missing_value = SHRT_MIN;
+  for (int64_t k = 0; k < n; k++) {
+    const float g = grid[k];
+    if (g == fspv) continue;
+    if (g < grmin) grmin = g;
+    else if (g > grmax) grmax = g;
+  }
+  *add_offset = grmin;
+  scale = (grmax - grmin) / ((float)SHRT_MAX);
+  *scale_factor = scale;
+  for (int64_t k = 0; k < n; k++) {
+    if (grid[k] == fspv) packed[k] = *missing_value;
+    else packed[k] = nc_to_short_x86(rint((grid[k] - grmin) / scale));
+  }
+}

@@ -82,6 +82,12 @@ int po_depth_sigma(int n_bands, const double *wl, double theta_sun_deg, double t
                    int nthreads, const double *sample_depth_in, int32_t *sample_pixel,
                    double *sample_depth, double *table, float *depth_sigma);
 
+/* netCDF short packing (model/nc.c:251-320): see photic_oracle.c. */
+void po_nc_decompress(const int16_t *packed, int64_t n, float add_offset, float scale_factor,
+                      int16_t missing_value, double spval, float *grid);
+void po_nc_compress(const float *grid, int64_t n, double spval, int16_t *packed,
+                    float *add_offset, float *scale_factor, int16_t *missing_value);
+
 #ifdef __cplusplus
 }
 #endif

@@ -4,6 +4,7 @@ the reference's modified AS 47 Nelder-Mead -- behind a C ABI
 (include/photic.h) and this thin Python host layer over it.
 """
 from . import api  # noqa: F401
+from . import ncgrid  # noqa: F401
 from .api import (Config, JointGraph, PhoticError, alloc_outputs, cost,  # noqa: F401
                   depth_sigma, fallbacks_first, region_invert, generate_joint, generate_scene, invert, joint_invert, sync,
                   version)

@@ -1,4 +1,5 @@
-"""ctypes binding of libphotic_gb300.so (the C ABI in include/photic.h).
+"""ctypes binding of libphotic_gb300.so (the C ABI in include/photic.h and
+include/photic_nc.h).
 
 The structs below mirror include/photic.h field for field.  Loading fails
 loudly when the library has not been built: there is no CPU fallback.
@@ -15,7 +16,7 @@ MAX_BANDS = 8
 MAX_SCENES = 8
 MAX_HSTARTS = 32
 
-OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT, ERR_UNSUPPORTED = range(6)
+OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_IO = range(7)
 PREC_FP64, PREC_DF64, PREC_FP32, PREC_GUARDED = 0, 1, 2, 3
 LAYOUT_REFERENCE, LAYOUT_SCENE_B = 0, 1
 TUNE_INVERT, TUNE_JOINT = 0, 1
@@ -61,6 +62,21 @@ class photic_outputs(C.Structure):
         ("evals_kept", C.c_void_p),
         ("status", C.c_void_p),
         ("params", C.c_void_p),
+    ]
+
+
+class photic_nc_grid_info(C.Structure):
+    """include/photic_nc.h"""
+    _fields_ = [
+        ("ncols", C.c_int32),
+        ("nrows", C.c_int32),
+        ("add_offset", C.c_float),
+        ("scale_factor", C.c_float),
+        ("missing_value", C.c_int16),
+        ("has_missing_value", C.c_int32),
+        ("spval", C.c_double),
+        ("has_spval", C.c_int32),
+        ("format", C.c_int32),
     ]
 
 
@@ -134,6 +150,26 @@ _SIGS = {
     "photic_surrogate_seed_polished": (C.c_int, [C.c_void_p, C.POINTER(photic_config),
                                                  C.c_void_p, C.c_int64, C.c_double, C.c_int32,
                                                  C.c_void_p, C.c_void_p, C.c_void_p]),
+    "photic_nc_read_info": (C.c_int, [C.c_char_p, C.POINTER(photic_nc_grid_info)]),
+    "photic_nc_read_raw": (C.c_int, [C.c_char_p, C.POINTER(photic_nc_grid_info), C.c_void_p,
+                                     C.c_void_p, C.c_void_p]),
+    "photic_nc_write_raw": (C.c_int, [C.c_char_p, C.POINTER(photic_nc_grid_info), C.c_void_p,
+                                      C.c_void_p, C.c_void_p]),
+    "photic_nc_unpack_bands": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(photic_nc_grid_info),
+                                         C.c_int32, C.c_int64, C.c_void_p, C.c_void_p]),
+    "photic_nc_pack": (C.c_int, [C.c_void_p, C.c_int64, C.c_double, C.c_void_p,
+                                 C.POINTER(photic_nc_grid_info), C.c_void_p]),
+    "photic_nc_read_bands": (C.c_int, [C.POINTER(C.c_char_p), C.c_int32, C.c_void_p, C.c_int64,
+                                       C.POINTER(photic_nc_grid_info), C.c_void_p, C.c_void_p,
+                                       C.c_void_p]),
+    "photic_nc_write_grid": (C.c_int, [C.c_char_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p,
+                                       C.c_void_p, C.c_double, C.c_void_p]),
+    "read_nc": (None, [C.c_char_p, C.POINTER(C.POINTER(C.POINTER(C.c_float))),
+                       C.POINTER(C.c_int), C.POINTER(C.c_int),
+                       C.POINTER(C.POINTER(C.c_float)), C.POINTER(C.POINTER(C.c_float)),
+                       C.POINTER(C.c_double)]),
+    "write_nc": (None, [C.c_char_p, C.POINTER(C.POINTER(C.c_float)), C.c_int, C.c_int,
+                        C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_double]),
     "photic_gemm_bf16": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,
                                    C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
     "photic_gemm_bf16_strides": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,

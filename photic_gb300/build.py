@@ -25,7 +25,7 @@ LIB = os.path.join(HERE, "libphotic_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["photic_host.cu", "photic_invert.cu", "photic_guarded.cu", "photic_joint.cu",
            "photic_joint_group.cu", "photic_region.cu",
-           "photic_gemm.cu", "photic_mlp.cu", "photic_aux.cu"]
+           "photic_gemm.cu", "photic_mlp.cu", "photic_aux.cu", "photic_ncgrid.cu"]
 
 
 def nvcc() -> str:
@@ -54,7 +54,7 @@ def _stale() -> bool:
         return True
     t = os.path.getmtime(LIB)
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
-    deps.append(os.path.join(HERE, "..", "include", "photic.h"))
+    deps += [os.path.join(HERE, "..", "include", h) for h in ("photic.h", "photic_nc.h")]
     deps.append(os.path.abspath(__file__))
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 

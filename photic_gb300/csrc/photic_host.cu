@@ -264,6 +264,14 @@ int default_invert_block(int precision) { return precision == PHOTIC_PREC_FP64 ?
 
 }  // namespace
 
+namespace photic {
+// Error reporting for the other translation units of the library.
+int report_error(int code, const char *message) {
+  g_err = message;
+  return code;
+}
+}  // namespace photic
+
 extern "C" {
 
 const char *photic_version(void) { return "photic-gb300 0.1"; }

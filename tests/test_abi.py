@@ -14,7 +14,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def _declared(header):
     txt = open(os.path.join(ROOT, "include", header)).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-    return sorted(set(re.findall(r"\b(photic_[a-z0-9_]+|samodel[a-z_]*)\s*\(", txt)))
+    return sorted(set(re.findall(r"\b(photic_[a-z0-9_]+|samodel[a-z_]*|read_nc|write_nc)\s*\(",
+                                 txt)))
 
 
 @pytest.fixture(scope="module")
