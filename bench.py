@@ -169,6 +169,8 @@ def main():
                     help="pixels of the 4096x4096 temporal grid for the joint-fit leg (0: skip)")
     ap.add_argument("--region-side", type=int, default=96,
                     help="side of the square grid for the spatial-region leg (0: skip)")
+    ap.add_argument("--nc-side", type=int, default=4096,
+                    help="side of the scene written to and read from netCDF band files (0: off)")
     ap.add_argument("--serve-requests", type=int, default=12,
                     help="tile requests of the serving leg (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=50.0)
@@ -323,6 +325,12 @@ def main():
         net, warm = warm_start_leg(args, dev)
     if rank == 0 and args.serve_requests > 0:
         serving = serving_leg(args, net)
+    ncgrid = None
+    if rank == 0 and args.nc_side > 0:
+        try:
+            ncgrid = ncgrid_leg(args, dev, rrs)
+        except Exception as e:  # the format leg must not cost the headline line
+            ncgrid = {"error": f"{type(e).__name__}: {e}"}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
@@ -342,7 +350,7 @@ def main():
                            "mean_evals": float(evals[fitted].mean()) if fitted.any() else 0.0},
                 "oracle_sample": sample_stats, "roofline": roof, "cpu_baseline": cpu,
                 "warm_start": warm, "serving": serving, "temporal": temporal,
-                "regions": regions,
+                "regions": regions, "ncgrid": ncgrid,
                 "e2e": e2e, "clocks": clk}
         print(json.dumps(line))
     if pg_ is not None:
@@ -542,6 +550,100 @@ def region_leg(args, dev):
             "oracle_sample": {"pixels": int(fit.sum()), "frac_within_1cm": within,
                               "median_abs_dH_m": float(np.median(d)) if fit.any() else 0.0},
             "cpu_oracle_px_s": k * k / t_cpu, "cpu_threads": os.cpu_count() or 1}
+
+
+def ncgrid_leg(args, dev, rrs):
+    """The scene's bands through the reference's netCDF grid files
+    (model/nc.c): each band written from the device (GPU packing, host
+    container), the four files read back into the inversion's layout (host
+    container, GPU unpacking), and the two kernels timed alone against the
+    measured HBM copy rate.  Algorithmic bytes: unpacking reads 2 B and
+    writes 4 B per cell and band; packing reads 4 B and writes 2 B per cell
+    (its three passes read the grid three times).  Parity: the unpacked
+    bands and the packed grid against the CPU oracle on a sample."""
+    import tempfile
+    import torch
+    from photic_gb300 import ncgrid as N
+    from oracle import oracle as O
+    import math
+    n = min(args.nc_side, math.isqrt(rrs.shape[0]))
+    npix = n * n
+    nodata = -9999.0
+    lons = np.linspace(150.0, 151.0, n).astype(np.float32)
+    lats = np.linspace(-24.0, -23.0, n).astype(np.float32)
+    bands = [rrs[:npix, b].reshape(n, n).contiguous() for b in range(4)]
+    tmp = tempfile.mkdtemp(prefix="photic_nc_")
+    paths = [os.path.join(tmp, f"band{b}.nc") for b in range(4)]
+    try:
+        N.write_grid(paths[0], bands[0], lons, lats, nodata)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for b in range(4):
+            N.write_grid(paths[b], bands[b], lons, lats, nodata)
+        t_write = time.perf_counter() - t0
+        N.read_bands(paths)  # warm-up (and page cache)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out, info, _, _ = N.read_bands(paths)
+        torch.cuda.synchronize()
+        t_read = time.perf_counter() - t0
+        packed, infos = [], []
+        for b in range(4):
+            pk, inf = N.pack(bands[b], nodata)
+            inf.update(ncols=n, nrows=n)
+            packed.append(pk)
+            infos.append(inf)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        reps = 5
+        N.unpack_bands(packed, infos, npix)
+        torch.cuda.synchronize()
+        ev[0].record()
+        for _ in range(reps):
+            N.unpack_bands(packed, infos, npix)
+        ev[1].record()
+        for _ in range(reps):
+            N.pack(bands[0], nodata)
+        ev[2].record()
+        torch.cuda.synchronize()
+        t_un = ev[0].elapsed_time(ev[1]) / reps * 1e-3
+        t_pk = ev[1].elapsed_time(ev[2]) / reps * 1e-3
+        peak = None
+        try:
+            with open(os.path.join(os.path.dirname(os.path.abspath(__file__)),
+                                   "MEASURED_PEAKS.json")) as f:
+                peak = float(json.load(f)["hbm_gbs"])
+        except (OSError, KeyError, ValueError):
+            pass
+        un_gbs = npix * 4 * 6 / t_un / 1e9
+        pk_gbs = npix * 6 / t_pk / 1e9
+        # parity on a sample of cells
+        k = min(npix, 1 << 20)
+        g0 = bands[0].reshape(-1)[:k].cpu().numpy().reshape(1, -1)
+        want, off, sc, mv = O.nc_compress(g0, nodata)
+        got_pk, inf0 = N.pack(bands[0].reshape(-1)[:k].contiguous(), nodata)
+        got = np.frombuffer(got_pk.cpu().numpy().tobytes(), dtype=">i2").astype(np.int16)
+        pack_ok = bool(np.array_equal(got, want.reshape(-1)) and
+                       np.float32(inf0["scale_factor"]) == np.float32(sc))
+        p_full = np.frombuffer(packed[0].cpu().numpy().tobytes(), dtype=">i2").astype(np.int16)
+        dec, _ = O.nc_decompress(p_full[:k], infos[0]["add_offset"], infos[0]["scale_factor"],
+                                 infos[0]["missing_value"], nodata)
+        unpack_ok = dec.tobytes() == out[:k, 0].contiguous().cpu().numpy().tobytes()
+        return {"workload": f"{n}x{n} scene, 4 band files (short-packed, {2 * npix >> 20} MiB each)",
+                "write_grid_px_s": 4 * npix / t_write, "read_bands_px_s": npix / t_read,
+                "unpack": {"ms": t_un * 1e3, "algorithmic_bytes_per_px": 24,
+                           "achieved_gbs": un_gbs,
+                           "frac_of_measured_hbm": un_gbs / peak if peak else None},
+                "pack": {"ms": t_pk * 1e3, "algorithmic_bytes_per_cell": 6,
+                         "achieved_gbs": pk_gbs,
+                         "frac_of_measured_hbm": pk_gbs / peak if peak else None,
+                         "note": "three passes read the grid three times (14 B/cell moved)"},
+                "oracle_sample": {"cells": k, "pack_identical": pack_ok,
+                                  "unpack_identical": bool(unpack_ok)}}
+    finally:
+        for p in paths:
+            if os.path.exists(p):
+                os.remove(p)
+        os.rmdir(tmp)
 
 
 def serving_leg(args, net):
