@@ -96,7 +96,10 @@ int photic_nc_read_bands(const char *const *paths, int32_t n_bands, float *d_rrs
                          int64_t capacity_px, photic_nc_grid_info *info, float *h_lons,
                          float *h_lats, void *stream);
 
-/* write_nc of a device grid (nrows * ncols floats, rows of lons). */
+/* write_nc of a device grid (nrows * ncols floats, rows of lons); the file
+ * name, and its filename attribute, with leading and trailing white space
+ * removed as the reference's trim() does (read_nc / write_nc trim the
+ * caller's string in place, as the reference does). */
 int photic_nc_write_grid(const char *path, const float *d_grid, int32_t ncols, int32_t nrows,
                          const float *h_lons, const float *h_lats, double spval, void *stream);
 

@@ -5,6 +5,7 @@
 // model/common.c:298) and the subsurface-angle secants once per call, and
 // launching the kernels.  No pixel is ever processed on the host.
 #include <cuda_runtime.h>
+#include <ctype.h>
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
@@ -15,6 +16,7 @@
 #include <vector>
 
 #include "../../include/photic.h"
+#include "../../include/photic_nc.h"
 #include "photic_kernels.h"
 #include "photic_params.h"
 #include "photic_tables.h"
@@ -1513,6 +1515,134 @@ void samodel_Rrs(double P, double G, double X, double B[], double q[], double H,
   cudaFree(mem);
 }
 
+}  // extern "C"
+
+namespace {
+
+// The result grids samodel() writes when it ends (model/samodel.c:1492-1690),
+// as netCDF files in the current directory: for each scene
+// <scene>_K_coastal / _K_blue / _K_green / _K_red.nc (K of bands 0..3 at the
+// fit, :1153-1156) and <scene>_P / _G / _X.nc (:1157-1159), then
+// modelled_H, _H_sigma, _error, _albedo, _bottom_sand, _bottom_seagrass,
+// _bottom_coral, _min_K, _bottom_type and _index_optical_depth.nc from the
+// caller's grids.  Coordinates and spval come from the first band grid of
+// the first scene (:1498-1510).  K is the forward model's K at the fitted
+// P, G, X with the pixel's measured Rrs(440)/Rrs(490): from the fit's
+// double parameters for one scene fitted pixel by pixel, from the stored
+// float P, G, X for the joint and region fits.  Unfitted pixels hold 0.
+int samodel_write_files(const photic_config &cfg, const photic_scene *scene_data,
+                        const photic_geogrid *gridded_data, const int *scene_indexes,
+                        int nscenes, int nrows, int ncols, const std::vector<float> &h_rrs,
+                        const std::vector<int32_t> &st, const std::vector<float> &pgx,
+                        const std::vector<double> &params6, float **const *outs) {
+  const int nb = cfg.n_bands;
+  const int64_t npix = (int64_t)nrows * ncols, nobs = npix * nscenes;
+  const photic_geogrid &g0 = gridded_data[scene_data[scene_indexes[0]].band_indexes[0]];
+  std::vector<float> lons((size_t)ncols), lats((size_t)nrows);
+  for (int n = 0; n < ncols; n++) lons[n] = g0.wlon + ((float)n) * g0.cellsize;
+  for (int n = 0; n < nrows; n++) lats[n] = g0.slat + ((float)n) * g0.cellsize;
+  const double spval = g0.nodata_value;
+  float *d_grid = nullptr;
+  double *d_buf = nullptr;
+  const size_t nbuf = (size_t)npix * (7 + 2 + 2 * (size_t)nb);
+  if (cudaMalloc((void **)&d_grid, (size_t)npix * sizeof(float)) != cudaSuccess ||
+      cudaMalloc((void **)&d_buf, nbuf * sizeof(double)) != cudaSuccess) {
+    cudaFree(d_grid);
+    return fail(PHOTIC_ERR_NOMEM, "samodel: result-file buffers");
+  }
+  double *d_p7 = d_buf, *d_440 = d_p7 + 7 * npix, *d_490 = d_440 + npix;
+  double *d_rm = d_490 + npix, *d_K = d_rm + (size_t)nb * npix;
+  std::vector<float> host((size_t)npix);
+  int rc = PHOTIC_OK;
+  auto put = [&](const std::string &name) {
+    if (rc != PHOTIC_OK) return;
+    printf("\nWriting file %s...", name.c_str());
+    cudaError_t e = cudaMemcpy(d_grid, host.data(), (size_t)npix * sizeof(float),
+                               cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      rc = cuda_fail(e, "samodel: result grid upload");
+      return;
+    }
+    rc = photic_nc_write_grid(name.c_str(), d_grid, ncols, nrows, lons.data(), lats.data(),
+                              spval, nullptr);
+  };
+  auto fitted = [&](int64_t p) { return (st[p] & 0xFF) == PHOTIC_PX_FITTED; };
+  std::vector<double> p7((size_t)npix * 7), r440((size_t)npix), r490((size_t)npix);
+  std::vector<double> K((size_t)npix * nb);
+  const char *kname[4] = {"K_coastal", "K_blue", "K_green", "K_red"};
+  for (int k = 0; k < nscenes && rc == PHOTIC_OK; k++) {
+    const photic_scene &sk = scene_data[scene_indexes[k]];
+    std::string sname(sk.scene_name, strnlen(sk.scene_name, sizeof sk.scene_name));
+    size_t b0 = 0, e0 = sname.size();
+    while (b0 < e0 && isspace((unsigned char)sname[b0])) b0++;
+    while (e0 > b0 && isspace((unsigned char)sname[e0 - 1])) e0--;
+    sname = sname.substr(b0, e0 - b0);
+    for (int64_t p = 0; p < npix; p++) {
+      const size_t o = (size_t)(p * nscenes + k);
+      double P = 0.01, G = 0.01, X = 0.01;
+      if (fitted(p)) {
+        if (!params6.empty()) {
+          P = 0.01 * fabs(params6[(size_t)p * 6 + 3]);
+          G = 0.01 * fabs(params6[(size_t)p * 6 + 4]);
+          X = 0.01 * fabs(params6[(size_t)p * 6 + 5]);
+        } else {
+          P = pgx[o];
+          G = pgx[(size_t)nobs + o];
+          X = pgx[2 * (size_t)nobs + o];
+        }
+      }
+      double rr[PHOTIC_MAX_BANDS];
+      for (int b = 0; b < nb; b++) rr[b] = h_rrs[o * nb + b];
+      double a440 = photic_interp_1d(cfg.wavelengths, rr, nb, 440.0);
+      if (a440 < 0.0) a440 = 0.0001;  // model/samodel.c:1785-1799
+      r440[p] = a440;
+      r490[p] = photic_interp_1d(cfg.wavelengths, rr, nb, 490.0);
+      const double row[7] = {P, G, X, 0.0, 1.0, 1.0, 0.0};
+      memcpy(&p7[(size_t)p * 7], row, sizeof row);
+    }
+    photic_config ck = cfg;
+    ck.theta_sun_deg = sk.theta_w;
+    cudaMemcpy(d_p7, p7.data(), p7.size() * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_440, r440.data(), r440.size() * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_490, r490.data(), r490.size() * sizeof(double), cudaMemcpyHostToDevice);
+    rc = photic_forward_batch(&ck, d_p7, d_440, d_490, npix, d_rm, d_K, nullptr);
+    if (rc == PHOTIC_OK) rc = photic_sync(nullptr);
+    if (rc != PHOTIC_OK) break;
+    cudaMemcpy(K.data(), d_K, K.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    for (int kb = 0; kb < 4; kb++) {
+      for (int64_t p = 0; p < npix; p++)
+        host[p] = fitted(p) && kb < nb ? (float)K[(size_t)p * nb + kb] : 0.0f;
+      put(sname + "_" + kname[kb] + ".nc");
+    }
+    const char *pname[3] = {"P", "G", "X"};
+    for (int c = 0; c < 3; c++) {
+      for (int64_t p = 0; p < npix; p++) {
+        const size_t o = (size_t)(p * nscenes + k);
+        host[p] = fitted(p) ? pgx[(size_t)c * nobs + o] : 0.0f;
+      }
+      put(sname + "_" + pname[c] + ".nc");
+    }
+  }
+  const char *gname[10] = {"modelled_H.nc", "modelled_H_sigma.nc", "modelled_error.nc",
+                           "modelled_albedo.nc", "modelled_bottom_sand.nc",
+                           "modelled_bottom_seagrass.nc", "modelled_bottom_coral.nc",
+                           "modelled_min_K.nc", "modelled_bottom_type.nc",
+                           "modelled_index_optical_depth.nc"};
+  for (int f = 0; f < 10 && rc == PHOTIC_OK; f++) {
+    for (int i = 0; i < nrows; i++)
+      for (int j = 0; j < ncols; j++) host[(size_t)i * ncols + j] = outs[f] ? outs[f][i][j] : 0.0f;
+    put(gname[f]);
+  }
+  if (rc == PHOTIC_OK) printf("\n... finished.\n");
+  cudaFree(d_grid);
+  cudaFree(d_buf);
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
 void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scene_indexes,
              int nscenes, int empirical_depth_present, photic_geogrid empirical_depths,
              int n_smoothing_radius, int n_spatial, int n_bottoms, float **depth,
@@ -1586,12 +1716,17 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
   // device buffers
   float *d_rrs = nullptr;
   double *d_depth = nullptr, *d_seeds = nullptr, *d_emp = nullptr, *d_th = nullptr;
-  float *d_f = nullptr;
+  float *d_f = nullptr, *d_pgx = nullptr;
+  double *d_params = nullptr;
   int32_t *d_status = nullptr, *d_off = nullptr;
+  const bool one_by_one = nscenes == 1 && !regions;
   bool ok = cudaMalloc((void **)&d_rrs, h_rrs.size() * sizeof(float)) == cudaSuccess &&
             cudaMalloc((void **)&d_depth, npix * sizeof(double)) == cudaSuccess &&
             cudaMalloc((void **)&d_f, 4 * npix * sizeof(float)) == cudaSuccess &&
-            cudaMalloc((void **)&d_status, npix * sizeof(int32_t)) == cudaSuccess;
+            cudaMalloc((void **)&d_status, npix * sizeof(int32_t)) == cudaSuccess &&
+            cudaMalloc((void **)&d_pgx, 3 * nobs * sizeof(float)) == cudaSuccess &&
+            (!one_by_one ||
+             cudaMalloc((void **)&d_params, 6 * npix * sizeof(double)) == cudaSuccess);
   if (!ok) {
     fail(PHOTIC_ERR_NOMEM, "samodel: device buffers");
   } else {
@@ -1604,6 +1739,10 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
     o.K_min = d_f + 2 * npix;
     o.iod = d_f + 3 * npix;
     o.status = d_status;
+    o.P = d_pgx;  // per observation for the joint fit
+    o.G = d_pgx + nobs;
+    o.X = d_pgx + 2 * nobs;
+    o.params = d_params;
     int rc;
     if (nscenes == 1) {
       if (!h_emp.empty()) {
@@ -1685,11 +1824,28 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
           bottom_type[i][j] = fit ? 1.0f : -9999.0f;
           index_optical_depth[i][j] = fit ? f[3 * npix + p] : 0.0f;
         }
+      if (rc == PHOTIC_OK) {
+        std::vector<float> pgx((size_t)3 * nobs);
+        std::vector<double> params6;
+        cudaMemcpy(pgx.data(), d_pgx, pgx.size() * sizeof(float), cudaMemcpyDeviceToHost);
+        if (one_by_one) {
+          params6.resize((size_t)6 * npix);
+          cudaMemcpy(params6.data(), d_params, params6.size() * sizeof(double),
+                     cudaMemcpyDeviceToHost);
+        }
+        float **const outs[10] = {depth,     depth_sigma, model_error, bottom_albedo,
+                                  bottom_sand, bottom_seagrass, bottom_coral, K_min,
+                                  bottom_type, index_optical_depth};
+        samodel_write_files(cfg, scene_data, gridded_data, scene_indexes, nscenes, nrows, ncols,
+                            h_rrs, st, pgx, params6, outs);
+      }
     }
   }
   cudaFree(d_rrs);
   cudaFree(d_depth);
   cudaFree(d_f);
+  cudaFree(d_pgx);
+  cudaFree(d_params);
   cudaFree(d_status);
   if (d_emp) cudaFree(d_emp);
   if (d_seeds) cudaFree(d_seeds);

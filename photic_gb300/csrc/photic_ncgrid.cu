@@ -14,6 +14,7 @@
 // minimum of every earlier cell), and the quantisation.
 #include <cuda_runtime.h>
 #include <float.h>
+#include <ctype.h>
 #include <limits.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -734,12 +735,20 @@ cudaError_t unpack(const UnpackArgs &a, int nb, cudaStream_t s) {
   }
 }
 
+// The file name as trim() leaves it (model/common.c:715-751): leading and
+// trailing white space removed.
 std::string trimmed(const char *file) {
   std::string s(file);
-  while (!s.empty() && (s.back() == ' ' || s.back() == '\n' || s.back() == '\r' ||
-                        s.back() == '\t'))
-    s.pop_back();
-  return s;
+  size_t b = 0, e = s.size();
+  while (b < e && isspace((unsigned char)s[b])) b++;
+  while (e > b && isspace((unsigned char)s[e - 1])) e--;
+  return s.substr(b, e - b);
+}
+
+// trim() edits the caller's string in place; the drop-ins do the same.
+void trim_in_place(char *file) {
+  const std::string t = trimmed(file);
+  memcpy(file, t.c_str(), t.size() + 1);
 }
 
 // The reference's ERR macro (model/nc.h:6): message and exit(1).
@@ -915,7 +924,9 @@ int photic_nc_write_grid(const char *path, const float *d_grid, int32_t ncols, i
     info.ncols = ncols;
     info.nrows = nrows;
     info.format = 0;
-    rc = write_grid_file(trimmed(path), path, info, hpk, h_lons, h_lats);
+    // the filename attribute is the name trim() left in place (model/nc.c:38-44)
+    const std::string name = trimmed(path);
+    rc = write_grid_file(name, name, info, hpk, h_lons, h_lats);
   }
   cudaFreeAsync(dpk, s);
   cudaStreamSynchronize(s);
@@ -928,7 +939,8 @@ int photic_nc_write_grid(const char *path, const float *d_grid, int32_t ncols, i
 // (model/common.c:562-572); lons and lats malloc'd.
 void read_nc(char *file, float ***grid, int *ncols, int *nrows, float **lons, float **lats,
              double *spval) {
-  const std::string path = trimmed(file);
+  trim_in_place(file);
+  const std::string path(file);
   photic_nc_grid_info info;
   if (photic_nc_read_info(path.c_str(), &info)) die(photic_last_error());
   if (!info.has_spval) printf("\nWARNING: 'decompressed_missing_value' not present. Setting to zero.\n");
@@ -969,6 +981,7 @@ void read_nc(char *file, float ***grid, int *ncols, int *nrows, float **lons, fl
 // write_nc (model/nc.c:14-134).
 void write_nc(char *file, float **grid, int ncols, int nrows, float *lons, float *lats,
               double spval) {
+  trim_in_place(file);
   if (ncols < 1 || nrows < 1) die("empty grid");
   const int64_t n = (int64_t)ncols * nrows;
   std::vector<float> host((size_t)n);

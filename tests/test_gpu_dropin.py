@@ -35,7 +35,9 @@ def _write_input(path, rrs, params=None, nrows=0, ncols=0):
 
 
 def _run(exe, mode, inp, out):
-    r = subprocess.run([exe, mode, inp, out], capture_output=True, text=True, timeout=600)
+    # samodel() writes its result files into the working directory
+    r = subprocess.run([exe, mode, inp, out], capture_output=True, text=True, timeout=600,
+                       cwd=os.path.dirname(inp))
     assert r.returncode == 0, (mode, r.returncode, r.stderr[-2000:])
 
 
@@ -157,6 +159,40 @@ def test_samodel_grid_matches_oracle(driver, port, tmp_path):
     np.testing.assert_allclose(g[2, fit][same], ref[fit, 3][same].astype(np.float32), rtol=1e-6)
     np.testing.assert_allclose(g[3, fit][same], ref[fit, 1][same].astype(np.float32), rtol=1e-6)
     np.testing.assert_allclose(g[7, fit][same], ref[fit, 4][same].astype(np.float32), rtol=1e-6)
+    # the result files samodel() ends with (model/samodel.c:1492-1690)
+    from photic_gb300 import ncgrid as N
+    glob = ["modelled_H", "modelled_H_sigma", "modelled_error", "modelled_albedo",
+            "modelled_bottom_sand", "modelled_bottom_seagrass", "modelled_bottom_coral",
+            "modelled_min_K", "modelled_bottom_type", "modelled_index_optical_depth"]
+    for k, name in enumerate(glob):
+        packed, lons, lats, info = N.read_raw(str(tmp_path / f"{name}.nc"))
+        want, off, sc, mv = port.nc_compress(g[k].reshape(nrows, ncols), -9999.0)
+        np.testing.assert_array_equal(packed, want, err_msg=name)
+        assert np.float32(info["add_offset"]) == np.float32(off), name
+        assert np.float32(info["scale_factor"]) == np.float32(sc), name
+        assert info["spval"] == -9999.0 and (lons == 0).all() and (lats == 0).all()
+
+    def decoded(name):
+        packed, _, _, info = N.read_raw(str(tmp_path / f"synthetic_{name}.nc"))
+        v, _ = port.nc_decompress(packed, info["add_offset"], info["scale_factor"],
+                                  info["missing_value"], info["spval"])
+        return v.reshape(-1), info["scale_factor"]
+
+    # (cell 0 is left out: when it is the grid's maximum, compress_2d never
+    # compares it with the maximum and its packed value wraps, as in the
+    # reference)
+    rest = np.arange(nrows * ncols) > 0
+    agree = np.zeros(nrows * ncols, bool)
+    agree[np.flatnonzero(fit)[same]] = True
+    for name, col in (("P", 11), ("G", 19), ("X", 27)):
+        v, step = decoded(name)
+        m = agree & rest
+        assert (np.abs(v[m] - ref[m, col]) <= 0.51 * step + 1e-7).all(), name
+        assert (np.abs(v[~fit & rest]) <= 0.51 * step).all(), name
+    for name in ("K_coastal", "K_blue", "K_green", "K_red"):
+        v, step = decoded(name)
+        m = fit & rest
+        assert (v[m] > 0).all() and (v[m] <= 2.5 + step).all(), name
 
 
 def test_samodel_grid_regions_matches_oracle(driver, port, tmp_path):
