@@ -32,19 +32,26 @@ enum NmPhase : int32_t {
   PH_FINAL,           // re-evaluation at the kept optimum
 };
 
-// Loops over the simplex unroll fully for the small single-scene simplex
-// (n = 6) and stay rolled for the temporal fit (n up to 33).
-template <int N>
-struct NmUnroll {
-  static constexpr int kV = N <= 8 ? N + 1 : 1;  // loops over vertices
-  static constexpr int kC = N <= 8 ? N : 1;      // loops over coordinates
-};
+// Loops over the simplex: fully unrolled for the single-scene simplex
+// (n <= 8), so that the lane's vectors stay in registers, and rolled for the
+// temporal fit (n up to 33).  (An unroll count that depends on a template
+// parameter was not honoured: the n = 6 loops stayed rolled, and their
+// dynamic indexes put the lane's vectors in local memory.)
+template <int B, int E, bool kUnroll, class F>
+__device__ __forceinline__ void nm_for(F &&f) {
+  if constexpr (kUnroll) {
+#pragma unroll
+    for (int i = B; i < E; i++) f(i);
+  } else {
+#pragma unroll 1
+    for (int i = B; i < E; i++) f(i);
+  }
+}
 
 template <int N, class P, int BS>
 struct NmLane {
   using T = typename P::T;
-  static constexpr int UV = NmUnroll<N>::kV;
-  static constexpr int UC = NmUnroll<N>::kC;
+  static constexpr bool kU = N <= 8;  // unroll the loops over the simplex
   T *v, *f;  // shared: v[(j * N + i) * BS + tid], f[j * BS + tid]
   T x[N];    // point to evaluate next
   T cen[N], refl[N], trial[N], xmin[N], start[N], step[N];
@@ -58,15 +65,11 @@ struct NmLane {
 
   static __device__ __forceinline__ T pick(const T (&a)[N], int k) {
     T r = a[0];
-#pragma unroll UC
-    for (int i = 1; i < N; i++)
-      if (i == k) r = a[i];
+    nm_for<1, N, kU>([&](int i) { if (i == k) r = a[i]; });
     return r;
   }
   static __device__ __forceinline__ void put(T (&a)[N], int k, T val) {
-#pragma unroll UC
-    for (int i = 0; i < N; i++)
-      if (i == k) a[i] = val;
+    nm_for<0, N, kU>([&](int i) { if (i == k) a[i] = val; });
   }
 
   // Begin a nelmin call from start[]/step[] (model/asa047.c:161-170).
@@ -83,24 +86,22 @@ struct NmLane {
   }
 
   __device__ __forceinline__ void restart_simplex() {
-#pragma unroll UC
-    for (int i = 0; i < N; i++) {
+    nm_for<0, N, kU>([&](int i) {
       x[i] = start[i];
       V(N, i) = start[i];
-    }
+    });
     phase = PH_INIT_BASE;
   }
 
   // Vertex j: the start point moved by step[j] * scale along coordinate j
   // (model/asa047.c:181-194).
   __device__ __forceinline__ void make_vertex(int j) {
-#pragma unroll UC
-    for (int i = 0; i < N; i++) {
+    nm_for<0, N, kU>([&](int i) {
       T s = start[i];
       if (i == j) s = P::add(start[i], P::mul(step[i], scale));
       x[i] = s;
       V(j, i) = s;
-    }
+    });
     jj = j;
     phase = PH_INIT_VERT;
   }
@@ -108,14 +109,13 @@ struct NmLane {
   __device__ __forceinline__ void find_lo() {
     ylo = F(0);
     lo = 0;
-#pragma unroll UV
-    for (int j = 1; j <= N; j++) {
+    nm_for<1, N + 1, kU>([&](int j) {
       T fj = F(j);
       if (P::lt(fj, ylo)) {
         ylo = fj;
         lo = j;
       }
-    }
+    });
   }
 
   // Top of the inner loop (model/asa047.c:213-250): budget check, worst
@@ -124,34 +124,29 @@ struct NmLane {
     if (kcount <= icount) return false;
     T yhi = F(0);
     hi = 0;
-#pragma unroll UV
-    for (int j = 1; j <= N; j++) {
+    nm_for<1, N + 1, kU>([&](int j) {
       T fj = F(j);
       if (P::lt(yhi, fj)) {
         yhi = fj;
         hi = j;
       }
-    }
-#pragma unroll UC
-    for (int i = 0; i < N; i++) {
+    });
+    nm_for<0, N, kU>([&](int i) {
       T z = P::zero();
-#pragma unroll UV
-      for (int j = 0; j <= N; j++) z = P::add(z, V(j, i));
+      nm_for<0, N + 1, kU>([&](int j) { z = P::add(z, V(j, i)); });
       z = P::sub(z, V(hi, i));
       cen[i] = P::div_n(z, N);
-    }
-#pragma unroll UC
-    for (int i = 0; i < N; i++) {
+    });
+    nm_for<0, N, kU>([&](int i) {
       refl[i] = P::add(cen[i], P::sub(cen[i], V(hi, i)));
       x[i] = refl[i];
-    }
+    });
     phase = PH_REFLECT;
     return true;
   }
 
   __device__ __forceinline__ void replace_hi(const T (&p)[N], T y) {
-#pragma unroll UC
-    for (int i = 0; i < N; i++) V(hi, i) = p[i];
+    nm_for<0, N, kU>([&](int i) { V(hi, i) = p[i]; });
     F(hi) = y;
   }
 
@@ -168,15 +163,13 @@ struct NmLane {
     if (icount <= kcount) {
       countdown = konvge;
       T z = P::zero();
-#pragma unroll UV
-      for (int j = 0; j <= N; j++) z = P::add(z, F(j));
+      nm_for<0, N + 1, kU>([&](int j) { z = P::add(z, F(j)); });
       T mean = P::div_n(z, N + 1);
       z = P::zero();
-#pragma unroll UV
-      for (int j = 0; j <= N; j++) {
+      nm_for<0, N + 1, kU>([&](int j) {
         T d = P::sub(F(j), mean);
         z = P::add(z, P::mul(d, d));
-      }
+      });
       if (P::le(z, var_limit)) return true;
     }
     return false;
@@ -205,33 +198,28 @@ struct NmLane {
         fr = y;
         icount++;
         if (P::lt(fr, ylo)) {
-#pragma unroll UC
-          for (int i = 0; i < N; i++) {
+          nm_for<0, N, kU>([&](int i) {
             trial[i] = P::add(cen[i], P::mul2(P::sub(refl[i], cen[i])));
             x[i] = trial[i];
-          }
+          });
           phase = PH_EXPAND;
         } else {
           int worse = 0;
-#pragma unroll UV
-          for (int j = 0; j <= N; j++)
-            if (P::lt(fr, F(j))) worse++;
+          nm_for<0, N + 1, kU>([&](int j) { if (P::lt(fr, F(j))) worse++; });
           if (worse > 1) {
             replace_hi(refl, fr);
             cs = CS_ITER_END;
           } else if (worse == 0) {
-#pragma unroll UC
-            for (int i = 0; i < N; i++) {
+            nm_for<0, N, kU>([&](int i) {
               trial[i] = P::add(cen[i], P::half(P::sub(V(hi, i), cen[i])));
               x[i] = trial[i];
-            }
+            });
             phase = PH_CONTRACT_IN;
           } else {
-#pragma unroll UC
-            for (int i = 0; i < N; i++) {
+            nm_for<0, N, kU>([&](int i) {
               trial[i] = P::add(cen[i], P::half(P::sub(refl[i], cen[i])));
               x[i] = trial[i];
-            }
+            });
             phase = PH_CONTRACT_OUT;
           }
         }
@@ -246,12 +234,11 @@ struct NmLane {
         icount++;
         if (P::lt(F(hi), y)) {
           // shrink every vertex towards the best (model/asa047.c:331-351)
-#pragma unroll UC
-          for (int i = 0; i < N; i++) {
+          nm_for<0, N, kU>([&](int i) {
             T s = P::half(P::add(V(0, i), V(lo, i)));
             V(0, i) = s;
             x[i] = s;
-          }
+          });
           jj = 0;
           phase = PH_SHRINK;
         } else {
@@ -264,12 +251,11 @@ struct NmLane {
         icount++;
         if (jj < N) {
           const int j = jj + 1;
-#pragma unroll UC
-          for (int i = 0; i < N; i++) {
+          nm_for<0, N, kU>([&](int i) {
             T s = P::half(P::add(V(j, i), V(lo, i)));
             V(j, i) = s;
             x[i] = s;
-          }
+          });
           jj = j;
         } else {
           cs = CS_READY;
@@ -289,8 +275,7 @@ struct NmLane {
         } else {
           const T del = P::eps_step(pick(step, jj));
           put(xmin, jj, P::sub(P::sub(pick(xmin, jj), del), del));
-#pragma unroll UC
-          for (int i = 0; i < N; i++) x[i] = xmin[i];
+          nm_for<0, N, kU>([&](int i) { x[i] = xmin[i]; });
           phase = PH_PROBE_MINUS;
         }
         break;
@@ -325,8 +310,7 @@ struct NmLane {
           cs = iteration_end() ? CS_END_INNER : CS_TOP;
           break;
         case CS_END_INNER:
-#pragma unroll UC
-          for (int i = 0; i < N; i++) xmin[i] = V(lo, i);
+          nm_for<0, N, kU>([&](int i) { xmin[i] = V(lo, i); });
           floor_lo = P::trunc10(F(lo));
           if (kcount < icount) {
             ifault = 2;
@@ -340,8 +324,7 @@ struct NmLane {
         case CS_PROBE_PLUS: {
           const T del = P::eps_step(pick(step, jj));
           put(xmin, jj, P::add(pick(xmin, jj), del));
-#pragma unroll UC
-          for (int i = 0; i < N; i++) x[i] = xmin[i];
+          nm_for<0, N, kU>([&](int i) { x[i] = xmin[i]; });
           phase = PH_PROBE_PLUS;
           cs = CS_NONE;
           break;
@@ -351,8 +334,7 @@ struct NmLane {
             cs = CS_NM_DONE;
           } else {
             // restart from the probe point with a 1e-6 simplex
-#pragma unroll UC
-            for (int i = 0; i < N; i++) start[i] = xmin[i];
+            nm_for<0, N, kU>([&](int i) { start[i] = xmin[i]; });
             scale = P::eps_scale();
             numres++;
             restart_simplex();
