@@ -277,7 +277,9 @@ def main():
             "unit": "TFLOP/s", "frac": achieved / float(p64[0]),
             "traffic": TRAFFIC_BYTES_PER_PIXEL * npix,
             "traffic_note": "DRAM bytes per launch, scaled by pixels from an ncu capture of "
-                            "a 65536-pixel launch of the same kernel",
+                            "a 65536-pixel launch of this kernel taken before its simplex "
+                            "vectors moved from local memory to registers (most of those "
+                            "bytes were the local-memory stack frame); not yet recaptured",
             "peak_source": "measured by photic_measure_peaks (DFMA chains) in this run",
             "evals_per_s": total_evals / (ms_step * 1e-3),
             "flops_per_eval": flops_per_eval}
