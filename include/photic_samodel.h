@@ -160,7 +160,10 @@ typedef struct photic_scene {
  * Monte Carlo estimate computed by photic_depth_sigma with the scene's
  * R_sigma, 128 samples per 0.25 m interval and a fixed seed; 0 for more
  * scenes or n_spatial == 2.  Depth is written negative below the datum, as the reference does
- * (model/samodel.c:1486). */
+ * (model/samodel.c:1486).  Like the reference, it ends by writing the result
+ * grids as netCDF files in the working directory (model/samodel.c:1492-1690):
+ * <scene>_K_coastal/_K_blue/_K_green/_K_red/_P/_G/_X.nc per scene and the ten
+ * modelled_*.nc grids, packed as write_nc packs them (photic_nc.h). */
 void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scene_indexes,
              int nscenes, int empirical_depth_present, photic_geogrid empirical_depths,
              int n_smoothing_radius, int n_spatial, int n_bottoms, float **depth,
