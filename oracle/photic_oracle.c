@@ -816,6 +816,19 @@ double po_cost(int n_bands, const double *wl, double theta_sun_deg, double theta
   return c;
 }
 
+/* nelmin (model/asa047.c:10-502) over a caller's cost, n <= PO_MAX_PARAMS:
+ * lets the tests run the device state machines against this restatement
+ * at any simplex size.  start is not modified. */
+void po_nelmin_fn(double (*fn)(const double *x, void *ctx), void *ctx, int n,
+                  const double *start_in, const double *step, double reqmin, int konvge,
+                  int kcount, double *xmin, double *ynewlo, int *icount, int *numres,
+                  int *ifault) {
+  double start[PO_MAX_PARAMS];
+  memcpy(start, start_in, (size_t)n * sizeof(double));
+  po_nelmin(fn, ctx, n, start, xmin, ynewlo, reqmin, step, konvge, kcount, icount, numres,
+            ifault);
+}
+
 void po_nelmin_pixel(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
                      const double *rrs_measured, const double *start_in, const double *step,
                      double reqmin, int konvge, int kcount, double *xmin, double *ynewlo,

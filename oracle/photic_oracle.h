@@ -48,6 +48,10 @@ void po_band_constants(int n_bands, const double *wl, double theta_sun_deg,
 double po_cost(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
                double h_tide, const double *rrs_measured, const double *params,
                double *rrs_modelled, double *K_out);
+void po_nelmin_fn(double (*fn)(const double *x, void *ctx), void *ctx, int n,
+                  const double *start_in, const double *step, double reqmin, int konvge,
+                  int kcount, double *xmin, double *ynewlo, int *icount, int *numres,
+                  int *ifault);
 void po_nelmin_pixel(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
                      const double *rrs_measured, const double *start, const double *step,
                      double reqmin, int konvge, int kcount, double *xmin, double *ynewlo,
