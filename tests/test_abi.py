@@ -61,3 +61,22 @@ def test_band_constants_match_oracle(lib, port, theta):
     out = np.zeros((4, 8))
     assert lib.photic_band_constants(C.byref(cfg), out.ctypes.data_as(C.POINTER(C.c_double))) == 0
     np.testing.assert_array_equal(out, port.band_constants(theta_sun=theta))
+
+
+def test_headers_are_plain_c(tmp_path):
+    """The public headers compile as C99 (-pedantic) and as C++: callers in
+    the reference's own language include them unchanged."""
+    import shutil
+    import subprocess
+    src = tmp_path / "h.c"
+    src.write_text('#include "photic.h"\n#include "photic_nc.h"\n#include "photic_samodel.h"\n'
+                   "int main(void) { photic_nc_grid_info i; (void)i; return PHOTIC_ERR_IO; }\n")
+    inc = os.path.join(ROOT, "include")
+    cc, cxx = shutil.which("gcc") or shutil.which("cc"), shutil.which("g++")
+    if cc is None or cxx is None:
+        pytest.skip("no C / C++ compiler")
+    for cmd in ([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror"],
+                [cxx, "-std=c++11", "-Wall", "-Werror", "-x", "c++"]):
+        r = subprocess.run(cmd + ["-fsyntax-only", "-I", inc, str(src)], capture_output=True,
+                           text=True)
+        assert r.returncode == 0, r.stderr
