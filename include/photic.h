@@ -156,9 +156,12 @@ int photic_invert_batch_ordered(const photic_config *cfg, const float *d_rrs, in
  * the library's kernels), so make it before any stream capture.  All calls
  * share the one array and each clears it before its launch, so calls whose
  * kernels overlap on the GPU (two streams at once) race: serialise them.
- * Kernel-detected errors show in the per-pixel status (PHOTIC_PX_INVALID);
- * photic_sync() does not see them.  Arguments and results are those of
- * photic_invert_batch. */
+ * Kernel-detected errors show only in the per-pixel status
+ * (PHOTIC_PX_INVALID), so out->status must not be NULL (PHOTIC_ERR_INVALID
+ * otherwise); photic_sync() does not see them.  Precisions PHOTIC_PREC_FP64
+ * and PHOTIC_PREC_DF64 only: PHOTIC_PREC_GUARDED (whose request ring needs
+ * its own scratch) and PHOTIC_PREC_FP32 return PHOTIC_ERR_UNSUPPORTED.
+ * Otherwise arguments and results are those of photic_invert_batch. */
 int photic_invert_batch_noalloc(const photic_config *cfg, const float *d_rrs, int64_t npix,
                                 int64_t pixel_stride, int64_t band_stride,
                                 const double *d_seeds, const photic_outputs *out,
@@ -267,7 +270,10 @@ int photic_gemm_bf16(const void *d_A, int32_t lda, const void *d_B, int32_t ldb,
                      int32_t ldc, int32_t M, int32_t N, int32_t K, void *stream);
 /* The same with explicit core-matrix strides of the shared-memory operand
  * layout (lbo: between core matrices along K, sbo: along M/N; bytes);
- * photic_gemm_bf16 uses 128 / 1024.  For layout diagnostics. */
+ * photic_gemm_bf16 uses 128 / 1024.  For layout diagnostics.  Both must be
+ * positive multiples of 16 with 768 + 15 * sbo + lbo + 128 <= 16384, so
+ * that every core matrix the tensor core reads lies in the staged 128 x 64
+ * tile; anything else returns PHOTIC_ERR_INVALID before any launch. */
 int photic_gemm_bf16_strides(const void *d_A, int32_t lda, const void *d_B, int32_t ldb,
                              float *d_C, int32_t ldc, int32_t M, int32_t N, int32_t K,
                              int32_t lbo, int32_t sbo, void *stream);

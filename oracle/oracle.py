@@ -40,10 +40,18 @@ _ip = C.POINTER(C.c_int)
 _i32p = C.POINTER(C.c_int32)
 
 
+# Where the reference checkout is read from when the reference is compiled
+# in place (PHOTIC_REFERENCE overrides; absent on machines without it).
+REFERENCE_ROOT = os.environ.get("PHOTIC_REFERENCE", "/root/reference")
+
+
 def build(ref: bool = True) -> None:
     """Compile the port (and the reference harness when its sources exist)."""
     targets = ["all"] if ref else ["libphotic_oracle.so"]
-    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+    ref_dir = os.path.join(REFERENCE_ROOT, "model")
+    extra = [f"REF_DIR={ref_dir}"] if ref and os.path.isfile(os.path.join(ref_dir, "samodel.c")) \
+        else []
+    subprocess.run(["make", "-s", "-C", HERE] + targets + extra, check=True)
 
 
 def _ptr(a, t):

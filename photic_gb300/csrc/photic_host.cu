@@ -580,6 +580,15 @@ int photic_gemm_bf16_strides(const void *d_A, int32_t lda, const void *d_B, int3
   if ((lda % 8) || (ldb % 8) || lda < K || ldb < K || ldc < N ||
       ((uintptr_t)d_A & 15u) || ((uintptr_t)d_B & 15u))
     return fail(PHOTIC_ERR_INVALID, "GEMM operands need 16-byte aligned rows (ld % 8 == 0)");
+  // The descriptors of one K = 16 step name 16 core matrices along M/N (sbo
+  // apart) and 2 along K (lbo apart), 128 bytes each, starting up to 3 * 256
+  // bytes into a 128 x 64 BF16 tile of 16 KB; every byte they name must lie
+  // inside that tile.
+  if (lbo <= 0 || sbo <= 0 || (lbo % 16) || (sbo % 16) ||
+      (int64_t)3 * 256 + (int64_t)15 * sbo + lbo + 128 > (int64_t)128 * 64 * 2)
+    return fail(PHOTIC_ERR_INVALID,
+                "core-matrix strides lbo %d / sbo %d must be positive multiples of 16 that "
+                "stay inside the 16 KB staged tile", lbo, sbo);
   unsigned int *err = nullptr;
   int sms = 0;
   int rc = device_state(&err, &sms);
@@ -988,8 +997,15 @@ extern "C" int photic_invert_batch_noalloc(const photic_config *cfg, const float
   if (!d_rrs || !out) return fail(PHOTIC_ERR_INVALID, "NULL input or output");
   if (pixel_stride < 1 || band_stride < 1)
     return fail(PHOTIC_ERR_INVALID, "strides must be >= 1");
-  if (cfg->precision == PHOTIC_PREC_FP32)
-    return fail(PHOTIC_ERR_UNSUPPORTED, "precision %d not built in this version", cfg->precision);
+  if (cfg->precision == PHOTIC_PREC_FP32 || cfg->precision == PHOTIC_PREC_GUARDED)
+    return fail(PHOTIC_ERR_UNSUPPORTED,
+                "precision %d is not offered without allocation (fp64 and df64 are)",
+                cfg->precision);
+  // Kernel-detected errors (the evaluation cap) reach the caller only
+  // through the per-pixel status: the error word in the static array is
+  // cleared by the next call and never read back.
+  if (!out->status)
+    return fail(PHOTIC_ERR_INVALID, "the allocation-free inversion needs out->status");
   // queue head (8 bytes) + error word (4 bytes, padded to 8)
   const size_t needed = 2 * sizeof(unsigned long long);
   if (needed > (size_t)PHOTIC_NOALLOC_SCRATCH_BYTES)

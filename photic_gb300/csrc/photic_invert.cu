@@ -394,8 +394,6 @@ size_t invert_smem_bytes(int block, int nb) {
          (size_t)(block / 32) * 32 * (nb <= 4 ? 4 : 8) * sizeof(float);
 }
 
-// PHOTIC_PREC_GUARDED reaching here (the allocation-free entry point) runs
-// the FP64 kernel: same decisions, same results.
 cudaError_t launch_invert(const InvertArgs &a, int precision, int block, int grid,
                           cudaStream_t s) {
   if (precision == PHOTIC_PREC_DF64) return launch_prec<PrecDF>(a, block, grid, s, nullptr);

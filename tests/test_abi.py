@@ -80,3 +80,17 @@ def test_headers_are_plain_c(tmp_path):
         r = subprocess.run(cmd + ["-fsyntax-only", "-I", inc, str(src)], capture_output=True,
                            text=True)
         assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.parametrize("lbo,sbo", [(0, 1024), (128, 0), (120, 1024), (128, 1000),
+                                     (128, 1040), (16384, 16), (-128, 1024)])
+def test_gemm_strides_outside_the_tile_are_refused(lib, lbo, sbo):
+    """Core-matrix strides that would point the tensor core outside the
+    staged shared-memory tile are rejected on the host, before any device
+    work (the pointers below are never dereferenced)."""
+    from photic_gb300 import _lib as L
+    fake = 1 << 20  # 16-byte aligned, never touched
+    rc = lib.photic_gemm_bf16_strides(fake, 64, fake, 64, fake, 128, 128, 128, 64, lbo, sbo,
+                                      None)
+    assert rc == L.ERR_INVALID
+    assert b"stride" in lib.photic_last_error()

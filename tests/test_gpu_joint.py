@@ -45,6 +45,7 @@ def test_joint_fp64_parity(gpu, port, layout, npix):
     print(f"joint {layout}: same {same:.4f} median {np.median(d):.3g} p99 "
           f"{np.quantile(d, 0.99):.3g} within1cm {np.mean(d <= 0.01):.4f}")
     assert np.median(d) <= 0.01
+    assert np.quantile(d, 0.99) <= 0.05
     assert same >= 0.90
     # per-observation P/G/X where the trajectories agree
     agree = np.where(fit & (out["depth_f64"] == ref[:, 0]))[0]

@@ -1,0 +1,180 @@
+"""Distribution parity of every fit the GPU runs, against the FP64 oracle.
+
+The spec bar for each workload is median |dH| <= 1 cm and p99 |dH| <=
+5 cm against the FP64 oracle on the same inputs, with the relative errors of
+P, G, X and the bottom albedo stated beside it.  The oracle is the C
+restatement (oracle/photic_oracle.c), pinned bit for bit to the reference
+(tests/test_oracle_vs_reference.py); the golden fixtures come from the
+reference itself (tests/golden/make_golden.py), made on the x86-64 host.
+
+Depth differences arise only where a last-ulp difference between the
+device's and the host's exp / log / pow decides a Nelder-Mead comparison on
+a near-flat valley of the underdetermined fit (4 bands, 5 unknowns and a
+null q); both fits then lie on the same solution curve.  P, G, X and the
+albedo move along that curve with the depth, so their relative errors are
+reported as median and p99 and only the median is bounded (float rounding
+of the outputs where the trajectories agree).
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+NTHREADS = os.cpu_count() or 1
+# OLCI-like 8-band set inside the 400-800 nm spectral tables
+WL8 = (412.5, 442.5, 490.0, 510.0, 560.0, 620.0, 665.0, 708.75)
+
+
+def _rel(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return np.abs(a - b) / np.maximum(np.abs(b), 1e-30)
+
+
+def check(name, h_gpu, h_ref, fields, n_min=1):
+    """Assert the depth bar, print depth and P/G/X/B statistics."""
+    d = np.abs(np.asarray(h_gpu, np.float64) - np.asarray(h_ref, np.float64))
+    assert d.size >= n_min, (name, d.size)
+    med, p99 = float(np.median(d)), float(np.quantile(d, 0.99))
+    parts = [f"{name}: {d.size} px, same {np.mean(d == 0):.4f}, median |dH| {med:.3g} m, "
+             f"p99 {p99:.3g} m, within 1 cm {np.mean(d <= 0.01):.4f}"]
+    for k, (g, r) in fields.items():
+        e = _rel(g, r)
+        parts.append(f"{k} rel median {np.median(e):.2g} p99 {np.quantile(e, 0.99):.2g}")
+        assert np.median(e) <= 1e-5, (name, k, np.median(e))
+    print("; ".join(parts))
+    assert med <= 0.01, (name, med)
+    assert p99 <= 0.05, (name, p99)
+    return d
+
+
+def test_config0_full_scene(gpu, port):
+    """The CPU-runnable plain method in full: 1024 x 320 pixels, 15 % masked,
+    cold start, reqmin 1e-10, kcount 2000."""
+    npix = 1024 * 320
+    rrs, _ = port.generate_single(20260101, npix)
+    out = gpu.invert(torch.tensor(rrs, device="cuda"), gpu.Config())
+    gpu.sync()
+    out = {k: v.cpu().numpy() for k, v in out.items()}
+    ref = port.invert_batch(rrs, nthreads=NTHREADS)
+    st = out["status"] & 0xFF
+    np.testing.assert_array_equal(st, ref[:, 9].astype(np.int32))
+    fit = st == 0
+    assert 0.80 < fit.mean() < 0.90  # 15 % masked
+    conv = ((out["status"] >> 8) & 1).astype(bool)
+    assert np.mean(conv[fit] == (ref[fit, 8] == 1)) >= 0.97
+    check("config0 1024x320", out["depth_f64"][fit], ref[fit, 0],
+          {"P": (out["P"][fit], ref[fit, 11]), "G": (out["G"][fit], ref[fit, 19]),
+           "X": (out["X"][fit], ref[fit, 27]),
+           "B": (out["bottom_albedo"][fit], ref[fit, 1])}, n_min=200000)
+
+
+def test_eight_band_single_scene(gpu, port):
+    """More than four bands: the 8-band instantiation of the inversion kernel."""
+    rrs, _ = port.generate_single(20260808, 4096, wl=WL8)
+    out = gpu.invert(torch.tensor(rrs, device="cuda"), gpu.Config(wavelengths=WL8))
+    gpu.sync()
+    out = {k: v.cpu().numpy() for k, v in out.items()}
+    ref = port.invert_batch(rrs, wl=WL8, nthreads=NTHREADS)
+    st = out["status"] & 0xFF
+    np.testing.assert_array_equal(st, ref[:, 9].astype(np.int32))
+    fit = st == 0
+    check("8 bands single scene", out["depth_f64"][fit], ref[fit, 0],
+          {"P": (out["P"][fit], ref[fit, 11]), "X": (out["X"][fit], ref[fit, 27]),
+           "B": (out["bottom_albedo"][fit], ref[fit, 1])}, n_min=3000)
+
+
+def _joint(gpu, offs, th, rrs, cfg):
+    t = lambda a: torch.tensor(a, device="cuda")
+    out = gpu.joint_invert(t(offs), t(th), t(rrs), cfg)
+    gpu.sync()
+    return {k: v.cpu().numpy() for k, v in out.items()}
+
+
+def _first_obs_p(out, offs):
+    return out["P"][offs[:-1]]
+
+
+def test_eight_band_joint(gpu, port):
+    """The temporal joint fit with more than four bands per scene."""
+    offs, th, rrs, _ = port.generate_joint(20260909, 240, wl=WL8)
+    out = _joint(gpu, offs, th, rrs, gpu.Config(wavelengths=WL8))
+    ref = port.joint_invert_batch(offs, th, rrs, wl=WL8, nthreads=NTHREADS)
+    st = out["status"] & 0xFF
+    np.testing.assert_array_equal(st, ref[:, 9].astype(np.int32))
+    fit = st == 0
+    check("8 bands joint", out["depth_f64"][fit], ref[fit, 0],
+          {"P(scene 0)": (_first_obs_p(out, offs)[fit], ref[fit, 11])}, n_min=200)
+
+
+@pytest.mark.parametrize("layout,npix", [("reference", 1500), ("scene_b", 800)])
+def test_joint_distribution(gpu, port, layout, npix):
+    """Temporal joint fit, k ~ U{2..8}: the median and p99 bars on a larger
+    sample than the trajectory test of test_gpu_joint.py."""
+    offs, th, rrs, _ = port.generate_joint(20261010, npix)
+    out = _joint(gpu, offs, th, rrs, gpu.Config(layout=layout))
+    ref = port.joint_invert_batch(offs, th, rrs, layout=0 if layout == "reference" else 1,
+                                  nthreads=NTHREADS)
+    st = out["status"] & 0xFF
+    np.testing.assert_array_equal(st, ref[:, 9].astype(np.int32))
+    fit = st == 0
+    check(f"joint {layout}", out["depth_f64"][fit], ref[fit, 0],
+          {"P(scene 0)": (_first_obs_p(out, offs)[fit], ref[fit, 11]),
+           "B": (out["bottom_albedo"][fit], ref[fit, 1])}, n_min=npix // 2)
+
+
+def test_joint_golden(gpu, golden_dir):
+    """The reference's own joint fit (tests/golden/joint.npz) against the
+    CUDA kernels."""
+    g = np.load(os.path.join(golden_dir, "joint.npz"))
+    offs = g["offsets"]
+    out = _joint(gpu, offs, g["theta_sun"], g["rrs"], gpu.Config())
+    ref = g["ref"]  # columns 0..34 of the oracle record: H B cost ... status, P[8] G[8] X[8]
+    st = out["status"] & 0xFF
+    np.testing.assert_array_equal(st, ref[:, 9].astype(np.int32))
+    fit = st == 0
+    check("joint golden (reference)", out["depth_f64"][fit], ref[fit, 0],
+          {"P(scene 0)": (_first_obs_p(out, offs)[fit], ref[fit, 11]),
+           "B": (out["bottom_albedo"][fit], ref[fit, 1])}, n_min=60)
+
+
+def test_region_golden(gpu, golden_dir):
+    """The reference's own 3 x 3 region fit (tests/golden/regions.npz, made
+    through its extract_Rrs_data + samodel_optimise) against the CUDA
+    kernel."""
+    g = np.load(os.path.join(golden_dir, "regions.npz"))
+    cols = list(g["cols"])
+    ref = g["ref"]
+    out = gpu.region_invert(torch.tensor(g["grid"], device="cuda"),
+                            gpu.Config(kcount=int(g["kcount"])))
+    gpu.sync()
+    out = {k: v.cpu().numpy() for k, v in out.items()}
+    st = out["status"]
+    np.testing.assert_array_equal(st & 0xFF, ref[:, cols.index(9)].astype(np.int32))
+    fit = (st & 0xFF) == 0
+    np.testing.assert_array_equal((st[fit] >> 24) & 0xF, ref[fit, cols.index(38)].astype(np.int32))
+    check("region golden (reference)", out["depth_f64"][fit], ref[fit, 0],
+          {"P": (out["P"][fit], ref[fit, cols.index(11)]),
+           "X": (out["X"][fit], ref[fit, cols.index(27)]),
+           "B": (out["bottom_albedo"][fit], ref[fit, cols.index(1)])}, n_min=100)
+
+
+def test_region_distribution(gpu, port):
+    """3 x 3 regions on a 40 x 40 grid with masked pixels: the median and p99
+    bars."""
+    nr = nc = 40
+    rrs, _ = port.generate_single(20261111, nr * nc, pix0=77, mask_frac=0.15)
+    grid = rrs.reshape(nr, nc, 4)
+    out = gpu.region_invert(torch.tensor(grid, device="cuda"), gpu.Config(kcount=1000))
+    gpu.sync()
+    out = {k: v.cpu().numpy() for k, v in out.items()}
+    ref = port.region_invert_batch(grid, kcount=1000, nthreads=NTHREADS)
+    st = out["status"] & 0xFF
+    np.testing.assert_array_equal(st, ref[:, 9].astype(np.int32))
+    fit = st == 0
+    check("regions 40x40", out["depth_f64"][fit], ref[fit, 0],
+          {"P": (out["P"][fit], ref[fit, 11]),
+           "B": (out["bottom_albedo"][fit], ref[fit, 1])}, n_min=1000)

@@ -30,8 +30,9 @@ def test_region_fit_matches_oracle(gpu, port, kcount):
     assert len(np.unique(ref[fit, 38])) > 1  # ragged region counts
     d = np.abs(out["depth_f64"][fit] - ref[fit, 0])
     same = d == 0
-    print(f"regions kcount {kcount}: same {same.mean():.3f} median {np.median(d):.3g}")
-    assert same.mean() >= 0.9 and np.median(d) <= 0.01
+    print(f"regions kcount {kcount}: same {same.mean():.3f} median {np.median(d):.3g} "
+          f"p99 {np.quantile(d, 0.99):.3g}")
+    assert same.mean() >= 0.9 and np.median(d) <= 0.01 and np.quantile(d, 0.99) <= 0.05
     # where the trajectories agree, every product agrees
     # (total evaluations also count the starts that were not kept, whose
     # trajectories may split on a last-ulp difference without changing the

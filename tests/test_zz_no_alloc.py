@@ -48,3 +48,22 @@ def test_noalloc_matches_allocating_entry_point(gpu, precision):
             # same kernel, same inputs: the per-pixel results are identical
             np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
         assert np.any((got["status"] & 0xFF) == 0)
+
+
+def test_noalloc_rejects_what_it_cannot_serve(gpu):
+    """Guarded precision needs scratch of its own, and kernel-detected errors
+    reach the caller only through the status array: both are refused."""
+    from photic_gb300 import _lib as L
+    rrs, _ = gpu.generate_scene(64, seed=4444)
+    torch.cuda.synchronize()
+    out = gpu.alloc_outputs(64, rrs.device, ("depth", "status"))
+    for precision, drop_status in (("guarded", False), ("fp64", True)):
+        o = dict(out)
+        if drop_status:
+            o.pop("status")
+        os_ = gpu.api._outputs_struct(o)
+        c = gpu.Config(precision=precision).to_c()
+        rc = L.lib().photic_invert_batch_noalloc(C.byref(c), rrs.data_ptr(), 64, 4, 1, None,
+                                                 C.byref(os_),
+                                                 torch.cuda.current_stream().cuda_stream)
+        assert rc == (L.ERR_UNSUPPORTED if precision == "guarded" else L.ERR_INVALID)
