@@ -1,24 +1,33 @@
-"""Benchmark: converged pixels/s of the batched plain-method inversion.
+"""Benchmark: converged pixels/s of the surrogate-warm batched inversion
+against the plain cold-start Nelder-Mead, on one GB300.
 
-Workload (one "step"): the whole synthetic 4096 x 4096 single scene of the
-plain method -- 4 OLI-like bands (443/482/561/655 nm), sun 35 deg, nadir,
-truth H~U(0.5,25) m, P~logU(0.005,0.1), G~logU(0.005,0.2),
-X~logU(0.001,0.05), B~U(0.05,0.5) on sand, N(0, 2e-4) noise, 15 % of pixels
-masked -- inverted with the cold-start Nelder-Mead at reqmin 1e-10,
-kcount 2000 on one GPU.  The scene is generated on the device with the
-seeded generator (synthetic data: the reference ships no dataset).
+Workload of the headline (one "step"): one tile of the synthetic 8192 x 8192
+single scene of the plain method -- 4 OLI-like bands (443/482/561/655 nm),
+sun 35 deg, nadir, truth H~U(0.5,25) m, P~logU(0.005,0.1),
+G~logU(0.005,0.2), X~logU(0.001,0.05), B~U(0.05,0.5) on sand, N(0, 2e-4)
+noise, 15 % of pixels masked.  The scene (67 108 864 pixels) is processed
+as 4 tiles of 2048 x 8192 pixels; a step seeds one tile from the learned
+warm start (network prediction + Levenberg-Marquardt polish, cold
+multi-start where the seed's spectral residual exceeds 3 sigma of the
+noise) and fits it with the batched Nelder-Mead at reqmin 1e-10, kcount
+2000, FP64.  Steps cycle through the tiles.  The network is trained first
+(untimed) on photic's own forward-model samples and converged inversions.
+The scene is generated on the device by the seeded generator (synthetic
+data: the reference ships no dataset).
 
 metric: converged pixels per second whose depth is within 1 cm of the FP64
-oracle.  The full-scene FP64 reference is the FP64 kernel (its parity with
-the CPU oracle is what tests/test_gpu_invert.py asserts); a random sample
-of pixels is also re-fitted by the CPU oracle in the same run and the
-within-1-cm fraction of that sample is reported and applied.
+oracle started from the same seeds (a random sample of the timed pixels is
+re-fitted by the CPU oracle in the same run; its within-1-cm fraction is
+applied).  Beside it: the plain cold-start method over the same full scene
+(plain_value, warm_over_plain), what the network adds over the same polish
+started from the reference's cold-start guess, the 4096 x 4096 plain scene,
+the temporal joint fit, 3 x 3 regions, netCDF band files and the serving
+loop.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl photic|reference]
-                  [--npix P] [--precision fp64|df64|fp32]
 
-Under torchrun each rank inverts its own scene shard of the same size
-(pixels are independent: weak scaling, no collective on the data path).
+Under torchrun each rank fits its own 8192 x 8192 scene shard (pixels are
+independent: weak scaling, no collective on the data path).
 """
 from __future__ import annotations
 
@@ -36,8 +45,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 SEED = 20260101
-METRIC = "converged pixels/s at |dH|<=1cm vs FP64 (plain cold-start Nelder-Mead, 1 GB300)"
+SCENE_SEED = SEED + 2  # the 8192 x 8192 scene
+METRIC = ("converged pixels/s at |dH|<=1cm vs FP64 (surrogate-warm Nelder-Mead, "
+          "8192x8192 scene, 1 GB300)")
 UNIT = "px/s"
+WORKLOAD = ("learned warm start, 8192x8192 single scene (4 tiles of 2048x8192 px), 4 bands, "
+            "reqmin 1e-10, kcount 2000, FP64; network + 25 Levenberg-Marquardt steps, cold "
+            "fallback above 3 sigma")
 
 
 def _dist():
@@ -95,11 +109,35 @@ class Clocks:
                 "samples": len(self.rows)}
 
 
-def cpu_oracle_rate(npix: int, seed: int):
+def _rel(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return np.abs(a - b) / np.maximum(np.abs(b), 1e-30)
+
+
+def oracle_stats(h_gpu, ref, mask, gpu_pgxb=None):
+    """|dH| against the oracle record `ref` (oracle/oracle.py columns) over
+    `mask`, with the relative P/G/X/bottom-albedo errors when given."""
+    d = np.abs(np.asarray(h_gpu)[mask] - ref[mask, 0])
+    if d.size == 0:
+        return {"pixels": 0, "frac_within_1cm": 1.0}
+    s = {"pixels": int(d.size), "median_abs_dH_m": float(np.median(d)),
+         "p99_abs_dH_m": float(np.quantile(d, 0.99)), "frac_within_1cm": float(np.mean(d <= 0.01)),
+         "identical_depth": float(np.mean(d == 0))}
+    if gpu_pgxb is not None:
+        for k, col in (("P", 11), ("G", 19), ("X", 27), ("B", 1)):
+            if k in gpu_pgxb:
+                e = _rel(np.asarray(gpu_pgxb[k])[mask], ref[mask, col])
+                s[f"rel_err_{k}"] = {"median": float(np.median(e)),
+                                     "p99": float(np.quantile(e, 0.99))}
+    return s
+
+
+def cpu_oracle_rate(npix: int, seed: int, pix0: int):
     """The CPU oracle (C restatement of the reference path, OpenMP over
-    pixels) on a bounded sample of the same workload."""
+    pixels) on a bounded sample of the same workload, cold start."""
     from oracle import oracle as O
-    rrs, _ = O.generate_single(seed, npix, pix0=7_000_000)
+    rrs, _ = O.generate_single(seed, npix, pix0=pix0)
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
     out = O.invert_batch(rrs, nthreads=threads)
@@ -110,14 +148,16 @@ def cpu_oracle_rate(npix: int, seed: int):
 
 def run_reference(args, ws, rank):
     """--impl reference: the reference path on the host cores (the oracle
-    port of it; the reference's own build needs sources absent here)."""
+    port of it, pinned bit for bit to the reference; the reference's own
+    build needs sources absent on the GPU host), cold start -- the method
+    the reference runs -- on pixels of the same 8192 x 8192 scene."""
     if rank != 0:
         return
     from oracle import oracle as O
     kind = "reference" if O.reference_available() else "port"
     threads = os.cpu_count() or 1
     n = args.ref_sample
-    rrs, _ = O.generate_single(SEED, n, pix0=7_000_000)
+    rrs, _ = O.generate_single(SCENE_SEED, n, pix0=8192 * 4096)
     which = "reference" if kind == "reference" else "port"
     for _ in range(args.warmup):
         O.invert_batch(rrs[: max(1, n // 16)], which=which, nthreads=threads)
@@ -133,8 +173,9 @@ def run_reference(args, ws, rank):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded generator, plain-method prior)",
-            "config": {"workload": "plain method, 4096x4096 single scene, 4 bands, "
-                                   "reqmin 1e-10 kcount 2000 (bounded sample per step)",
+            "config": {"workload": "the reference's cold-start method on the 8192x8192 "
+                                   "single scene, 4 bands, reqmin 1e-10 kcount 2000 (bounded "
+                                   "sample per step)",
                        "sample_pixels": n, "host_threads": threads},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
                              "sample": f"{n} pixels of the same generator per step"},
@@ -143,21 +184,34 @@ def run_reference(args, ws, rank):
     print(json.dumps(line))
 
 
+def train_network(args, dev):
+    """The learned warm start's network, trained on the device by photic's
+    own kernels on forward-model samples and converged inversions."""
+    from photic_gb300 import surrogate as S
+    t0 = time.perf_counter()
+    net = S.Surrogate(seed=1)
+    x, t = S.training_data(args.train_forward, args.train_inverted, seed=31, device=dev)
+    t_data = time.perf_counter() - t0
+    hist = S.train(net, x, t, epochs=args.train_epochs, batch=8192, lr=2e-3)
+    return net, {"samples": hist["samples"], "epochs": args.train_epochs,
+                 "seconds": hist["seconds"], "data_seconds": t_data,
+                 "final_loss": hist["loss"][-1]}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="photic", choices=["photic", "reference"])
-    ap.add_argument("--npix", type=int, default=4096 * 4096)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "df64", "fp32", "guarded"])
-    ap.add_argument("--warmup-npix", type=int, default=1 << 20)
+    ap.add_argument("--side", type=int, default=8192, help="side of the headline scene")
+    ap.add_argument("--tiles", type=int, default=4, help="tiles (steps) per scene pass")
     ap.add_argument("--sample", type=int, default=2048, help="pixels re-fitted by the CPU oracle")
-    ap.add_argument("--cpu-sample", type=int, default=1 << 16)
+    ap.add_argument("--cpu-sample", type=int, default=1 << 20)
     ap.add_argument("--ref-sample", type=int, default=1 << 16)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--warm-npix", type=int, default=1 << 22,
-                    help="pixels of the 8192x8192 scene for the warm-start comparison (0: skip)")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain pass over the scene")
+    ap.add_argument("--gain", type=int, default=1, help="network-gain leg on one tile (0: skip)")
     ap.add_argument("--train-forward", type=int, default=1 << 23)
     ap.add_argument("--train-inverted", type=int, default=1 << 20)
     ap.add_argument("--train-epochs", type=int, default=4)
@@ -165,6 +219,8 @@ def main():
                     help="Levenberg-Marquardt steps on each surrogate seed (0: raw prediction)")
     ap.add_argument("--seed-step-scale", type=float, default=0.1,
                     help="initial simplex of a seeded fit, relative to the cold-start steps")
+    ap.add_argument("--plain-side", type=int, default=4096,
+                    help="side of the plain-method scene leg (0: skip)")
     ap.add_argument("--joint-npix", type=int, default=1 << 18,
                     help="pixels of the 4096x4096 temporal grid for the joint-fit leg (0: skip)")
     ap.add_argument("--region-side", type=int, default=96,
@@ -186,24 +242,54 @@ def main():
     import torch
     import photic_gb300 as pg
     from photic_gb300 import _lib as L
-
     from photic_gb300 import replicas
+    from photic_gb300 import surrogate as S
+
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     pg_ = replicas.init("nccl", dev)
     stream = torch.cuda.current_stream()
-    cfg = pg.Config(precision=args.precision)
-    npix = args.npix
+    cfg = pg.Config()
+    wcfg = pg.Config(seed_step_scale=args.seed_step_scale)
+    npix = args.side * args.side
+    tiles = args.tiles
+    if npix % tiles:
+        ap.error("--tiles must divide the scene")
+    tile = npix // tiles
     pix0 = replicas.shard_start(rank, npix)
-    rrs, truth = pg.generate_scene(npix, seed=SEED, config=cfg, pix0=pix0, device=dev)
-    out = pg.alloc_outputs(npix, dev, ("depth", "depth_f64", "P", "G", "X", "bottom_albedo",
-                                       "model_error", "evals", "status"))
+    scene, truth = pg.generate_scene(npix, seed=SCENE_SEED, config=cfg, pix0=pix0, device=dev)
+    truth_h = truth[:, 0].cpu().numpy()
+    del truth
+    fields = ("depth_f64", "status", "evals")
+    out = pg.alloc_outputs(npix, dev, fields)
+    seeds_all = torch.empty(npix, 6, dtype=torch.float64, device=dev)
 
-    counter = torch.zeros(1, dtype=torch.int64, device=dev)
-    L.check(L.lib().photic_set_counter(counter.data_ptr()))
-    # warm-up on a slice of the scene (W launches)
-    for _ in range(args.warmup):
-        pg.invert(rrs[: min(npix, args.warmup_npix)], cfg)
+    net, train = train_network(args, dev)
+
+    def tile_of(k):
+        k %= tiles
+        return k, slice(k * tile, (k + 1) * tile)
+
+    inv_ms = []
+
+    def step(i, time_inv=False):
+        k, sl = tile_of(i)
+        t = scene[sl]
+        seeds, _ = net.seeds(t, cfg, polish_iters=args.polish_iters)
+        order = pg.fallbacks_first(seeds)
+        o = {f: out[f][sl] for f in fields}
+        if time_inv:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        pg.invert(t, wcfg, seeds=seeds, order=order, out=o)
+        if time_inv:
+            e1.record(stream)
+            inv_ms.append((e0, e1))
+        seeds_all[sl].copy_(seeds)
+
+    for i in range(args.warmup):
+        step(i)
     pg.sync()
 
     def barrier():
@@ -217,15 +303,15 @@ def main():
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
-    for _ in range(args.steps):
-        pg.invert(rrs, cfg, out=out)
+    for i in range(args.steps):
+        step(args.warmup + i, time_inv=True)
     ev1.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
     barrier()
     pg.sync()
     ms_step = ev0.elapsed_time(ev1) / args.steps
-    L.check(L.lib().photic_set_counter(None))
+    ms_inv = sum(a.elapsed_time(b) for a, b in inv_ms) / args.steps
     ms_step = replicas.max_over_ranks(ms_step, pg_, dev)
 
     status = out["status"].cpu().numpy()
@@ -233,217 +319,290 @@ def main():
     conv = fitted & ((status >> 8) & 1).astype(bool)
     evals = out["evals"].cpu().numpy().astype(np.int64)
     h = out["depth_f64"].cpu().numpy()
+    seeds_np = seeds_all.cpu().numpy()
+    timed_tiles = [tile_of(args.warmup + i)[0] for i in range(args.steps)]
+    conv_per_tile = [int(conv[k * tile:(k + 1) * tile].sum()) for k in range(tiles)]
+    evals_per_tile = [float(evals[k * tile:(k + 1) * tile].sum()) for k in range(tiles)]
+    timed_pix = sorted(set(timed_tiles))
 
-    # FP64 reference of the full scene: the FP64 kernel itself, or a run of it.
-    if args.precision == "fp64":
-        h64 = h
-    else:
-        ref = pg.invert(rrs, pg.Config(precision="fp64"),
-                        fields=("depth_f64", "status"))
-        pg.sync()
-        h64 = ref["depth_f64"].cpu().numpy()
-    within = conv & (np.abs(h - h64) <= 0.01)
-
-    # CPU-oracle sample: same pixels, FP64 C restatement of the reference.
-    sample_frac, sample_stats = 1.0, None
+    # CPU oracle started from the same seeds on a sample of the timed pixels
+    sample_frac, warm_stats = 1.0, None
+    from oracle import oracle as O
+    nthreads = os.cpu_count() or 1
+    rng = np.random.default_rng(1)
+    pool = np.concatenate([np.arange(k * tile, (k + 1) * tile) for k in timed_pix])
     if rank == 0 and args.sample > 0:
-        from oracle import oracle as O
-        rng = np.random.default_rng(1)
-        idx = np.sort(rng.choice(npix, size=min(args.sample, npix), replace=False))
-        r_np = rrs[torch.tensor(idx, device=dev)].cpu().numpy()
-        o = O.invert_batch(r_np, nthreads=os.cpu_count() or 1)
+        idx = np.sort(rng.choice(pool, size=min(args.sample, pool.size), replace=False))
+        r_np = scene[torch.tensor(idx, device=dev)].cpu().numpy()
+        o = O.invert_batch(r_np, seeds=seeds_np[idx], seed_step_scale=args.seed_step_scale,
+                           nthreads=nthreads)
         m = (o[:, 9] == 0) & conv[idx]
-        d = np.abs(h[idx][m] - o[m, 0])
-        sample_frac = float(np.mean(d <= 0.01)) if m.any() else 1.0
-        sample_stats = {"pixels": int(m.sum()), "median_abs_dH_m": float(np.median(d)),
-                        "p99_abs_dH_m": float(np.quantile(d, 0.99)),
-                        "frac_within_1cm": sample_frac}
-    good = float(np.sum(within)) * sample_frac
+        warm_stats = oracle_stats(h[idx], o, m)
+        warm_stats["seeded_share"] = float(np.mean(~np.isnan(seeds_np[idx, 0])))
+        sample_frac = warm_stats["frac_within_1cm"]
+    good = float(sum(conv_per_tile[k] for k in timed_tiles)) * sample_frac
     good = replicas.sum_over_ranks(good, pg_, dev)
-    value = good / (ms_step * 1e-3)
+    value = good / (ms_step * 1e-3 * args.steps)
 
-    # Roofline of the inversion kernel: FP64 pipe.
-    p64 = np.zeros(1)
-    p32 = np.zeros(1)
-    pmu = np.zeros(1)
+    # Roofline of the dominant kernel (the inversion, FP64 pipe)
     import ctypes as C
+    p64, p32, pmu = np.zeros(1), np.zeros(1), np.zeros(1)
     L.check(L.lib().photic_measure_peaks(p64.ctypes.data_as(C.POINTER(C.c_double)),
                                          p32.ctypes.data_as(C.POINTER(C.c_double)),
                                          pmu.ctypes.data_as(C.POINTER(C.c_double))))
-    total_evals = float(evals.sum())
-    flops_per_eval = FLOPS_PER_EVAL_F64
-    achieved = total_evals * flops_per_eval / (ms_step * 1e-3) / 1e12
+    ev_step = sum(evals_per_tile[k] for k in timed_tiles) / args.steps
+    achieved = ev_step * FLOPS_PER_EVAL_F64 / (ms_inv * 1e-3) / 1e12
     roof = {"bound": "fp64-pipe", "achieved": achieved, "peak": float(p64[0]),
             "unit": "TFLOP/s", "frac": achieved / float(p64[0]),
-            "traffic": TRAFFIC_BYTES_PER_PIXEL * npix,
-            "traffic_note": "DRAM bytes per launch, scaled by pixels from an ncu capture of "
-                            "a 65536-pixel launch of this kernel taken before its simplex "
-                            "vectors moved from local memory to registers (most of those "
-                            "bytes were the local-memory stack frame); not yet recaptured",
-            "peak_source": "measured by photic_measure_peaks (DFMA chains) in this run",
-            "evals_per_s": total_evals / (ms_step * 1e-3),
-            "flops_per_eval": flops_per_eval}
+            "traffic": TRAFFIC_BYTES_PER_PIXEL * tile,
+            "traffic_note": TRAFFIC_NOTE,
+            "kernel": "invert_kernel<PrecF64, 4, 256>",
+            "kernel_ms_per_launch": ms_inv, "kernel_share_of_step": ms_inv / ms_step,
+            "peak_source": "FP64 FMA rate measured by photic_measure_peaks in this run "
+                           "(MEASURED_PEAKS.json holds only the HBM copy and bf16 GEMM peaks)",
+            "evals_per_s": ev_step / (ms_inv * 1e-3), "flops_per_eval": FLOPS_PER_EVAL_F64,
+            "fp64_instructions_per_eval": FP64_INST_PER_EVAL}
 
-    # End to end through the public API with host buffers.
+    # Plain cold-start method over the same full scene
+    plain = None
+    plain_h = None
+    if not args.no_plain:
+        pout = pg.alloc_outputs(npix, dev, fields)
+        pg.invert(scene[:65536], cfg, fields=fields)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(tiles):
+            sl = slice(k * tile, (k + 1) * tile)
+            pg.invert(scene[sl], cfg, out={f: pout[f][sl] for f in fields})
+        e1.record(stream)
+        torch.cuda.synchronize()
+        pg.sync()
+        t_plain = e0.elapsed_time(e1) * 1e-3
+        pst = pout["status"].cpu().numpy()
+        pconv = ((pst & 0xFF) == 0) & ((pst >> 8) & 1).astype(bool)
+        plain_h = pout["depth_f64"].cpu().numpy()
+        pev = pout["evals"].cpu().numpy()
+        cold_stats, cold_frac = None, 1.0
+        if rank == 0 and args.sample > 0:
+            idx = np.sort(rng.choice(npix, size=min(args.sample, npix), replace=False))
+            o = O.invert_batch(scene[torch.tensor(idx, device=dev)].cpu().numpy(),
+                               nthreads=nthreads)
+            m = (o[:, 9] == 0) & pconv[idx]
+            cold_stats = oracle_stats(plain_h[idx], o, m)
+            cold_frac = cold_stats["frac_within_1cm"]
+        pgood = replicas.sum_over_ranks(float(pconv.sum()) * cold_frac, pg_, dev)
+        t_plain_max = replicas.max_over_ranks(t_plain, pg_, dev)
+        both = conv & pconv
+        dwc = np.abs(h[both] - plain_h[both])
+        vs_truth = {"pixels": int(both.sum()),
+                    "warm_median_abs_m": float(np.median(np.abs(h[both] - truth_h[both]))),
+                    "cold_median_abs_m": float(np.median(np.abs(plain_h[both] - truth_h[both]))),
+                    "warm_p90_abs_m": float(np.quantile(np.abs(h[both] - truth_h[both]), 0.9)),
+                    "cold_p90_abs_m": float(np.quantile(np.abs(plain_h[both] - truth_h[both]),
+                                                        0.9))}
+        plain = {"value": pgood / t_plain_max, "unit": UNIT, "seconds": t_plain,
+                 "pixels": npix, "converged_share": float(pconv.mean()),
+                 "evals_per_pixel": float(pev[pconv].mean()),
+                 "oracle_sample": cold_stats,
+                 "warm_vs_cold_depth": {
+                     "pixels": int(both.sum()),
+                     "median_abs_m": float(np.median(dwc)),
+                     "p90_abs_m": float(np.quantile(dwc, 0.9)),
+                     "frac_within_1cm": float(np.mean(dwc <= 0.01)),
+                     "note": "warm and cold fits land on different points of the "
+                             "underdetermined solution set; each is checked against the "
+                             "oracle started from its own start"},
+                 "depth_vs_generator_truth": vs_truth}
+        del pout
+        torch.cuda.empty_cache()
+
+    warm_evals = float(evals[conv].mean()) if conv.any() else 0.0
+    gain = None
+    if rank == 0 and args.gain:
+        gain = gain_leg(args, dev, net, scene[:tile], conv[:tile], evals[:tile], ms_step)
+
+    # End to end through the public API with host buffers, one full scene pass
     e2e = None
     if rank == 0:
-        host_in = rrs.cpu().pin_memory()
-        host_depth = torch.empty(npix, dtype=torch.float32).pin_memory()
-        host_status = torch.empty(npix, dtype=torch.int32).pin_memory()
-        dev_in = torch.empty_like(rrs)
-        o2 = pg.alloc_outputs(npix, dev, ("depth", "status"))
-        t0 = torch.cuda.Event(enable_timing=True)
-        t1 = torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        t0.record(stream)
-        dev_in.copy_(host_in, non_blocking=True)
-        pg.invert(dev_in, cfg, out=o2)
-        host_depth.copy_(o2["depth"], non_blocking=True)
-        host_status.copy_(o2["status"], non_blocking=True)
-        t1.record(stream)
-        torch.cuda.synchronize()
-        e2e_ms = t0.elapsed_time(t1)
-        st2 = host_status.numpy()
-        conv2 = ((st2 & 0xFF) == 0) & ((st2 >> 8) & 1).astype(bool)
-        within2 = conv2 & (np.abs(host_depth.numpy().astype(np.float64) - h64) <= 0.01)
-        e2e = {"value": float(np.sum(within2)) * sample_frac / (e2e_ms * 1e-3), "unit": UNIT,
-               "h2d_bytes_per_step": int(host_in.numel() * 4),
-               "d2h_bytes_per_step": int(npix * 8), "ms_per_step": e2e_ms}
+        e2e = e2e_leg(args, dev, net, scene, tile, tiles, sample_frac)
 
     cpu = None
     if rank == 0 and not args.no_cpu and args.cpu_sample > 0:
-        rate, threads, dt, n, _ = cpu_oracle_rate(args.cpu_sample, SEED)
+        rate, threads, dt, n, _ = cpu_oracle_rate(args.cpu_sample, SCENE_SEED, 8192 * 4096)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{n} pixels of the same generator, {dt:.1f} s on {threads} threads"}
+               "sample": f"{n} pixels of the 8192x8192 scene, cold start (the reference's "
+                         f"method), {dt:.1f} s on {threads} threads"}
 
+    plain4096 = None
+    if rank == 0 and args.plain_side > 0:
+        plain4096 = plain_scene_leg(args, dev)
     temporal = None
     if rank == 0 and args.joint_npix > 0:
         temporal = temporal_leg(args, dev)
     regions = None
     if rank == 0 and args.region_side > 0:
         regions = region_leg(args, dev)
-    warm, net, serving = None, None, None
-    if rank == 0 and args.warm_npix > 0:
-        net, warm = warm_start_leg(args, dev)
+    serving = None
     if rank == 0 and args.serve_requests > 0:
         serving = serving_leg(args, net)
     ncgrid = None
     if rank == 0 and args.nc_side > 0:
         try:
-            ncgrid = ncgrid_leg(args, dev, rrs)
+            ncgrid = ncgrid_leg(args, dev, scene)
         except Exception as e:  # the format leg must not cost the headline line
             ncgrid = {"error": f"{type(e).__name__}: {e}"}
 
     if rank == 0:
+        # kernels of this library per step: the surrogate's feature kernel,
+        # per 2^20-row chunk its standardisation + 4 GEMMs + de-normalisation,
+        # the seed polish and the inversion
+        launches = args.steps * (1 + 6 * ((tile + (1 << 20) - 1) >> 20) + 1 + 1)
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": {"fp64": "f64", "df64": "df64 (2 x f32)", "fp32": "f32",
-                          "guarded": "f64 decisions (df64 screening)"}[args.precision],
+                "dtype": "f64",
                 "data": "synthetic (seeded on-device generator, plain-method prior)",
-                "config": {"workload": "plain method, 4096x4096 single scene, 4 bands, "
-                                       "cold start, reqmin 1e-10, kcount 2000",
-                           "pixels_per_gpu": npix, "precision": args.precision,
-                           "l2": "inputs 268 MB > L2; compute-bound kernel"},
-                "gpu_launches": args.steps,
-                "exact_evals_per_step": int(counter.item()) // max(1, args.steps + args.warmup),
-                "pixels": {"fitted": int(fitted.sum()), "converged": int(conv.sum()),
-                           "within_1cm_of_fp64": int(within.sum()),
-                           "mean_evals": float(evals[fitted].mean()) if fitted.any() else 0.0},
-                "oracle_sample": sample_stats, "roofline": roof, "cpu_baseline": cpu,
-                "warm_start": warm, "serving": serving, "temporal": temporal,
-                "regions": regions, "ncgrid": ncgrid,
-                "e2e": e2e, "clocks": clk}
+                "config": {"workload": WORKLOAD, "pixels_per_gpu": npix,
+                           "pixels_per_step": tile, "precision": "fp64",
+                           "l2": "inputs 268 MB per step > L2; compute-bound kernel"},
+                "plain_value": plain["value"] if plain else None,
+                "warm_over_plain": value / plain["value"] if plain else None,
+                "gpu_launches": launches,
+                "pixels": {"fitted_share": float(fitted.mean()),
+                           "converged_share": float(conv.mean()),
+                           "seeded_share": float(np.mean(~np.isnan(seeds_np[fitted, 0]))),
+                           "evals_per_pixel_warm": warm_evals},
+                "oracle_sample": warm_stats, "roofline": roof, "cpu_baseline": cpu,
+                "plain": plain, "network_gain": gain, "train": train,
+                "seed_polish_ms_per_step": ms_step - ms_inv,
+                "plain_4096x4096": plain4096, "serving": serving, "temporal": temporal,
+                "regions": regions, "ncgrid": ncgrid, "e2e": e2e, "clocks": clk}
         print(json.dumps(line))
     if pg_ is not None:
         pg_.destroy_process_group()
 
 
-def warm_start_leg(args, dev):
-    """Surrogate-warm vs plain cold-start Nelder-Mead on a sample of the
-    8192 x 8192 scene: train the network on photic's own forward-model
-    samples and converged inversions, seed the fit (cold fallback where the
-    seed's spectral residual exceeds 3 sigma of the noise), and compare
-    converged pixels/s; parity of the seeded fits is checked against the
-    CPU oracle started from the same seeds."""
+def gain_leg(args, dev, net, rrs, conv_net, evals_net, ms_net):
+    """What the trained network earns on one tile: seeds from the raw
+    network prediction, and the same Levenberg-Marquardt polish and residual
+    test started without the network from the reference's cold-start guess
+    (model/samodel.c:2266-2273, 2342-2351, depth 10 m, also 4 m and 25 m);
+    each against the network + polish of the timed steps."""
     import torch
     import photic_gb300 as pg
     from photic_gb300 import surrogate as S
-    from oracle import oracle as O
-
-    t0 = time.perf_counter()
-    net = S.Surrogate(seed=1)
-    x, t = S.training_data(args.train_forward, args.train_inverted, seed=31, device=dev)
-    t_data = time.perf_counter() - t0
-    hist = S.train(net, x, t, epochs=args.train_epochs, batch=8192, lr=2e-3)
-    del x, t
-    n = args.warm_npix
-    # pixels of the 8192^2 scene (seeded generator; row-major pixel ids)
-    rrs, _ = pg.generate_scene(n, seed=SEED + 2, pix0=8192 * 4096, device=dev)
     cfg = pg.Config()
+    wcfg = pg.Config(seed_step_scale=args.seed_step_scale)
     fields = ("depth_f64", "status", "evals")
 
-    def timed(fn):
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
+    def run(make_seeds):
         torch.cuda.synchronize()
-        ev0.record()
-        r = fn()
-        ev1.record()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        seeds, _ = make_seeds()
+        o = pg.invert(rrs, wcfg, seeds=seeds, order=pg.fallbacks_first(seeds), fields=fields)
+        e1.record()
         torch.cuda.synchronize()
-        return r, ev0.elapsed_time(ev1) * 1e-3
+        t = e0.elapsed_time(e1) * 1e-3
+        st = o["status"].cpu().numpy()
+        c = ((st & 0xFF) == 0) & ((st >> 8) & 1).astype(bool)
+        fit = (st & 0xFF) == 0
+        sd = seeds.cpu().numpy()
+        return {"px_s": float(c.sum()) / t, "seconds": t,
+                "seeded_share": float(np.mean(~np.isnan(sd[fit, 0]))),
+                "evals_per_pixel": float(o["evals"].cpu().numpy()[c].mean())}
 
+    raw = run(lambda: net.seeds(rrs, cfg, polish_iters=0))
+    heur = run(lambda: S.heuristic_seeds(rrs, cfg, polish_iters=args.polish_iters, h_guess=10.0))
+    net_polish = {"px_s": float(conv_net.sum()) / (ms_net * 1e-3),
+                  "evals_per_pixel": float(evals_net[conv_net].mean())}
+    return {"tile_pixels": int(rrs.shape[0]),
+            "network_polished": net_polish, "network_raw": raw,
+            "heuristic_polished": heur,
+            "network_over_heuristic_px_s": net_polish["px_s"] / heur["px_s"],
+            "note": "px/s here without the oracle-sample factor; the same polish, residual "
+                    "test and simplex scale in both polished rows"}
+
+
+def e2e_leg(args, dev, net, scene, tile, tiles, sample_frac):
+    """The headline through the public API with host buffers: per tile the
+    pinned host spectra go to the device, are seeded and fitted, and depth
+    and status come back; one full pass over the scene."""
+    import torch
+    import photic_gb300 as pg
+    cfg = pg.Config()
     wcfg = pg.Config(seed_step_scale=args.seed_step_scale)
-    # warm the kernels (and the lazily loaded library code of each step)
-    pg.invert(rrs[:4096], cfg, fields=fields)
-    s_w, _ = net.seeds(rrs[:4096], cfg, polish_iters=args.polish_iters)
-    pg.invert(rrs[:4096], wcfg, seeds=s_w, order=pg.fallbacks_first(s_w), fields=fields)
+    host_in = scene.cpu().pin_memory()
+    host_depth = torch.empty(scene.shape[0], dtype=torch.float32).pin_memory()
+    host_status = torch.empty(scene.shape[0], dtype=torch.int32).pin_memory()
+    dev_in = torch.empty(tile, scene.shape[1], dtype=torch.float32, device=dev)
+    o = pg.alloc_outputs(tile, dev, ("depth", "status"))
+    stream = torch.cuda.current_stream()
     torch.cuda.synchronize()
-    cold, t_cold = timed(lambda: pg.invert(rrs, cfg, fields=fields))
-    # the raw network prediction as seed, for comparison
-    (seeds0, _), t_seed0 = timed(lambda: net.seeds(rrs, cfg))
-    warm0, t_warm0 = timed(lambda: pg.invert(rrs, wcfg, seeds=seeds0, fields=fields))
-    (seeds, res, order), t_seed = timed(
-        lambda: (*net.seeds(rrs, cfg, polish_iters=args.polish_iters), None))
-    order, t_order = timed(lambda: pg.fallbacks_first(seeds))
-    t_seed += t_order
-    warm, t_warm = timed(lambda: pg.invert(rrs, wcfg, seeds=seeds, order=order, fields=fields))
-    pg.sync()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for k in range(tiles):
+        sl = slice(k * tile, (k + 1) * tile)
+        dev_in.copy_(host_in[sl], non_blocking=True)
+        seeds, _ = net.seeds(dev_in, cfg, polish_iters=args.polish_iters)
+        pg.invert(dev_in, wcfg, seeds=seeds, order=pg.fallbacks_first(seeds), out=o)
+        host_depth[sl].copy_(o["depth"], non_blocking=True)
+        host_status[sl].copy_(o["status"], non_blocking=True)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1)
+    st = host_status.numpy()
+    conv = ((st & 0xFF) == 0) & ((st >> 8) & 1).astype(bool)
+    return {"value": float(conv.sum()) * sample_frac / (ms * 1e-3), "unit": UNIT,
+            "h2d_bytes_per_step": int(tile * scene.shape[1] * 4),
+            "d2h_bytes_per_step": int(tile * 8), "ms_per_step": ms / tiles,
+            "note": "one pass over the scene's tiles; per tile H2D of the spectra, seeding, "
+                    "the ordered inversion and D2H of depth and status"}
 
-    def conv(o):
-        st = o["status"]
-        return (((st & 0xFF) == 0) & ((st >> 8) & 1).bool())
-    cc, cw = conv(cold), conv(warm)
-    seeded = ~torch.isnan(seeds[:, 0]) & ((cold["status"] & 0xFF) == 0)
-    # parity of the warm path: the oracle started from the same seeds
-    idx = torch.arange(0, n, max(1, n // 1024), device=dev)
-    sd_np = seeds[idx].cpu().numpy()
-    ref = O.invert_batch(rrs[idx].cpu().numpy(), seeds=sd_np, seed_step_scale=args.seed_step_scale,
-                         nthreads=os.cpu_count() or 1)
-    m = (ref[:, 9] == 0) & cw[idx].cpu().numpy()
-    d = np.abs(warm["depth_f64"][idx].cpu().numpy()[m] - ref[m, 0])
-    within = float(np.mean(d <= 0.01)) if m.any() else 1.0
-    v_cold = float(cc.sum().item()) / t_cold
-    v_warm = float(cw.sum().item()) * within / (t_warm + t_seed)
-    v_warm0 = float(conv(warm0).sum().item()) / (t_warm0 + t_seed0)
-    seeded0 = ~torch.isnan(seeds0[:, 0]) & ((cold["status"] & 0xFF) == 0)
-    return net, {"workload": f"{n} pixels of the 8192x8192 plain-method scene",
-            "cold_px_s": v_cold, "warm_px_s": v_warm, "speedup": v_warm / v_cold,
-            "seed": f"network prediction + {args.polish_iters} Levenberg-Marquardt steps, "
-                    f"simplex scale {args.seed_step_scale}; cold-start fallbacks queued first",
-            "unpolished": {"warm_px_s": v_warm0, "speedup": v_warm0 / v_cold,
-                           "seeded_share": float(seeded0.float().mean().item())},
-            "seeded_share": float(seeded.float().mean().item()),
-            "evals_per_pixel_cold": float(cold["evals"].float()[cc].mean().item()),
-            "evals_per_pixel_warm": float(warm["evals"].float()[cw].mean().item()),
-            "seed_ms": t_seed * 1e3, "fallback": "seed spectral RMS > 3 x 2e-4",
-            "train": {"samples": hist["samples"], "epochs": args.train_epochs,
-                      "seconds": hist["seconds"], "data_seconds": t_data,
-                      "final_loss": hist["loss"][-1]},
-            "parity_vs_seeded_oracle": {"pixels": int(m.sum()),
-                                        "median_abs_dH_m": float(np.median(d)) if m.any() else 0.0,
-                                        "p99_abs_dH_m": float(np.quantile(d, 0.99)) if m.any() else 0.0,
-                                        "frac_within_1cm": within}}
+
+def plain_scene_leg(args, dev):
+    """The plain cold-start method on the 4096 x 4096 scene (one pass), with
+    its CPU-oracle sample."""
+    import torch
+    import photic_gb300 as pg
+    from oracle import oracle as O
+    n = args.plain_side * args.plain_side
+    rrs, _ = pg.generate_scene(n, seed=SEED, device=dev, with_truth=False)
+    cfg = pg.Config()
+    fields = ("depth_f64", "status", "evals", "P", "G", "X", "bottom_albedo")
+    pg.invert(rrs[:65536], cfg, fields=fields)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    out = pg.invert(rrs, cfg, fields=fields)
+    e1.record()
+    torch.cuda.synchronize()
+    pg.sync()
+    t = e0.elapsed_time(e1) * 1e-3
+    st = out["status"].cpu().numpy()
+    conv = ((st & 0xFF) == 0) & ((st >> 8) & 1).astype(bool)
+    h = out["depth_f64"].cpu().numpy()
+    rng = np.random.default_rng(2)
+    idx = np.sort(rng.choice(n, size=min(args.sample, n), replace=False))
+    o = O.invert_batch(rrs[torch.tensor(idx, device=dev)].cpu().numpy(),
+                       nthreads=os.cpu_count() or 1)
+    m = (o[:, 9] == 0) & conv[idx]
+    pgxb = {k: out[f].cpu().numpy()[idx] for k, f in
+            (("P", "P"), ("G", "G"), ("X", "X"), ("B", "bottom_albedo"))}
+    stats = oracle_stats(h[idx], o, m, pgxb)
+    ev = out["evals"].cpu().numpy()
+    res = {"workload": f"plain method, {args.plain_side}x{args.plain_side} scene, cold start",
+           "converged_px_s_within_1cm": float(conv.sum()) * stats["frac_within_1cm"] / t,
+           "seconds": t, "evals_per_s": float(ev.sum()) / t,
+           "evals_per_pixel": float(ev[conv].mean()), "oracle_sample": stats}
+    del rrs, out
+    torch.cuda.empty_cache()
+    return res
 
 
 def temporal_leg(args, dev):
@@ -461,7 +620,7 @@ def temporal_leg(args, dev):
     n_obs = rrs.shape[0]
     offs_h, th_h, rrs_h = offs.cpu().numpy(), th.cpu().numpy(), rrs.cpu().numpy()
     rng = np.random.default_rng(5)
-    sub = np.sort(rng.choice(n, size=min(n, 192), replace=False))
+    sub = np.sort(rng.choice(n, size=min(n, 1024), replace=False))
     counts = offs_h[1:] - offs_h[:-1]
     so = np.zeros(len(sub) + 1, dtype=np.int32)
     so[1:] = np.cumsum(counts[sub])
@@ -470,7 +629,8 @@ def temporal_leg(args, dev):
            "observations": int(n_obs), "mean_scenes": float(n_obs / n)}
     for layout in ("reference", "scene_b"):
         cfg = pg.Config(layout=layout)
-        g = pg.JointGraph(n, n_obs, cfg, fields=("depth_f64", "status", "evals"))
+        g = pg.JointGraph(n, n_obs, cfg, fields=("depth_f64", "status", "evals", "P", "G", "X",
+                                                 "bottom_albedo"))
         g.run(offs, th, rrs)
         pg.sync()
         ev0 = torch.cuda.Event(enable_timing=True)
@@ -487,9 +647,15 @@ def temporal_leg(args, dev):
         ref = O.joint_invert_batch(so, th_h[obs], rrs_h[obs],
                                    layout=0 if layout == "reference" else 1,
                                    nthreads=os.cpu_count() or 1)
-        m = (ref[:, 9] == 0) & conv[torch.tensor(sub, device=dev)].cpu().numpy()
-        d = np.abs(out["depth_f64"][torch.tensor(sub, device=dev)].cpu().numpy()[m] - ref[m, 0])
-        within = float(np.mean(d <= 0.01)) if m.any() else 1.0
+        tsub = torch.tensor(sub, device=dev)
+        m = (ref[:, 9] == 0) & conv[tsub].cpu().numpy()
+        first = torch.tensor(offs_h[sub], device=dev, dtype=torch.int64)
+        pgxb = {"P": out["P"][first].cpu().numpy(), "G": out["G"][first].cpu().numpy(),
+                "X": out["X"][first].cpu().numpy(),
+                "B": out["bottom_albedo"][tsub].cpu().numpy()}
+        stats = oracle_stats(out["depth_f64"][tsub].cpu().numpy(), ref, m, pgxb)
+        stats["note"] = "P, G, X of each pixel's first scene"
+        within = stats["frac_within_1cm"]
         t0 = time.perf_counter()
         O.joint_invert_batch(so, th_h[obs], rrs_h[obs], layout=0 if layout == "reference" else 1,
                              nthreads=os.cpu_count() or 1)
@@ -500,10 +666,7 @@ def temporal_leg(args, dev):
             "seconds": t, "converged_share": float(conv.float().mean().item()),
             "mean_evals": float(out["evals"].float().mean().item()),
             "graph": "one replay: binning + 8 per-k kernels on parallel branches",
-            "oracle_sample": {"pixels": int(m.sum()),
-                              "median_abs_dH_m": float(np.median(d)) if m.any() else 0.0,
-                              "p99_abs_dH_m": float(np.quantile(d, 0.99)) if m.any() else 0.0,
-                              "frac_within_1cm": within},
+            "oracle_sample": stats,
             "cpu_oracle_px_s": len(sub) / t_cpu, "cpu_threads": os.cpu_count() or 1}
         del g, out
     torch.cuda.empty_cache()
@@ -535,22 +698,24 @@ def region_leg(args, dev):
     conv = ((st & 0xFF) == 0) & ((st >> 8) & 1).bool()
     # parity on a 16 x 16 corner block fitted on its own (its edge pixels
     # see a clamped neighbourhood, as on the GPU for the same block)
-    k = min(16, n)
+    k = min(24, n)
     blk = grid[:k, :k].contiguous()
-    g_blk = pg.region_invert(blk, cfg, fields=("depth_f64", "status"))
+    g_blk = pg.region_invert(blk, cfg, fields=("depth_f64", "status", "P", "G", "X",
+                                               "bottom_albedo"))
     pg.sync()
     t0 = time.perf_counter()
     ref = O.region_invert_batch(blk.cpu().numpy(), nthreads=os.cpu_count() or 1)
     t_cpu = time.perf_counter() - t0
     fit = (g_blk["status"].cpu().numpy() & 0xFF) == 0
-    d = np.abs(g_blk["depth_f64"].cpu().numpy()[fit] - ref[fit, 0])
-    within = float(np.mean(d <= 0.01)) if fit.any() else 1.0
+    pgxb = {k: g_blk[f].cpu().numpy() for k, f in
+            (("P", "P"), ("G", "G"), ("X", "X"), ("B", "bottom_albedo"))}
+    stats = oracle_stats(g_blk["depth_f64"].cpu().numpy(), ref, fit, pgxb)
+    within = stats["frac_within_1cm"]
     return {"workload": f"{n}x{n} grid, 3x3 regions per pixel (n = 3R + 3 <= 30 unknowns)",
             "converged_px_s_within_1cm": float(conv.sum().item()) * within / t, "seconds": t,
             "converged_share": float(conv.float().mean().item()),
             "mean_evals": float(out["evals"].float().mean().item()),
-            "oracle_sample": {"pixels": int(fit.sum()), "frac_within_1cm": within,
-                              "median_abs_dH_m": float(np.median(d)) if fit.any() else 0.0},
+            "oracle_sample": stats,
             "cpu_oracle_px_s": k * k / t_cpu, "cpu_threads": os.cpu_count() or 1}
 
 
@@ -672,11 +837,19 @@ def serving_leg(args, net):
 # 43 per band (photic_fp64.cuh cost_f64) + 9 in the tail.
 FLOPS_PER_EVAL_F64 = 4 * 43 + 9
 
-# dram__bytes_read.sum + dram__bytes_write.sum of the FP64 inversion kernel
-# over a 65 536-pixel launch (26.730240 MB + 19.621888 MB), per pixel: 16 B
-# of spectra and the outputs, the rest the threads' local-memory stack frames
-# leaving L2.  Under 1 GB/s at the kernel's rate.
-TRAFFIC_BYTES_PER_PIXEL = (26.730240e6 + 19.621888e6) / 65536
+# FP64-pipe warp instructions per cost evaluation (cost + Nelder-Mead
+# bookkeeping), from the ncu capture of invert_kernel<PrecF64, 4, 256>
+# summarised in profiles/invert_fp64_262144px.md; None until measured.
+FP64_INST_PER_EVAL = None
+
+# dram__bytes_read.sum + dram__bytes_write.sum of invert_kernel<PrecF64, 4,
+# 256> over a 262 144-pixel launch (4.708608 MB + 0.181248 MB), per pixel:
+# the spectra (16 B) and a few local-memory reloads; at that size the
+# outputs stay in L2, so writes are undercounted.
+TRAFFIC_BYTES_PER_PIXEL = (4.708608e6 + 0.181248e6) / 262144
+TRAFFIC_NOTE = ("DRAM bytes per launch scaled by pixels from an ncu capture of a 262144-pixel "
+                "launch of this kernel (18.7 B/pixel, against 16 B of spectra read and 16 B of "
+                "outputs written; the outputs stayed in L2 at the captured size)")
 
 if __name__ == "__main__":
     main()

@@ -316,6 +316,17 @@ int photic_surrogate_seed_polished(photic_surrogate *s, const photic_config *cfg
                                    int32_t polish_iters, double *d_seeds, float *d_resid,
                                    void *stream);
 
+/* The same Levenberg-Marquardt polish and residual test as
+ * photic_surrogate_seed_polished, started without the network from the
+ * reference's own cold-start guess (B = 4 Rrs(490), P = 0.072
+ * (Rrs(490)/Rrs(550))^-1.7, G = 1.5 P, X = 30 a_w(640) Rrs(640);
+ * model/samodel.c:2266-2273, 2342-2351) at depth h_guess (m; the polish
+ * also tries 0.4 and 2.5 times it).  The baseline that shows what the
+ * trained network adds to the polish; no counterpart in the reference. */
+int photic_seed_polished_heuristic(const photic_config *cfg, const float *d_rrs, int64_t npix,
+                                   double h_guess, double resid_max, int32_t polish_iters,
+                                   double *d_seeds, float *d_resid, void *stream);
+
 /* Instrumentation: if d_counter (device, unsigned long long) is not NULL,
  * later PHOTIC_PREC_GUARDED inversions add the number of exact FP64
  * re-evaluations they served to it.  Pass NULL to stop. */

@@ -150,6 +150,9 @@ _SIGS = {
     "photic_surrogate_seed_polished": (C.c_int, [C.c_void_p, C.POINTER(photic_config),
                                                  C.c_void_p, C.c_int64, C.c_double, C.c_int32,
                                                  C.c_void_p, C.c_void_p, C.c_void_p]),
+    "photic_seed_polished_heuristic": (C.c_int, [C.POINTER(photic_config), C.c_void_p,
+                                                 C.c_int64, C.c_double, C.c_double, C.c_int32,
+                                                 C.c_void_p, C.c_void_p, C.c_void_p]),
     "photic_nc_read_info": (C.c_int, [C.c_char_p, C.POINTER(photic_nc_grid_info)]),
     "photic_nc_read_raw": (C.c_int, [C.c_char_p, C.POINTER(photic_nc_grid_info), C.c_void_p,
                                      C.c_void_p, C.c_void_p]),

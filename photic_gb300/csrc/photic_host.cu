@@ -855,6 +855,60 @@ int photic_surrogate_seed(photic_surrogate *s, const photic_config *cfg, const f
                                         stream);
 }
 
+}  // extern "C"
+
+namespace {
+
+// Polish the guesses y ([npix][5] ln P, ln G, ln X, B, H; NULL: the
+// reference's cold-start guess at depth h_guess) into nelmin seeds.
+cudaError_t launch_seed_polish(const photic_config &cfg, const float *d_rrs, int64_t npix,
+                               const float *y, double h_guess, double resid_max,
+                               int32_t polish_iters, double *d_seeds, float *d_resid,
+                               cudaStream_t st) {
+  SeedArgs a;
+  memset(&a, 0, sizeof a);
+  make_fit(cfg, a.fp);
+  make_scene(cfg, cfg.theta_sun_deg, a.sc);
+  a.rrs = d_rrs;
+  a.y = y;
+  a.h_guess = h_guess;
+  a.npix = npix;
+  a.resid_max = resid_max;
+  a.polish_iters = polish_iters;
+  for (int b = 0; b < 8; b++) {
+    a.sf.refl[b] = (float)a.sc.refl[b];
+    a.sf.aw[b] = (float)a.sc.aw[b];
+    a.sf.a0[b] = (float)a.sc.a0[b];
+    a.sf.a1[b] = (float)a.sc.a1[b];
+    a.sf.eS[b] = (float)a.sc.eS[b];
+    a.sf.bbw[b] = (float)a.sc.bbw[b];
+  }
+  a.sf.sec_sun = (float)a.sc.sec_sun;
+  a.sf.sec_view = (float)a.sc.sec_view;
+  a.seeds = d_seeds;
+  a.resid = d_resid;
+  return mlp_seeds(a, st);
+}
+
+}  // namespace
+
+extern "C" {
+
+int photic_seed_polished_heuristic(const photic_config *cfg, const float *d_rrs, int64_t npix,
+                                   double h_guess, double resid_max, int32_t polish_iters,
+                                   double *d_seeds, float *d_resid, void *stream) {
+  int rc = photic_config_check(cfg);
+  if (rc) return rc;
+  if (npix < 0 || (npix > 0 && (!d_rrs || !d_seeds)) || polish_iters < 0 ||
+      polish_iters > 100 || !(h_guess > 0.0))
+    return fail(PHOTIC_ERR_INVALID, "bad arguments");
+  if (npix == 0) return PHOTIC_OK;
+  cudaError_t e = launch_seed_polish(*cfg, d_rrs, npix, nullptr, h_guess, resid_max,
+                                     polish_iters, d_seeds, d_resid, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "heuristic seeds");
+  return PHOTIC_OK;
+}
+
 int photic_surrogate_seed_polished(photic_surrogate *s, const photic_config *cfg,
                                    const float *d_rrs, int64_t npix, double resid_max,
                                    int32_t polish_iters, double *d_seeds, float *d_resid,
@@ -874,30 +928,9 @@ int photic_surrogate_seed_polished(photic_surrogate *s, const photic_config *cfg
                    (float)cfg->theta_view_deg, x, st);
   if (e == cudaSuccess) {
     rc = photic_surrogate_infer(s, x, npix, y, stream);
-    if (rc == PHOTIC_OK) {
-      SeedArgs a;
-      memset(&a, 0, sizeof a);
-      make_fit(*cfg, a.fp);
-      make_scene(*cfg, cfg->theta_sun_deg, a.sc);
-      a.rrs = d_rrs;
-      a.y = y;
-      a.npix = npix;
-      a.resid_max = resid_max;
-      a.polish_iters = polish_iters;
-      for (int b = 0; b < 8; b++) {
-        a.sf.refl[b] = (float)a.sc.refl[b];
-        a.sf.aw[b] = (float)a.sc.aw[b];
-        a.sf.a0[b] = (float)a.sc.a0[b];
-        a.sf.a1[b] = (float)a.sc.a1[b];
-        a.sf.eS[b] = (float)a.sc.eS[b];
-        a.sf.bbw[b] = (float)a.sc.bbw[b];
-      }
-      a.sf.sec_sun = (float)a.sc.sec_sun;
-      a.sf.sec_view = (float)a.sc.sec_view;
-      a.seeds = d_seeds;
-      a.resid = d_resid;
-      e = mlp_seeds(a, st);
-    }
+    if (rc == PHOTIC_OK)
+      e = launch_seed_polish(*cfg, d_rrs, npix, y, 0.0, resid_max, polish_iters, d_seeds,
+                             d_resid, st);
   }
   cudaFreeAsync(x, st);
   cudaFreeAsync(y, st);

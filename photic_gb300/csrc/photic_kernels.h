@@ -169,6 +169,9 @@ struct SeedArgs {
   SceneF32 sf;
   const float *rrs;
   const float *y;     // [npix][5] surrogate outputs (ln P, ln G, ln X, B, H)
+  // y == nullptr: the guess is the reference's cold start of P, G, X and B
+  // (model/samodel.c:2266-2273, 2342-2351) with depth h_guess
+  double h_guess;
   int64_t npix;
   double resid_max;
   int32_t polish_iters;  // Levenberg-Marquardt steps on the seed (0: none)

@@ -320,7 +320,6 @@ __global__ void seeds_kernel(const __grid_constant__ SeedArgs a) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= a.npix) return;
   const int nb = a.fp.n_bands;
-  const float *yp = a.y + p * 5;
   double *sd = a.seeds + p * 6;
   double r[NB];
   bool bad = false;
@@ -331,7 +330,26 @@ __global__ void seeds_kernel(const __grid_constant__ SeedArgs a) {
   }
   PixelF64<NB> px;
   if (!bad) pixel_setup_f64<NB>(a.fp, a.sc, r, px);
-  float z[5] = {yp[0], yp[1], yp[2], fmaxf(yp[3], 0.001f), fmaxf(yp[4], 0.1f)};
+  float z[5];
+  if (a.y != nullptr) {
+    const float *yp = a.y + p * 5;
+    z[0] = yp[0];
+    z[1] = yp[1];
+    z[2] = yp[2];
+    z[3] = fmaxf(yp[3], 0.001f);
+    z[4] = fmaxf(yp[4], 0.1f);
+  } else {
+    // no network: the reference's cold start of B, P, G, X from the
+    // measured spectrum, depth h_guess
+    double st[6], sp[6];
+    st[1] = st[3] = st[4] = st[5] = 0.0;
+    if (!bad) cold_start_f64<NB>(a.fp, px, st, sp);
+    z[0] = (float)log(0.01 * st[3]);
+    z[1] = (float)log(0.01 * st[4]);
+    z[2] = (float)log(0.01 * st[5]);
+    z[3] = fmaxf((float)(0.01 * st[1]), 0.001f);
+    z[4] = fmaxf((float)a.h_guess, 0.1f);
+  }
   if (!bad && a.polish_iters > 0 && isfinite(z[0] + z[1] + z[2] + z[3] + z[4])) {
     // up to three attempts: the prediction, then its depth scaled by 0.4
     // and by 2.5 (the depth is the least determined parameter); the first

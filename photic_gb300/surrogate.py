@@ -90,6 +90,25 @@ class Surrogate:
         return sd, res
 
 
+def heuristic_seeds(rrs: torch.Tensor, config: Optional[Config] = None,
+                    resid_max: float = 3.0 * NOISE_SIGMA, polish_iters: int = 25,
+                    h_guess: float = 10.0):
+    """Seeds from the same Levenberg-Marquardt polish and residual test as
+    :meth:`Surrogate.seeds`, started without the network from the
+    reference's cold-start guess of B, P, G, X (model/samodel.c:2266-2273,
+    2342-2351) at depth ``h_guess`` (and 0.4 / 2.5 times it): the baseline
+    that isolates what the trained network adds."""
+    cfg = config or Config()
+    npix = rrs.shape[0]
+    sd = torch.empty(npix, 6, dtype=torch.float64, device=rrs.device)
+    res = torch.empty(npix, dtype=torch.float32, device=rrs.device)
+    c = cfg.to_c()
+    L.check(L.lib().photic_seed_polished_heuristic(
+        C.byref(c), rrs.data_ptr(), npix, float(h_guess), resid_max, int(polish_iters),
+        sd.data_ptr(), res.data_ptr(), _stream_handle(None)))
+    return sd, res
+
+
 def features(rrs: torch.Tensor, theta_sun: float = 35.0, theta_view: float = 0.0) -> torch.Tensor:
     x = torch.empty(rrs.shape[0], 6, dtype=torch.float32, device=rrs.device)
     x[:, :4] = rrs[:, :4]

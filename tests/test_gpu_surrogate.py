@@ -102,3 +102,21 @@ def test_training_reduces_loss_and_warm_start(surr, gpu, port):
     ep = out_p["evals"].cpu().numpy()[fit].mean()
     print(f"evals/pixel polished {ep:.0f}")
     assert ep < ew
+
+    # what the trained network itself earns: the same polish and the same
+    # residual test started from the reference's cold-start guess instead of
+    # the network's prediction
+    seeds_h, res_h = surr.heuristic_seeds(rrs, polish_iters=15)
+    out_h = gpu.invert(rrs, cfg_p, seeds=seeds_h)
+    gpu.sync()
+    sh_np = seeds_h.cpu().numpy()
+    warm_h = fit & ~np.isnan(sh_np[:, 0])
+    eh = out_h["evals"].cpu().numpy()[fit].mean()
+    ref_h = port.invert_batch(rrs.cpu().numpy(), seeds=sh_np, seed_step_scale=0.1,
+                              nthreads=NTHREADS)
+    fh = (out_h["status"].cpu().numpy() & 0xFF) == 0
+    d = np.abs(out_h["depth_f64"].cpu().numpy()[fh] - ref_h[fh, 0])
+    assert np.median(d) <= 0.01 and np.quantile(d, 0.99) <= 0.05
+    print(f"heuristic + polish: seeded share {warm_h.mean():.2f}, evals/pixel {eh:.0f}; "
+          f"network + polish: seeded share {warm_p.mean():.2f}, evals/pixel {ep:.0f}")
+    assert warm_p.mean() > warm_h.mean() and ep < eh
