@@ -24,7 +24,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "libphotic_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libphotic_ref.so")
-NOUT = 40
+NOUT = 44
 
 # Output record columns shared by the oracles and the GPU path.
 COL = dict(H=0, B=1, cost=2, rrs_error=3, K_min=4, iod=5, evals_kept=6, evals=7,
@@ -336,28 +336,56 @@ def depth_sigma(rrs, depth, r_sigma, *, n_samples=128, seed=1, wl=OLI_BANDS, the
 
 
 def region_invert_batch(grid, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0, h_tide=0.0,
-                        nodata=-9999.0, reqmin=1e-10, konvge=100, kcount=2000, nthreads=0,
-                        which="port"):
-    """Spatial-region fit (3 x 3 neighbourhood per pixel) of a [nrows, ncols,
-    n_bands] float32 grid; returns [nrows*ncols, NOUT] (o[38] regions,
-    o[39] origin)."""
+                        nodata=-9999.0, reqmin=1e-10, konvge=100, kcount=2000, n_spatial=2,
+                        n_bottoms=1, h_empirical=None, nthreads=0, which="port"):
+    """Region fit of a [nrows, ncols, n_bands] float32 grid: each pixel alone
+    (n_spatial = 1) or with its 3 x 3 neighbourhood (n_spatial = 2), with
+    n_bottoms bottom types (sand, seagrass, coral) mixed per region;
+    h_empirical (None or [nrows*ncols] with NaN for none) gives per-pixel
+    empirical depths.  Returns [nrows*ncols, NOUT] (o[38] regions, o[39]
+    origin, o[40..42] bottom shares (%), o[43] bottom type)."""
     g = np.ascontiguousarray(grid, dtype=np.float32)
     nrows, ncols, nb = g.shape
     wl = _f64(wl)
+    he = _f64(h_empirical) if h_empirical is not None else None
     out = np.zeros((nrows * ncols, NOUT), dtype=np.float64)
     if which == "reference":
-        f = reference().lib.photic_ref_region_invert_batch
+        f = reference().lib.photic_ref_region_fit_batch
         f.argtypes = [C.c_int, _dp, C.c_double, C.c_double, C.c_double, _fp, C.c_int, C.c_int,
-                      C.c_float, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, _dp]
+                      C.c_float, C.c_int, C.c_int, _dp, C.c_int, C.c_double, C.c_int, C.c_int,
+                      C.c_int, _dp]
         rc = f(nb, _ptr(wl, _dp), theta_sun, theta_view, h_tide, g.ctypes.data_as(_fp), nrows,
-               ncols, nodata, 2, 1, reqmin, konvge, kcount, nthreads, _ptr(out, _dp))
+               ncols, nodata, n_spatial, n_bottoms, _ptr(he, _dp), 1, reqmin, konvge, kcount,
+               nthreads, _ptr(out, _dp))
     else:
-        rc = port().lib.po_region_invert_batch(nb, _ptr(wl, _dp), theta_sun, theta_view, h_tide,
-                                               g.ctypes.data_as(_fp), nrows, ncols, nodata,
-                                               reqmin, konvge, kcount, nthreads, _ptr(out, _dp))
+        f = port().lib.po_region_fit_batch
+        f.argtypes = [C.c_int, _dp, C.c_double, C.c_double, C.c_double, _fp, C.c_int, C.c_int,
+                      C.c_float, C.c_int, C.c_int, _dp, C.c_double, C.c_int, C.c_int, C.c_int,
+                      _dp]
+        rc = f(nb, _ptr(wl, _dp), theta_sun, theta_view, h_tide, g.ctypes.data_as(_fp), nrows,
+               ncols, nodata, n_spatial, n_bottoms, _ptr(he, _dp), reqmin, konvge, kcount,
+               nthreads, _ptr(out, _dp))
     if rc:
         raise ValueError("region_invert_batch failed")
     return out
+
+
+def region_cost(rrs, params, *, origin=0, n_bottoms=1, wl=OLI_BANDS, theta_sun=35.0,
+                theta_view=0.0, h_tide=0.0):
+    """samodel_error of one parameter vector for a pixel given as its regions'
+    spectra rrs [R, n_bands]; returns (cost, details[5])."""
+    r = _f64(rrs)
+    R, nb = r.shape
+    p = _f64(params)
+    wl = _f64(wl)
+    det = np.zeros(5)
+    f = port().lib.po_region_cost
+    f.restype = C.c_double
+    f.argtypes = [C.c_int, _dp, C.c_double, C.c_double, C.c_double, _dp, C.c_int, C.c_int,
+                  C.c_int, _dp, _dp]
+    c = f(nb, _ptr(wl, _dp), theta_sun, theta_view, h_tide, _ptr(r, _dp), R, origin, n_bottoms,
+          _ptr(p, _dp), _ptr(det, _dp))
+    return c, det
 
 
 

@@ -1148,16 +1148,25 @@ int po_depth_sigma(int n_bands, const double *wl, double theta_sun_deg, double t
   return 0;
 }
 
-/* ---- spatial regions (n_spatial = 2; model/samodel.c:2957-3027) ----------
- * Each pixel is fitted together with its 3 x 3 neighbourhood (indexes
- * clamped at the grid's edges, neighbours with a nodata band left out;
- * smoothing radius 1): one depth, albedo and q per region, one P, G, X for
- * the scene, and the cost's depth- and bottom-continuity terms
- * (model/samodel.c:2594-2692).  One scene, one bottom type. */
+/* ---- spatial regions and bottom mixtures (model/samodel.c:2957-3027) ----
+ * Each pixel is fitted alone (n_spatial = 1) or together with its 3 x 3
+ * neighbourhood (n_spatial = 2: indexes clamped at the grid's edges,
+ * neighbours with a nodata band left out; smoothing radius 1).  Every region
+ * has its own depth and, for each of the n_bottoms bottom types (sand,
+ * seagrass, coral: the first entries of the reference's bottom table,
+ * model/samodel.c:464-475), its own albedo and mixing weight q; the scene's
+ * P, G, X are shared; the cost adds the depth- and bottom-continuity terms
+ * (model/samodel.c:2594-2692).  One scene.  With an empirical depth the
+ * pixel takes that single depth start, and a pixel deeper than 8 m is
+ * fitted with sand alone (model/samodel.c:1781, 1826-1830, 2208-2231; the
+ * reference's reduction to sand then stays in its per-thread model_data for
+ * the thread's later pixels, an order dependence not reproduced: here the
+ * rule applies pixel by pixel). */
 #define PO_MAX_REGIONS 9
+#define PO_MAX_MIX 3
 
 typedef struct {
-  int R, origin, n_bands;
+  int R, origin, n_bands, nb;
   const po_scene *sc;
   double rrs[PO_MAX_REGIONS][PO_MAX_BANDS];
   double r440[PO_MAX_REGIONS], r490[PO_MAX_REGIONS], r550[PO_MAX_REGIONS];
@@ -1167,25 +1176,33 @@ typedef struct {
   double bottom_albedo, rrs_error, model_error;
 } po_rpixel;
 
-/* samodel_error with R regions, one scene, one bottom type; parameters
- * [H_0..H_R-1 | 100 B_0.. | q_0.. | 100 P, 100 G, 100 X]. */
+static int region_n_params(const po_rpixel *px) { return px->R + 2 * px->nb * px->R + 3; }
+
+/* samodel_error with R regions, nb bottom types, one scene; parameters
+ * [H_r | 100 B_{r,k} at R + r nb + k | q_{r,k} at R + R nb + r nb + k |
+ *  100 P, 100 G, 100 X] (model/samodel.c:2463-2491). */
 static double region_cost(const double *x, void *ctx) {
   po_rpixel *px = (po_rpixel *)ctx;
   const po_scene *sc = px->sc;
-  const int R = px->R, off = 3 * R;
+  const int R = px->R, nb = px->nb, qo = R + R * nb, off = R + 2 * nb * R;
   double err = 0.0, tot = 0.0, rrs_error, depth_mean, th, error_depth, n_out, bottom_mean,
          bottom_total, error_bottom, H, K_error, K_min = 1.0e4, model;
-  int r, b, nobs = 0;
+  int r, b, k, kb, nobs = 0;
   for (r = 0; r < R; r++) {
     double Hr = fabs(x[r]), P = 0.01 * fabs(x[off]), G = 0.01 * fabs(x[off + 1]),
-           X = 0.01 * fabs(x[off + 2]), B = 0.01 * fabs(x[R + r]), q = fabs(x[2 * R + r]),
-           q_sum = 0.0;
-    q_sum += q;
-    q /= q_sum;
+           X = 0.01 * fabs(x[off + 2]), B[PO_MAX_MIX], q[PO_MAX_MIX], q_sum = 0.0;
+    for (k = 0; k < nb; k++) B[k] = 0.01 * fabs(x[R + r * nb + k]);
+    for (k = 0; k < nb; k++) {
+      q[k] = fabs(x[qo + r * nb + k]);
+      q_sum += q[k];
+    }
+    for (k = 0; k < nb; k++) q[k] /= q_sum;
     for (b = 0; b < px->n_bands; b++) {
       double rho = 0.0, albedo = 0.0, Rm, d;
-      albedo += q * B;
-      rho += q * B * sc->refl[0][b];
+      for (k = 0; k < nb; k++) { /* model/samodel.c:2878-2883 */
+        albedo += q[k] * B[k];
+        rho += q[k] * B[k] * sc->refl[k][b];
+      }
       px->bottom_albedo = albedo;
       Rm = hope_band(sc, b, P, G, X, rho, Hr, 0.0, px->r440[r], px->r490[r], &px->K[b],
                      &px->rrs_bot[r][b], &px->rrs_mod[r][b]);
@@ -1213,7 +1230,8 @@ static double region_cost(const double *x, void *ctx) {
       n_out += 1.0;
     }
   if (n_out > 0.5) error_depth = 100.0 * sqrt(error_depth / n_out) / depth_mean;
-  /* bottom continuity, model/samodel.c:2633-2692 (one bottom type) */
+  /* bottom continuity, model/samodel.c:2633-2692: per bottom type the mean
+   * over regions of |100 B| |q| / sum |q|, deviations beyond the threshold */
   if (depth_mean < 5.0) th = 0.25;
   else if (depth_mean < 10.0) th = 0.1;
   else if (depth_mean < 15.0) th = 0.05;
@@ -1221,25 +1239,27 @@ static double region_cost(const double *x, void *ctx) {
   error_bottom = 0.0;
   n_out = 0.0;
   bottom_total = 0.0;
-  bottom_mean = 0.0;
-  for (r = 0; r < R; r++) {
-    double q_sum = 0.0;
-    q_sum += fabs(x[2 * R + r]);
-    bottom_mean += fabs(x[R + r]) * fabs(x[2 * R + r]) / q_sum;
-  }
-  bottom_mean /= (double)R;
-  bottom_total += bottom_mean;
-  for (r = 0; r < R; r++) {
-    double q_sum = 0.0, bottom;
-    q_sum += fabs(x[2 * R + r]);
-    bottom = fabs(x[R + r]) * fabs(x[2 * R + r]) / q_sum;
-    if (bottom < (1.0 - th) * bottom_mean || bottom > (1.0 + th) * bottom_mean) {
-      error_bottom += pow(bottom - bottom_mean, 2.0);
-      n_out += 1.0;
+  for (k = 0; k < nb; k++) {
+    bottom_mean = 0.0;
+    for (r = 0; r < R; r++) {
+      double q_sum = 0.0;
+      for (kb = 0; kb < nb; kb++) q_sum += fabs(x[qo + r * nb + kb]);
+      bottom_mean += fabs(x[R + r * nb + k]) * fabs(x[qo + r * nb + k]) / q_sum;
+    }
+    bottom_mean /= (double)R;
+    bottom_total += bottom_mean;
+    for (r = 0; r < R; r++) {
+      double q_sum = 0.0, bottom;
+      for (kb = 0; kb < nb; kb++) q_sum += fabs(x[qo + r * nb + kb]);
+      bottom = fabs(x[R + r * nb + k]) * fabs(x[qo + r * nb + k]) / q_sum;
+      if (bottom < (1.0 - th) * bottom_mean || bottom > (1.0 + th) * bottom_mean) {
+        error_bottom += pow(bottom - bottom_mean, 2.0);
+        n_out += 1.0;
+      }
     }
   }
   if (n_out > 0.5) {
-    bottom_mean = bottom_total / ((double)1);
+    bottom_mean = bottom_total / ((double)nb);
     error_bottom = 100.0 * sqrt(error_bottom / n_out) / bottom_mean;
   }
   /* K penalties on the origin's depth and the scene's K (the last region's
@@ -1270,25 +1290,27 @@ static double region_cost(const double *x, void *ctx) {
   return model;
 }
 
-/* Cold start for R regions (model/samodel.c:2249-2353). */
+/* Cold start for R regions and nb bottom types (model/samodel.c:2249-2353). */
 static void region_cold_start(const po_rpixel *px, double H0, double *start, double *step) {
-  const int R = px->R, off = 3 * R;
+  const int R = px->R, nb = px->nb, off = R + 2 * nb * R;
   double m490 = 0.0, m550 = 0.0, m640 = 0.0;
-  int r;
+  int r, k;
   for (r = 0; r < R; r++) {
     start[r] = H0;
     step[r] = 1.25 * start[r];
   }
   for (r = 0; r < R; r++) m490 += px->r490[r];
   m490 /= (double)R * 1;
-  for (r = 0; r < R; r++) {
-    start[R + r] = 100.0 * 4.0 * m490;
-    step[R + r] = 1.5 * start[R + r];
-  }
-  for (r = 0; r < R; r++) {
-    start[2 * R + r] = 1.0;
-    step[2 * R + r] = 0.5 * start[2 * R + r];
-  }
+  for (k = 0; k < nb; k++)
+    for (r = 0; r < R; r++) {
+      start[R + r * nb + k] = 100.0 * 4.0 * m490;
+      step[R + r * nb + k] = 1.5 * start[R + r * nb + k];
+    }
+  for (k = 0; k < nb; k++)
+    for (r = 0; r < R; r++) {
+      start[R + nb * R + r * nb + k] = 1.0;
+      step[R + nb * R + r * nb + k] = 0.5 * start[R + nb * R + r * nb + k];
+    }
   m490 = 0.0;
   for (r = 0; r < R; r++) {
     m490 += px->r490[r];
@@ -1306,11 +1328,14 @@ static void region_cold_start(const po_rpixel *px, double H0, double *start, dou
   step[off + 2] = 2.0 * start[off + 2];
 }
 
-static void region_fit(po_rpixel *px, const po_fit *fit, double *o) {
-  const int R = px->R, n = 3 * R + 3;
+/* samodel_optimise for one pixel's regions (model/samodel.c:1768-2115):
+ * depth starts, nelmin, early exit, the final re-evaluation and the post-fit
+ * products.  h_emp: the empirical depth, or NaN for the 8 cold starts. */
+static void region_fit(po_rpixel *px, const po_fit *fit, double h_emp, double *o) {
+  const int R = px->R, n = region_n_params(px), nb = px->nb;
   double start[PO_MAX_PARAMS], step[PO_MAX_PARAMS], xm[PO_MAX_PARAMS], best[PO_MAX_PARAMS];
   double lowest = 1.0e4, y = 0.0;
-  int icount = 0, numres = 0, ifault = 0, k, r, b;
+  int icount = 0, numres = 0, ifault = 0, k, r, b, nst;
   long total = 0;
   int kept_evals = 0, kept_res = 0, kept_start = 0, kept_fault = 0, converged = 0;
   for (r = 0; r < R; r++) { /* model/samodel.c:1785-1799 */
@@ -1323,8 +1348,9 @@ static void region_fit(po_rpixel *px, const po_fit *fit, double *o) {
     if (px->r440[r] < 0.0) px->r440[r] = 0.0001;
   }
   memset(best, 0, sizeof best);
-  for (k = 0; k < fit->n_hstarts; k++) {
-    region_cold_start(px, fit->hstarts[k], start, step);
+  nst = isnan(h_emp) ? fit->n_hstarts : 1;
+  for (k = 0; k < nst; k++) {
+    region_cold_start(px, isnan(h_emp) ? fit->hstarts[k] : h_emp, start, step);
     po_nelmin(region_cost, px, n, start, xm, &y, fit->reqmin, step, fit->konvge, fit->kcount,
               &icount, &numres, &ifault);
     total += icount;
@@ -1342,6 +1368,7 @@ static void region_fit(po_rpixel *px, const po_fit *fit, double *o) {
   region_cost(best, px);
   {
     double K_min = 1.0e10, iod = 0.0, nobs = 0.0, depth = 0.0, ow = sqrt((double)R);
+    double q_sum = 0.0, pct[PO_MAX_MIX], largest = 0.0, type = 0.0;
     int found = 0;
     for (b = 0; b < px->n_bands; b++)
       if (!f_close((float)px->K[b], (float)0.0, 1.0e-4f) && px->K[b] < K_min) {
@@ -1355,6 +1382,15 @@ static void region_fit(po_rpixel *px, const po_fit *fit, double *o) {
       else depth += H;
     }
     depth /= ow + ((double)R) - 1.0;
+    /* bottom shares of the origin region and the bottom type,
+     * model/samodel.c:2021-2047 */
+    for (k = 0; k < nb; k++) q_sum += fabs(best[R + R * nb + px->origin * nb + k]);
+    for (k = 0; k < nb; k++) pct[k] = 100.0 * fabs(best[R + R * nb + px->origin * nb + k]) / q_sum;
+    for (k = 0; k < nb; k++)
+      if (pct[k] > largest) {
+        largest = pct[k];
+        type = 1.0 + k;
+      }
     for (r = 0; r < R; r++)
       for (b = 0; b < px->n_bands; b++) {
         iod += px->rrs_bot[r][b] / px->rrs_mod[r][b];
@@ -1367,15 +1403,17 @@ static void region_fit(po_rpixel *px, const po_fit *fit, double *o) {
     o[3] = px->rrs_error;
     o[4] = K_min;
     o[5] = iod;
+    for (k = 0; k < nb; k++) o[40 + k] = pct[k];
+    o[43] = type;
   }
   o[6] = (double)kept_evals;
   o[7] = (double)total;
   o[8] = converged ? 1.0 : 0.0;
   o[9] = 0.0;
   o[10] = 1.0;
-  o[11] = 0.01 * fabs(best[3 * R]);
-  o[19] = 0.01 * fabs(best[3 * R + 1]);
-  o[27] = 0.01 * fabs(best[3 * R + 2]);
+  o[11] = 0.01 * fabs(best[R + 2 * nb * R]);
+  o[19] = 0.01 * fabs(best[R + 2 * nb * R + 1]);
+  o[27] = 0.01 * fabs(best[R + 2 * nb * R + 2]);
   o[35] = (double)kept_res;
   o[36] = (double)kept_start;
   o[37] = (double)kept_fault;
@@ -1383,14 +1421,17 @@ static void region_fit(po_rpixel *px, const po_fit *fit, double *o) {
   o[39] = (double)px->origin;
 }
 
-int po_region_invert_batch(int n_bands, const double *wl, double theta_sun_deg,
-                           double theta_view_deg, double h_tide, const float *grid, int nrows,
-                           int ncols, float nodata, double reqmin, int konvge, int kcount,
-                           int nthreads, double *out) {
+int po_region_fit_batch(int n_bands, const double *wl, double theta_sun_deg,
+                        double theta_view_deg, double h_tide, const float *grid, int nrows,
+                        int ncols, float nodata, int n_spatial, int n_bottoms,
+                        const double *h_empirical, double reqmin, int konvge, int kcount,
+                        int nthreads, double *out) {
   po_scene sc;
   po_fit fit;
   int64_t p, npix = (int64_t)nrows * ncols;
-  if (n_bands < 2 || n_bands > PO_MAX_BANDS) return 1;
+  if (n_bands < 2 || n_bands > PO_MAX_BANDS || n_spatial < 1 || n_spatial > 2 ||
+      n_bottoms < 1 || n_bottoms > PO_MAX_MIX)
+    return 1;
   scene_init(&sc, n_bands, wl, theta_sun_deg, theta_view_deg, h_tide);
   fit.seed_step_scale = 1.0;
   fit.reqmin = reqmin;
@@ -1404,7 +1445,9 @@ int po_region_invert_batch(int n_bands, const double *wl, double theta_sun_deg,
 #endif
   for (p = 0; p < npix; p++) {
     const int i = (int)(p / ncols), j = (int)(p % ncols);
+    const int w = n_spatial - 1;
     double *o = out + p * PO_NOUT;
+    double h_emp = NAN;
     po_rpixel px;
     int ii, jj, b;
     memset(o, 0, PO_NOUT * sizeof(double));
@@ -1415,10 +1458,15 @@ int po_region_invert_batch(int n_bands, const double *wl, double theta_sun_deg,
     memset(&px, 0, sizeof px);
     px.sc = &sc;
     px.n_bands = n_bands;
+    px.nb = n_bottoms;
+    if (h_empirical && !isnan(h_empirical[p])) {
+      h_emp = h_empirical[p];
+      if (h_emp > 8.0) px.nb = 1; /* model/samodel.c:1781, 1826-1830 */
+    }
     /* extract_Rrs_data, model/samodel.c:2957-3027 */
-    for (ii = -1; ii <= 1; ii++) {
+    for (ii = -w; ii <= w; ii++) {
       const int iii = i + ii < 0 ? 0 : (i + ii > nrows - 1 ? nrows - 1 : i + ii);
-      for (jj = -1; jj <= 1; jj++) {
+      for (jj = -w; jj <= w; jj++) {
         const int jjj = j + jj < 0 ? 0 : (j + jj > ncols - 1 ? ncols - 1 : j + jj);
         const float *q = grid + ((int64_t)iii * ncols + jjj) * n_bands;
         int nodata_region = 0;
@@ -1435,9 +1483,55 @@ int po_region_invert_batch(int n_bands, const double *wl, double theta_sun_deg,
       }
     }
     if (px.R == 0) continue;
-    region_fit(&px, &fit, o);
+    region_fit(&px, &fit, h_emp, o);
   }
   return 0;
+}
+
+int po_region_invert_batch(int n_bands, const double *wl, double theta_sun_deg,
+                           double theta_view_deg, double h_tide, const float *grid, int nrows,
+                           int ncols, float nodata, double reqmin, int konvge, int kcount,
+                           int nthreads, double *out) {
+  return po_region_fit_batch(n_bands, wl, theta_sun_deg, theta_view_deg, h_tide, grid, nrows,
+                             ncols, nodata, 2, 1, NULL, reqmin, konvge, kcount, nthreads, out);
+}
+
+/* Cost, with its side outputs, of one explicit parameter vector for a pixel
+ * given as its regions' spectra (rrs [R][n_bands], origin region, nb bottom
+ * types): samodel_error (model/samodel.c:2432-2759) for samodel_error's
+ * drop-in test.  Outputs: cost; details[5] = Rrs error, model error,
+ * bottom albedo, K_min (last region's bands), 0. */
+double po_region_cost(int n_bands, const double *wl, double theta_sun_deg,
+                      double theta_view_deg, double h_tide, const double *rrs, int R, int origin,
+                      int n_bottoms, const double *params, double *details) {
+  po_scene sc;
+  po_rpixel px;
+  int r, b;
+  double c, K_min = 1.0e4;
+  scene_init(&sc, n_bands, wl, theta_sun_deg, theta_view_deg, h_tide);
+  memset(&px, 0, sizeof px);
+  px.sc = &sc;
+  px.n_bands = n_bands;
+  px.nb = n_bottoms;
+  px.R = R;
+  px.origin = origin;
+  for (r = 0; r < R; r++) {
+    for (b = 0; b < n_bands; b++) px.rrs[r][b] = rrs[r * n_bands + b];
+    px.r440[r] = po_interp_1d(sc.wl, px.rrs[r], n_bands, 440.0);
+    px.r490[r] = po_interp_1d(sc.wl, px.rrs[r], n_bands, 490.0);
+    if (px.r440[r] < 0.0) px.r440[r] = 0.0001;
+  }
+  c = region_cost(params, &px);
+  for (b = 0; b < n_bands; b++)
+    if (!f_close((float)px.K[b], 0.0f, 1.0e-6f) && px.K[b] < K_min) K_min = px.K[b];
+  if (details) {
+    details[0] = px.rrs_error;
+    details[1] = px.model_error;
+    details[2] = px.bottom_albedo;
+    details[3] = K_min;
+    details[4] = 0.0;
+  }
+  return c;
 }
 
 

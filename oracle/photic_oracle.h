@@ -25,9 +25,9 @@
 
 #define PO_MAX_BANDS 8
 #define PO_MAX_SCENES 8
-#define PO_MAX_PARAMS 40
+#define PO_MAX_PARAMS 72
 #define PO_N_BOTTOM_TYPES 8
-#define PO_NOUT 40
+#define PO_NOUT 44
 
 /* Output record per pixel (doubles), shared with oracle/_ref and the GPU:
  *  0 depth H   1 bottom albedo   2 model error (cost)   3 Rrs error (%)
@@ -35,7 +35,10 @@
  *  7 evaluations over all starts          8 converged (ifault == 0)
  *  9 status (0 fitted, 1 masked, 2 invalid)   10 scene count
  * 11..18 P per scene   19..26 G per scene   27..34 X per scene
- * 35 restarts of the kept start   36 index of the kept start   37 ifault */
+ * 35 restarts of the kept start   36 index of the kept start   37 ifault
+ * 38 regions  39 origin region (region fits)
+ * 40..42 bottom shares (%) of sand, seagrass, coral in the origin region
+ * 43 bottom type (1 + index of the largest share; region fits) */
 
 #ifdef __cplusplus
 extern "C" {
@@ -80,6 +83,14 @@ int po_region_invert_batch(int n_bands, const double *wl, double theta_sun_deg,
                            double theta_view_deg, double h_tide, const float *grid, int nrows,
                            int ncols, float nodata, double reqmin, int konvge, int kcount,
                            int nthreads, double *out);
+int po_region_fit_batch(int n_bands, const double *wl, double theta_sun_deg,
+                        double theta_view_deg, double h_tide, const float *grid, int nrows,
+                        int ncols, float nodata, int n_spatial, int n_bottoms,
+                        const double *h_empirical, double reqmin, int konvge, int kcount,
+                        int nthreads, double *out);
+double po_region_cost(int n_bands, const double *wl, double theta_sun_deg,
+                      double theta_view_deg, double h_tide, const double *rrs, int R, int origin,
+                      int n_bottoms, const double *params, double *details);
 int po_depth_sigma(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
                    const float *rrs, int64_t npix, const float *depth, const double *r_sigma,
                    int n_samples, uint64_t seed, double reqmin, int konvge, int kcount,

@@ -41,7 +41,7 @@ extern double bottom_type_sand[], bottom_type_seagrass[], bottom_type_coral[],
 #define REF_MAX_SCENES 8
 #define REF_MAX_BANDS 8
 #define REF_N_BOTTOM_TABLE 8
-#define REF_NOUT 40
+#define REF_NOUT 44
 
 typedef struct {
   int active;
@@ -329,19 +329,27 @@ int photic_ref_joint_invert_batch(int n_bands, const double *wl, double theta_vi
 }
 
 /* Spatial-region fit (n_spatial = 2: the 3 x 3 neighbourhood of each pixel,
- * edges clamped, neighbours with nodata left out; model/samodel.c:2957-3027)
- * through the reference's own extract_Rrs_data and samodel_optimise, one
- * scene, smoothing radius 1.  grid is [nrows][ncols][n_bands] float; out is
- * [npix][REF_NOUT] with o[38] = regions, o[39] = origin region. */
-int photic_ref_region_invert_batch(int n_bands, const double *wl, double theta_sun_deg,
-                                   double theta_view_deg, double h_tide, const float *grid,
-                                   int nrows, int ncols, float nodata, int n_spatial,
-                                   int use_override, double reqmin, int konvge, int kcount,
-                                   int nthreads, double *out) {
+ * edges clamped, neighbours with nodata left out; n_spatial = 1: the pixel
+ * alone; model/samodel.c:2957-3027) with n_bottoms bottom types (the first
+ * entries of the bottom table, all at once as ALL_BOTTOMS selects,
+ * model/samodel.c:1822-1858), through the reference's own extract_Rrs_data
+ * and samodel_optimise, one scene, smoothing radius 1.  grid is
+ * [nrows][ncols][n_bands] float; h_empirical (NULL, or [npix] with NaN for
+ * none) gives a pixel's empirical depth as samodel() sets it
+ * (model/samodel.c:958-967).  out is [npix][REF_NOUT] with o[38] = regions,
+ * o[39] = origin region, o[40..42] = B_type_percent of sand, seagrass and
+ * coral, o[43] = bottom_type. */
+int photic_ref_region_fit_batch(int n_bands, const double *wl, double theta_sun_deg,
+                                double theta_view_deg, double h_tide, const float *grid,
+                                int nrows, int ncols, float nodata, int n_spatial, int n_bottoms,
+                                const double *h_empirical, int use_override, double reqmin,
+                                int konvge, int kcount, int nthreads, double *out) {
   geogrid *gd;
   scene *sc;
   int b, R;
-  if (n_bands < 2 || n_bands > REF_MAX_BANDS || n_spatial < 1 || n_spatial > 2) return 1;
+  if (n_bands < 2 || n_bands > REF_MAX_BANDS || n_spatial < 1 || n_spatial > 2 ||
+      n_bottoms < 1 || n_bottoms > 3)
+    return 1;
   R = (2 * n_spatial - 1) * (2 * n_spatial - 1);
   gd = (geogrid *)calloc(n_bands, sizeof(geogrid));
   sc = (scene *)calloc(1, sizeof(scene));
@@ -388,6 +396,11 @@ int photic_ref_region_invert_batch(int n_bands, const double *wl, double theta_s
           md->rrs_dp[r][0][bb] = 0.0;
           md->rho[r][0][bb] = 0.0;
         }
+      md->n_bottoms = n_bottoms;
+      if (h_empirical && !isnan(h_empirical[p])) {
+        md->empirical_depth_present = true;
+        md->h_empirical = h_empirical[p];
+      }
       extract_Rrs_data(i, j, sc, gd, &scene_index, 1, n_spatial, 1, nrows, ncols, md, 0.0);
       if (md->n_regions == 0) continue;
       set_tol(use_override, reqmin, konvge, kcount);
@@ -395,6 +408,8 @@ int photic_ref_region_invert_batch(int n_bands, const double *wl, double theta_s
       store_result(md, o, g_tol.evals);
       o[38] = (double)md->n_regions;
       o[39] = (double)md->origin;
+      for (bb = 0; bb < 3; bb++) o[40 + bb] = md->B_type_percent[bb];
+      o[43] = md->bottom_type;
     }
     md_free(md);
   }
@@ -402,6 +417,16 @@ int photic_ref_region_invert_batch(int n_bands, const double *wl, double theta_s
   free(gd);
   free(sc);
   return 0;
+}
+
+int photic_ref_region_invert_batch(int n_bands, const double *wl, double theta_sun_deg,
+                                   double theta_view_deg, double h_tide, const float *grid,
+                                   int nrows, int ncols, float nodata, int n_spatial,
+                                   int use_override, double reqmin, int konvge, int kcount,
+                                   int nthreads, double *out) {
+  return photic_ref_region_fit_batch(n_bands, wl, theta_sun_deg, theta_view_deg, h_tide, grid,
+                                     nrows, ncols, nodata, n_spatial, 1, NULL, use_override,
+                                     reqmin, konvge, kcount, nthreads, out);
 }
 
 /* Forward model + cost at given parameters, through samodel_error

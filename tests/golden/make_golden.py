@@ -81,6 +81,27 @@ def regions():
                         cols=np.array(cols), kcount=np.array(400))
 
 
+def bottoms():
+    # sand / seagrass / coral mixtures (n_bottoms = 3, the reference's
+    # default), pixels alone and with 3 x 3 regions, some with empirical
+    # depths; a reduced evaluation budget keeps the fixture quick
+    nr, nc = 10, 12
+    rrs, truth = O.generate_single(20260707, nr * nc, pix0=4000, mask_frac=0.15)
+    grid = rrs.reshape(nr, nc, rrs.shape[1])
+    he = truth[:, 0] * np.random.default_rng(9).uniform(0.7, 1.3, truth.shape[0])
+    he[::2] = np.nan
+    cols = KEEP + [38, 39, 40, 41, 42, 43]
+    out = {}
+    for ns in (1, 2):
+        out[f"ref_s{ns}"] = O.region_invert_batch(grid, kcount=600, n_spatial=ns, n_bottoms=3,
+                                                  which="reference", nthreads=os.cpu_count())[:, cols]
+        out[f"ref_s{ns}_emp"] = O.region_invert_batch(grid, kcount=600, n_spatial=ns, n_bottoms=3,
+                                                      h_empirical=he, which="reference",
+                                                      nthreads=os.cpu_count())[:, cols]
+    np.savez_compressed(os.path.join(OUT, "bottoms.npz"), grid=grid, h_empirical=he,
+                        cols=np.array(cols), kcount=np.array(600), **out)
+
+
 if __name__ == "__main__":
     O.build(ref=True)
     if not O.reference_available():
@@ -89,6 +110,7 @@ if __name__ == "__main__":
     joint()
     cost_and_nelmin()
     regions()
+    bottoms()
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)), "bytes")

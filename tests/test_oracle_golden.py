@@ -93,3 +93,16 @@ def test_regions_golden(port, golden_dir):
     g = np.load(os.path.join(golden_dir, "regions.npz"))
     out = port.region_invert_batch(g["grid"], kcount=int(g["kcount"]), nthreads=4)
     np.testing.assert_array_equal(out[:, g["cols"]], g["ref"])
+
+
+@pytest.mark.parametrize("key", ["ref_s1", "ref_s1_emp", "ref_s2", "ref_s2_emp"])
+def test_bottom_mixtures_golden(port, golden_dir, key):
+    """Sand / seagrass / coral mixtures (n_bottoms = 3), pixels alone and with
+    3 x 3 regions, with and without empirical depths, against the reference's
+    own samodel_optimise (tests/golden/bottoms.npz)."""
+    g = np.load(os.path.join(golden_dir, "bottoms.npz"))
+    ns = 1 if key.startswith("ref_s1") else 2
+    he = g["h_empirical"] if key.endswith("_emp") else None
+    out = port.region_invert_batch(g["grid"], kcount=int(g["kcount"]), n_spatial=ns, n_bottoms=3,
+                                   h_empirical=he, nthreads=4)
+    np.testing.assert_array_equal(out[:, g["cols"]], g[key])

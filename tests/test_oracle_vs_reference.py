@@ -54,3 +54,23 @@ def test_regions_bit_exact():
     b = O.region_invert_batch(grid, reqmin=1e-2, konvge=100, kcount=5000, nthreads=8,
                               which="reference")
     np.testing.assert_array_equal(a[:, cols], b[:, cols])
+
+
+@pytest.mark.parametrize("n_spatial,n_bottoms", [(1, 2), (1, 3), (2, 2), (2, 3)])
+def test_bottom_mixtures_bit_exact(n_spatial, n_bottoms):
+    """Sand/seagrass/coral mixtures per region (the reference's default
+    n_bottoms = 3), alone and with 3 x 3 regions, with and without empirical
+    depths (pixels deeper than 8 m are fitted with sand alone)."""
+    rrs, truth = O.generate_single(41 + n_bottoms, 8 * 13, pix0=500, mask_frac=0.15)
+    grid = rrs.reshape(8, 13, 4)
+    he = truth[:, 0] * np.random.default_rng(n_bottoms).uniform(0.7, 1.3, truth.shape[0])
+    he[::3] = np.nan
+    cols = [c for c in range(O.NOUT) if c not in (36, 37)]  # kept start / ifault: port only
+    for h in (None, he):
+        a = O.region_invert_batch(grid, kcount=600, n_spatial=n_spatial, n_bottoms=n_bottoms,
+                                  h_empirical=h, nthreads=8)
+        b = O.region_invert_batch(grid, kcount=600, n_spatial=n_spatial, n_bottoms=n_bottoms,
+                                  h_empirical=h, nthreads=8, which="reference")
+        np.testing.assert_array_equal(a[:, cols], b[:, cols])
+        fit = a[:, 9] == 0
+        assert len(np.unique(a[fit, 43])) > 1  # several bottom types win
