@@ -111,6 +111,9 @@ typedef struct photic_outputs {
   int32_t *status;       /* PHOTIC_PX_* | PHOTIC_PX_CONVERGED | start << 16 */
   double *params;        /* single-scene calls: [npix * 6] kept parameter vector
                             (H, 100B, q, 100P, 100G, 100X) as nelmin returned it */
+  float *bottom_percent; /* photic_region_fit_batch: [npix * 3] share (%) of sand,
+                            seagrass and coral in the pixel's own region */
+  float *bottom_type;    /* photic_region_fit_batch: 1 + index of the largest share */
 } photic_outputs;
 
 /* Defaults: OLI-like bands 443/482/561/655 nm, sun 35 deg, nadir, the
@@ -207,6 +210,13 @@ double photic_interp_1d(const double *X, const double *Y, int32_t n, double x);
  * a_w(640). */
 int photic_band_constants(const photic_config *cfg, double *out);
 
+/* The reference's bottom reflectance table (model/samodel.c:236-287, in the
+ * order of :464-475: sand, seagrass, coral, macrophytes, dark sediment,
+ * coral sand, green algae, red algae) at cfg's bands (host function):
+ * out[k * n_bands + b] for the first n_types (1..8) types, interpolated as
+ * samodel() does (:550-618). */
+int photic_bottom_reflectances(const photic_config *cfg, int32_t n_types, double *out);
+
 /* Spatial-region fit (model/samodel.c:2957-3027 with n_spatial = 2): every
  * pixel of the [nrows][ncols][n_bands] grid (device, float) is fitted with
  * its 3 x 3 neighbourhood -- indexes clamped at the edges, neighbours with a
@@ -214,10 +224,33 @@ int photic_band_constants(const photic_config *cfg, double *out);
  * q per region, shared P, G, X, and the cost's depth- and bottom-continuity
  * terms; depth is the origin-weighted mean (model/samodel.c:1999-2017).
  * Outputs per pixel; status carries the region count in bits 24-27.  One
- * scene, one bottom type, up to 4 bands, n_spatial = 2 only. */
+ * scene, one bottom type, n_spatial = 2 only (photic_region_fit_batch with
+ * n_bottoms = 1). */
 int photic_region_invert_batch(const photic_config *cfg, const float *d_grid, int32_t nrows,
                                int32_t ncols, int32_t n_spatial, const photic_outputs *out,
                                void *stream);
+
+/* The general fit of the reference's samodel() pixel loop
+ * (model/samodel.c:901-1166 over samodel_optimise, :1768-2115).  d_grid
+ * (device, float) is [n_scenes][nrows][ncols][n_bands]: n_scenes scenes of
+ * the same place and bands, scene s with subsurface sun zenith
+ * theta_sun_deg[s] (host array; NULL: cfg->theta_sun_deg for all).  Every
+ * pixel is fitted alone (n_spatial = 1) or with its 3 x 3 neighbourhood
+ * (n_spatial = 2, as photic_region_invert_batch), with n_bottoms = 1..3
+ * bottom types (sand, seagrass, coral) mixed in every region: per region a
+ * depth and per type an albedo and a mixing weight q, per scene P, G, X;
+ * n = R + 2 n_bottoms R + 3 n_scenes unknowns (at most 96).  The
+ * reference's default call is n_spatial = 2, n_bottoms = 3
+ * (model/common.c:152).  d_h_empirical (NULL, or device [npix] doubles, NaN
+ * for none) gives empirical depths: such a pixel takes that single depth
+ * start, and one deeper than 8 m is fitted with sand alone
+ * (model/samodel.c:1781, 1826-1830, 2208-2231).  Outputs per pixel, with P,
+ * G, X as [npix][n_scenes], bottom_percent and bottom_type; status carries
+ * the region count in bits 24-27.  Up to 128 regions x scenes x bands. */
+int photic_region_fit_batch(const photic_config *cfg, const float *d_grid, int32_t n_scenes,
+                            const double *theta_sun_deg, int32_t nrows, int32_t ncols,
+                            int32_t n_spatial, int32_t n_bottoms, const double *d_h_empirical,
+                            const photic_outputs *out, void *stream);
 
 /* Depth uncertainty, the reference's ad hoc estimate (model/samodel.c:
  * 1368-1479): for each 0.25 m interval up to the deepest fitted depth (whole

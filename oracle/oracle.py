@@ -338,32 +338,40 @@ def depth_sigma(rrs, depth, r_sigma, *, n_samples=128, seed=1, wl=OLI_BANDS, the
 def region_invert_batch(grid, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0, h_tide=0.0,
                         nodata=-9999.0, reqmin=1e-10, konvge=100, kcount=2000, n_spatial=2,
                         n_bottoms=1, h_empirical=None, nthreads=0, which="port"):
-    """Region fit of a [nrows, ncols, n_bands] float32 grid: each pixel alone
-    (n_spatial = 1) or with its 3 x 3 neighbourhood (n_spatial = 2), with
-    n_bottoms bottom types (sand, seagrass, coral) mixed per region;
-    h_empirical (None or [nrows*ncols] with NaN for none) gives per-pixel
-    empirical depths.  Returns [nrows*ncols, NOUT] (o[38] regions, o[39]
-    origin, o[40..42] bottom shares (%), o[43] bottom type)."""
+    """The general fit of a grid: [nrows, ncols, n_bands] (one scene) or
+    [n_scenes, nrows, ncols, n_bands] float32 with theta_sun one sun zenith
+    per scene; each pixel alone (n_spatial = 1) or with its 3 x 3
+    neighbourhood (n_spatial = 2), n_bottoms bottom types (sand, seagrass,
+    coral) mixed per region; h_empirical (None or [nrows*ncols] with NaN for
+    none) gives per-pixel empirical depths.  Returns [nrows*ncols, NOUT]
+    (o[38] regions, o[39] origin, o[40..42] bottom shares (%), o[43] bottom
+    type)."""
     g = np.ascontiguousarray(grid, dtype=np.float32)
-    nrows, ncols, nb = g.shape
+    if g.ndim == 3:
+        g = g[None]
+    ns, nrows, ncols, nb = g.shape
+    override = reqmin is not None  # None: the reference's own 1e-2 / 100 / 5000
+    if not override:
+        reqmin, konvge, kcount = 1e-2, 100, 5000
+    th = _f64(np.broadcast_to(np.asarray(theta_sun, dtype=np.float64), (ns,)))
     wl = _f64(wl)
     he = _f64(h_empirical) if h_empirical is not None else None
     out = np.zeros((nrows * ncols, NOUT), dtype=np.float64)
     if which == "reference":
         f = reference().lib.photic_ref_region_fit_batch
-        f.argtypes = [C.c_int, _dp, C.c_double, C.c_double, C.c_double, _fp, C.c_int, C.c_int,
+        f.argtypes = [C.c_int, _dp, _dp, C.c_double, C.c_double, _fp, C.c_int, C.c_int, C.c_int,
                       C.c_float, C.c_int, C.c_int, _dp, C.c_int, C.c_double, C.c_int, C.c_int,
                       C.c_int, _dp]
-        rc = f(nb, _ptr(wl, _dp), theta_sun, theta_view, h_tide, g.ctypes.data_as(_fp), nrows,
-               ncols, nodata, n_spatial, n_bottoms, _ptr(he, _dp), 1, reqmin, konvge, kcount,
-               nthreads, _ptr(out, _dp))
+        rc = f(nb, _ptr(wl, _dp), _ptr(th, _dp), theta_view, h_tide, g.ctypes.data_as(_fp), ns,
+               nrows, ncols, nodata, n_spatial, n_bottoms, _ptr(he, _dp), 1 if override else 0,
+               reqmin, konvge, kcount, nthreads, _ptr(out, _dp))
     else:
         f = port().lib.po_region_fit_batch
-        f.argtypes = [C.c_int, _dp, C.c_double, C.c_double, C.c_double, _fp, C.c_int, C.c_int,
+        f.argtypes = [C.c_int, _dp, _dp, C.c_double, C.c_double, _fp, C.c_int, C.c_int, C.c_int,
                       C.c_float, C.c_int, C.c_int, _dp, C.c_double, C.c_int, C.c_int, C.c_int,
                       _dp]
-        rc = f(nb, _ptr(wl, _dp), theta_sun, theta_view, h_tide, g.ctypes.data_as(_fp), nrows,
-               ncols, nodata, n_spatial, n_bottoms, _ptr(he, _dp), reqmin, konvge, kcount,
+        rc = f(nb, _ptr(wl, _dp), _ptr(th, _dp), theta_view, h_tide, g.ctypes.data_as(_fp), ns,
+               nrows, ncols, nodata, n_spatial, n_bottoms, _ptr(he, _dp), reqmin, konvge, kcount,
                nthreads, _ptr(out, _dp))
     if rc:
         raise ValueError("region_invert_batch failed")
@@ -373,19 +381,25 @@ def region_invert_batch(grid, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0, h
 def region_cost(rrs, params, *, origin=0, n_bottoms=1, wl=OLI_BANDS, theta_sun=35.0,
                 theta_view=0.0, h_tide=0.0):
     """samodel_error of one parameter vector for a pixel given as its regions'
-    spectra rrs [R, n_bands]; returns (cost, details[5])."""
+    spectra rrs [R, n_bands] or [R, S, n_bands]; returns (cost, details[5],
+    modelled Rrs [R, S, n_bands])."""
     r = _f64(rrs)
-    R, nb = r.shape
+    if r.ndim == 2:
+        r = r[:, None, :]
+    R, S, nb = r.shape
+    r = np.ascontiguousarray(r)
+    th = _f64(np.broadcast_to(np.asarray(theta_sun, dtype=np.float64), (S,)))
     p = _f64(params)
     wl = _f64(wl)
     det = np.zeros(5)
+    rm = np.zeros((R, S, nb))
     f = port().lib.po_region_cost
     f.restype = C.c_double
-    f.argtypes = [C.c_int, _dp, C.c_double, C.c_double, C.c_double, _dp, C.c_int, C.c_int,
-                  C.c_int, _dp, _dp]
-    c = f(nb, _ptr(wl, _dp), theta_sun, theta_view, h_tide, _ptr(r, _dp), R, origin, n_bottoms,
-          _ptr(p, _dp), _ptr(det, _dp))
-    return c, det
+    f.argtypes = [C.c_int, _dp, _dp, C.c_double, C.c_double, _dp, C.c_int, C.c_int, C.c_int,
+                  C.c_int, _dp, _dp, _dp]
+    c = f(nb, _ptr(wl, _dp), _ptr(th, _dp), theta_view, h_tide, _ptr(r, _dp), R, S, origin,
+          n_bottoms, _ptr(p, _dp), _ptr(det, _dp), _ptr(rm, _dp))
+    return c, det, rm
 
 
 

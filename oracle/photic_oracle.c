@@ -1148,68 +1148,92 @@ int po_depth_sigma(int n_bands, const double *wl, double theta_sun_deg, double t
   return 0;
 }
 
-/* ---- spatial regions and bottom mixtures (model/samodel.c:2957-3027) ----
- * Each pixel is fitted alone (n_spatial = 1) or together with its 3 x 3
- * neighbourhood (n_spatial = 2: indexes clamped at the grid's edges,
- * neighbours with a nodata band left out; smoothing radius 1).  Every region
- * has its own depth and, for each of the n_bottoms bottom types (sand,
- * seagrass, coral: the first entries of the reference's bottom table,
- * model/samodel.c:464-475), its own albedo and mixing weight q; the scene's
- * P, G, X are shared; the cost adds the depth- and bottom-continuity terms
- * (model/samodel.c:2594-2692).  One scene.  With an empirical depth the
- * pixel takes that single depth start, and a pixel deeper than 8 m is
- * fitted with sand alone (model/samodel.c:1781, 1826-1830, 2208-2231; the
- * reference's reduction to sand then stays in its per-thread model_data for
- * the thread's later pixels, an order dependence not reproduced: here the
- * rule applies pixel by pixel). */
+/* ---- regions, bottom mixtures and scenes (model/samodel.c:1768-2115) ----
+ * The general fit of samodel_optimise: each pixel alone (n_spatial = 1) or
+ * together with its 3 x 3 neighbourhood (n_spatial = 2; extract_Rrs_data,
+ * model/samodel.c:2957-3027: indexes clamped at the grid's edges,
+ * neighbours with a nodata band in any scene left out; smoothing radius 1),
+ * over n_scenes scenes of the same bands (each with its own sun zenith),
+ * with n_bottoms bottom types (sand, seagrass, coral: the first entries of
+ * the reference's bottom table, model/samodel.c:464-475).  Every region has
+ * its own depth and, per bottom type, its own albedo and mixing weight q;
+ * every scene its own P, G, X; the cost adds the depth- and
+ * bottom-continuity terms (model/samodel.c:2594-2692).  With an empirical
+ * depth the pixel takes that single depth start, and a pixel deeper than
+ * 8 m is fitted with sand alone (model/samodel.c:1781, 1826-1830,
+ * 2208-2231; the bottom-type count is restored after the pixel,
+ * model/samodel.c:2104). */
 #define PO_MAX_REGIONS 9
 #define PO_MAX_MIX 3
 
 typedef struct {
-  int R, origin, n_bands, nb;
-  const po_scene *sc;
-  double rrs[PO_MAX_REGIONS][PO_MAX_BANDS];
-  double r440[PO_MAX_REGIONS], r490[PO_MAX_REGIONS], r550[PO_MAX_REGIONS];
-  double r640[PO_MAX_REGIONS], r750[PO_MAX_REGIONS];
-  double K[PO_MAX_BANDS]; /* md->K[scene][band]: the last region's */
-  double rrs_mod[PO_MAX_REGIONS][PO_MAX_BANDS], rrs_bot[PO_MAX_REGIONS][PO_MAX_BANDS];
+  int R, S, origin, n_bands, nb;
+  const po_scene *sc[PO_MAX_SCENES];
+  double rrs[PO_MAX_REGIONS][PO_MAX_SCENES][PO_MAX_BANDS];
+  double r440[PO_MAX_REGIONS][PO_MAX_SCENES], r490[PO_MAX_REGIONS][PO_MAX_SCENES];
+  double r550[PO_MAX_REGIONS][PO_MAX_SCENES], r640[PO_MAX_REGIONS][PO_MAX_SCENES];
+  double r750[PO_MAX_REGIONS][PO_MAX_SCENES];
+  double K[PO_MAX_SCENES][PO_MAX_BANDS]; /* md->K[scene][band]: the last region's */
+  double rrs_mod[PO_MAX_REGIONS][PO_MAX_SCENES][PO_MAX_BANDS];
+  double rrs_bot[PO_MAX_REGIONS][PO_MAX_SCENES][PO_MAX_BANDS];
   double bottom_albedo, rrs_error, model_error;
 } po_rpixel;
 
-static int region_n_params(const po_rpixel *px) { return px->R + 2 * px->nb * px->R + 3; }
+static int region_n_params(const po_rpixel *px) {
+  return px->R + 2 * px->nb * px->R + 3 * px->S; /* model/samodel.c:1806-1855 */
+}
 
-/* samodel_error with R regions, nb bottom types, one scene; parameters
+static double k_penalty(double H, double K_min) {
+  const double mean_c = 0.275, min_c = 0.185;
+  double K_error = 0.0;
+  if (H < 1.0 && K_min < mean_c) {
+    K_error += 100.0 * pow(1.0 / (0.01 + K_min) - 1.0 / (0.01 + min_c), 2);
+  } else if (H < 2.0 && K_min < 0.5 * (1.5 * min_c + 0.5 * mean_c)) {
+    K_error += 100.0 * pow(1.0 / (0.01 + K_min) - 1.0 / (0.01 + 0.5 * (1.5 * min_c + 0.5 * mean_c)), 2);
+  } else if (H < 3.0 && K_min < 0.5 * (1.25 * min_c + 0.75 * mean_c)) {
+    K_error += 100.0 * pow(1.0 / (0.01 + K_min) - 1.0 / (0.01 + 0.5 * (1.25 * min_c + 0.75 * mean_c)), 2);
+  } else if (H < 4.0 && K_min < 0.5 * (1.5 * min_c + 0.5 * mean_c)) {
+    K_error += 100.0 * pow(1.0 / (0.01 + K_min) - 1.0 / (0.01 + 0.5 * (1.5 * min_c + 0.5 * mean_c)), 2);
+  } else if (H < 5.0 && K_min < 0.5 * (1.75 * min_c + 0.25 * mean_c)) {
+    K_error += 100.0 * pow(1.0 / (0.01 + K_min) - 1.0 / (0.01 + 0.5 * (1.75 * min_c + 0.25 * mean_c)), 2);
+  }
+  return K_error;
+}
+
+/* samodel_error with R regions, S scenes and nb bottom types; parameters
  * [H_r | 100 B_{r,k} at R + r nb + k | q_{r,k} at R + R nb + r nb + k |
- *  100 P, 100 G, 100 X] (model/samodel.c:2463-2491). */
+ *  100 P_s, 100 G_s, 100 X_s at R + 2 nb R + 3 s] (model/samodel.c:2463-2491). */
 static double region_cost(const double *x, void *ctx) {
   po_rpixel *px = (po_rpixel *)ctx;
-  const po_scene *sc = px->sc;
-  const int R = px->R, nb = px->nb, qo = R + R * nb, off = R + 2 * nb * R;
+  const int R = px->R, S = px->S, nb = px->nb, qo = R + R * nb, off = R + 2 * nb * R;
   double err = 0.0, tot = 0.0, rrs_error, depth_mean, th, error_depth, n_out, bottom_mean,
          bottom_total, error_bottom, H, K_error, K_min = 1.0e4, model;
-  int r, b, k, kb, nobs = 0;
+  int r, s, b, k, kb, nobs = 0;
   for (r = 0; r < R; r++) {
-    double Hr = fabs(x[r]), P = 0.01 * fabs(x[off]), G = 0.01 * fabs(x[off + 1]),
-           X = 0.01 * fabs(x[off + 2]), B[PO_MAX_MIX], q[PO_MAX_MIX], q_sum = 0.0;
-    for (k = 0; k < nb; k++) B[k] = 0.01 * fabs(x[R + r * nb + k]);
-    for (k = 0; k < nb; k++) {
-      q[k] = fabs(x[qo + r * nb + k]);
-      q_sum += q[k];
-    }
-    for (k = 0; k < nb; k++) q[k] /= q_sum;
-    for (b = 0; b < px->n_bands; b++) {
-      double rho = 0.0, albedo = 0.0, Rm, d;
-      for (k = 0; k < nb; k++) { /* model/samodel.c:2878-2883 */
-        albedo += q[k] * B[k];
-        rho += q[k] * B[k] * sc->refl[k][b];
+    for (s = 0; s < S; s++) {
+      const po_scene *sc = px->sc[s];
+      double Hr = fabs(x[r]), P = 0.01 * fabs(x[off + 3 * s]), G = 0.01 * fabs(x[off + 1 + 3 * s]),
+             X = 0.01 * fabs(x[off + 2 + 3 * s]), B[PO_MAX_MIX], q[PO_MAX_MIX], q_sum = 0.0;
+      for (k = 0; k < nb; k++) B[k] = 0.01 * fabs(x[R + r * nb + k]);
+      for (k = 0; k < nb; k++) {
+        q[k] = fabs(x[qo + r * nb + k]);
+        q_sum += q[k];
       }
-      px->bottom_albedo = albedo;
-      Rm = hope_band(sc, b, P, G, X, rho, Hr, 0.0, px->r440[r], px->r490[r], &px->K[b],
-                     &px->rrs_bot[r][b], &px->rrs_mod[r][b]);
-      d = Rm - px->rrs[r][b];
-      err += pow(d, 2.0);
-      tot += px->rrs[r][b];
-      nobs++;
+      for (k = 0; k < nb; k++) q[k] /= q_sum;
+      for (b = 0; b < px->n_bands; b++) {
+        double rho = 0.0, albedo = 0.0, Rm, d;
+        for (k = 0; k < nb; k++) { /* model/samodel.c:2878-2883 */
+          albedo += q[k] * B[k];
+          rho += q[k] * B[k] * sc->refl[k][b];
+        }
+        px->bottom_albedo = albedo;
+        Rm = hope_band(sc, b, P, G, X, rho, Hr, 0.0, px->r440[r][s], px->r490[r][s],
+                       &px->K[s][b], &px->rrs_bot[r][s][b], &px->rrs_mod[r][s][b]);
+        d = Rm - px->rrs[r][s][b];
+        err += pow(d, 2.0);
+        tot += px->rrs[r][s][b];
+        nobs++;
+      }
     }
   }
   rrs_error = 100.0 * sqrt(err / (double)nobs) / (tot / (double)nobs);
@@ -1262,45 +1286,35 @@ static double region_cost(const double *x, void *ctx) {
     bottom_mean = bottom_total / ((double)nb);
     error_bottom = 100.0 * sqrt(error_bottom / n_out) / bottom_mean;
   }
-  /* K penalties on the origin's depth and the scene's K (the last region's
-   * bands), model/samodel.c:2696-2732 */
-  {
-    const double mean_c = 0.275, min_c = 0.185;
-    H = fabs(x[px->origin]);
-    K_error = 0.0;
+  /* K penalties on the origin's depth and each scene's K (the last region's
+   * bands); the very-high-K term on the last scene's, model/samodel.c:2696-2732 */
+  H = fabs(x[px->origin]);
+  K_error = 0.0;
+  for (s = 0; s < S; s++) {
     K_min = 1.0e4;
     for (b = 0; b < px->n_bands; b++)
-      if (!f_close((float)px->K[b], 0.0f, 1.0e-6f) && px->K[b] < K_min) K_min = px->K[b];
-    if (H < 1.0 && K_min < mean_c) {
-      K_error += 100.0 * pow(1.0 / (0.01 + K_min) - 1.0 / (0.01 + min_c), 2);
-    } else if (H < 2.0 && K_min < 0.5 * (1.5 * min_c + 0.5 * mean_c)) {
-      K_error += 100.0 * pow(1.0 / (0.01 + K_min) - 1.0 / (0.01 + 0.5 * (1.5 * min_c + 0.5 * mean_c)), 2);
-    } else if (H < 3.0 && K_min < 0.5 * (1.25 * min_c + 0.75 * mean_c)) {
-      K_error += 100.0 * pow(1.0 / (0.01 + K_min) - 1.0 / (0.01 + 0.5 * (1.25 * min_c + 0.75 * mean_c)), 2);
-    } else if (H < 4.0 && K_min < 0.5 * (1.5 * min_c + 0.5 * mean_c)) {
-      K_error += 100.0 * pow(1.0 / (0.01 + K_min) - 1.0 / (0.01 + 0.5 * (1.5 * min_c + 0.5 * mean_c)), 2);
-    } else if (H < 5.0 && K_min < 0.5 * (1.75 * min_c + 0.25 * mean_c)) {
-      K_error += 100.0 * pow(1.0 / (0.01 + K_min) - 1.0 / (0.01 + 0.5 * (1.75 * min_c + 0.25 * mean_c)), 2);
-    }
-    if (K_min > 0.7) K_error += 100.0 * pow(4.0 * (K_min - 0.7), 2);
+      if (!f_close((float)px->K[s][b], 0.0f, 1.0e-6f) && px->K[s][b] < K_min) K_min = px->K[s][b];
+    K_error += k_penalty(H, K_min);
   }
+  if (K_min > 0.7) K_error += 100.0 * pow(4.0 * (K_min - 0.7), 2);
   model = 80.0 * rrs_error + 15.0 * error_depth + 10.0 * error_bottom + 15.0 * K_error;
   model /= 80.0 + 15.0 + 10.0 + 15.0;
   px->model_error = model;
   return model;
 }
 
-/* Cold start for R regions and nb bottom types (model/samodel.c:2249-2353). */
+/* Cold start (model/samodel.c:2249-2353). */
 static void region_cold_start(const po_rpixel *px, double H0, double *start, double *step) {
-  const int R = px->R, nb = px->nb, off = R + 2 * nb * R;
-  double m490 = 0.0, m550 = 0.0, m640 = 0.0;
-  int r, k;
+  const int R = px->R, S = px->S, nb = px->nb, off = R + 2 * nb * R;
+  double m490 = 0.0, m550, m640;
+  int r, s, k;
   for (r = 0; r < R; r++) {
     start[r] = H0;
     step[r] = 1.25 * start[r];
   }
-  for (r = 0; r < R; r++) m490 += px->r490[r];
-  m490 /= (double)R * 1;
+  for (r = 0; r < R; r++)
+    for (s = 0; s < S; s++) m490 += px->r490[r][s];
+  m490 /= (double)R * S;
   for (k = 0; k < nb; k++)
     for (r = 0; r < R; r++) {
       start[R + r * nb + k] = 100.0 * 4.0 * m490;
@@ -1311,42 +1325,52 @@ static void region_cold_start(const po_rpixel *px, double H0, double *start, dou
       start[R + nb * R + r * nb + k] = 1.0;
       step[R + nb * R + r * nb + k] = 0.5 * start[R + nb * R + r * nb + k];
     }
-  m490 = 0.0;
-  for (r = 0; r < R; r++) {
-    m490 += px->r490[r];
-    m550 += px->r550[r];
-    m640 += px->r640[r];
+  for (s = 0; s < S; s++) {
+    m490 = 0.0;
+    m550 = 0.0;
+    m640 = 0.0;
+    for (r = 0; r < R; r++) {
+      m490 += px->r490[r][s];
+      m550 += px->r550[r][s];
+      m640 += px->r640[r][s];
+    }
+    m490 /= (double)R;
+    m550 /= (double)R;
+    m640 /= (double)R;
+    start[off + 3 * s] = 100.0 * 0.072 * pow(m490 / m550, -1.7);
+    start[off + 1 + 3 * s] = 1.5 * start[off + 3 * s];
+    start[off + 2 + 3 * s] = 100.0 * 30.0 * px->sc[s]->aw640 * m640;
+    step[off + 3 * s] = 2.0 * start[off + 3 * s];
+    step[off + 1 + 3 * s] = 2.0 * start[off + 1 + 3 * s];
+    step[off + 2 + 3 * s] = 2.0 * start[off + 2 + 3 * s];
   }
-  m490 /= (double)R;
-  m550 /= (double)R;
-  m640 /= (double)R;
-  start[off] = 100.0 * 0.072 * pow(m490 / m550, -1.7);
-  start[off + 1] = 1.5 * start[off];
-  start[off + 2] = 100.0 * 30.0 * px->sc->aw640 * m640;
-  step[off] = 2.0 * start[off];
-  step[off + 1] = 2.0 * start[off + 1];
-  step[off + 2] = 2.0 * start[off + 2];
+}
+
+static void region_reference_rrs(po_rpixel *px) {
+  int r, s;
+  for (r = 0; r < px->R; r++) /* model/samodel.c:1785-1799 */
+    for (s = 0; s < px->S; s++) {
+      const double *wl = px->sc[s]->wl;
+      px->r440[r][s] = po_interp_1d(wl, px->rrs[r][s], px->n_bands, 440.0);
+      px->r490[r][s] = po_interp_1d(wl, px->rrs[r][s], px->n_bands, 490.0);
+      px->r550[r][s] = po_interp_1d(wl, px->rrs[r][s], px->n_bands, 550.0);
+      px->r640[r][s] = po_interp_1d(wl, px->rrs[r][s], px->n_bands, 640.0);
+      px->r750[r][s] = po_interp_1d(wl, px->rrs[r][s], px->n_bands, 750.0);
+      if (px->r440[r][s] < 0.0) px->r440[r][s] = 0.0001;
+    }
 }
 
 /* samodel_optimise for one pixel's regions (model/samodel.c:1768-2115):
  * depth starts, nelmin, early exit, the final re-evaluation and the post-fit
  * products.  h_emp: the empirical depth, or NaN for the 8 cold starts. */
 static void region_fit(po_rpixel *px, const po_fit *fit, double h_emp, double *o) {
-  const int R = px->R, n = region_n_params(px), nb = px->nb;
+  const int R = px->R, S = px->S, n = region_n_params(px), nb = px->nb, off = R + 2 * nb * R;
   double start[PO_MAX_PARAMS], step[PO_MAX_PARAMS], xm[PO_MAX_PARAMS], best[PO_MAX_PARAMS];
   double lowest = 1.0e4, y = 0.0;
-  int icount = 0, numres = 0, ifault = 0, k, r, b, nst;
+  int icount = 0, numres = 0, ifault = 0, k, r, s, b, nst;
   long total = 0;
   int kept_evals = 0, kept_res = 0, kept_start = 0, kept_fault = 0, converged = 0;
-  for (r = 0; r < R; r++) { /* model/samodel.c:1785-1799 */
-    const double *wl = px->sc->wl;
-    px->r440[r] = po_interp_1d(wl, px->rrs[r], px->n_bands, 440.0);
-    px->r490[r] = po_interp_1d(wl, px->rrs[r], px->n_bands, 490.0);
-    px->r550[r] = po_interp_1d(wl, px->rrs[r], px->n_bands, 550.0);
-    px->r640[r] = po_interp_1d(wl, px->rrs[r], px->n_bands, 640.0);
-    px->r750[r] = po_interp_1d(wl, px->rrs[r], px->n_bands, 750.0);
-    if (px->r440[r] < 0.0) px->r440[r] = 0.0001;
-  }
+  region_reference_rrs(px);
   memset(best, 0, sizeof best);
   nst = isnan(h_emp) ? fit->n_hstarts : 1;
   for (k = 0; k < nst; k++) {
@@ -1362,7 +1386,7 @@ static void region_fit(po_rpixel *px, const po_fit *fit, double h_emp, double *o
       kept_start = k;
       kept_fault = ifault;
       converged = (ifault == 0);
-      if (lowest < 2.5 * ((float)1)) break; /* model/samodel.c:2404 */
+      if (lowest < 2.5 * ((float)S)) break; /* model/samodel.c:2404 */
     }
   }
   region_cost(best, px);
@@ -1370,11 +1394,12 @@ static void region_fit(po_rpixel *px, const po_fit *fit, double h_emp, double *o
     double K_min = 1.0e10, iod = 0.0, nobs = 0.0, depth = 0.0, ow = sqrt((double)R);
     double q_sum = 0.0, pct[PO_MAX_MIX], largest = 0.0, type = 0.0;
     int found = 0;
-    for (b = 0; b < px->n_bands; b++)
-      if (!f_close((float)px->K[b], (float)0.0, 1.0e-4f) && px->K[b] < K_min) {
-        K_min = px->K[b];
-        found = 1;
-      }
+    for (s = 0; s < S; s++) /* array_min_double2 over md->K, model/samodel.c:1994 */
+      for (b = 0; b < px->n_bands; b++)
+        if (!f_close((float)px->K[s][b], (float)0.0, 1.0e-4f) && px->K[s][b] < K_min) {
+          K_min = px->K[s][b];
+          found = 1;
+        }
     if (!found) K_min = 0.0;
     for (r = 0; r < R; r++) { /* origin-weighted depth, model/samodel.c:1999-2017 */
       double H = fabs(best[r]);
@@ -1391,11 +1416,12 @@ static void region_fit(po_rpixel *px, const po_fit *fit, double h_emp, double *o
         largest = pct[k];
         type = 1.0 + k;
       }
-    for (r = 0; r < R; r++)
-      for (b = 0; b < px->n_bands; b++) {
-        iod += px->rrs_bot[r][b] / px->rrs_mod[r][b];
-        nobs += 1.0;
-      }
+    for (s = 0; s < S; s++) /* model/samodel.c:2051-2064 */
+      for (r = 0; r < R; r++)
+        for (b = 0; b < px->n_bands; b++) {
+          iod += px->rrs_bot[r][s][b] / px->rrs_mod[r][s][b];
+          nobs += 1.0;
+        }
     iod = 100.0 * iod / nobs;
     o[0] = depth;
     o[1] = px->bottom_albedo;
@@ -1410,10 +1436,12 @@ static void region_fit(po_rpixel *px, const po_fit *fit, double h_emp, double *o
   o[7] = (double)total;
   o[8] = converged ? 1.0 : 0.0;
   o[9] = 0.0;
-  o[10] = 1.0;
-  o[11] = 0.01 * fabs(best[R + 2 * nb * R]);
-  o[19] = 0.01 * fabs(best[R + 2 * nb * R + 1]);
-  o[27] = 0.01 * fabs(best[R + 2 * nb * R + 2]);
+  o[10] = (double)S;
+  for (s = 0; s < S; s++) {
+    o[11 + s] = 0.01 * fabs(best[off + 3 * s]);
+    o[19 + s] = 0.01 * fabs(best[off + 1 + 3 * s]);
+    o[27 + s] = 0.01 * fabs(best[off + 2 + 3 * s]);
+  }
   o[35] = (double)kept_res;
   o[36] = (double)kept_start;
   o[37] = (double)kept_fault;
@@ -1421,18 +1449,21 @@ static void region_fit(po_rpixel *px, const po_fit *fit, double h_emp, double *o
   o[39] = (double)px->origin;
 }
 
-int po_region_fit_batch(int n_bands, const double *wl, double theta_sun_deg,
-                        double theta_view_deg, double h_tide, const float *grid, int nrows,
-                        int ncols, float nodata, int n_spatial, int n_bottoms,
+/* grid: [n_scenes][nrows][ncols][n_bands]; theta_sun_deg: [n_scenes]. */
+int po_region_fit_batch(int n_bands, const double *wl, const double *theta_sun_deg,
+                        double theta_view_deg, double h_tide, const float *grid, int n_scenes,
+                        int nrows, int ncols, float nodata, int n_spatial, int n_bottoms,
                         const double *h_empirical, double reqmin, int konvge, int kcount,
                         int nthreads, double *out) {
-  po_scene sc;
+  po_scene sc[PO_MAX_SCENES];
   po_fit fit;
   int64_t p, npix = (int64_t)nrows * ncols;
+  int s;
   if (n_bands < 2 || n_bands > PO_MAX_BANDS || n_spatial < 1 || n_spatial > 2 ||
-      n_bottoms < 1 || n_bottoms > PO_MAX_MIX)
+      n_bottoms < 1 || n_bottoms > PO_MAX_MIX || n_scenes < 1 || n_scenes > PO_MAX_SCENES)
     return 1;
-  scene_init(&sc, n_bands, wl, theta_sun_deg, theta_view_deg, h_tide);
+  for (s = 0; s < n_scenes; s++)
+    scene_init(&sc[s], n_bands, wl, theta_sun_deg[s], theta_view_deg, h_tide);
   fit.seed_step_scale = 1.0;
   fit.reqmin = reqmin;
   fit.konvge = konvge;
@@ -1449,16 +1480,19 @@ int po_region_fit_batch(int n_bands, const double *wl, double theta_sun_deg,
     double *o = out + p * PO_NOUT;
     double h_emp = NAN;
     po_rpixel px;
-    int ii, jj, b;
+    int ii, jj, b, sk, bad = 0;
     memset(o, 0, PO_NOUT * sizeof(double));
-    if (masked(grid + p * n_bands, n_bands, nodata)) {
+    for (sk = 0; sk < n_scenes && !bad; sk++) /* model/samodel.c:933-947 */
+      bad = masked(grid + ((int64_t)sk * npix + p) * n_bands, n_bands, nodata);
+    if (bad) {
       o[9] = 1.0;
       continue;
     }
     memset(&px, 0, sizeof px);
-    px.sc = &sc;
     px.n_bands = n_bands;
     px.nb = n_bottoms;
+    px.S = n_scenes;
+    for (sk = 0; sk < n_scenes; sk++) px.sc[sk] = &sc[sk];
     if (h_empirical && !isnan(h_empirical[p])) {
       h_emp = h_empirical[p];
       if (h_emp > 8.0) px.nb = 1; /* model/samodel.c:1781, 1826-1830 */
@@ -1468,14 +1502,16 @@ int po_region_fit_batch(int n_bands, const double *wl, double theta_sun_deg,
       const int iii = i + ii < 0 ? 0 : (i + ii > nrows - 1 ? nrows - 1 : i + ii);
       for (jj = -w; jj <= w; jj++) {
         const int jjj = j + jj < 0 ? 0 : (j + jj > ncols - 1 ? ncols - 1 : j + jj);
-        const float *q = grid + ((int64_t)iii * ncols + jjj) * n_bands;
         int nodata_region = 0;
-        for (b = 0; b < n_bands; b++) {
-          if (!f_close(q[b], nodata, 1.0e-6f)) {
-            px.rrs[px.R][b] = q[b];
-          } else {
-            nodata_region = 1;
-            break;
+        for (sk = 0; sk < n_scenes && !nodata_region; sk++) {
+          const float *q = grid + ((int64_t)sk * npix + (int64_t)iii * ncols + jjj) * n_bands;
+          for (b = 0; b < n_bands; b++) {
+            if (!f_close(q[b], nodata, 1.0e-6f)) {
+              px.rrs[px.R][sk][b] = q[b];
+            } else {
+              nodata_region = 1;
+              break;
+            }
           }
         }
         if (i == iii && j == jjj) px.origin = px.R;
@@ -1492,38 +1528,42 @@ int po_region_invert_batch(int n_bands, const double *wl, double theta_sun_deg,
                            double theta_view_deg, double h_tide, const float *grid, int nrows,
                            int ncols, float nodata, double reqmin, int konvge, int kcount,
                            int nthreads, double *out) {
-  return po_region_fit_batch(n_bands, wl, theta_sun_deg, theta_view_deg, h_tide, grid, nrows,
+  return po_region_fit_batch(n_bands, wl, &theta_sun_deg, theta_view_deg, h_tide, grid, 1, nrows,
                              ncols, nodata, 2, 1, NULL, reqmin, konvge, kcount, nthreads, out);
 }
 
 /* Cost, with its side outputs, of one explicit parameter vector for a pixel
- * given as its regions' spectra (rrs [R][n_bands], origin region, nb bottom
- * types): samodel_error (model/samodel.c:2432-2759) for samodel_error's
- * drop-in test.  Outputs: cost; details[5] = Rrs error, model error,
- * bottom albedo, K_min (last region's bands), 0. */
-double po_region_cost(int n_bands, const double *wl, double theta_sun_deg,
-                      double theta_view_deg, double h_tide, const double *rrs, int R, int origin,
-                      int n_bottoms, const double *params, double *details) {
-  po_scene sc;
+ * given as its regions' spectra (rrs [R][S][n_bands], origin region, nb
+ * bottom types, one sun zenith per scene): samodel_error
+ * (model/samodel.c:2432-2759).  details[5] = Rrs error, model error, bottom
+ * albedo, the last scene's K_min (the cost's test), 0; rm [R][S][n_bands]
+ * (optional) the modelled Rrs. */
+double po_region_cost(int n_bands, const double *wl, const double *theta_sun_deg,
+                      double theta_view_deg, double h_tide, const double *rrs, int R, int S,
+                      int origin, int n_bottoms, const double *params, double *details,
+                      double *rm) {
+  po_scene sc[PO_MAX_SCENES];
   po_rpixel px;
-  int r, b;
+  int r, s, b;
   double c, K_min = 1.0e4;
-  scene_init(&sc, n_bands, wl, theta_sun_deg, theta_view_deg, h_tide);
   memset(&px, 0, sizeof px);
-  px.sc = &sc;
+  for (s = 0; s < S; s++) {
+    scene_init(&sc[s], n_bands, wl, theta_sun_deg[s], theta_view_deg, h_tide);
+    px.sc[s] = &sc[s];
+  }
   px.n_bands = n_bands;
   px.nb = n_bottoms;
   px.R = R;
+  px.S = S;
   px.origin = origin;
-  for (r = 0; r < R; r++) {
-    for (b = 0; b < n_bands; b++) px.rrs[r][b] = rrs[r * n_bands + b];
-    px.r440[r] = po_interp_1d(sc.wl, px.rrs[r], n_bands, 440.0);
-    px.r490[r] = po_interp_1d(sc.wl, px.rrs[r], n_bands, 490.0);
-    if (px.r440[r] < 0.0) px.r440[r] = 0.0001;
-  }
+  for (r = 0; r < R; r++)
+    for (s = 0; s < S; s++)
+      for (b = 0; b < n_bands; b++) px.rrs[r][s][b] = rrs[(r * S + s) * n_bands + b];
+  region_reference_rrs(&px);
   c = region_cost(params, &px);
   for (b = 0; b < n_bands; b++)
-    if (!f_close((float)px.K[b], 0.0f, 1.0e-6f) && px.K[b] < K_min) K_min = px.K[b];
+    if (!f_close((float)px.K[S - 1][b], 0.0f, 1.0e-6f) && px.K[S - 1][b] < K_min)
+      K_min = px.K[S - 1][b];
   if (details) {
     details[0] = px.rrs_error;
     details[1] = px.model_error;
@@ -1531,6 +1571,13 @@ double po_region_cost(int n_bands, const double *wl, double theta_sun_deg,
     details[3] = K_min;
     details[4] = 0.0;
   }
+  if (rm)
+    for (r = 0; r < R; r++)
+      for (s = 0; s < S; s++)
+        for (b = 0; b < n_bands; b++) {
+          const double rr = px.rrs_mod[r][s][b];
+          rm[(r * S + s) * n_bands + b] = 0.5 * rr / (1.0 - 1.5 * rr);
+        }
   return c;
 }
 

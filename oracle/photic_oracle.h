@@ -25,7 +25,7 @@
 
 #define PO_MAX_BANDS 8
 #define PO_MAX_SCENES 8
-#define PO_MAX_PARAMS 72
+#define PO_MAX_PARAMS 96
 #define PO_N_BOTTOM_TYPES 8
 #define PO_NOUT 44
 
@@ -83,14 +83,15 @@ int po_region_invert_batch(int n_bands, const double *wl, double theta_sun_deg,
                            double theta_view_deg, double h_tide, const float *grid, int nrows,
                            int ncols, float nodata, double reqmin, int konvge, int kcount,
                            int nthreads, double *out);
-int po_region_fit_batch(int n_bands, const double *wl, double theta_sun_deg,
-                        double theta_view_deg, double h_tide, const float *grid, int nrows,
-                        int ncols, float nodata, int n_spatial, int n_bottoms,
+int po_region_fit_batch(int n_bands, const double *wl, const double *theta_sun_deg,
+                        double theta_view_deg, double h_tide, const float *grid, int n_scenes,
+                        int nrows, int ncols, float nodata, int n_spatial, int n_bottoms,
                         const double *h_empirical, double reqmin, int konvge, int kcount,
                         int nthreads, double *out);
-double po_region_cost(int n_bands, const double *wl, double theta_sun_deg,
-                      double theta_view_deg, double h_tide, const double *rrs, int R, int origin,
-                      int n_bottoms, const double *params, double *details);
+double po_region_cost(int n_bands, const double *wl, const double *theta_sun_deg,
+                      double theta_view_deg, double h_tide, const double *rrs, int R, int S,
+                      int origin, int n_bottoms, const double *params, double *details,
+                      double *rm);
 int po_depth_sigma(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
                    const float *rrs, int64_t npix, const float *depth, const double *r_sigma,
                    int n_samples, uint64_t seed, double reqmin, int konvge, int kcount,

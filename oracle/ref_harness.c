@@ -328,43 +328,51 @@ int photic_ref_joint_invert_batch(int n_bands, const double *wl, double theta_vi
   return 0;
 }
 
-/* Spatial-region fit (n_spatial = 2: the 3 x 3 neighbourhood of each pixel,
- * edges clamped, neighbours with nodata left out; n_spatial = 1: the pixel
- * alone; model/samodel.c:2957-3027) with n_bottoms bottom types (the first
- * entries of the bottom table, all at once as ALL_BOTTOMS selects,
- * model/samodel.c:1822-1858), through the reference's own extract_Rrs_data
- * and samodel_optimise, one scene, smoothing radius 1.  grid is
- * [nrows][ncols][n_bands] float; h_empirical (NULL, or [npix] with NaN for
- * none) gives a pixel's empirical depth as samodel() sets it
+/* The general fit of samodel()'s pixel loop through the reference's own
+ * extract_Rrs_data and samodel_optimise: each pixel alone (n_spatial = 1)
+ * or with its 3 x 3 neighbourhood (n_spatial = 2: edges clamped, neighbours
+ * with nodata left out; model/samodel.c:2957-3027), over n_scenes scenes of
+ * the same bands (sun zenith theta_sun_deg[s]), with n_bottoms bottom types
+ * (the first entries of the bottom table, all at once as ALL_BOTTOMS
+ * selects, model/samodel.c:1822-1858), smoothing radius 1.  grid is
+ * [n_scenes][nrows][ncols][n_bands] float; h_empirical (NULL, or [npix]
+ * with NaN for none) gives a pixel's empirical depth as samodel() sets it
  * (model/samodel.c:958-967).  out is [npix][REF_NOUT] with o[38] = regions,
  * o[39] = origin region, o[40..42] = B_type_percent of sand, seagrass and
  * coral, o[43] = bottom_type. */
-int photic_ref_region_fit_batch(int n_bands, const double *wl, double theta_sun_deg,
+int photic_ref_region_fit_batch(int n_bands, const double *wl, const double *theta_sun_deg,
                                 double theta_view_deg, double h_tide, const float *grid,
-                                int nrows, int ncols, float nodata, int n_spatial, int n_bottoms,
-                                const double *h_empirical, int use_override, double reqmin,
-                                int konvge, int kcount, int nthreads, double *out) {
+                                int n_scenes, int nrows, int ncols, float nodata, int n_spatial,
+                                int n_bottoms, const double *h_empirical, int use_override,
+                                double reqmin, int konvge, int kcount, int nthreads,
+                                double *out) {
   geogrid *gd;
   scene *sc;
-  int b, R;
+  int b, s, R, scene_indexes[REF_MAX_SCENES];
+  const long long npix = (long long)nrows * ncols;
   if (n_bands < 2 || n_bands > REF_MAX_BANDS || n_spatial < 1 || n_spatial > 2 ||
-      n_bottoms < 1 || n_bottoms > 3)
+      n_bottoms < 1 || n_bottoms > 3 || n_scenes < 1 || n_scenes > REF_MAX_SCENES)
     return 1;
   R = (2 * n_spatial - 1) * (2 * n_spatial - 1);
-  gd = (geogrid *)calloc(n_bands, sizeof(geogrid));
-  sc = (scene *)calloc(1, sizeof(scene));
-  sc->n_bands = n_bands;
-  sc->nrows = nrows;
-  sc->ncols = ncols;
-  for (b = 0; b < n_bands; b++) {
-    int i, j;
-    sc->band_indexes[b] = b;
-    gd[b].nrows = nrows;
-    gd[b].ncols = ncols;
-    gd[b].nodata_value = nodata;
-    allocate_float_array_2d(&gd[b].array, nrows, ncols);
-    for (i = 0; i < nrows; i++)
-      for (j = 0; j < ncols; j++) gd[b].array[i][j] = grid[((size_t)i * ncols + j) * n_bands + b];
+  gd = (geogrid *)calloc((size_t)n_scenes * n_bands, sizeof(geogrid));
+  sc = (scene *)calloc(n_scenes, sizeof(scene));
+  for (s = 0; s < n_scenes; s++) {
+    scene_indexes[s] = s;
+    sc[s].n_bands = n_bands;
+    sc[s].nrows = nrows;
+    sc[s].ncols = ncols;
+    for (b = 0; b < n_bands; b++) {
+      geogrid *g = &gd[s * n_bands + b];
+      int i, j;
+      sc[s].band_indexes[b] = s * n_bands + b;
+      g->nrows = nrows;
+      g->ncols = ncols;
+      g->nodata_value = nodata;
+      allocate_float_array_2d(&g->array, nrows, ncols);
+      for (i = 0; i < nrows; i++)
+        for (j = 0; j < ncols; j++)
+          g->array[i][j] = grid[(((size_t)s * nrows + i) * ncols + j) * n_bands + b];
+    }
   }
 #if _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -372,36 +380,41 @@ int photic_ref_region_fit_batch(int n_bands, const double *wl, double theta_sun_
 #endif
   {
     model_data *md = md_new_r(R);
-    int scene_index = 0;
-    long long p, npix = (long long)nrows * ncols;
-    md_set_scene(md, 0, n_bands, wl, theta_sun_deg, theta_view_deg, h_tide);
+    long long p;
+    int ks;
+    for (ks = 0; ks < n_scenes; ks++)
+      md_set_scene(md, ks, n_bands, wl, theta_sun_deg[ks], theta_view_deg, h_tide);
 #if _OPENMP
 #pragma omp for schedule(dynamic, 4)
 #endif
     for (p = 0; p < npix; p++) {
-      int i = (int)(p / ncols), j = (int)(p % ncols), r, bb;
+      int i = (int)(p / ncols), j = (int)(p % ncols), r, ss, bb, bad = 0;
       double *o = out + p * REF_NOUT;
       memset(o, 0, REF_NOUT * sizeof(double));
-      if (pixel_masked(grid + p * n_bands, n_bands, nodata)) {
+      for (ss = 0; ss < n_scenes && !bad; ss++) /* model/samodel.c:933-947 */
+        bad = pixel_masked(grid + ((size_t)ss * npix + p) * n_bands, n_bands, nodata);
+      if (bad) {
         o[9] = 1.0;
         continue;
       }
-      md_reset_pixel(md, 1, n_bands);
-      for (r = 0; r < R; r++) /* the loop's defaults, model/samodel.c:921-932 */
-        for (bb = 0; bb < n_bands; bb++) {
-          md->Rrs_measured[r][0][bb] = 0.0;
-          md->Rrs_modelled[r][0][bb] = 0.0;
-          md->rrs_modelled[r][0][bb] = 0.0;
-          md->rrs_bottom[r][0][bb] = 0.0;
-          md->rrs_dp[r][0][bb] = 0.0;
-          md->rho[r][0][bb] = 0.0;
-        }
+      md_reset_pixel(md, n_scenes, n_bands);
+      for (r = 0; r < R; r++) /* the loop's defaults, model/samodel.c:917-928 */
+        for (ss = 0; ss < n_scenes; ss++)
+          for (bb = 0; bb < n_bands; bb++) {
+            md->Rrs_measured[r][ss][bb] = 0.0;
+            md->Rrs_modelled[r][ss][bb] = 0.0;
+            md->rrs_modelled[r][ss][bb] = 0.0;
+            md->rrs_bottom[r][ss][bb] = 0.0;
+            md->rrs_dp[r][ss][bb] = 0.0;
+            md->rho[r][ss][bb] = 0.0;
+          }
       md->n_bottoms = n_bottoms;
       if (h_empirical && !isnan(h_empirical[p])) {
         md->empirical_depth_present = true;
         md->h_empirical = h_empirical[p];
       }
-      extract_Rrs_data(i, j, sc, gd, &scene_index, 1, n_spatial, 1, nrows, ncols, md, 0.0);
+      extract_Rrs_data(i, j, sc, gd, scene_indexes, n_scenes, n_spatial, 1, nrows, ncols, md,
+                       0.0);
       if (md->n_regions == 0) continue;
       set_tol(use_override, reqmin, konvge, kcount);
       samodel_optimise(md);
@@ -413,7 +426,7 @@ int photic_ref_region_fit_batch(int n_bands, const double *wl, double theta_sun_
     }
     md_free(md);
   }
-  for (b = 0; b < n_bands; b++) free_float_array_2d(gd[b].array, nrows);
+  for (b = 0; b < n_scenes * n_bands; b++) free_float_array_2d(gd[b].array, nrows);
   free(gd);
   free(sc);
   return 0;
@@ -424,8 +437,8 @@ int photic_ref_region_invert_batch(int n_bands, const double *wl, double theta_s
                                    int nrows, int ncols, float nodata, int n_spatial,
                                    int use_override, double reqmin, int konvge, int kcount,
                                    int nthreads, double *out) {
-  return photic_ref_region_fit_batch(n_bands, wl, theta_sun_deg, theta_view_deg, h_tide, grid,
-                                     nrows, ncols, nodata, n_spatial, 1, NULL, use_override,
+  return photic_ref_region_fit_batch(n_bands, wl, &theta_sun_deg, theta_view_deg, h_tide, grid,
+                                     1, nrows, ncols, nodata, n_spatial, 1, NULL, use_override,
                                      reqmin, konvge, kcount, nthreads, out);
 }
 

@@ -62,6 +62,8 @@ class photic_outputs(C.Structure):
         ("evals_kept", C.c_void_p),
         ("status", C.c_void_p),
         ("params", C.c_void_p),
+        ("bottom_percent", C.c_void_p),
+        ("bottom_type", C.c_void_p),
     ]
 
 
@@ -128,6 +130,12 @@ _SIGS = {
     "photic_region_invert_batch": (C.c_int, [C.POINTER(photic_config), C.c_void_p, C.c_int32,
                                              C.c_int32, C.c_int32, C.POINTER(photic_outputs),
                                              C.c_void_p]),
+    "photic_bottom_reflectances": (C.c_int, [C.POINTER(photic_config), C.c_int32,
+                                             C.POINTER(C.c_double)]),
+    "photic_region_fit_batch": (C.c_int, [C.POINTER(photic_config), C.c_void_p, C.c_int32,
+                                          C.POINTER(C.c_double), C.c_int32, C.c_int32,
+                                          C.c_int32, C.c_int32, C.c_void_p,
+                                          C.POINTER(photic_outputs), C.c_void_p]),
     "photic_depth_sigma": (C.c_int, [C.POINTER(photic_config), C.c_void_p, C.c_int64, C.c_void_p,
                                      C.POINTER(C.c_double), C.c_int32, C.c_uint64, C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

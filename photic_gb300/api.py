@@ -27,6 +27,8 @@ PRECISIONS = {"fp64": L.PREC_FP64, "df64": L.PREC_DF64, "fp32": L.PREC_FP32,
 LAYOUTS = {"reference": L.LAYOUT_REFERENCE, "scene_b": L.LAYOUT_SCENE_B}
 OUTPUT_FIELDS = ("depth", "depth_f64", "P", "G", "X", "bottom_albedo", "model_error",
                  "rrs_error", "K_min", "iod", "evals", "evals_kept", "status", "params")
+# extra outputs of the bottom-mixture fit (region_fit)
+MIX_FIELDS = ("bottom_percent", "bottom_type")
 _DTYPES = {"depth_f64": torch.float64, "evals": torch.int32, "evals_kept": torch.int32,
            "status": torch.int32, "params": torch.float64}
 
@@ -123,6 +125,9 @@ def alloc_outputs(npix: int, device, fields: Sequence[str] = OUTPUT_FIELDS,
             if n_obs is None:
                 out[f] = torch.empty(npix, 6, dtype=torch.float64, device=device)
             continue
+        if f == "bottom_percent":
+            out[f] = torch.empty(npix, 3, dtype=torch.float32, device=device)
+            continue
         n = n_obs if (n_obs is not None and f in ("P", "G", "X")) else npix
         out[f] = torch.empty(n, dtype=_DTYPES.get(f, torch.float32), device=device)
     return out
@@ -130,7 +135,7 @@ def alloc_outputs(npix: int, device, fields: Sequence[str] = OUTPUT_FIELDS,
 
 def _outputs_struct(out: Dict[str, torch.Tensor]) -> L.photic_outputs:
     s = L.photic_outputs()
-    for f in OUTPUT_FIELDS:
+    for f in OUTPUT_FIELDS + MIX_FIELDS:
         setattr(s, f, _ptr(out.get(f)))
     return s
 
@@ -197,6 +202,45 @@ def region_invert(grid: torch.Tensor, config: Optional[Config] = None, *,
     os_ = _outputs_struct(out)
     L.check(L.lib().photic_region_invert_batch(C.byref(c), _ptr(grid), nrows, ncols, 2,
                                                C.byref(os_), _stream_handle(stream)))
+    return out
+
+
+def region_fit(grid: torch.Tensor, config: Optional[Config] = None, *, n_spatial: int = 2,
+               n_bottoms: int = 3, theta_sun: Optional[Sequence[float]] = None,
+               h_empirical: Optional[torch.Tensor] = None,
+               fields: Sequence[str] = OUTPUT_FIELDS + MIX_FIELDS,
+               stream: Optional[torch.cuda.Stream] = None) -> Dict[str, torch.Tensor]:
+    """The reference's default inversion call (model/bam.c:3236-3241 with
+    n_spatial = 2, n_bottoms = 3): every pixel of a [nrows, ncols, n_bands]
+    (one scene) or [n_scenes, nrows, ncols, n_bands] float32 grid, fitted
+    alone (``n_spatial`` = 1) or with its 3 x 3 neighbourhood (2),
+    ``n_bottoms`` bottom types (sand, seagrass, coral) mixed in every region,
+    the scenes jointly (each with its own P, G, X and sun zenith
+    ``theta_sun``, default the config's).  ``h_empirical`` ([nrows * ncols]
+    float64, NaN for none) gives empirical depths (single depth start; deeper
+    than 8 m: sand alone).  Outputs per pixel (P, G, X: [npix, n_scenes]),
+    with ``bottom_percent`` [npix, 3] and ``bottom_type``."""
+    cfg = config or Config()
+    _check_cuda(grid, "grid", torch.float32)
+    g4 = grid if grid.dim() == 4 else grid.unsqueeze(0)
+    if g4.dim() != 4 or g4.shape[3] != cfg.n_bands:
+        raise ValueError(f"grid must be [(n_scenes,) nrows, ncols, {cfg.n_bands}]")
+    S, nrows, ncols = int(g4.shape[0]), int(g4.shape[1]), int(g4.shape[2])
+    if h_empirical is not None:
+        _check_cuda(h_empirical, "h_empirical", torch.float64)
+    out = alloc_outputs(nrows * ncols, grid.device, [f for f in fields if f != "params"],
+                        n_obs=nrows * ncols * S if S > 1 else None)
+    c = cfg.to_c()
+    th = (C.c_double * S)(*([cfg.theta_sun_deg] * S if theta_sun is None else
+                            [float(t) for t in theta_sun]))
+    os_ = _outputs_struct(out)
+    L.check(L.lib().photic_region_fit_batch(C.byref(c), _ptr(g4), S, th, nrows, ncols,
+                                            int(n_spatial), int(n_bottoms), _ptr(h_empirical),
+                                            C.byref(os_), _stream_handle(stream)))
+    if S > 1:
+        for f in ("P", "G", "X"):
+            if f in out:
+                out[f] = out[f].view(nrows * ncols, S)
     return out
 
 

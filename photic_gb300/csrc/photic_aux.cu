@@ -185,8 +185,14 @@ __global__ void forward_kernel(const __grid_constant__ ForwardArgs a) {
   const double qB = x[4] * x[3];
   for (int b = 0; b < a.fp.n_bands; b++) {
     double K, parts[4];
-    const double r = forward_band_f64(a.sc, b, x[0], x[1], x[2], qB, x[5], x[6],
-                                      pow(a.sc.ratio440[b], Y), &K, parts);
+    double rho = qB * a.sc.refl[b];
+    if (a.mix) {  // sum_i q_i B_i rho_i(lambda), model/samodel.c:2878-2883
+      const double *m = a.mix + i * 6;
+      rho = 0.0;
+      for (int k = 0; k < a.n_bottoms; k++) rho += m[3 + k] * m[k] * a.sc.refl_k[k][b];
+    }
+    const double r = forward_band_rho_f64(a.sc, b, x[0], x[1], x[2], rho, x[5], x[6],
+                                          pow(a.sc.ratio440[b], Y), &K, parts);
     a.rrs[i * a.fp.n_bands + b] = r;
     if (a.K) a.K[i * a.fp.n_bands + b] = K;
     if (a.parts)

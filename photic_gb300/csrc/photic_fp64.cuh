@@ -187,11 +187,10 @@ __device__ __forceinline__ void cold_start_f64(const FitParams &fp, const PixelF
 // samodel_Rrs (model/samodel.c:2846-2949) as the reference calls it: the
 // physical parameters as given (fabs only where the reference takes it),
 // Y from the caller's Rrs(440)/Rrs(490).  Returns Rrs; writes K.
-__device__ __forceinline__ double forward_band_f64(const SceneConsts &sc, int b, double P,
-                                                   double G, double X, double qB, double H,
-                                                   double Delta, double pw, double *K_out,
-                                                   double *parts = nullptr) {
-  const double rho = qB * sc.refl[b];
+__device__ __forceinline__ double forward_band_rho_f64(const SceneConsts &sc, int b, double P,
+                                                       double G, double X, double rho, double H,
+                                                       double Delta, double pw, double *K_out,
+                                                       double *parts = nullptr) {
   const double a_phi = (sc.a0[b] + sc.a1[b] * log(fabs(P))) * fabs(P);
   const double a_g = fabs(G) * sc.eS[b];
   const double a = sc.aw[b] + a_phi + a_g;
@@ -216,6 +215,14 @@ __device__ __forceinline__ double forward_band_f64(const SceneConsts &sc, int b,
     parts[3] = rrs;
   }
   return 0.5 * rrs / (1.0 - 1.5 * rrs) + Delta;
+}
+
+// The same with one bottom type: rho = (q B) rho_sand(lambda).
+__device__ __forceinline__ double forward_band_f64(const SceneConsts &sc, int b, double P,
+                                                   double G, double X, double qB, double H,
+                                                   double Delta, double pw, double *K_out,
+                                                   double *parts = nullptr) {
+  return forward_band_rho_f64(sc, b, P, G, X, qB * sc.refl[b], H, Delta, pw, K_out, parts);
 }
 
 // (long)(10 * y) of the local-minimum test (model/asa047.c:438-470).  C

@@ -13,6 +13,7 @@
 
 #include <mutex>
 #include <string>
+#include <algorithm>
 #include <vector>
 
 #include "../../include/photic.h"
@@ -122,6 +123,7 @@ void make_scene(const photic_config &cfg, double theta_sun_deg, SceneConsts &sc)
     sc.bbw[b] = table_at(tables::bbw, l);
     sc.aw[b] = table_at(tables::aw, l);
     sc.refl[b] = table_at(tables::bottom[0], l);
+    for (int k = 0; k < 3; k++) sc.refl_k[k][b] = table_at(tables::bottom[k], l);
     sc.eS[b] = exp(-S * (l - 440.0));
     sc.ratio440[b] = 440.0 / l;
   }
@@ -353,6 +355,17 @@ int photic_band_constants(const photic_config *cfg, double *out) {
     out[b * 8 + 6] = sc.sec_view;
     out[b * 8 + 7] = aw640;
   }
+  return PHOTIC_OK;
+}
+
+int photic_bottom_reflectances(const photic_config *cfg, int32_t n_types, double *out) {
+  int rc = photic_config_check(cfg);
+  if (rc) return rc;
+  if (n_types < 1 || n_types > tables::kNBottom || !out)
+    return fail(PHOTIC_ERR_INVALID, "n_types must be 1..%d", tables::kNBottom);
+  for (int k = 0; k < n_types; k++)
+    for (int b = 0; b < cfg->n_bands; b++)
+      out[k * cfg->n_bands + b] = table_at(tables::bottom[k], cfg->wavelengths[b]);
   return PHOTIC_OK;
 }
 
@@ -1202,7 +1215,58 @@ int cost_prepared(const photic_config &cfg, const FitParams &fp, const SceneCons
   return PHOTIC_OK;
 }
 
-// Device scratch for the per-pixel drop-ins (one pixel at a time).
+// Launch the general fit over a prepared RegionArgs (grid or list mode); allocates and frees the queue head on the stream.
+int run_region(RegionArgs &a, int max_params, int per_sm, cudaStream_t s) {
+  unsigned int *err = nullptr;
+  int sms = 0;
+  int rc = device_state(&err, &sms);
+  if (rc) return rc;
+  a.error = err;
+  unsigned long long *queue = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&queue, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return fail(PHOTIC_ERR_NOMEM, "queue head");
+  cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
+  a.queue = queue;
+  e = launch_region(a, max_params, sms, per_sm, s);
+  cudaFreeAsync(queue, s);
+  if (e != cudaSuccess) return cuda_fail(e, "region launch");
+  return PHOTIC_OK;
+}
+
+// Device scratch of the per-pixel drop-ins: one block per host thread and
+// device, allocated on the thread's first call and reused by every later one
+// (a caller that drives its own nelmin over samodel_error makes about a
+// thousand calls per pixel; none of them allocates).  It is released when the
+// thread exits.
+constexpr size_t kArenaBytes = 1 << 16;
+struct DropinArena {
+  unsigned char *mem = nullptr;
+  int dev = -1;
+  ~DropinArena() {
+    if (mem) cudaFree(mem);
+  }
+};
+thread_local DropinArena g_arena;
+
+unsigned char *dropin_arena() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  if (g_arena.mem && g_arena.dev == dev) return g_arena.mem;
+  if (g_arena.mem) {  // the thread moved to another device
+    cudaSetDevice(g_arena.dev);
+    cudaFree(g_arena.mem);
+    cudaSetDevice(dev);
+    g_arena.mem = nullptr;
+  }
+  if (cudaMalloc((void **)&g_arena.mem, kArenaBytes) != cudaSuccess) {
+    g_arena.mem = nullptr;
+    return nullptr;
+  }
+  g_arena.dev = dev;
+  return g_arena.mem;
+}
+
+// Views into the arena for the one-region, one-bottom drop-ins.
 struct PixelScratch {
   unsigned char *mem = nullptr;
   float *rrs;
@@ -1210,10 +1274,8 @@ struct PixelScratch {
   float *f[9];
   int32_t *evals_kept, *status;
   int alloc() {
-    const size_t bytes = 4096;
-    if (cudaMalloc((void **)&mem, bytes) != cudaSuccess)
-      return fail(PHOTIC_ERR_NOMEM, "drop-in scratch");
-    cudaMemset(mem, 0, bytes);
+    mem = dropin_arena();
+    if (!mem) return fail(PHOTIC_ERR_NOMEM, "drop-in scratch");
     rrs = (float *)(mem);
     params = (double *)(mem + 128);
     cost = (double *)(mem + 256);
@@ -1225,10 +1287,112 @@ struct PixelScratch {
     status = (int32_t *)(mem + 1344);
     return PHOTIC_OK;
   }
-  ~PixelScratch() {
-    if (mem) cudaFree(mem);
-  }
 };
+
+// A model_data problem for the general kernel (photic_region.cu): regions,
+// scenes and bottom types as the caller set them, fitted (eval == nullptr)
+// or its cost evaluated at eval.  The arena above 4 KB holds its inputs and
+// outputs; one copy in and one copy out.
+struct MixIn {
+  float rrs[kRegionMaxR * PHOTIC_MAX_SCENES * PHOTIC_MAX_BANDS];
+  int32_t R, origin;
+  double h_emp;
+  double params[96];
+};
+struct MixOut {
+  double depth, kept[96];
+  float P[PHOTIC_MAX_SCENES], G[PHOTIC_MAX_SCENES], X[PHOTIC_MAX_SCENES];
+  float albedo, model_error, rrs_error, K_min, iod, pct[3], type;
+  int32_t evals_kept, status;
+  double cost, det[8], rm[kRegionMaxR * PHOTIC_MAX_SCENES * PHOTIC_MAX_BANDS];
+};
+
+int mix_call(photic_model_data *md, const photic_config &cfg, const FitParams &fp,
+             const SceneConsts &sc, const double *eval, MixOut &res) {
+  const int R = md->n_regions, S = md->n_scenes, nbt = md->n_bottoms, nb = cfg.n_bands;
+  if (R < 1 || R > kRegionMaxR || S < 1 || S > PHOTIC_MAX_SCENES || nbt < 1 || nbt > 3)
+    return fail(PHOTIC_ERR_UNSUPPORTED, "1..9 regions, 1..8 scenes and 1..3 bottom types");
+  if (R * S * nb > 128 || R * S > 64 || region_max_params(R, nbt, S) > 96)
+    return fail(PHOTIC_ERR_UNSUPPORTED, "regions x scenes x bands beyond 128");
+  if (md->origin < 0 || md->origin >= R) return fail(PHOTIC_ERR_INVALID, "origin region");
+  for (int s = 1; s < S; s++) {
+    if (md->n_bands[s] != nb) return fail(PHOTIC_ERR_UNSUPPORTED, "scenes with other bands");
+    for (int b = 0; b < nb; b++)
+      if (md->wavelengths[s][b] != md->wavelengths[0][b])
+        return fail(PHOTIC_ERR_UNSUPPORTED, "scenes with other wavelengths");
+  }
+  unsigned char *mem = dropin_arena();
+  if (!mem) return fail(PHOTIC_ERR_NOMEM, "drop-in scratch");
+  MixIn in;
+  memset(&in, 0, sizeof in);
+  for (int r = 0; r < R; r++)
+    for (int s = 0; s < S; s++)
+      for (int b = 0; b < nb; b++)
+        in.rrs[(r * S + s) * nb + b] = (float)md->Rrs_measured[r][s][b];
+  in.R = R;
+  in.origin = md->origin;
+  // the empirical depth picks the starts (and sand alone below 8 m) of a fit
+  in.h_emp = (!eval && md->empirical_depth_present) ? md->h_empirical : NAN;
+  const int n = region_max_params(R, nbt, S);
+  if (eval)
+    for (int i = 0; i < n; i++) in.params[i] = eval[i];
+  MixIn *d_in = (MixIn *)(mem + 4096);
+  MixOut *d_out = (MixOut *)(mem + 4096 + ((sizeof(MixIn) + 255) / 256) * 256);
+  cudaError_t e = cudaMemcpy(d_in, &in, sizeof in, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "drop-in inputs");
+  RegionArgs a;
+  memset(&a, 0, sizeof a);
+  a.fp = fp;
+  a.sc = sc;
+  for (int s = 0; s < S; s++) a.sec_sun[s] = md->sec_theta_sun[s];
+  a.npix = 1;
+  a.n_scenes = S;
+  a.n_spatial = 1;
+  a.n_bottoms = nbt;
+  a.no_mask = 1;
+  a.h_emp = &d_in->h_emp;
+  a.list_rrs = d_in->rrs;
+  a.list_R = &d_in->R;
+  a.list_origin = &d_in->origin;
+  a.eval_stride = 96;
+  photic_outputs &o = a.out;
+  if (eval) {
+    a.eval_params = d_in->params;
+    a.eval_cost = &d_out->cost;
+    a.eval_rm = d_out->rm;
+    a.eval_det = d_out->det;
+  } else {
+    a.list_params = d_out->kept;
+    o.depth_f64 = &d_out->depth;
+    o.P = d_out->P;
+    o.G = d_out->G;
+    o.X = d_out->X;
+    o.bottom_albedo = &d_out->albedo;
+    o.model_error = &d_out->model_error;
+    o.rrs_error = &d_out->rrs_error;
+    o.K_min = &d_out->K_min;
+    o.iod = &d_out->iod;
+    o.bottom_percent = d_out->pct;
+    o.bottom_type = &d_out->type;
+    o.evals_kept = &d_out->evals_kept;
+    o.status = &d_out->status;
+  }
+  int rc = run_region(a, n, 0, 0);
+  if (rc == PHOTIC_OK) rc = photic_sync(0);
+  if (rc) return rc;
+  e = cudaMemcpy(&res, d_out, sizeof res, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "drop-in outputs");
+  if (!eval && (res.status & 0xFF) != PHOTIC_PX_FITTED)
+    return fail(PHOTIC_ERR_CUDA, "the fit did not complete");
+  return PHOTIC_OK;
+}
+
+// Band constants of all bottom types a model_data mixes.
+void mix_bottoms(const photic_model_data *md, SceneConsts &sc, int nb) {
+  for (int k = 0; k < md->n_bottoms && k < 3; k++)
+    for (int b = 0; b < nb; b++)
+      sc.refl_k[k][b] = md->bottom_reflectance[md->bottom_type_indexes[k]][0][b];
+}
 
 // Post-fit products of samodel_optimise (model/samodel.c:1994-2097) for
 // one region and one bottom type, from the kept vector and its details.
@@ -1330,14 +1494,104 @@ int photic_forward_batch(const photic_config *cfg, const double *d_params,
   return PHOTIC_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Rrs at 440/490/550/640/750 nm of every region and scene, stored as the
+// reference does (model/samodel.c:1783-1799).
+void store_reference_rrs(photic_model_data *md) {
+  const double targets[5] = {440.0, 490.0, 550.0, 640.0, 750.0};
+  double **dst[5] = {md->Rrs440, md->Rrs490, md->Rrs550, md->Rrs640, md->Rrs750};
+  for (int r = 0; r < md->n_regions; r++)
+    for (int s = 0; s < md->n_scenes; s++)
+      for (int t = 0; t < 5; t++) {
+        double v = interp_apply(resolve_interp(md->wavelengths[s], md->n_bands[s], targets[t]),
+                                md->Rrs_measured[r][s]);
+        if (t == 0 && v < 0.0) v = 0.0001;
+        if (dst[t]) dst[t][r][s] = v;
+      }
+}
+
+// samodel_optimise for regions, bottom mixtures and scene stacks through the
+// general kernel: the fit, then the cost at the kept vector for the modelled
+// spectra, then the post-fit products (model/samodel.c:1994-2104).
+// params (optional) receives |kept vector| as
+// samodel_optimise_one_bottom_combination returns it (:2413-2417).
+void optimise_general(photic_model_data *md, double *params) {
+  if (md->start_at_previous) {
+    fail(PHOTIC_ERR_UNSUPPORTED,
+         "samodel_optimise: the hot start is built for one region and one bottom type");
+    return;
+  }
+  if (md->n_bottoms < 1 || md->n_bottoms > 3) {
+    fail(PHOTIC_ERR_UNSUPPORTED, "samodel_optimise: 1..3 bottom types");
+    return;
+  }
+  // ALL_BOTTOMS: every type at once, in table order (model/samodel.c:1836-1840)
+  for (int k = 0; k < md->n_bottoms; k++) md->bottom_type_indexes[k] = k;
+  photic_config cfg;
+  FitParams fp;
+  SceneConsts sc;
+  if (from_md(md, 0, cfg, fp, sc)) return;
+  mix_bottoms(md, sc, cfg.n_bands);
+  store_reference_rrs(md);
+  MixOut fit, ev;
+  if (mix_call(md, cfg, fp, sc, nullptr, fit)) return;
+  // a pixel deeper than 8 m was fitted with sand alone (model/samodel.c:1826-1830)
+  const int nbt = (md->empirical_depth_present && md->h_empirical > 8.0) ? 1 : md->n_bottoms;
+  const int saved = md->n_bottoms;
+  md->n_bottoms = nbt;
+  const int R = md->n_regions, S = md->n_scenes, nb = cfg.n_bands;
+  const int n = region_max_params(R, nbt, S), off = R + 2 * nbt * R;
+  int rc = mix_call(md, cfg, fp, sc, fit.kept, ev);
+  md->n_bottoms = saved;  // restored as the reference does (:2104)
+  if (rc) return;
+  md->depth = fit.depth;
+  md->K_min = fit.K_min;
+  md->bottom_albedo = fit.albedo;
+  md->index_optical_depth = fit.iod;
+  md->Rrs_error = fit.rrs_error;
+  md->model_error = fit.model_error;
+  for (int k = 0; k < 12; k++) md->B_type_percent[k] = 0.0;
+  for (int k = 0; k < nbt; k++) md->B_type_percent[k] = fit.pct[k];
+  md->bottom_type = (int)fit.type;
+  for (int s = 0; s < S; s++) {
+    md->P[s] = 0.01 * fabs(fit.kept[off + 3 * s]);
+    md->G[s] = 0.01 * fabs(fit.kept[off + 1 + 3 * s]);
+    md->X[s] = 0.01 * fabs(fit.kept[off + 2 + 3 * s]);
+    if (md->prev) {
+      md->prev[3 * s] = fabs(fit.kept[off + 3 * s]);
+      md->prev[3 * s + 1] = fabs(fit.kept[off + 1 + 3 * s]);
+      md->prev[3 * s + 2] = fabs(fit.kept[off + 2 + 3 * s]);
+    }
+  }
+  for (int r = 0; r < R; r++)
+    for (int s = 0; s < S; s++)
+      for (int b = 0; b < nb; b++)
+        md->Rrs_modelled[r][s][b] = ev.rm[(r * S + s) * nb + b];
+  md->n_iterations = fit.evals_kept;
+  md->converged = (fit.status & PHOTIC_PX_CONVERGED) != 0;
+  if (params)
+    for (int i = 0; i < n; i++) params[i] = fabs(fit.kept[i]);
+}
+
+bool needs_general(const photic_model_data *md) {
+  return md->n_regions != 1 || md->n_bottoms != 1;
+}
+
+}  // namespace
+
+extern "C" {
+
 void samodel_optimise(photic_model_data *md) {
   g_err.clear();
   if (!md) {
     fail(PHOTIC_ERR_INVALID, "NULL model_data");
     return;
   }
-  if (md->n_regions != 1 || md->n_bottoms != 1) {
-    fail(PHOTIC_ERR_UNSUPPORTED, "samodel_optimise: one region and one bottom type only");
+  if (needs_general(md)) {
+    optimise_general(md, nullptr);
     return;
   }
   PixelScratch ps;
@@ -1446,9 +1700,8 @@ void samodel_optimise_one_bottom_combination(photic_model_data *md, double *para
     fail(PHOTIC_ERR_INVALID, "NULL argument");
     return;
   }
-  if (md->n_regions != 1 || md->n_bottoms != 1 || md->n_scenes != 1) {
-    fail(PHOTIC_ERR_UNSUPPORTED,
-         "samodel_optimise_one_bottom_combination: one region, scene and bottom type");
+  if (needs_general(md) || md->n_scenes != 1) {
+    optimise_general(md, params);
     return;
   }
   photic_config cfg;
@@ -1477,9 +1730,27 @@ double samodel_error(double *params, photic_model_data *md) {
     fail(PHOTIC_ERR_INVALID, "NULL argument");
     return NAN;
   }
-  if (md->n_regions != 1 || md->n_bottoms != 1 || md->n_scenes != 1) {
-    fail(PHOTIC_ERR_UNSUPPORTED, "samodel_error: one region, one scene, one bottom type");
-    return NAN;
+  if (needs_general(md) || md->n_scenes != 1) {
+    // regions, bottom mixtures or scenes: the general kernel's cost at params
+    photic_config cfg;
+    FitParams fp;
+    SceneConsts sc;
+    if (md->n_bottoms < 1 || md->n_bottoms > 3) {
+      fail(PHOTIC_ERR_UNSUPPORTED, "samodel_error: 1..3 bottom types");
+      return NAN;
+    }
+    if (from_md(md, 0, cfg, fp, sc)) return NAN;
+    mix_bottoms(md, sc, cfg.n_bands);
+    MixOut ev;
+    if (mix_call(md, cfg, fp, sc, params, ev)) return NAN;
+    const int R = md->n_regions, S = md->n_scenes, nb = cfg.n_bands;
+    for (int r = 0; r < R; r++)
+      for (int s = 0; s < S; s++)
+        for (int b = 0; b < nb; b++) md->Rrs_modelled[r][s][b] = ev.rm[(r * S + s) * nb + b];
+    md->Rrs_error = ev.det[0];
+    md->model_error = ev.det[1];
+    md->bottom_albedo = ev.det[2];
+    return ev.cost;
   }
   photic_config cfg;
   FitParams fp;
@@ -1508,8 +1779,8 @@ double samodel_error(double *params, photic_model_data *md) {
 void samodel_Rrs(double P, double G, double X, double B[], double q[], double H, double Delta,
                  photic_model_data *md, int k_scene, int k_band, int k_region) {
   g_err.clear();
-  if (!md || !B || !q || md->n_bottoms != 1) {
-    fail(PHOTIC_ERR_UNSUPPORTED, "samodel_Rrs: one bottom type");
+  if (!md || !B || !q || md->n_bottoms < 1 || md->n_bottoms > 3) {
+    fail(PHOTIC_ERR_UNSUPPORTED, "samodel_Rrs: 1..3 bottom types");
     return;
   }
   photic_config cfg;
@@ -1520,48 +1791,67 @@ void samodel_Rrs(double P, double G, double X, double B[], double q[], double H,
     fail(PHOTIC_ERR_INVALID, "k_band out of range");
     return;
   }
-  unsigned char *mem = nullptr;
-  if (cudaMalloc((void **)&mem, 1024) != cudaSuccess) {
+  // reflectances of the bottom types md mixes (model/samodel.c:2880-2883)
+  for (int k = 0; k < md->n_bottoms; k++)
+    for (int b = 0; b < cfg.n_bands; b++)
+      sc.refl_k[k][b] = md->bottom_reflectance[md->bottom_type_indexes[k]][k_scene][b];
+  unsigned char *mem = dropin_arena();
+  if (!mem) {
     fail(PHOTIC_ERR_NOMEM, "drop-in scratch");
     return;
   }
+  // one upload: row, Rrs(440), Rrs(490), mixture; one download of the band
+  struct In {
+    double row[8], r440, r490, mix[6];
+  } in;
+  struct Out {
+    double rrs[PHOTIC_MAX_BANDS], K[PHOTIC_MAX_BANDS], parts[PHOTIC_MAX_BANDS * 4];
+  } out;
+  memset(&in, 0, sizeof in);
   const double row[7] = {P, G, X, B[0], q[0], H, Delta};
-  const double r440 = md->Rrs440[k_region][k_scene], r490 = md->Rrs490[k_region][k_scene];
-  double *d_row = (double *)mem, *d_440 = d_row + 8, *d_490 = d_row + 9;
-  double *d_out = d_row + 16, *d_K = d_row + 32, *d_parts = d_row + 48;
-  cudaMemcpy(d_row, row, sizeof row, cudaMemcpyHostToDevice);
-  cudaMemcpy(d_440, &r440, sizeof r440, cudaMemcpyHostToDevice);
-  cudaMemcpy(d_490, &r490, sizeof r490, cudaMemcpyHostToDevice);
+  memcpy(in.row, row, sizeof row);
+  in.r440 = md->Rrs440[k_region][k_scene];
+  in.r490 = md->Rrs490[k_region][k_scene];
+  for (int k = 0; k < md->n_bottoms; k++) {
+    in.mix[k] = B[k];
+    in.mix[3 + k] = q[k];
+  }
+  In *d_in = (In *)(mem + 8192);
+  Out *d_out = (Out *)(mem + 8192 + 1024);
+  cudaError_t e = cudaMemcpy(d_in, &in, sizeof in, cudaMemcpyHostToDevice);
   ForwardArgs a;
   memset(&a, 0, sizeof a);
   a.fp = fp;
   a.sc = sc;
-  a.params = d_row;
-  a.rrs440 = d_440;
-  a.rrs490 = d_490;
+  a.params = d_in->row;
+  a.rrs440 = &d_in->r440;
+  a.rrs490 = &d_in->r490;
   a.n = 1;
-  a.rrs = d_out;
-  a.K = d_K;
-  a.parts = d_parts;
-  cudaError_t e = launch_forward(a, 0);
-  if (e == cudaSuccess) e = cudaDeviceSynchronize();
-  if (e == cudaSuccess) {
-    double out[PHOTIC_MAX_BANDS], K[PHOTIC_MAX_BANDS], parts[4];
-    cudaMemcpy(out, d_out, cfg.n_bands * sizeof(double), cudaMemcpyDeviceToHost);
-    cudaMemcpy(K, d_K, cfg.n_bands * sizeof(double), cudaMemcpyDeviceToHost);
-    cudaMemcpy(parts, d_parts + 4 * k_band, sizeof parts, cudaMemcpyDeviceToHost);
-    md->Rrs_modelled[k_region][k_scene][k_band] = out[k_band];
-    md->K[k_scene][k_band] = K[k_band];
-    if (md->rho) md->rho[k_region][k_scene][k_band] = parts[0];
-    if (md->rrs_dp) md->rrs_dp[k_region][k_scene][k_band] = parts[1];
-    if (md->rrs_bottom) md->rrs_bottom[k_region][k_scene][k_band] = parts[2];
-    if (md->rrs_modelled) md->rrs_modelled[k_region][k_scene][k_band] = parts[3];
-    md->depth = H + sc.h_tide;       // the reference's side effects (:2873-2883)
-    md->bottom_albedo = q[0] * B[0];
-  } else {
-    cuda_fail(e, "samodel_Rrs");
+  a.rrs = d_out->rrs;
+  a.K = d_out->K;
+  a.parts = d_out->parts;
+  if (md->n_bottoms > 1) {
+    a.mix = d_in->mix;
+    a.n_bottoms = md->n_bottoms;
   }
-  cudaFree(mem);
+  if (e == cudaSuccess) e = launch_forward(a, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(&out, d_out, sizeof out, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    cuda_fail(e, "samodel_Rrs");
+    return;
+  }
+  md->Rrs_modelled[k_region][k_scene][k_band] = out.rrs[k_band];
+  md->K[k_scene][k_band] = out.K[k_band];
+  const double *parts = out.parts + 4 * k_band;
+  if (md->rho) md->rho[k_region][k_scene][k_band] = parts[0];
+  if (md->rrs_dp) md->rrs_dp[k_region][k_scene][k_band] = parts[1];
+  if (md->rrs_bottom) md->rrs_bottom[k_region][k_scene][k_band] = parts[2];
+  if (md->rrs_modelled) md->rrs_modelled[k_region][k_scene][k_band] = parts[3];
+  // the reference's side effects (model/samodel.c:2873-2883)
+  md->depth = H + sc.h_tide;
+  double albedo = 0.0;
+  for (int k = 0; k < md->n_bottoms; k++) albedo += q[k] * B[k];
+  md->bottom_albedo = albedo;
 }
 
 }  // extern "C"
@@ -1583,7 +1873,8 @@ int samodel_write_files(const photic_config &cfg, const photic_scene *scene_data
                         const photic_geogrid *gridded_data, const int *scene_indexes,
                         int nscenes, int nrows, int ncols, const std::vector<float> &h_rrs,
                         const std::vector<int32_t> &st, const std::vector<float> &pgx,
-                        const std::vector<double> &params6, float **const *outs) {
+                        const std::vector<double> &params6, const std::vector<int64_t> &kpix,
+                        float **const *outs) {
   const int nb = cfg.n_bands;
   const int64_t npix = (int64_t)nrows * ncols, nobs = npix * nscenes;
   const photic_geogrid &g0 = gridded_data[scene_data[scene_indexes[0]].band_indexes[0]];
@@ -1640,8 +1931,11 @@ int samodel_write_files(const photic_config &cfg, const photic_scene *scene_data
           X = pgx[2 * (size_t)nobs + o];
         }
       }
+      // md->K holds the last region's K (model/samodel.c:2911-2915): Y from
+      // that region's spectrum (kpix: its pixel; empty: the pixel itself)
+      const size_t ok = kpix.empty() ? o : (size_t)(kpix[p] * nscenes + k);
       double rr[PHOTIC_MAX_BANDS];
-      for (int b = 0; b < nb; b++) rr[b] = h_rrs[o * nb + b];
+      for (int b = 0; b < nb; b++) rr[b] = h_rrs[ok * nb + b];
       double a440 = photic_interp_1d(cfg.wavelengths, rr, nb, 440.0);
       if (a440 < 0.0) a440 = 0.0001;  // model/samodel.c:1785-1799
       r440[p] = a440;
@@ -1707,10 +2001,9 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
     fail(PHOTIC_ERR_INVALID, "samodel: bad scenes");
     return;
   }
-  if (n_spatial > 2 || n_bottoms != 1 ||
-      (n_spatial == 2 && (nscenes != 1 || empirical_depth_present))) {
-    fail(PHOTIC_ERR_UNSUPPORTED,
-         "samodel: n_bottoms == 1, and n_spatial == 2 only for one scene without empirical depths");
+  if (n_spatial > 2 || n_bottoms < 1 || n_bottoms > 3) {
+    fail(PHOTIC_ERR_UNSUPPORTED, "samodel: n_spatial <= 2 and n_bottoms 1..3 (sand, seagrass, "
+                                 "coral)");
     return;
   }
   if (n_smoothing_radius > 1) {
@@ -1752,8 +2045,20 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
         }
     }
   }
+  // The general fit (bottom mixtures, 3 x 3 regions, or a scene stack with
+  // empirical depths) takes scene-major grids; the plain single-pixel and
+  // joint paths take [pixel][scene][band].
+  const bool general = n_bottoms > 1 || regions || (nscenes > 1 && empirical_depth_present);
+  std::vector<float> h_grid;
+  if (general) {
+    h_grid.resize(h_rrs.size());
+    for (int64_t p = 0; p < npix; p++)
+      for (int k = 0; k < nscenes; k++)
+        for (int b = 0; b < nb; b++)
+          h_grid[((size_t)k * npix + p) * nb + b] = h_rrs[((size_t)p * nscenes + k) * nb + b];
+  }
   std::vector<double> h_emp;
-  if (empirical_depth_present && nscenes == 1) {
+  if (empirical_depth_present) {
     h_emp.assign((size_t)npix, NAN);
     for (int i = 0; i < nrows; i++)
       for (int j = 0; j < ncols; j++) {
@@ -1765,21 +2070,23 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
   // device buffers
   float *d_rrs = nullptr;
   double *d_depth = nullptr, *d_seeds = nullptr, *d_emp = nullptr, *d_th = nullptr;
-  float *d_f = nullptr, *d_pgx = nullptr;
+  float *d_f = nullptr, *d_pgx = nullptr, *d_mix = nullptr;
   double *d_params = nullptr;
   int32_t *d_status = nullptr, *d_off = nullptr;
-  const bool one_by_one = nscenes == 1 && !regions;
+  const bool one_by_one = nscenes == 1 && !general;
   bool ok = cudaMalloc((void **)&d_rrs, h_rrs.size() * sizeof(float)) == cudaSuccess &&
             cudaMalloc((void **)&d_depth, npix * sizeof(double)) == cudaSuccess &&
             cudaMalloc((void **)&d_f, 4 * npix * sizeof(float)) == cudaSuccess &&
             cudaMalloc((void **)&d_status, npix * sizeof(int32_t)) == cudaSuccess &&
             cudaMalloc((void **)&d_pgx, 3 * nobs * sizeof(float)) == cudaSuccess &&
             (!one_by_one ||
-             cudaMalloc((void **)&d_params, 6 * npix * sizeof(double)) == cudaSuccess);
+             cudaMalloc((void **)&d_params, 6 * npix * sizeof(double)) == cudaSuccess) &&
+            (!general || cudaMalloc((void **)&d_mix, 4 * npix * sizeof(float)) == cudaSuccess);
   if (!ok) {
     fail(PHOTIC_ERR_NOMEM, "samodel: device buffers");
   } else {
-    cudaMemcpy(d_rrs, h_rrs.data(), h_rrs.size() * sizeof(float), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_rrs, general ? h_grid.data() : h_rrs.data(), h_rrs.size() * sizeof(float),
+               cudaMemcpyHostToDevice);
     photic_outputs o;
     memset(&o, 0, sizeof o);
     o.depth_f64 = d_depth;
@@ -1793,7 +2100,19 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
     o.X = d_pgx + 2 * nobs;
     o.params = d_params;
     int rc;
-    if (nscenes == 1) {
+    if (general) {
+      // P, G, X come out as [pixel][scene], the joint fit's layout
+      o.bottom_percent = d_mix;
+      o.bottom_type = d_mix + 3 * npix;
+      double th[PHOTIC_MAX_SCENES];
+      for (int k = 0; k < nscenes; k++) th[k] = scene_data[scene_indexes[k]].theta_w;
+      if (!h_emp.empty()) {
+        cudaMalloc((void **)&d_emp, npix * sizeof(double));
+        cudaMemcpy(d_emp, h_emp.data(), npix * sizeof(double), cudaMemcpyHostToDevice);
+      }
+      rc = photic_region_fit_batch(&cfg, d_rrs, nscenes, th, nrows, ncols, regions ? 2 : 1,
+                                   n_bottoms, d_emp, &o, 0);
+    } else if (nscenes == 1) {
       if (!h_emp.empty()) {
         cudaMalloc((void **)&d_emp, npix * sizeof(double));
         cudaMalloc((void **)&d_seeds, npix * 6 * sizeof(double));
@@ -1808,10 +2127,7 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
         ea.seeds = d_seeds;
         launch_empirical_seeds(ea, 0);
       }
-      // one scene: [pixel][band] is the [nrows][ncols][band] grid the
-      // region fit takes (model/samodel.c:2957-3027 for n_spatial = 2)
-      rc = regions ? photic_region_invert_batch(&cfg, d_rrs, nrows, ncols, 2, &o, 0)
-                   : photic_invert_batch(&cfg, d_rrs, npix, nb, 1, d_seeds, &o, 0);
+      rc = photic_invert_batch(&cfg, d_rrs, npix, nb, 1, d_seeds, &o, 0);
     } else {
       std::vector<int32_t> offs((size_t)npix + 1);
       std::vector<double> th((size_t)nobs);
@@ -1830,12 +2146,17 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
       std::vector<double> H((size_t)npix);
       std::vector<float> f((size_t)4 * npix);
       std::vector<int32_t> st((size_t)npix);
+      std::vector<float> mix;
+      if (general) {
+        mix.resize((size_t)4 * npix);
+        cudaMemcpy(mix.data(), d_mix, mix.size() * sizeof(float), cudaMemcpyDeviceToHost);
+      }
       cudaMemcpy(H.data(), d_depth, npix * sizeof(double), cudaMemcpyDeviceToHost);
       cudaMemcpy(f.data(), d_f, 4 * npix * sizeof(float), cudaMemcpyDeviceToHost);
       cudaMemcpy(st.data(), d_status, npix * sizeof(int32_t), cudaMemcpyDeviceToHost);
       // depth uncertainty of the fitted grid (:1368-1479), one scene
       std::vector<float> sig((size_t)npix, 0.0f);
-      if (depth_sigma && nscenes == 1 && !regions) {
+      if (depth_sigma && nscenes == 1 && !general) {
         std::vector<float> hpos((size_t)npix);
         for (int64_t p = 0; p < npix; p++)
           hpos[p] = (st[p] & 0xFF) == PHOTIC_PX_FITTED ? (float)H[p] : 0.0f;
@@ -1866,11 +2187,13 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
           if (depth_sigma) depth_sigma[i][j] = sig[p];
           model_error[i][j] = fit ? f[p] : 0.0f;
           bottom_albedo[i][j] = fit ? f[npix + p] : 0.0f;
-          bottom_sand[i][j] = fit ? 100.0f : -9999.0f;
-          bottom_seagrass[i][j] = fit ? 0.0f : -9999.0f;
-          bottom_coral[i][j] = fit ? 0.0f : -9999.0f;
+          // shares of sand, seagrass and coral and the bottom type
+          // (model/samodel.c:2021-2047, stored at :1120-1164)
+          bottom_sand[i][j] = fit ? (general ? mix[3 * p] : 100.0f) : -9999.0f;
+          bottom_seagrass[i][j] = fit ? (general ? mix[3 * p + 1] : 0.0f) : -9999.0f;
+          bottom_coral[i][j] = fit ? (general ? mix[3 * p + 2] : 0.0f) : -9999.0f;
           K_min[i][j] = fit ? f[2 * npix + p] : 0.0f;
-          bottom_type[i][j] = fit ? 1.0f : -9999.0f;
+          bottom_type[i][j] = fit ? (general ? mix[3 * npix + p] : 1.0f) : -9999.0f;
           index_optical_depth[i][j] = fit ? f[3 * npix + p] : 0.0f;
         }
       if (rc == PHOTIC_OK) {
@@ -1885,8 +2208,31 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
         float **const outs[10] = {depth,     depth_sigma, model_error, bottom_albedo,
                                   bottom_sand, bottom_seagrass, bottom_coral, K_min,
                                   bottom_type, index_optical_depth};
+        // the last region of each pixel's 3 x 3 neighbourhood in
+        // extract_Rrs_data's order (model/samodel.c:2970-3025)
+        std::vector<int64_t> kpix;
+        if (regions) {
+          kpix.resize((size_t)npix);
+          for (int i = 0; i < nrows; i++)
+            for (int j = 0; j < ncols; j++) {
+              int64_t last = (int64_t)i * ncols + j;
+              for (int ii = -1; ii <= 1; ii++)
+                for (int jj = -1; jj <= 1; jj++) {
+                  const int iii = std::min(std::max(i + ii, 0), nrows - 1);
+                  const int jjj = std::min(std::max(j + jj, 0), ncols - 1);
+                  const int64_t q = (int64_t)iii * ncols + jjj;
+                  bool nodata = false;
+                  for (int k = 0; k < nscenes && !nodata; k++)
+                    for (int b = 0; b < nb; b++)
+                      if (h_rrs[((size_t)q * nscenes + k) * nb + b] == cfg.nodata_value)
+                        nodata = true;
+                  if (!nodata) last = q;
+                }
+              kpix[(size_t)i * ncols + j] = last;
+            }
+        }
         samodel_write_files(cfg, scene_data, gridded_data, scene_indexes, nscenes, nrows, ncols,
-                            h_rrs, st, pgx, params6, outs);
+                            h_rrs, st, pgx, params6, kpix, outs);
       }
     }
   }
@@ -1896,6 +2242,7 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
   cudaFree(d_pgx);
   cudaFree(d_params);
   cudaFree(d_status);
+  if (d_mix) cudaFree(d_mix);
   if (d_emp) cudaFree(d_emp);
   if (d_seeds) cudaFree(d_seeds);
   if (d_off) cudaFree(d_off);
@@ -2083,38 +2430,54 @@ extern "C" int photic_depth_sigma(const photic_config *cfg, const float *d_rrs, 
 // ---------------------------------------------------------------------------
 // Spatial-region fit (model/samodel.c:2957-3027 with n_spatial = 2).
 // ---------------------------------------------------------------------------
-extern "C" int photic_region_invert_batch(const photic_config *cfg, const float *d_grid,
-                                          int32_t nrows, int32_t ncols, int32_t n_spatial,
-                                          const photic_outputs *out, void *stream) {
+
+extern "C" int photic_region_fit_batch(const photic_config *cfg, const float *d_grid,
+                                       int32_t n_scenes, const double *theta_sun_deg,
+                                       int32_t nrows, int32_t ncols, int32_t n_spatial,
+                                       int32_t n_bottoms, const double *d_h_empirical,
+                                       const photic_outputs *out, void *stream) {
   int rc = photic_config_check(cfg);
   if (rc) return rc;
-  if (n_spatial != 2) return fail(PHOTIC_ERR_UNSUPPORTED, "n_spatial must be 2 (3 x 3 regions)");
-  if (cfg->n_bands > 4) return fail(PHOTIC_ERR_UNSUPPORTED, "the region fit takes up to 4 bands");
+  if (n_spatial < 1 || n_spatial > 2)
+    return fail(PHOTIC_ERR_UNSUPPORTED, "n_spatial must be 1 (pixels alone) or 2 (3 x 3 regions)");
+  if (n_bottoms < 1 || n_bottoms > 3)
+    return fail(PHOTIC_ERR_UNSUPPORTED, "n_bottoms must be 1..3 (sand, seagrass, coral)");
+  if (n_scenes < 1 || n_scenes > PHOTIC_MAX_SCENES)
+    return fail(PHOTIC_ERR_UNSUPPORTED, "n_scenes must be 1..%d", PHOTIC_MAX_SCENES);
+  const int Rmax = n_spatial == 2 ? kRegionMaxR : 1;
+  if (Rmax * n_scenes * cfg->n_bands > 128 || Rmax * n_scenes > 64)
+    return fail(PHOTIC_ERR_UNSUPPORTED, "regions x scenes x bands beyond 128");
+  const int nmax = region_max_params(Rmax, n_bottoms, n_scenes);
+  if (nmax > 96) return fail(PHOTIC_ERR_UNSUPPORTED, "%d unknowns beyond 96", nmax);
   if (nrows < 0 || ncols < 0 || !out || ((int64_t)nrows * ncols > 0 && !d_grid))
     return fail(PHOTIC_ERR_INVALID, "bad arguments");
   if ((int64_t)nrows * ncols == 0) return PHOTIC_OK;
-  cudaStream_t s = (cudaStream_t)stream;
-  unsigned int *err = nullptr;
-  int sms = 0;
-  rc = device_state(&err, &sms);
-  if (rc) return rc;
   RegionArgs a;
   memset(&a, 0, sizeof a);
   make_fit(*cfg, a.fp);
   make_scene(*cfg, cfg->theta_sun_deg, a.sc);
+  for (int s = 0; s < n_scenes; s++) {
+    SceneConsts ss;
+    make_scene(*cfg, theta_sun_deg ? theta_sun_deg[s] : cfg->theta_sun_deg, ss);
+    a.sec_sun[s] = ss.sec_sun;
+  }
   a.grid = d_grid;
   a.nrows = nrows;
   a.ncols = ncols;
+  a.npix = (int64_t)nrows * ncols;
+  a.n_scenes = n_scenes;
+  a.n_spatial = n_spatial;
+  a.n_bottoms = n_bottoms;
+  a.h_emp = d_h_empirical;
   a.out = *out;
-  a.error = err;
-  unsigned long long *queue = nullptr;
-  cudaError_t e = cudaMallocAsync((void **)&queue, sizeof(unsigned long long), s);
-  if (e != cudaSuccess) return fail(PHOTIC_ERR_NOMEM, "queue head");
-  cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
-  a.queue = queue;
-  e = launch_region(a, sms, cfg->blocks_per_sm, s);
-  cudaFreeAsync(queue, s);
-  if (e != cudaSuccess) return cuda_fail(e, "region launch");
-  return PHOTIC_OK;
+  return run_region(a, nmax, cfg->blocks_per_sm, (cudaStream_t)stream);
+}
+
+extern "C" int photic_region_invert_batch(const photic_config *cfg, const float *d_grid,
+                                          int32_t nrows, int32_t ncols, int32_t n_spatial,
+                                          const photic_outputs *out, void *stream) {
+  if (n_spatial != 2) return fail(PHOTIC_ERR_UNSUPPORTED, "n_spatial must be 2 (3 x 3 regions)");
+  return photic_region_fit_batch(cfg, d_grid, 1, nullptr, nrows, ncols, n_spatial, 1, nullptr, out,
+                                 stream);
 }
 

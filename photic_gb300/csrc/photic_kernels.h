@@ -197,6 +197,11 @@ struct ForwardArgs {
   int64_t n;
   double *rrs, *K;       // [n][n_bands]
   double *parts;         // optional [n][n_bands][4]: rho, rrs_dp, rrs_bottom, rrs
+  // optional bottom mixture per row: [n][6] = B_0..B_2, q_0..q_2 (q already
+  // normalised, as samodel_Rrs takes them) of n_bottoms types with
+  // reflectances sc.refl_k; replaces the row's B and q
+  const double *mix;
+  int32_t n_bottoms;
 };
 cudaError_t launch_forward(const ForwardArgs &a, cudaStream_t s);
 
@@ -211,17 +216,46 @@ struct EmpSeedArgs {
 cudaError_t launch_empirical_seeds(const EmpSeedArgs &a, cudaStream_t s);
 
 // Spatial-region fit, 3 x 3 neighbourhoods (photic_region.cu).
+// The general single-scene fit (photic_region.cu): pixels alone or with
+// their 3 x 3 neighbourhood, 1..3 bottom types mixed per region.
+constexpr int kRegionMaxR = 9;        // regions of a 3 x 3 neighbourhood
+constexpr int kRegionMaxParams = 66;  // 9 + 2 * 3 * 9 + 3 (one scene)
 struct RegionArgs {
   FitParams fp;
   SceneConsts sc;
-  const float *grid;            // [nrows][ncols][n_bands]
+  const float *grid;            // grid mode: [nrows][ncols][n_bands]
   int nrows, ncols;
+  int64_t npix;                 // problems (grid: nrows * ncols)
+  int32_t n_scenes;             // scenes of the same bands; grid: [S][nrows][ncols][n_bands]
+  double sec_sun[kMaxScenes];   // per-scene secant of the subsurface sun zenith
+  int32_t n_spatial;            // 1: each pixel alone, 2: 3 x 3 regions
+  int32_t n_bottoms;            // bottom types 1..3 (sand, seagrass, coral)
+  const double *h_emp;          // optional [npix] empirical depth (NaN: none)
+  int32_t no_mask;              // skip the pixel loop's mask test (list mode)
+  // list mode (the per-pixel drop-ins): problem p has list_R[p] regions with
+  // spectra list_rrs[((p * 9 + r) * n_scenes + s) * n_bands + b] and origin
+  // list_origin[p]
+  const float *list_rrs;
+  const int32_t *list_R, *list_origin;
+  // optional [npix][eval_stride] in: parameters to evaluate instead of
+  // fitting (samodel_error); out: the kept parameter vector of a fit
+  const double *eval_params;
+  double *list_params;
+  int32_t eval_stride;
+  double *eval_cost;            // [npix] cost at eval_params
+  double *eval_rm;              // [npix][9][n_scenes][n_bands] modelled Rrs
+  double *eval_det;             // [npix][8]: Rrs error, model error, albedo, the last
+                                // scene's K_min (the cost's), IOD
   unsigned long long *queue;    // work-queue head (zeroed)
-  photic_outputs out;           // per pixel; status carries the region count << 24
+  photic_outputs out;           // per pixel (P, G, X: [npix][n_scenes]); status carries
+                                // the region count << 24
   unsigned int *error;
 };
-size_t region_smem_bytes();
-cudaError_t launch_region(const RegionArgs &a, int sms, int per_sm, cudaStream_t s);
+// Parameters of a fit with up to max_regions regions, n_bottoms types and
+// n_scenes scenes.
+int region_max_params(int max_regions, int n_bottoms, int n_scenes);
+cudaError_t launch_region(const RegionArgs &a, int max_params, int sms, int per_sm,
+                          cudaStream_t s);
 
 // Depth uncertainty by re-inversion of perturbed samples (photic_aux.cu).
 constexpr int kDsMaxIntervals = 120;  // 30 m in 0.25 m steps

@@ -27,6 +27,7 @@ struct InterpPlan {
 struct SceneConsts {
   double a0[kMaxBands], a1[kMaxBands], aw[kMaxBands], bbw[kMaxBands];
   double refl[kMaxBands];     // sand bottom reflectance
+  double refl_k[3][kMaxBands];  // sand, seagrass, coral (model/samodel.c:464-475)
   double wl[kMaxBands];
   double eS[kMaxBands];       // exp(-0.015 * (lambda - 440)), host libm
   double ratio440[kMaxBands]; // 440 / lambda

@@ -22,9 +22,18 @@
  *        rrs      : OUT = double [npix][2 * n_bands] (Rrs_modelled, K) at
  *                   the model inputs samodel_error derives from params
  *        grid     : samodel() over an nrows x ncols grid (grid2: with
- *                   n_spatial = 2, 3 x 3 regions per pixel); OUT = float
+ *                   n_spatial = 2, 3 x 3 regions per pixel; grid3: 3 x 3
+ *                   regions and n_bottoms = 3, the reference's default call;
+ *                   grid13: pixels alone, n_bottoms = 3); OUT = float
  *                   [10][nrows][ncols] (depth, depth sigma, model error,
- *                   albedo, sand, seagrass, coral, K_min, type, IOD) */
+ *                   albedo, sand, seagrass, coral, K_min, type, IOD)
+ *        optimise3: samodel_optimise with n_bottoms = 3 (sand, seagrass,
+ *                   coral); OUT = double [npix][15]: depth, P, G, X, albedo,
+ *                   model error, Rrs error, K_min, IOD, n_iterations,
+ *                   converged, the three bottom shares, bottom type
+ *        error3   : samodel_error with n_bottoms = 3 at the 10-vector
+ *                   (H, 100B, 70B, 130B, q, q/2, q/4, 100P, 100G, 100X) made
+ *                   from each 6-vector; OUT = double [npix][1 + n_bands] */
 #include <math.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -78,13 +87,18 @@ static photic_model_data *md_new(int nb, const double *wl, double th_sun, double
   md->n_bottoms = 1;
   md->n_scenes = 1;
   md->n_regions = 1;
+  double refl[3 * PHOTIC_MAX_BANDS];
+  if (photic_bottom_reflectances(&cfg, 3, refl)) {
+    fprintf(stderr, "bottom reflectances: %s\n", photic_last_error());
+    exit(3);
+  }
   md->max_n_bands = nb;
   md->max_n_regions = 1;
   md->n_bands = xcalloc(1, sizeof(int));
   md->n_bands[0] = nb;
   md->Rrs_measured = mat3(1, 1, nb);
   md->wavelengths = mat2(1, nb);
-  md->bottom_reflectance = mat3(1, 1, nb);
+  md->bottom_reflectance = mat3(3, 1, nb);
   md->a_0 = mat2(1, nb);
   md->a_1 = mat2(1, nb);
   md->a_w = mat2(1, nb);
@@ -95,7 +109,7 @@ static photic_model_data *md_new(int nb, const double *wl, double th_sun, double
     md->a_1[0][b] = bc[b * 8 + 1];
     md->a_w[0][b] = bc[b * 8 + 2];
     md->b_bw[0][b] = bc[b * 8 + 3];
-    md->bottom_reflectance[0][0][b] = bc[b * 8 + 4];
+    for (int k = 0; k < 3; k++) md->bottom_reflectance[k][0][b] = refl[k * nb + b];
   }
   md->a_w640 = bc[7];
   md->H_tide = xcalloc(1, sizeof(double));
@@ -113,8 +127,10 @@ static photic_model_data *md_new(int nb, const double *wl, double th_sun, double
   md->Rrs640 = mat2(1, 1);
   md->Rrs750 = mat2(1, 1);
   md->rrs_noise = mat2(1, nb);
-  md->bottom_type_indexes[0] = 0;
+  for (int k = 0; k < 3; k++) md->bottom_type_indexes[k] = k;
   strcpy(md->B_type_name[0], "sand");
+  strcpy(md->B_type_name[1], "seagrass");
+  strcpy(md->B_type_name[2], "coral");
   md->P = xcalloc(1, sizeof(double));
   md->G = xcalloc(1, sizeof(double));
   md->X = xcalloc(1, sizeof(double));
@@ -154,8 +170,10 @@ int main(int argc, char **argv) {
   FILE *o = fopen(argv[3], "wb");
   if (!o) return 1;
 
-  if (!strcmp(mode, "grid") || !strcmp(mode, "grid2")) {
-    const int n_spatial = !strcmp(mode, "grid2") ? 2 : 0;
+  if (!strcmp(mode, "grid") || !strcmp(mode, "grid2") || !strcmp(mode, "grid3") ||
+      !strcmp(mode, "grid13")) {
+    const int n_spatial = (!strcmp(mode, "grid2") || !strcmp(mode, "grid3")) ? 2 : 0;
+    const int n_bottoms = (!strcmp(mode, "grid3") || !strcmp(mode, "grid13")) ? 3 : 1;
     if (nrows * ncols != npix) return 1;
     photic_scene *sc = xcalloc(1, sizeof *sc);
     photic_geogrid *grids = xcalloc((size_t)nb, sizeof *grids);
@@ -180,7 +198,7 @@ int main(int argc, char **argv) {
     float **g[10];
     for (int k = 0; k < 10; k++) g[k] = fgrid(nrows, ncols);
     int idx = 0;
-    samodel(sc, grids, &idx, 1, 0, none, 1, n_spatial, 1, g[0], g[1], g[2], g[3], g[4], g[5],
+    samodel(sc, grids, &idx, 1, 0, none, 1, n_spatial, n_bottoms, g[0], g[1], g[2], g[3], g[4], g[5],
             g[6], g[7], g[8], g[9], 0.0f, 0, 0);
     if (photic_last_error()[0]) {
       fprintf(stderr, "samodel: %s\n", photic_last_error());
@@ -207,6 +225,24 @@ int main(int argc, char **argv) {
                               md->B_type_percent[0], md->bottom_type};
       fwrite(row, sizeof row, 1, o);
       md->depth_prev = md->depth;
+    } else if (!strcmp(mode, "optimise3")) {
+      md->n_bottoms = 3;
+      samodel_optimise(md);
+      const double row[15] = {md->depth,         md->P[0],          md->G[0],
+                              md->X[0],          md->bottom_albedo, md->model_error,
+                              md->Rrs_error,     md->K_min,         md->index_optical_depth,
+                              md->n_iterations,  md->converged,     md->B_type_percent[0],
+                              md->B_type_percent[1], md->B_type_percent[2], md->bottom_type};
+      fwrite(row, sizeof row, 1, o);
+    } else if (!strcmp(mode, "error3")) {
+      const double *x6 = params + (size_t)p * 6;
+      double x[10] = {x6[0], x6[1], 0.7 * x6[1], 1.3 * x6[1], x6[2], 0.5 * x6[2],
+                      0.25 * x6[2], x6[3], x6[4], x6[5]};
+      md->n_bottoms = 3;
+      double row[1 + PHOTIC_MAX_BANDS];
+      row[0] = samodel_error(x, md);
+      for (int b = 0; b < nb; b++) row[1 + b] = md->Rrs_modelled[0][0][b];
+      fwrite(row, sizeof(double), (size_t)(1 + nb), o);
     } else if (!strcmp(mode, "combo")) {
       double x[8];
       samodel_optimise_one_bottom_combination(md, x);

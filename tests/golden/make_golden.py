@@ -98,8 +98,27 @@ def bottoms():
         out[f"ref_s{ns}_emp"] = O.region_invert_batch(grid, kcount=600, n_spatial=ns, n_bottoms=3,
                                                       h_empirical=he, which="reference",
                                                       nthreads=os.cpu_count())[:, cols]
+    # samodel()'s own call: the reference's hard-coded tolerances
+    # (model/samodel.c:2142-2144), for the drop-in test
+    for ns in (1, 2):
+        out[f"ref_default_s{ns}"] = O.region_invert_batch(grid, reqmin=None, n_spatial=ns,
+                                                          n_bottoms=3, which="reference",
+                                                          nthreads=os.cpu_count())[:, cols]
+    # a two-scene stack of the same place (own sun zeniths and masks), 3 x 3
+    # regions and three bottom types: n = 9 + 18 * 3 + 3 * 2 unknowns
+    stack = []
+    for s in range(2):
+        r, _ = O.generate_single(20260808 + s, 6 * 7, pix0=100, mask_frac=0.1,
+                                 theta_sun=30.0 + 8.0 * s)
+        stack.append(r.reshape(6, 7, r.shape[1]))
+    stack = np.stack(stack)
+    stack_th = np.array([30.0, 38.0])
+    out["ref_stack"] = O.region_invert_batch(stack, theta_sun=stack_th, kcount=600, n_spatial=2,
+                                             n_bottoms=3, which="reference",
+                                             nthreads=os.cpu_count())[:, cols + [12, 20, 28]]
     np.savez_compressed(os.path.join(OUT, "bottoms.npz"), grid=grid, h_empirical=he,
-                        cols=np.array(cols), kcount=np.array(600), **out)
+                        cols=np.array(cols), kcount=np.array(600), stack=stack,
+                        stack_theta_sun=stack_th, **out)
 
 
 if __name__ == "__main__":

@@ -211,3 +211,67 @@ def test_samodel_grid_regions_matches_oracle(driver, port, tmp_path):
     assert (g[4, ~fit] == -9999).all() and (g[4, fit] == 100).all()
     dh = np.abs(-g[0, fit] - ref[fit, 0].astype(np.float32))
     assert np.median(dh) <= 0.01 and np.mean(dh == 0) >= 0.95, (np.median(dh), np.mean(dh == 0))
+
+
+@pytest.mark.parametrize("mode,key", [("grid3", "ref_default_s2"), ("grid13", "ref_default_s1")])
+def test_samodel_default_call_matches_reference(driver, golden_dir, tmp_path, mode, key):
+    """samodel() as the reference's bam.c calls it by default (n_spatial = 2,
+    n_bottoms = 3: sand, seagrass and coral mixed in every 3 x 3 region;
+    model/bam.c:3236-3241, model/common.c:152), and with pixels alone,
+    against the reference's own samodel_optimise at its own tolerances
+    (tests/golden/bottoms.npz): depth, bottom shares and bottom type."""
+    g = np.load(os.path.join(golden_dir, "bottoms.npz"))
+    cols = list(g["cols"])
+    ref = g[key]
+    nrows, ncols = g["grid"].shape[:2]
+    inp, out = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    _write_input(inp, g["grid"].reshape(-1, 4), nrows=nrows, ncols=ncols)
+    _run(driver, mode, inp, out)
+    grids = np.fromfile(out, dtype=np.float32).reshape(10, nrows * ncols)
+    fit = ref[:, cols.index(9)] == 0
+    assert (grids[4, ~fit] == -9999).all()
+    d = np.abs(-grids[0, fit].astype(np.float64) - ref[fit, 0].astype(np.float32))
+    same = d == 0
+    print(f"samodel {mode}: {fit.sum()} px, same depth {same.mean():.4f}, median |dH| "
+          f"{np.median(d):.3g} m, p99 {np.quantile(d, 0.99):.3g} m")
+    assert np.median(d) <= 0.01 and np.quantile(d, 0.99) <= 0.05
+    agree = np.where(fit)[0][same]
+    for k, c in ((4, 40), (5, 41), (6, 42)):
+        np.testing.assert_allclose(grids[k, agree], ref[agree, cols.index(c)].astype(np.float32),
+                                   rtol=1e-6, atol=1e-5)
+    np.testing.assert_array_equal(grids[8, agree], ref[agree, cols.index(43)].astype(np.float32))
+    assert len(np.unique(grids[8, fit])) > 1  # several bottom types win
+
+
+def test_samodel_optimise_and_error_with_three_bottoms(driver, port, tmp_path):
+    """The per-pixel drop-ins with n_bottoms = 3: samodel_optimise against the
+    oracle (reference tolerances), samodel_error against the oracle's cost."""
+    rrs, _ = port.generate_single(20261313, 160, pix0=3, mask_frac=0.0)
+    rng = np.random.default_rng(8)
+    params = np.column_stack([rng.uniform(0.5, 25, 160), rng.uniform(5, 50, 160),
+                              rng.uniform(0.2, 2, 160), rng.uniform(0.5, 10, 160),
+                              rng.uniform(0.5, 20, 160), rng.uniform(0.1, 5, 160)])
+    inp, out = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    _write_input(inp, rrs, params)
+    _run(driver, "optimise3", inp, out)
+    r = np.fromfile(out, dtype=np.float64).reshape(160, 15)
+    ref = port.region_invert_batch(rrs.reshape(1, 160, 4), reqmin=None, n_spatial=1, n_bottoms=3,
+                                   nthreads=os.cpu_count() or 1)
+    d = np.abs(r[:, 0] - ref[:, 0])
+    print(f"samodel_optimise n_bottoms 3: same depth {np.mean(d == 0):.4f}, median |dH| "
+          f"{np.median(d):.3g}, p99 {np.quantile(d, 0.99):.3g}")
+    assert np.median(d) <= 0.01 and np.quantile(d, 0.99) <= 0.05
+    agree = d == 0
+    np.testing.assert_allclose(r[agree][:, 11:14], ref[agree][:, 40:43], rtol=1e-12, atol=1e-12)
+    np.testing.assert_array_equal(r[agree, 14], ref[agree, 43])
+    np.testing.assert_allclose(r[agree, 1], ref[agree, 11], rtol=1e-12)
+    # samodel_error at a 10-parameter vector
+    _run(driver, "error3", inp, out)
+    e = np.fromfile(out, dtype=np.float64).reshape(160, 5)
+    for i in range(0, 160, 7):
+        x6 = params[i]
+        x10 = [x6[0], x6[1], 0.7 * x6[1], 1.3 * x6[1], x6[2], 0.5 * x6[2], 0.25 * x6[2],
+               x6[3], x6[4], x6[5]]
+        c, _, rm = port.region_cost(rrs[i:i + 1].astype(np.float64), x10, n_bottoms=3)
+        assert abs(e[i, 0] - c) <= 1e-12 * abs(c), (i, e[i, 0], c)
+        np.testing.assert_allclose(e[i, 1:], rm[0, 0], rtol=1e-12)

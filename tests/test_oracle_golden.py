@@ -95,14 +95,26 @@ def test_regions_golden(port, golden_dir):
     np.testing.assert_array_equal(out[:, g["cols"]], g["ref"])
 
 
-@pytest.mark.parametrize("key", ["ref_s1", "ref_s1_emp", "ref_s2", "ref_s2_emp"])
+@pytest.mark.parametrize("key", ["ref_s1", "ref_s1_emp", "ref_s2", "ref_s2_emp",
+                                 "ref_default_s1", "ref_default_s2"])
 def test_bottom_mixtures_golden(port, golden_dir, key):
     """Sand / seagrass / coral mixtures (n_bottoms = 3), pixels alone and with
     3 x 3 regions, with and without empirical depths, against the reference's
     own samodel_optimise (tests/golden/bottoms.npz)."""
     g = np.load(os.path.join(golden_dir, "bottoms.npz"))
-    ns = 1 if key.startswith("ref_s1") else 2
+    ns = 1 if "_s1" in key else 2
     he = g["h_empirical"] if key.endswith("_emp") else None
-    out = port.region_invert_batch(g["grid"], kcount=int(g["kcount"]), n_spatial=ns, n_bottoms=3,
-                                   h_empirical=he, nthreads=4)
+    tol = dict(reqmin=None) if "default" in key else dict(kcount=int(g["kcount"]))
+    out = port.region_invert_batch(g["grid"], n_spatial=ns, n_bottoms=3, h_empirical=he,
+                                   nthreads=4, **tol)
     np.testing.assert_array_equal(out[:, g["cols"]], g[key])
+
+
+def test_scene_stack_golden(port, golden_dir):
+    """A two-scene stack with 3 x 3 regions and three bottom types against
+    the reference's own samodel_optimise (tests/golden/bottoms.npz)."""
+    g = np.load(os.path.join(golden_dir, "bottoms.npz"))
+    out = port.region_invert_batch(g["stack"], theta_sun=g["stack_theta_sun"],
+                                   kcount=int(g["kcount"]), n_spatial=2, n_bottoms=3, nthreads=4)
+    cols = list(g["cols"]) + [12, 20, 28]
+    np.testing.assert_array_equal(out[:, cols], g["ref_stack"])

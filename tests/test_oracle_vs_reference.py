@@ -74,3 +74,23 @@ def test_bottom_mixtures_bit_exact(n_spatial, n_bottoms):
         np.testing.assert_array_equal(a[:, cols], b[:, cols])
         fit = a[:, 9] == 0
         assert len(np.unique(a[fit, 43])) > 1  # several bottom types win
+
+
+@pytest.mark.parametrize("n_scenes,n_spatial,n_bottoms", [(2, 1, 1), (2, 1, 3), (2, 2, 3),
+                                                          (3, 2, 1)])
+def test_scene_stacks_bit_exact(n_scenes, n_spatial, n_bottoms):
+    """Several scenes of one place (their own sun zeniths and masks), fitted
+    jointly with regions and bottom mixtures: n = R + 2 Nb R + 3 Ns."""
+    grids = []
+    for s in range(n_scenes):
+        r, _ = O.generate_single(900 + s, 6 * 8, pix0=300, mask_frac=0.1, theta_sun=28.0 + 6 * s)
+        grids.append(r.reshape(6, 8, 4))
+    grid = np.stack(grids)
+    th = [28.0 + 6 * s for s in range(n_scenes)]
+    cols = [c for c in range(O.NOUT) if c not in (36, 37)]
+    a = O.region_invert_batch(grid, theta_sun=th, kcount=500, n_spatial=n_spatial,
+                              n_bottoms=n_bottoms, nthreads=8)
+    b = O.region_invert_batch(grid, theta_sun=th, kcount=500, n_spatial=n_spatial,
+                              n_bottoms=n_bottoms, nthreads=8, which="reference")
+    np.testing.assert_array_equal(a[:, cols], b[:, cols])
+    assert np.all(a[a[:, 9] == 0, 10] == n_scenes)
