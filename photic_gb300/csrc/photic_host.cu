@@ -1547,15 +1547,25 @@ void optimise_general(photic_model_data *md, double *params) {
   int rc = mix_call(md, cfg, fp, sc, fit.kept, ev);
   md->n_bottoms = saved;  // restored as the reference does (:2104)
   if (rc) return;
+  // the products in double precision, as the reference keeps them: from the
+  // re-evaluation at the kept vector and from the vector itself
   md->depth = fit.depth;
-  md->K_min = fit.K_min;
-  md->bottom_albedo = fit.albedo;
-  md->index_optical_depth = fit.iod;
-  md->Rrs_error = fit.rrs_error;
-  md->model_error = fit.model_error;
+  md->Rrs_error = ev.det[0];
+  md->model_error = ev.det[1];
+  md->bottom_albedo = ev.det[2];
+  md->index_optical_depth = ev.det[4];
+  md->K_min = ev.det[5];
   for (int k = 0; k < 12; k++) md->B_type_percent[k] = 0.0;
-  for (int k = 0; k < nbt; k++) md->B_type_percent[k] = fit.pct[k];
-  md->bottom_type = (int)fit.type;
+  double q_sum = 0.0, largest = 0.0;  // model/samodel.c:2021-2047
+  const int qo = R + R * nbt + md->origin * nbt;
+  for (int k = 0; k < nbt; k++) q_sum += fabs(fit.kept[qo + k]);
+  for (int k = 0; k < nbt; k++) {
+    md->B_type_percent[k] = 100.0 * fabs(fit.kept[qo + k]) / q_sum;
+    if (md->B_type_percent[k] > largest) {
+      largest = md->B_type_percent[k];
+      md->bottom_type = (int)(1.0 + k);
+    }
+  }
   for (int s = 0; s < S; s++) {
     md->P[s] = 0.01 * fabs(fit.kept[off + 3 * s]);
     md->G[s] = 0.01 * fabs(fit.kept[off + 1 + 3 * s]);

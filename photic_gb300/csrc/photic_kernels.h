@@ -245,7 +245,8 @@ struct RegionArgs {
   double *eval_cost;            // [npix] cost at eval_params
   double *eval_rm;              // [npix][9][n_scenes][n_bands] modelled Rrs
   double *eval_det;             // [npix][8]: Rrs error, model error, albedo, the last
-                                // scene's K_min (the cost's), IOD
+                                // scene's K_min (the cost's), IOD, K_min over all
+                                // scenes (the post-fit product's)
   unsigned long long *queue;    // work-queue head (zeroed)
   photic_outputs out;           // per pixel (P, G, X: [npix][n_scenes]); status carries
                                 // the region count << 24

@@ -459,6 +459,7 @@ __global__ void __launch_bounds__(BLOCK) region_kernel(const __grid_constant__ R
             a.eval_det[p * 8 + 2] = misc[2];
             a.eval_det[p * 8 + 3] = misc[5];
             a.eval_det[p * 8 + 4] = misc[4];
+            a.eval_det[p * 8 + 5] = misc[3];
           }
         }
         break;
