@@ -522,3 +522,12 @@ void photic_ref_nelmin(int n_bands, const double *wl, double theta_sun_deg, doub
          ifault);
   md_free(md);
 }
+
+/* The reference's own interval statistic of the depth uncertainty
+ * (model/samodel.c:1459-1460): vec_mean2_double then vec_stddev_double
+ * (model/common.c:877-940) with spval 0 over one interval's refitted sample
+ * depths. */
+double photic_ref_depth_sigma_stat(double *depths, int n) {
+  double mean_trial_depths = vec_mean2_double(depths, n, 0.0);
+  return vec_stddev_double(depths, n, 0.0, mean_trial_depths);
+}

@@ -94,3 +94,32 @@ def test_scene_stacks_bit_exact(n_scenes, n_spatial, n_bottoms):
                               n_bottoms=n_bottoms, nthreads=8, which="reference")
     np.testing.assert_array_equal(a[:, cols], b[:, cols])
     assert np.all(a[a[:, 9] == 0, 10] == n_scenes)
+
+
+def test_depth_sigma_statistics_bit_exact():
+    """The depth uncertainty's per-interval statistic (model/samodel.c:
+    1459-1460) -- the reference's vec_mean2_double / vec_stddev_double with
+    samples at 0 (no pixel found) and within 1e-4 of 0 left out -- against the
+    oracle's restatement, which the GPU's table reproduces given the same
+    refitted depths (tests/test_gpu_depth_sigma.py)."""
+    import ctypes as C
+    ref = O.reference().lib.photic_ref_depth_sigma_stat
+    ref.restype = C.c_double
+    ref.argtypes = [C.POINTER(C.c_double), C.c_int]
+    rng = np.random.default_rng(17)
+    n_samples, n_int = 32, 40
+    samples = rng.uniform(0.1, 30.0, size=(n_int, n_samples))
+    samples[rng.uniform(size=samples.shape) < 0.3] = 0.0      # intervals with misses
+    samples[3] = 0.0                                           # an empty interval
+    samples[4, :5] = 5e-5                                      # inside the 1e-4 tolerance
+    samples[5, 1:] = 0.0                                       # a single refit
+    samples[6] = np.float32(7.3)                               # all equal
+    depth = np.full(16, 0.0, dtype=np.float32)
+    depth[0] = n_int / 4.0 + 0.1                               # intervals up to n_int / 4 m
+    rrs = np.full((16, 4), 0.01, dtype=np.float32)
+    _, table, _, _ = O.depth_sigma(rrs, depth, [2e-4] * 4, n_samples=n_samples, seed=3,
+                                   sample_depth=np.pad(samples, ((0, 120 - n_int), (0, 0))).ravel())
+    for k in range(n_int):
+        v = np.ascontiguousarray(samples[k])
+        want = ref(v.ctypes.data_as(C.POINTER(C.c_double)), n_samples)
+        assert table[k] == want, (k, table[k], want)
