@@ -151,6 +151,38 @@ typedef struct photic_scene {
   int ps_x;
 } photic_scene;
 
+/* The reference's SCENE command (model/bam.c:1300-1543), parsed from its
+ * text into the scene record run_scene fills: name, band count, band
+ * wavelengths (stored as int, as the record holds them), THETAVIEW and
+ * THETASUN (subsurface, degrees), and the optional RINF, HTIDE, K, RSIGMA,
+ * KSIGMA (an absent KSIGMA is K / 10) and P / G / X grid names.  The band
+ * grid names are returned in band_names; band_indexes are 0..n_bands-1 and
+ * a caller maps them onto its own grids.  Where the reference fills an
+ * absent RINF, K or RSIGMA from deep-water estimates of other commands, the
+ * record keeps zeros and `given` lacks that bit.  Host function;
+ * PHOTIC_ERR_INVALID with the reference's usage text on a malformed line. */
+#define PHOTIC_SCENE_MAX_BANDS 64
+#define PHOTIC_SCENE_NAME_LEN 256
+enum {
+  PHOTIC_SCENE_RINF = 1,
+  PHOTIC_SCENE_HTIDE = 2,
+  PHOTIC_SCENE_K = 4,
+  PHOTIC_SCENE_RSIGMA = 8,
+  PHOTIC_SCENE_KSIGMA = 16
+};
+typedef struct photic_scene_spec {
+  photic_scene scene;
+  char band_names[PHOTIC_SCENE_MAX_BANDS][PHOTIC_SCENE_NAME_LEN];
+  char pgx_names[3][PHOTIC_SCENE_NAME_LEN];
+  int32_t given; /* PHOTIC_SCENE_* of the optional items present */
+} photic_scene_spec;
+int photic_parse_scene(const char *line, photic_scene_spec *out);
+
+/* The inversion's configuration for a scene record: its bands and
+ * wavelengths, THETASUN / THETAVIEW as the subsurface angles samodel() uses
+ * (model/samodel.c:534-548) and HTIDE; everything else the defaults. */
+int photic_config_from_scene(const photic_scene *scene, photic_config *cfg);
+
 /* model/samodel.h:8-19.  Fits every pixel that has data in all bands of all
  * scenes (model/samodel.c:672-700); n_bottoms == 1 (sand) is required;
  * n_spatial <= 1 fits each pixel alone, n_spatial == 2 (one scene, no

@@ -25,7 +25,8 @@ LIB = os.path.join(HERE, "libphotic_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["photic_host.cu", "photic_invert.cu", "photic_guarded.cu", "photic_joint.cu",
            "photic_joint_group.cu", "photic_region.cu",
-           "photic_gemm.cu", "photic_mlp.cu", "photic_aux.cu", "photic_ncgrid.cu"]
+           "photic_gemm.cu", "photic_mlp.cu", "photic_aux.cu", "photic_ncgrid.cu",
+           "photic_scene.cu"]
 
 
 def nvcc() -> str:

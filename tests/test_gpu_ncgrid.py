@@ -142,3 +142,34 @@ def test_reference_entry_points(gpu, port, tmp_path):
     libc.free(C.cast(g, C.c_void_p))
     libc.free(C.cast(plons, C.c_void_p))
     libc.free(C.cast(plats, C.c_void_p))
+
+
+def test_scene_command_feeds_the_inversion(gpu, port, tmp_path):
+    """A scene given the reference's way -- a SCENE line naming its band grids
+    (model/bam.c:1300-1543) and the grids as netCDF files -- read into the
+    device layout and inverted: the same fits as the unpacked bands inverted
+    directly, and the configuration the line gives (sun 31.5 deg)."""
+    import torch
+    from photic_gb300 import ncgrid as N
+    from photic_gb300 import scene as S
+    nr, nc = 24, 32
+    rrs, _ = port.generate_single(4711, nr * nc, mask_frac=0.1, theta_sun=31.5)
+    lons = np.linspace(150.0, 150.3, nc).astype(np.float32)
+    lats = np.linspace(-24.0, -23.8, nr).astype(np.float32)
+    names = ["coastal", "blue", "green", "red"]
+    for b, n in enumerate(names):
+        band = np.ascontiguousarray(rrs[:, b].reshape(nr, nc))
+        N.write_grid(str(tmp_path / f"{n}.nc"), torch.from_numpy(band).cuda(), lons, lats,
+                     -9999.0)
+    line = ("SCENE NAME oli BANDS coastal blue green red WAVELENGTHS 443 482 561 655 "
+            "THETAVIEW 0 THETASUN 31.5 HTIDE 0.25")
+    cfg, dev_rrs, info, _, _, rec = S.load(line, lambda n: str(tmp_path / f"{n}.nc"))
+    assert rec["bands"] == names and cfg.theta_sun_deg == 31.5 and cfg.h_tide == 0.25
+    assert info["nrows"] == nr and info["ncols"] == nc
+    out = gpu.invert(dev_rrs, cfg)
+    ref = gpu.invert(dev_rrs.clone(), gpu.Config(theta_sun_deg=31.5, h_tide=0.25))
+    gpu.sync()
+    for f in ("depth_f64", "status", "P"):
+        assert torch.equal(out[f], ref[f]), f
+    st = out["status"].cpu().numpy() & 0xFF
+    assert (st == 0).sum() > 0.8 * nr * nc
