@@ -221,6 +221,8 @@ def main():
                     help="initial simplex of a seeded fit, relative to the cold-start steps")
     ap.add_argument("--plain-side", type=int, default=4096,
                     help="side of the plain-method scene leg (0: skip)")
+    ap.add_argument("--precision-npix", type=int, default=1 << 20,
+                    help="pixels of the precision-policy leg (0: skip)")
     ap.add_argument("--joint-npix", type=int, default=1 << 18,
                     help="pixels of the 4096x4096 temporal grid for the joint-fit leg (0: skip)")
     ap.add_argument("--region-side", type=int, default=96,
@@ -438,6 +440,9 @@ def main():
     plain4096 = None
     if rank == 0 and args.plain_side > 0:
         plain4096 = plain_scene_leg(args, dev)
+    precision = None
+    if rank == 0 and args.precision_npix > 0:
+        precision = precision_leg(args, dev)
     temporal = None
     if rank == 0 and args.joint_npix > 0:
         temporal = temporal_leg(args, dev)
@@ -477,7 +482,8 @@ def main():
                 "oracle_sample": warm_stats, "roofline": roof, "cpu_baseline": cpu,
                 "plain": plain, "network_gain": gain, "train": train,
                 "seed_polish_ms_per_step": ms_step - ms_inv,
-                "plain_4096x4096": plain4096, "serving": serving, "temporal": temporal,
+                "plain_4096x4096": plain4096, "precision": precision,
+                "serving": serving, "temporal": temporal,
                 "regions": regions, "ncgrid": ncgrid, "e2e": e2e, "clocks": clk}
         print(json.dumps(line))
     if pg_ is not None:
@@ -562,6 +568,61 @@ def e2e_leg(args, dev, net, scene, tile, tiles, sample_frac):
             "d2h_bytes_per_step": int(tile * 8), "ms_per_step": ms / tiles,
             "note": "one pass over the scene's tiles; per tile H2D of the spectra, seeding, "
                     "the ordered inversion and D2H of depth and status"}
+
+
+def precision_leg(args, dev):
+    """The precision policies on the same 2^20 pixels of the 4096 x 4096
+    scene: FP64 (the headline), the FP32 forward model with the
+    special-function unit, double-float, and guarded (double-float screening,
+    FP64 decisions), each against the FP64 oracle on a sample, with the
+    guarded kernel's tally of how its decisions were taken."""
+    import torch
+    import photic_gb300 as pg
+    from photic_gb300 import _lib as L
+    from oracle import oracle as O
+    n = args.precision_npix
+    rrs, _ = pg.generate_scene(n, seed=SEED, pix0=4096 * 1024, device=dev, with_truth=False)
+    rng = np.random.default_rng(3)
+    idx = np.sort(rng.choice(n, size=min(args.sample, n), replace=False))
+    ref = O.invert_batch(rrs[torch.tensor(idx, device=dev)].cpu().numpy(),
+                         nthreads=os.cpu_count() or 1)
+    stats = torch.zeros(5, dtype=torch.int64, device=dev)
+    res = {"workload": f"{n} pixels of the 4096x4096 plain-method scene, cold start"}
+    fields = ("depth_f64", "status", "evals")
+    for prec in ("fp64", "fp32", "df64", "guarded"):
+        cfg = pg.Config(precision=prec)
+        pg.invert(rrs[:8192], cfg, fields=fields)
+        torch.cuda.synchronize()
+        stats.zero_()
+        L.check(L.lib().photic_set_guard_stats(stats.data_ptr()))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = pg.invert(rrs, cfg, fields=fields)
+        e1.record()
+        torch.cuda.synchronize()
+        L.check(L.lib().photic_set_guard_stats(None))
+        pg.sync()
+        t = e0.elapsed_time(e1) * 1e-3
+        st = out["status"].cpu().numpy()
+        conv = ((st & 0xFF) == 0) & ((st >> 8) & 1).astype(bool)
+        h = out["depth_f64"].cpu().numpy()
+        m = (ref[:, 9] == 0) & conv[idx]
+        s = oracle_stats(h[idx], ref, m)
+        ev = out["evals"].cpu().numpy()
+        r = {"converged_px_s": float(conv.sum()) / t, "seconds": t,
+             "evals_per_s": float(ev.sum()) / t, "oracle_sample": s,
+             "converged_px_s_within_1cm": float(conv.sum()) * s["frac_within_1cm"] / t}
+        if prec == "guarded":
+            g = stats.cpu().numpy().astype(float)
+            dec = g[0] + g[1] + g[2]
+            r["decisions"] = {"exact_known": g[0] / dec, "screened": g[1] / dec,
+                              "deferred_to_fp64": g[2] / dec,
+                              "lane_trips_waiting": g[3] / max(g[4], 1.0)}
+        res[prec] = r
+    del rrs
+    torch.cuda.empty_cache()
+    return res
 
 
 def plain_scene_leg(args, dev):

@@ -54,8 +54,10 @@ enum {
 enum {
   PHOTIC_PREC_FP64 = 0, /* IEEE double in the reference's operation order */
   PHOTIC_PREC_DF64 = 1, /* double-float (two FP32 words) on the FP32 pipes */
-  PHOTIC_PREC_FP32 = 2, /* FP32 forward model; FP64 for the convergence and
-                           local-minimum tests only */
+  PHOTIC_PREC_FP32 = 2, /* forward model in FP32 with the special-function
+                           unit's exp and log; the simplex, its decisions, the
+                           convergence and local-minimum tests and the final
+                           re-evaluation in FP64 (not FP64-faithful) */
   PHOTIC_PREC_GUARDED = 3 /* FP64 decisions: every cost screened in
                              double-float, near ties re-evaluated in IEEE
                              double; same trajectory as PHOTIC_PREC_FP64 */
@@ -364,6 +366,14 @@ int photic_seed_polished_heuristic(const photic_config *cfg, const float *d_rrs,
  * later PHOTIC_PREC_GUARDED inversions add the number of exact FP64
  * re-evaluations they served to it.  Pass NULL to stop. */
 int photic_set_counter(unsigned long long *d_counter);
+
+/* Instrumentation of PHOTIC_PREC_GUARDED: if d_stats (device, 5 unsigned
+ * long long) is not NULL, later guarded inversions add to it the number of
+ * Nelder-Mead decisions taken on exact FP64 values already known, on the
+ * double-float screen, and deferred to an exact FP64 evaluation, then the
+ * lane-trips of the kernel's loop spent waiting for an exact value and
+ * the lane-trips spent on a pixel.  Pass NULL to stop. */
+int photic_set_guard_stats(unsigned long long *d_stats);
 
 /* Message of the most recent error on this host thread. */
 const char *photic_last_error(void);

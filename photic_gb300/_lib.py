@@ -142,6 +142,7 @@ _SIGS = {
     "photic_autotune": (C.c_int, [C.POINTER(photic_config), C.c_int32, C.c_int64,
                                   C.POINTER(C.c_double), C.c_int32, C.POINTER(C.c_int32)]),
     "photic_set_counter": (C.c_int, [C.c_void_p]),
+    "photic_set_guard_stats": (C.c_int, [C.c_void_p]),
     "photic_surrogate_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_uint64]),
     "photic_surrogate_destroy": (C.c_int, [C.c_void_p]),
     "photic_surrogate_num_params": (C.c_int32, []),

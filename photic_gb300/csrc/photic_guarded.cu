@@ -88,25 +88,48 @@ __device__ __forceinline__ float screen_tol(const Lv &a, const Lv &b, float tol_
   return kTau * (dabs_hi(a.df) + dabs_hi(b.df)) + tol_abs;
 }
 
+// Per-lane tally of how decisions were taken (photic_set_guard_stats):
+// on exact values already known, on the double-float screen, or deferred to
+// an exact FP64 evaluation.
+struct Tally {
+  unsigned long long exact, screened, deferred;
+};
+
 // a < b decided on double-float values when the gap is clear of the
 // screening tolerance; returns 0/1, or 2 when exact values are needed.
-__device__ __forceinline__ int lz_lt(const Lv &a, const Lv &b, float tol_abs) {
-  if (a.has && b.has) return a.ex < b.ex;
+__device__ __forceinline__ int lz_lt(const Lv &a, const Lv &b, float tol_abs, Tally &t) {
+  if (a.has && b.has) {
+    t.exact++;
+    return a.ex < b.ex;
+  }
   df64 d = df_sub(a.df, b.df);
-  if (fabsf(d.hi) > screen_tol(a, b, tol_abs)) return d.hi < 0.0f;
+  if (fabsf(d.hi) > screen_tol(a, b, tol_abs)) {
+    t.screened++;
+    return d.hi < 0.0f;
+  }
+  t.deferred++;
   return 2;
 }
-__device__ __forceinline__ int lz_le(const Lv &a, const Lv &b, float tol_abs) {
-  if (a.has && b.has) return a.ex <= b.ex;
+__device__ __forceinline__ int lz_le(const Lv &a, const Lv &b, float tol_abs, Tally &t) {
+  if (a.has && b.has) {
+    t.exact++;
+    return a.ex <= b.ex;
+  }
   df64 d = df_sub(a.df, b.df);
-  if (fabsf(d.hi) > screen_tol(a, b, tol_abs)) return d.hi < 0.0f;
+  if (fabsf(d.hi) > screen_tol(a, b, tol_abs)) {
+    t.screened++;
+    return d.hi < 0.0f;
+  }
+  t.deferred++;
   return 2;
 }
 
 // trunc((long)(10*y)) from a double-float value when no integer lies within
 // the screening tolerance of 10*y; sets *ok = false otherwise.
-__device__ __forceinline__ long long lz_trunc10(const Lv &a, bool *ok, float tol_abs) {
+__device__ __forceinline__ long long lz_trunc10(const Lv &a, bool *ok, float tol_abs,
+                                                Tally &t) {
   if (a.has) {
+    t.exact++;
     *ok = true;
     return trunc10(a.ex);
   }
@@ -115,9 +138,11 @@ __device__ __forceinline__ long long lz_trunc10(const Lv &a, bool *ok, float tol
   df64 dist = df_add_f(w, -r);
   float tol = 10.0f * (kTau * dabs_hi(a.df) + tol_abs);
   if (!(fabsf(dist.hi) > tol) || !(fabsf(w.hi) < 1.0e15f)) {
+    t.deferred++;
     *ok = false;
     return 0;
   }
+  t.screened++;
   *ok = true;
   return df_trunc10(a.df);
 }
@@ -135,6 +160,7 @@ struct Shared {
   int32_t ring[BS];              // requesting thread + 1, 0 = empty
   int32_t ring_head, ring_tail, lock;
   unsigned long long served;     // exact evaluations served by this block
+  unsigned long long stats[5];   // exact, screened, deferred decisions; wait and busy trips
   float chunk[BS / 32][32][NB];
 };
 
@@ -150,6 +176,7 @@ __global__ void __launch_bounds__(BS) guarded_kernel(const __grid_constant__ Inv
     S.ring_tail = 0;
     S.lock = 0;
     S.served = 0;
+    for (int i = 0; i < 5; i++) S.stats[i] = 0;
   }
   S.ring[tid] = 0;
   S.rq_state[tid] = 0;
@@ -157,6 +184,8 @@ __global__ void __launch_bounds__(BS) guarded_kernel(const __grid_constant__ Inv
 
   const photic_outputs &o = args.out;
   const double var_limit = fp.reqmin * (double)kN;
+  Tally tally = {0ull, 0ull, 0ull};
+  unsigned long long wait_trips = 0, busy_trips = 0;
 
   // ---- per-lane state ----------------------------------------------------
   PixelDF<NB> pd;
@@ -313,7 +342,7 @@ __global__ void __launch_bounds__(BS) guarded_kernel(const __grid_constant__ Inv
           int bl = 0;
           for (int j = 1; j <= kN; j++) {
             Lv fj = Fv(j);
-            int r = lz_lt(fj, best_v, tol_abs);
+            int r = lz_lt(fj, best_v, tol_abs, tally);
             if (r == 2) {
               cs_resume = CX_READY;
               need(pick_need(fj, j, best_v, bl));
@@ -339,7 +368,7 @@ __global__ void __launch_bounds__(BS) guarded_kernel(const __grid_constant__ Inv
           int h = 0;
           for (int j = 1; j <= kN; j++) {
             Lv fj = Fv(j);
-            int r = lz_lt(yhi, fj, tol_abs);
+            int r = lz_lt(yhi, fj, tol_abs, tally);
             if (r == 2) {
               cs_resume = CX_TOP;
               need(pick_need(yhi, h, fj, j));
@@ -366,7 +395,7 @@ __global__ void __launch_bounds__(BS) guarded_kernel(const __grid_constant__ Inv
           return 0;
         }
         case CX_DEC_REFLECT: {  // model/asa047.c:251-329
-          int r = lz_lt(fr, ylo, tol_abs);
+          int r = lz_lt(fr, ylo, tol_abs, tally);
           if (r == 2) {
             cs_resume = CX_DEC_REFLECT;
             need(pick_need(fr, SL_REFL, ylo, ylo_src));
@@ -382,7 +411,7 @@ __global__ void __launch_bounds__(BS) guarded_kernel(const __grid_constant__ Inv
           int worse = 0;
           for (int j = 0; j <= kN; j++) {
             Lv fj = Fv(j);
-            int q = lz_lt(fr, fj, tol_abs);
+            int q = lz_lt(fr, fj, tol_abs, tally);
             if (q == 2) {
               cs_resume = CX_DEC_REFLECT;
               need(pick_need(fr, SL_REFL, fj, j));
@@ -413,7 +442,7 @@ __global__ void __launch_bounds__(BS) guarded_kernel(const __grid_constant__ Inv
           break;
         }
         case CX_DEC_EXPAND: {
-          int r = lz_lt(fr, ft, tol_abs);
+          int r = lz_lt(fr, ft, tol_abs, tally);
           if (r == 2) {
             cs_resume = CX_DEC_EXPAND;
             need(pick_need(fr, SL_REFL, ft, SL_TRIAL));
@@ -430,7 +459,7 @@ __global__ void __launch_bounds__(BS) guarded_kernel(const __grid_constant__ Inv
         }
         case CX_DEC_CIN: {
           Lv fh = Fv(hi);
-          int r = lz_lt(fh, ft, tol_abs);
+          int r = lz_lt(fh, ft, tol_abs, tally);
           if (r == 2) {
             cs_resume = CX_DEC_CIN;
             need(pick_need(fh, hi, ft, SL_TRIAL));
@@ -459,7 +488,7 @@ __global__ void __launch_bounds__(BS) guarded_kernel(const __grid_constant__ Inv
           break;
         }
         case CX_DEC_COUT: {
-          int r = lz_le(ft, fr, tol_abs);
+          int r = lz_le(ft, fr, tol_abs, tally);
           if (r == 2) {
             cs_resume = CX_DEC_COUT;
             need(pick_need(ft, SL_TRIAL, fr, SL_REFL));
@@ -476,7 +505,7 @@ __global__ void __launch_bounds__(BS) guarded_kernel(const __grid_constant__ Inv
         }
         case CX_ITER_END: {  // model/asa047.c:395-405
           Lv fh = Fv(hi);
-          int r = lz_lt(fh, ylo, tol_abs);
+          int r = lz_lt(fh, ylo, tol_abs, tally);
           if (r == 2) {
             cs_resume = CX_ITER_END;
             need(pick_need(fh, hi, ylo, ylo_src));
@@ -544,7 +573,7 @@ __global__ void __launch_bounds__(BS) guarded_kernel(const __grid_constant__ Inv
         case CX_END_INNER: {  // model/asa047.c:436-453
           Lv fl = Fv(lo);
           bool ok;
-          long long f10 = lz_trunc10(fl, &ok, tol_abs);
+          long long f10 = lz_trunc10(fl, &ok, tol_abs, tally);
           if (!ok) {
             cs_resume = CX_END_INNER;
             need(lo);
@@ -578,7 +607,7 @@ __global__ void __launch_bounds__(BS) guarded_kernel(const __grid_constant__ Inv
         case CX_DEC_PROBE_PLUS:
         case CX_DEC_PROBE_MINUS: {
           bool ok;
-          long long t = lz_trunc10(fpb, &ok, tol_abs);
+          long long t = lz_trunc10(fpb, &ok, tol_abs, tally);
           if (!ok) {
             cs_resume = cs;
             need(SL_PROBE);
@@ -622,7 +651,7 @@ __global__ void __launch_bounds__(BS) guarded_kernel(const __grid_constant__ Inv
           break;
         case CX_NM_DONE: {  // model/samodel.c:2380-2405
           Lv yn = Fv(lo);
-          int r = lz_lt(yn, lowest, tol_abs);
+          int r = lz_lt(yn, lowest, tol_abs, tally);
           if (r == 2) {
             cs_resume = CX_NM_DONE;
             need(pick_need(yn, lo, lowest, SL_BEST));
@@ -659,7 +688,7 @@ __global__ void __launch_bounds__(BS) guarded_kernel(const __grid_constant__ Inv
           ee.df = df_from_double(args.early_exit);
           ee.ex = args.early_exit;
           ee.has = true;
-          int r = lz_lt(lowest, ee, tol_abs);
+          int r = lz_lt(lowest, ee, tol_abs, tally);
           if (r == 2) {
             cs_resume = CX_NM_DONE2;
             need(SL_BEST);
@@ -831,6 +860,8 @@ __global__ void __launch_bounds__(BS) guarded_kernel(const __grid_constant__ Inv
 
     // ---- one double-float evaluation per lane, then the bookkeeping --------
     if (has) {
+      busy_trips++;
+      if (phase == PHX_WAIT) wait_trips++;
       if (phase == PHX_WAIT) {
         if (*((volatile int32_t *)&S.rq_state[tid]) == 2) {
           __threadfence_block();
@@ -1012,9 +1043,18 @@ __global__ void __launch_bounds__(BS) guarded_kernel(const __grid_constant__ Inv
       }
     }
   }
-  // exact-evaluation count for the roofline
+  // exact-evaluation count for the roofline, and how the decisions went
+  if (args.guard_stats) {
+    atomicAdd(&S.stats[0], tally.exact);
+    atomicAdd(&S.stats[1], tally.screened);
+    atomicAdd(&S.stats[2], tally.deferred);
+    atomicAdd(&S.stats[3], wait_trips);
+    atomicAdd(&S.stats[4], busy_trips);
+  }
   __syncthreads();
   if (tid == 0 && args.counters) atomicAdd(args.counters, S.served);
+  if (tid == 0 && args.guard_stats)
+    for (int i = 0; i < 5; i++) atomicAdd(args.guard_stats + i, S.stats[i]);
 }
 
 template <int NB, int BS>

@@ -196,6 +196,7 @@ void make_df(const photic_config &cfg, const FitParams &fp, const SceneConsts &s
 // Optional device counter of exact evaluations served by the guarded
 // kernel (photic_set_counter); NULL when unset.
 unsigned long long *g_counter_ptr = nullptr;
+unsigned long long *g_guard_stats_ptr = nullptr;
 
 // Sticky per-device error word the kernels OR their error bits into.
 std::mutex g_dev_mu;
@@ -387,8 +388,6 @@ int photic_invert_batch_ordered(const photic_config *cfg, const float *d_rrs, in
   if (!d_rrs || !out) return fail(PHOTIC_ERR_INVALID, "NULL input or output");
   if (pixel_stride < 1 || band_stride < 1)
     return fail(PHOTIC_ERR_INVALID, "strides must be >= 1");
-  if (cfg->precision == PHOTIC_PREC_FP32)
-    return fail(PHOTIC_ERR_UNSUPPORTED, "precision %d not built in this version", cfg->precision);
   if (d_order && cfg->precision == PHOTIC_PREC_GUARDED)
     return fail(PHOTIC_ERR_UNSUPPORTED, "a pixel order is not supported in guarded precision");
   if (d_order && npix > 0x7fffffffLL) return fail(PHOTIC_ERR_INVALID, "npix beyond 2^31-1");
@@ -437,6 +436,7 @@ int photic_invert_batch_ordered(const photic_config *cfg, const float *d_rrs, in
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
   a.queue = queue;
   a.counters = g_counter_ptr;
+  a.guard_stats = g_guard_stats_ptr;
   e = guarded ? launch_guarded(a, block, (int)grid, s)
               : launch_invert(a, cfg->precision, block, (int)grid, s);
   cudaError_t e2 = cudaFreeAsync(queue, s);
@@ -949,6 +949,11 @@ int photic_surrogate_seed_polished(photic_surrogate *s, const photic_config *cfg
   cudaFreeAsync(y, st);
   if (rc) return rc;
   if (e != cudaSuccess) return cuda_fail(e, "surrogate seeds");
+  return PHOTIC_OK;
+}
+
+int photic_set_guard_stats(unsigned long long *d_stats) {
+  g_guard_stats_ptr = d_stats;
   return PHOTIC_OK;
 }
 

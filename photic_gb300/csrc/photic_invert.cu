@@ -13,7 +13,9 @@
 // never leave a lane idle while work remains.
 //
 // The arithmetic is a policy: PrecF64 (IEEE double, reference operation
-// order, --fmad=false) or PrecDF (double-float on the FP32 pipes).
+// order, --fmad=false), PrecF32 (the forward model in float with the
+// special-function unit, the simplex in double) or PrecDF (double-float on
+// the FP32 pipes).
 //
 // Scratch: one 64-bit queue head per call (stream-ordered allocation in
 // photic_host.cu) and the per-device sticky error word.
@@ -92,6 +94,106 @@ struct PrecF64 {
     d.bottom_albedo = det.bottom_albedo;
     d.K_min = det.K_min;
     d.iod = det.iod;
+  }
+};
+
+// Single-precision forward model (the north star's "FP32 with SFU expf"):
+// the cost of a double parameter vector evaluated in float with the
+// special-function unit's exp and log and approximate divisions, returned as
+// a double; the simplex, its decisions, the convergence and local-minimum
+// tests and the final re-evaluation at the kept optimum stay in FP64.
+template <int NB>
+struct PixelF32 {
+  PixelF64<NB> d;        // the double set-up (cold starts, details)
+  float rrs[NB], pw[NB];
+  float mean;
+};
+
+struct PrecF32 : PrecF64 {
+  template <int NB>
+  using Pixel = PixelF32<NB>;
+  template <int NB>
+  static __device__ __forceinline__ void setup(const InvertArgs &a, const float *r, Pixel<NB> &px) {
+    PrecF64::setup<NB>(a, r, px.d);
+#pragma unroll
+    for (int b = 0; b < NB; b++) {
+      px.rrs[b] = (float)px.d.rrs[b];
+      px.pw[b] = (float)px.d.pw[b];
+    }
+    px.mean = (float)px.d.mean;
+  }
+  template <int NB>
+  static __device__ __forceinline__ void cold_start(const InvertArgs &a, const Pixel<NB> &px,
+                                                    T *start, T *step) {
+    cold_start_f64<NB>(a.fp, px.d, start, step);
+  }
+  // samodel_error (model/samodel.c:2432-2759) over samodel_Rrs (:2846-2949)
+  // for one region, scene and bottom type, in float
+  template <int NB>
+  static __device__ __forceinline__ T cost(const InvertArgs &a, const Pixel<NB> &px, const T *x) {
+    const FitParams &fp = a.fp;
+    const SceneConsts &sc = a.sc;
+    const int nb = fp.n_bands;
+    const float H = fabsf((float)x[0]);
+    const float B = 0.01f * fabsf((float)x[1]);
+    const float qa = fabsf((float)x[2]);
+    const float q = qa / qa;
+    const float P = 0.01f * fabsf((float)x[3]);
+    const float G = 0.01f * fabsf((float)x[4]);
+    const float X = 0.01f * fabsf((float)x[5]);
+    const float lnP = __logf(P);
+    const float qB = q * B;
+    const float ss = (float)sc.sec_sun, sv = (float)sc.sec_view;
+    float err = 0.0f, K_min = 1.0e4f;
+#pragma unroll
+    for (int b = 0; b < NB; b++) {
+      if (b < nb) {
+        const float rho = qB * (float)sc.refl[b];
+        const float a_phi = ((float)sc.a0[b] + (float)sc.a1[b] * lnP) * P;
+        const float a_g = G * (float)sc.eS[b];
+        const float aa = (float)sc.aw[b] + a_phi + a_g;
+        const float bb = (float)sc.bbw[b] + X * px.pw[b];
+        const float u = __fdividef(bb, aa + bb);
+        float K = aa + bb;
+        K = fminf(fmaxf(K, 0.0f), 2.5f);
+        const float rrs_dp = (0.084f + 0.170f * u) * u;
+        const float DuC = 1.03f * sqrtf(1.0f + 2.4f * u);
+        const float DuB = 1.04f * sqrtf(1.0f + 5.4f * u);
+        const float rrs_C = rrs_dp * (1.0f - __expf(-(ss + DuC * sv) * K * H));
+        const float rrs_B = rho * 0.31830988618f * __expf(-(ss + DuB * sv) * K * H);
+        const float rrs = rrs_C + rrs_B;
+        const float Rm = __fdividef(0.5f * rrs, 1.0f - 1.5f * rrs);
+        const float d = Rm - px.rrs[b];
+        err += d * d;
+        if (K != 0.0f && K < K_min) K_min = K;
+      }
+    }
+    const float E = __fdividef(100.0f * sqrtf(err / (float)nb), px.mean);
+    float Ke = 0.0f;
+    int c = -1;
+    const KPenalty &kp = fp.kp;
+    if (H < 1.0f && K_min < (float)kp.k_thr[0]) c = 0;
+    else if (H < 2.0f && K_min < (float)kp.k_thr[1]) c = 1;
+    else if (H < 3.0f && K_min < (float)kp.k_thr[2]) c = 2;
+    else if (H < 4.0f && K_min < (float)kp.k_thr[3]) c = 3;
+    else if (H < 5.0f && K_min < (float)kp.k_thr[4]) c = 4;
+    if (c >= 0) {
+      float it = (float)kp.inv_t[0];
+      for (int i = 1; i < 5; i++)
+        if (i == c) it = (float)kp.inv_t[i];
+      const float d = __fdividef(1.0f, 0.01f + K_min) - it;
+      Ke = 100.0f * d * d;
+    }
+    if (K_min > 0.7f) {
+      const float d = 4.0f * (K_min - 0.7f);
+      Ke += 100.0f * d * d;
+    }
+    return (double)((80.0f * E + 15.0f * Ke) * (1.0f / 120.0f));
+  }
+  template <int NB>
+  static __device__ __forceinline__ void details(const InvertArgs &a, const Pixel<NB> &px,
+                                                 const T *x, Details &d) {
+    PrecF64::details<NB>(a, px.d, x, d);
   }
 };
 
@@ -397,13 +499,15 @@ size_t invert_smem_bytes(int block, int nb) {
 cudaError_t launch_invert(const InvertArgs &a, int precision, int block, int grid,
                           cudaStream_t s) {
   if (precision == PHOTIC_PREC_DF64) return launch_prec<PrecDF>(a, block, grid, s, nullptr);
+  if (precision == PHOTIC_PREC_FP32) return launch_prec<PrecF32>(a, block, grid, s, nullptr);
   return launch_prec<PrecF64>(a, block, grid, s, nullptr);
 }
 
 int invert_blocks_per_sm(const InvertArgs &a, int precision, int block) {
   int n = 0;
-  cudaError_t e = precision == PHOTIC_PREC_DF64 ? launch_prec<PrecDF>(a, block, 0, 0, &n)
-                                                : launch_prec<PrecF64>(a, block, 0, 0, &n);
+  cudaError_t e = precision == PHOTIC_PREC_DF64   ? launch_prec<PrecDF>(a, block, 0, 0, &n)
+                  : precision == PHOTIC_PREC_FP32 ? launch_prec<PrecF32>(a, block, 0, 0, &n)
+                                                  : launch_prec<PrecF64>(a, block, 0, 0, &n);
   return e == cudaSuccess ? n : 0;
 }
 

@@ -29,6 +29,9 @@ struct InvertArgs {
   unsigned long long *queue;
   unsigned int *error;
   unsigned long long *counters;  // optional: exact evaluations served (guarded)
+  unsigned long long *guard_stats;  // optional [5] (guarded): decisions taken on exact
+                                    // values, on the double-float screen, deferred to FP64;
+                                    // lane trips waiting for an exact value, lane trips busy
   double early_exit;  // early-exit cost threshold (per-scene value * scenes)
   int32_t no_mask;    // fit every pixel: samodel_optimise has no mask test
   const int32_t *order;  // optional queue position -> pixel (e.g. long fits first)
