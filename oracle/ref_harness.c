@@ -531,3 +531,57 @@ double photic_ref_depth_sigma_stat(double *depths, int n) {
   double mean_trial_depths = vec_mean2_double(depths, n, 0.0);
   return vec_stddev_double(depths, n, 0.0, mean_trial_depths);
 }
+
+/* The reference's own product path: samodel() (model/samodel.c:289-1763)
+ * over one scene's [nrows][ncols][n_bands] float grid with its compiled-in
+ * dynamic LUT, spectral ordering and hot starts (LUT 1, model/samodel.c:97),
+ * run on one thread so that its order-dependent results are reproducible,
+ * at the reference's own tolerances.  Outputs the depth grid (positive) and
+ * the model-error grid as samodel() leaves them; its depth-uncertainty pass
+ * and result files run as well (the netCDF stand-in keeps the files). */
+int photic_ref_samodel_grid(int n_bands, const double *wl, double theta_sun_deg,
+                            double theta_view_deg, const float *grid, int nrows, int ncols,
+                            float nodata, int n_spatial, int n_bottoms, float *depth_out,
+                            float *error_out) {
+  scene sc;
+  geogrid *gd, none;
+  float **out[10];
+  int b, i, j, k, idx = 0;
+  if (n_bands < 2 || n_bands > REF_MAX_BANDS) return 1;
+  memset(&sc, 0, sizeof sc);
+  memset(&none, 0, sizeof none);
+  strcpy(sc.scene_name, "harness");
+  sc.n_bands = n_bands;
+  sc.nrows = nrows;
+  sc.ncols = ncols;
+  sc.theta_w = theta_sun_deg;
+  sc.theta_v = theta_view_deg;
+  gd = (geogrid *)calloc(n_bands, sizeof(geogrid));
+  for (b = 0; b < n_bands; b++) {
+    sc.band_indexes[b] = b;
+    sc.wavelengths[b] = (int)wl[b];
+    gd[b].nrows = nrows;
+    gd[b].ncols = ncols;
+    gd[b].cellsize = 1.0f;
+    gd[b].nodata_value = nodata;
+    allocate_float_array_2d(&gd[b].array, nrows, ncols);
+    for (i = 0; i < nrows; i++)
+      for (j = 0; j < ncols; j++) gd[b].array[i][j] = grid[((size_t)i * ncols + j) * n_bands + b];
+  }
+  for (k = 0; k < 10; k++) allocate_float_array_2d(&out[k], nrows, ncols);
+  set_tol(0, 0.0, 0, 0);
+#if _OPENMP
+  omp_set_num_threads(1);
+#endif
+  samodel(&sc, gd, &idx, 1, false, none, 1, n_spatial, n_bottoms, out[0], out[1], out[2],
+          out[3], out[4], out[5], out[6], out[7], out[8], out[9], 10.0f, 0, 1);
+  for (i = 0; i < nrows; i++)
+    for (j = 0; j < ncols; j++) {
+      depth_out[(size_t)i * ncols + j] = -out[0][i][j];
+      error_out[(size_t)i * ncols + j] = out[2][i][j];
+    }
+  for (k = 0; k < 10; k++) free_float_array_2d(out[k], nrows);
+  for (b = 0; b < n_bands; b++) free_float_array_2d(gd[b].array, nrows);
+  free(gd);
+  return 0;
+}
