@@ -913,19 +913,22 @@ def serving_leg(args, net):
 # 43 per band (photic_fp64.cuh cost_f64) + 9 in the tail.
 FLOPS_PER_EVAL_F64 = 4 * 43 + 9
 
-# FP64-pipe warp instructions per cost evaluation (cost + Nelder-Mead
-# bookkeeping), from the ncu capture of invert_kernel<PrecF64, 4, 256>
-# summarised in profiles/invert_fp64_262144px.md; None until measured.
-FP64_INST_PER_EVAL = None
+# FP64 thread instructions per cost evaluation of the seeded headline fit
+# (cost + Nelder-Mead bookkeeping): 160.6 G over 307.75 M evaluations in the
+# ncu capture of invert_kernel<PrecF64, 4, 256> on a 1024 x 1024 tile
+# (profiles/invert_kernel_warm_1024x1024_full.md); issued as 779 lane-slots
+# of FP64 warp instructions (67 % of lanes live).
+FP64_INST_PER_EVAL = 522
 
-# dram__bytes_read.sum + dram__bytes_write.sum of invert_kernel<PrecF64, 4,
-# 256> over a 262 144-pixel launch (4.708608 MB + 0.181248 MB), per pixel:
-# the spectra (16 B) and a few local-memory reloads; at that size the
-# outputs stay in L2, so writes are undercounted.
-TRAFFIC_BYTES_PER_PIXEL = (4.708608e6 + 0.181248e6) / 262144
-TRAFFIC_NOTE = ("DRAM bytes per launch scaled by pixels from an ncu capture of a 262144-pixel "
-                "launch of this kernel (18.7 B/pixel, against 16 B of spectra read and 16 B of "
-                "outputs written; the outputs stayed in L2 at the captured size)")
+# dram__bytes_read.sum + dram__bytes_write.sum of the same capture
+# (76.49 MB + 5.50 MB over 1 048 576 seeded pixels), per pixel: the spectra
+# (16 B) and seed vector (48 B) read, depth, status and evaluation count
+# (16 B) written -- the algorithm's 80 B, no re-reads.
+TRAFFIC_BYTES_PER_PIXEL = (76.485888e6 + 5.499904e6) / 1048576
+TRAFFIC_NOTE = ("DRAM bytes per launch scaled by pixels from an ncu capture of this kernel on a "
+                "1048576-pixel seeded tile (78.2 B/pixel, against the 80 B/pixel the algorithm "
+                "moves: 16 B spectra + 48 B seed read, 16 B written)")
+
 
 if __name__ == "__main__":
     main()

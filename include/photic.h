@@ -68,6 +68,8 @@ enum {
  * of the kept depth start. */
 enum { PHOTIC_PX_FITTED = 0, PHOTIC_PX_MASKED = 1, PHOTIC_PX_INVALID = 2 };
 #define PHOTIC_PX_CONVERGED 0x100
+#define PHOTIC_PX_SERVED 0x200 /* photic_lut_invert_batch: outputs copied from a table entry */
+#define PHOTIC_PX_HOT 0x400    /* photic_lut_invert_batch: fit hot-started from the previous pixel */
 
 /* Parameter layouts of the temporal joint fit. */
 enum {
@@ -253,6 +255,48 @@ int photic_region_fit_batch(const photic_config *cfg, const float *d_grid, int32
                             const double *theta_sun_deg, int32_t nrows, int32_t ncols,
                             int32_t n_spatial, int32_t n_bottoms, const double *d_h_empirical,
                             const photic_outputs *out, void *stream);
+
+/* samodel()'s pixel loop with its dynamic lookup table, one scene, one
+ * region, one bottom type (LUT 1, model/samodel.c:97, 649-660, 701-773,
+ * 901-1215).  The shallow pixels of d_rrs (device, [npix][n_bands] float)
+ * are sorted by the spectral index |(Rrs_1, Rrs_2, Rrs_3)| -- times the
+ * spectral angle to rrs_noise[1..3] when use_noise and every band of
+ * rrs_noise is at least 1e-6 (:590-600, 749-767) -- and the sorted list is
+ * cut into n_chains contiguous slices (0: one per resident lane).  Each
+ * slice runs the reference's loop as one of its threads does: a pixel whose
+ * spectrum matches a stored fit within the match threshold (entries within
+ * 10 % of the previous pixel's depth and K_min, model_spectral_diff_mean
+ * :2792-2842) takes that fit's outputs (status PHOTIC_PX_SERVED, model_error
+ * = the spectral difference, evals 0); any other pixel is fitted with cfg's
+ * tolerances (the reference's are reqmin 1e-2, konvge 100, kcount 5000),
+ * hot-started from the previous pixel when the last two were continuous
+ * (PHOTIC_PX_HOT), and stored in the slice's table of n_lut slots (the
+ * reference: 16000) when its model error is below the entry threshold and
+ * its depth below 32 m; both thresholds adapt every 0.1 % of the slice.
+ * Optional device outputs: d_source [npix] (-2 masked, -1 fitted, else the
+ * pixel whose fit served it), d_order [npix] (the sorted shallow pixels,
+ * first *n_shallow entries), d_chain_stats [n_chains][4] (served, fitted,
+ * final match and entry thresholds).  Host outputs: *n_shallow and
+ * *n_chains_used (either may be NULL).  One slice is the reference on one
+ * thread.  FP64 only (cfg->precision other than PHOTIC_PREC_FP64 returns
+ * PHOTIC_ERR_UNSUPPORTED). */
+typedef struct photic_lut_config {
+  int32_t n_lut;                        /* slots per slice (the reference: 16000) */
+  int64_t n_chains;                     /* slices; 0: one per resident lane */
+  int32_t use_noise;                    /* order by the spectral angle to rrs_noise */
+  double rrs_noise[PHOTIC_MAX_BANDS];   /* the scene's noise spectrum (R_sigma) */
+} photic_lut_config;
+
+void photic_lut_config_default(photic_lut_config *lut);
+
+/* The slice count n_chains = 0 stands for: one per lane the kernel keeps
+ * resident on this device (0 on error). */
+int64_t photic_lut_default_chains(const photic_config *cfg);
+
+int photic_lut_invert_batch(const photic_config *cfg, const photic_lut_config *lut,
+                            const float *d_rrs, int64_t npix, const photic_outputs *out,
+                            int64_t *d_source, int64_t *d_order, double *d_chain_stats,
+                            int64_t *n_shallow, int64_t *n_chains_used, void *stream);
 
 /* Depth uncertainty, the reference's ad hoc estimate (model/samodel.c:
  * 1368-1479): for each 0.25 m interval up to the deepest fitted depth (whole

@@ -472,3 +472,99 @@ def nc_reference_layout(grid, spval=-9999.0):
     buf = C.create_string_buffer(1 << 16)
     reference().lib.photic_ref_nc_layout(buf, C.c_int(len(buf)))
     return buf.value.decode().splitlines()
+
+
+# --------------------------------------------------------------------------
+# Spatially coherent scene and the pixel loop with the dynamic lookup table
+# (model/samodel.c:649-1215).
+# --------------------------------------------------------------------------
+_i64p = C.POINTER(C.c_int64)
+
+
+def generate_field(seed, nrows, ncols, *, row0=0, n_rows=None, wl=OLI_BANDS, theta_sun=35.0,
+                   theta_view=0.0, mask_frac=0.15, noise_sigma=2e-4, nodata=-9999.0):
+    """Rows [row0, row0 + n_rows) of a nrows x ncols scene whose parameters
+    are smooth fields; returns ([n_rows*ncols, n_bands] float32 spectra,
+    [n_rows*ncols, 5] truth H P G X B)."""
+    n_rows = nrows - row0 if n_rows is None else n_rows
+    wl = _f64(wl)
+    n = n_rows * ncols
+    rrs = np.zeros((n, len(wl)), dtype=np.float32)
+    truth = np.zeros((n, 5))
+    L = port().lib
+    L.po_generate_field.argtypes = [C.c_uint64, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
+                                    C.c_int, _dp, C.c_double, C.c_double, C.c_double,
+                                    C.c_double, C.c_float, _fp, _dp]
+    L.po_generate_field(seed, nrows, ncols, row0, n_rows, len(wl), _ptr(wl, _dp), theta_sun,
+                        theta_view, mask_frac, noise_sigma, nodata, _ptr(rrs, _fp),
+                        _ptr(truth, _dp))
+    return rrs, truth
+
+
+def lut_key(rrs, *, nodata=-9999.0, rrs_noise=None):
+    """The spectral index samodel() sorts the pixels by, per pixel."""
+    rrs = _f32(rrs)
+    L = port().lib
+    L.po_lut_key.restype = C.c_float
+    L.po_lut_key.argtypes = [_fp, C.c_int, C.c_float, _dp]
+    nz = _f64(rrs_noise) if rrs_noise is not None else None
+    nb = rrs.shape[1]
+    return np.array([L.po_lut_key(_ptr(rrs[p], _fp), nb, nodata, _ptr(nz, _dp))
+                     for p in range(rrs.shape[0])], dtype=np.float32)
+
+
+def lut_invert(rrs, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0, h_tide=0.0,
+               nodata=-9999.0, rrs_noise=None, reqmin=None, konvge=100, kcount=2000,
+               n_lut=16000, n_chains=1, nthreads=0):
+    """samodel()'s loop with the dynamic lookup table over [npix, n_bands]
+    float32 spectra, the sorted shallow pixels cut into n_chains slices.
+    reqmin None: the reference's tolerances (1e-2 / 100 / 5000).  Returns
+    (records [npix, NOUT], source [npix] (-1 fitted, -2 masked, else the
+    pixel whose fit served it), order [n_shallow], chain_stats [n_chains, 4]
+    (served, fitted, final match and entry thresholds))."""
+    rrs = _f32(rrs)
+    npix, nb = rrs.shape
+    wl = _f64(wl)
+    if reqmin is None:
+        reqmin, konvge, kcount = 1e-2, 100, 5000
+    out = np.zeros((npix, NOUT))
+    source = np.zeros(npix, dtype=np.int64)
+    order = np.zeros(max(npix, 1), dtype=np.int64)
+    n_sh = C.c_int64(0)
+    stats = np.zeros((max(1, n_chains), 4))
+    nz = _f64(rrs_noise) if rrs_noise is not None else None
+    L = port().lib
+    L.po_lut_invert.argtypes = [C.c_int, _dp, C.c_double, C.c_double, C.c_double, _fp,
+                                C.c_int64, C.c_float, _dp, C.c_double, C.c_int, C.c_int, C.c_int,
+                                C.c_int64, C.c_int, _i64p, _i64p, _dp, _i64p, _dp]
+    rc = L.po_lut_invert(nb, _ptr(wl, _dp), theta_sun, theta_view, h_tide, _ptr(rrs, _fp), npix,
+                         nodata, _ptr(nz, _dp), reqmin, konvge, kcount, n_lut, n_chains,
+                         nthreads, _ptr(order, _i64p), C.byref(n_sh), _ptr(out, _dp),
+                         _ptr(source, _i64p), _ptr(stats, _dp))
+    if rc:
+        raise ValueError(f"po_lut_invert failed ({rc})")
+    S = n_sh.value
+    return out, source, order[:S], stats[:min(n_chains, max(S, 1))]
+
+
+def reference_samodel_grid(grid, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0,
+                           nodata=-9999.0, r_sigma=None, n_spatial=1, n_bottoms=1):
+    """The reference's own samodel() with its lookup table over a
+    [nrows, ncols, n_bands] grid on one thread; returns [10, nrows, ncols]
+    float32 grids as samodel() leaves them (depth negative below the datum,
+    depth sigma, model error, bottom albedo, sand, seagrass, coral, K_min,
+    bottom type, index of optical depth)."""
+    grid = _f32(grid)
+    nr, nc, nb = grid.shape
+    wl = _f64(wl)
+    out = np.zeros((10, nr, nc), dtype=np.float32)
+    rs = _f64(r_sigma) if r_sigma is not None else None
+    L = reference().lib
+    L.photic_ref_samodel_grid.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _fp, C.c_int,
+                                          C.c_int, C.c_float, _dp, C.c_int, C.c_int, _fp]
+    rc = L.photic_ref_samodel_grid(nb, _ptr(wl, _dp), theta_sun, theta_view, _ptr(grid, _fp),
+                                   nr, nc, nodata, _ptr(rs, _dp), n_spatial, n_bottoms,
+                                   _ptr(out, _fp))
+    if rc:
+        raise ValueError(f"photic_ref_samodel_grid failed ({rc})")
+    return out

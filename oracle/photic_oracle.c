@@ -614,7 +614,17 @@ static void seeded_start(const po_pixel *px, const double *seed, double scale, d
   }
 }
 
+/* fit_pixel, also handing back the kept vector (signed, as nelmin left it)
+ * when best_out is given. */
+static void fit_pixel_ex(po_pixel *px, const po_fit *fit, const double *seed, double *o,
+                         double *best_out);
+
 static void fit_pixel(po_pixel *px, const po_fit *fit, const double *seed, double *o) {
+  fit_pixel_ex(px, fit, seed, o, NULL);
+}
+
+static void fit_pixel_ex(po_pixel *px, const po_fit *fit, const double *seed, double *o,
+                         double *best_out) {
   const int n = n_params_of(px);
   double start[PO_MAX_PARAMS], step[PO_MAX_PARAMS], xm[PO_MAX_PARAMS], best[PO_MAX_PARAMS];
   double lowest = 1.0e4, y = 0.0;
@@ -688,6 +698,7 @@ static void fit_pixel(po_pixel *px, const po_fit *fit, const double *seed, doubl
   o[35] = (double)kept_res;
   o[36] = (double)kept_start;
   o[37] = (double)kept_fault;
+  if (best_out) memcpy(best_out, best, n * sizeof(double));
 }
 
 /* Mask test of model/samodel.c:937-941: nodata or negative in any band. */
@@ -1634,4 +1645,346 @@ void po_nc_compress(const float *grid, int64_t n, double spval, int16_t *packed,
     if (grid[k] == fspv) packed[k] = *missing_value;
     else packed[k] = nc_to_short_x86(rint((grid[k] - grmin) / scale));
   }
+}
+
+/* ------------------------------------------------------------------------
+ * Spatially coherent synthetic scene: smooth parameter fields over the
+ * grid (three seeded harmonics each), so that neighbouring pixels -- and
+ * pixels far apart on the same depth contour and bottom class -- have
+ * nearly equal spectra, as an image has.  This is the workload of the dynamic lookup table; the
+ * per-pixel generator above draws independent pixels, which a table never
+ * matches.  New: the reference has no generator.
+ * ---------------------------------------------------------------------- */
+static double field_value(uint64_t seed, uint32_t which, double u, double v) {
+  double s = 0.0, norm = 0.0;
+  int h;
+  for (h = 0; h < 3; h++) {
+    double w[4], amp = 1.0 / (double)(1 << h);
+    draw4(seed, (uint64_t)(which * 4u + (uint32_t)h), 7u, 1u, w);
+    {
+      double fx = 1.0 + floor(4.0 * w[0]), fy = 1.0 + floor(4.0 * w[1]);
+      double ph = 2.0 * PO_PI * w[2];
+      s += amp * sin(2.0 * PO_PI * (fx * u + fy * v) + ph);
+    }
+    norm += amp;
+  }
+  return 0.5 + 0.5 * s / norm; /* in [0, 1] */
+}
+
+void po_field_truth(uint64_t seed, int64_t nrows, int64_t ncols, int64_t i, int64_t j,
+                    double *t5) {
+  /* one water mass over the scene (P, G, X within +/-10 % of values drawn
+   * once), depth a smooth field over 0.5-25 m, and the bottom in three
+   * albedo classes (dark, mixed, bright) with +/-5 % texture */
+  const double u = ((double)i + 0.5) / (double)nrows, v = ((double)j + 0.5) / (double)ncols;
+  static const double classes[3] = {0.08, 0.2, 0.4};
+  double w[4], tH = field_value(seed, 0u, u, v), tB = field_value(seed, 4u, u, v);
+  int cls = tB < 0.4 ? 0 : (tB < 0.6 ? 1 : 2);
+  draw4(seed, 0u, 9u, 1u, w);
+  t5[0] = 0.5 + 24.5 * tH * tH;
+  t5[1] = log_uniform(w[0], 0.01, 0.05) * (0.9 + 0.2 * field_value(seed, 1u, u, v));
+  t5[2] = log_uniform(w[1], 0.01, 0.08) * (0.9 + 0.2 * field_value(seed, 2u, u, v));
+  t5[3] = log_uniform(w[2], 0.002, 0.02) * (0.9 + 0.2 * field_value(seed, 3u, u, v));
+  t5[4] = classes[cls] * (0.95 + 0.1 * field_value(seed, 5u, u, v));
+}
+
+void po_generate_field(uint64_t seed, int64_t nrows, int64_t ncols, int64_t row0, int64_t n_rows,
+                       int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
+                       double mask_frac, double noise_sigma, float nodata, float *rrs_out,
+                       double *truth_out) {
+  po_scene sc;
+  int64_t k, n = n_rows * ncols;
+  scene_init(&sc, n_bands, wl, theta_sun_deg, theta_view_deg, 0.0);
+#if _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+  for (k = 0; k < n; k++) {
+    const int64_t i = row0 + k / ncols, j = k % ncols;
+    const uint64_t p = (uint64_t)(i * ncols + j);
+    double t5[5], u1[4], r[PO_MAX_BANDS];
+    int b;
+    po_field_truth(seed, nrows, ncols, i, j, t5);
+    synthesise(&sc, t5[0], t5[1], t5[2], t5[3], t5[4], r);
+    add_noise(seed, p, 0u, n_bands, noise_sigma, r);
+    for (b = 0; b < n_bands; b++) rrs_out[k * n_bands + b] = (float)r[b];
+    draw4(seed, p, 1u, 0u, u1);
+    apply_mask(u1[1], u1[2], mask_frac, n_bands, nodata, rrs_out + k * n_bands);
+    if (truth_out) memcpy(truth_out + k * 5, t5, sizeof t5);
+  }
+}
+
+/* ------------------------------------------------------------------------
+ * samodel()'s pixel loop with its dynamic lookup table, one scene, one
+ * region, one bottom type (model/samodel.c:649-660, 701-773, 901-1215).
+ *
+ *   order    the shallow pixels (no band nodata or negative, :933-947)
+ *            sorted ascending by the spectral index |(Rrs_blue, Rrs_green,
+ *            Rrs_red)| (bands 1, 2, 3), times the spectral angle to the
+ *            noise spectrum when every band's noise is at least 1e-6
+ *            (:706-770); the index is a float and ties keep the pixel
+ *            order (glibc's qsort, a merge sort, is stable);
+ *   chains   the sorted list cut into n_chains contiguous slices; each
+ *            slice runs the reference's loop on its own, as one OpenMP
+ *            thread of the reference runs it over the pixels it is given,
+ *            with the slice's length as n_shallow (one chain is the
+ *            reference run on one thread);
+ *   lookup   over the table's slots in order, the entries whose depth and
+ *            K_min are within 10 % of the previous pixel's (relative to it
+ *            plus epsilon = 1e-4f, common.c:93), the smallest
+ *            model_spectral_diff_mean (:2792-2842; strict <, first slot);
+ *   serve    when that difference is at most the match threshold: the
+ *            entry's outputs (partial_copy_md, :3031-3139), model error =
+ *            the difference (:1066-1073);
+ *   fit      otherwise samodel_optimise, hot-started from the previous
+ *            pixel when the last two pixels were continuous (:2234-2309),
+ *            then entered into the oldest slot when its model error is
+ *            below the entry threshold and its depth below 32 m
+ *            (:1035-1063);
+ *   adapt    both thresholds every 0.1 % of the slice from the model
+ *            errors and the served share since the previous update
+ *            (:1182-1211; the sums restart at every update, :1326-1352).
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  double depth, kmin, rm[3], prev[3];
+  int64_t src;
+} po_lut_entry;
+
+typedef struct {
+  float value;
+  int64_t idx;
+} po_key;
+
+static int po_key_cmp(const void *a, const void *b) {
+  const po_key *x = (const po_key *)a, *y = (const po_key *)b;
+  if (x->value < y->value) return -1;
+  if (x->value > y->value) return 1;
+  return (x->idx > y->idx) - (x->idx < y->idx);
+}
+
+/* approx_equal of model/common.c:392-394: float arguments, double product */
+static int ref_approx_eq(float a, float b, float eps) {
+  return fabs(a - b) <= ((fabs(a) < fabs(b) ? fabs(b) : fabs(a)) * eps);
+}
+
+/* model_spectral_diff_mean (model/samodel.c:2792-2842) for one region and
+ * one scene: bands 1..3 below n_bands. */
+static float lut_spectral_diff(const double *meas, const double *lut_rm, int n_bands) {
+  double error = 0.0;
+  int k, n_total = 0;
+  for (k = 1; k <= 3 && k < n_bands; k++) {
+    double current = 0.0, previous = 0.0, nobs = 0.0;
+    if (!ref_approx_eq((float)meas[k], 0.0f, 1.0e-6f) &&
+        !ref_approx_eq((float)lut_rm[k - 1], 0.0f, 1.0e-6f)) {
+      current += meas[k];
+      previous += lut_rm[k - 1];
+      nobs += 1.0;
+    }
+    if (nobs > 0.5) {
+      current /= nobs;
+      previous /= nobs;
+    }
+    error += pow((current - previous) / current, 2.0);
+    n_total++;
+  }
+  error = 100.0 * sqrt(error / ((double)n_total));
+  return (float)error;
+}
+
+/* The spectral index of one pixel (model/samodel.c:711-767), one scene. */
+float po_lut_key(const float *r, int n_bands, float nodata, const double *noise) {
+  float blue_sum = 0.0f, green_sum = 0.0f, red_sum = 0.0f, index;
+  if (n_bands > 1 && !ref_approx_eq(r[1], nodata, 1.0e-6f)) blue_sum += r[1];
+  if (n_bands > 2 && !ref_approx_eq(r[2], nodata, 1.0e-6f)) green_sum += r[2];
+  if (n_bands > 3 && !ref_approx_eq(r[3], nodata, 1.0e-6f)) red_sum += r[3];
+  index = (float)sqrt(pow(blue_sum, 2) + pow(green_sum, 2) + pow(red_sum, 2));
+  if (noise) {
+    double bn = 0.0, gn = 0.0, rn = 0.0, angle;
+    bn += noise[1];
+    gn += noise[2];
+    rn += noise[3];
+    angle = blue_sum * bn + green_sum * gn + red_sum * rn;
+    angle /= index * sqrt(pow(bn, 2) + pow(gn, 2) + pow(rn, 2));
+    angle = acos(angle);
+    index *= angle;
+  }
+  return index;
+}
+
+static void lut_chain(const po_scene *sc, const po_fit *fit, const float *rrs, int nb,
+                      const int64_t *order, int64_t n, int n_lut, double *out, int64_t *source,
+                      double *stats) {
+  const double eps = (double)1.0e-4f; /* the reference's global float epsilon */
+  const double continuity = 0.1;
+  const int64_t cap = n < (int64_t)n_lut ? n : (int64_t)n_lut;
+  po_lut_entry *lut = (po_lut_entry *)calloc((size_t)(cap > 0 ? cap : 1), sizeof(po_lut_entry));
+  int64_t total_lut = 0, k, n_complete = 0, err_count = 0, n_opt = 0;
+  double md_depth = 0.0, md_kmin = 0.0, depth_prev = 0.0, kmin_prev = 0.0, prev[3] = {0, 0, 0};
+  double match = 1.125 > 1.5 ? 1.125 : 1.5, entry; /* MAX(1.5, 1.125 n_scenes) */
+  double n_modelled = 0.0, n_skipped = 0.0, total_model_error = 0.0, err_total = 0.0;
+  int hot = 0, nprev = 0, nperc;
+  entry = match;
+  for (k = 0; k < n; k++) {
+    const int64_t p = order[k];
+    const float *r = rrs + p * nb;
+    double meas[PO_MAX_BANDS], best = 1.0e4, model_error;
+    int64_t pos = 0, j, in_use = total_lut < cap ? total_lut : cap;
+    int b;
+    for (b = 0; b < nb; b++) meas[b] = (double)r[b];
+    for (j = 0; j < in_use; j++) {
+      const po_lut_entry *e = lut + j;
+      if (fabs(e->depth - md_depth) / (md_depth + eps) < continuity &&
+          fabs(e->kmin - md_kmin) / (md_kmin + eps) < continuity) {
+        double d = (double)lut_spectral_diff(meas, e->rm, nb);
+        if (d < best) {
+          best = d;
+          pos = j;
+        }
+      }
+    }
+    if (best > match) {
+      po_pixel px;
+      double seed[6], bestv[PO_MAX_PARAMS], *o = out + p * PO_NOUT;
+      memset(&px, 0, sizeof px);
+      px.n_scenes = 1;
+      px.n_bands = nb;
+      px.n_bottoms = 1;
+      px.layout = PO_LAYOUT_REFERENCE;
+      px.sc[0] = sc;
+      for (b = 0; b < nb; b++) px.rrs[0][b] = meas[b];
+      pixel_reference_rrs(&px);
+      if (hot) {
+        seed[0] = depth_prev;
+        seed[1] = 100.0 * 4.0 * (px.r490[0] / (double)1);
+        seed[2] = 1.0;
+        seed[3] = prev[0];
+        seed[4] = prev[1];
+        seed[5] = prev[2];
+      }
+      fit_pixel_ex(&px, fit, hot ? seed : NULL, o, bestv);
+      source[p] = -1;
+      md_depth = o[0];
+      md_kmin = o[4];
+      model_error = o[2];
+      prev[0] = fabs(bestv[3]);
+      prev[1] = fabs(bestv[4]);
+      prev[2] = fabs(bestv[5]);
+      n_opt++;
+      if (!ref_approx_eq((float)model_error, 0.0f, 1.0e-4f)) { /* vec_mean2_double */
+        err_total += model_error;
+        err_count++;
+      }
+      if (model_error < entry && md_depth < 32.0) {
+        po_lut_entry *e = lut + (total_lut % cap);
+        e->depth = md_depth;
+        e->kmin = md_kmin;
+        for (b = 0; b < 3; b++) e->rm[b] = b + 1 < nb ? px.Rm[0][b + 1] : 0.0;
+        memcpy(e->prev, prev, sizeof prev);
+        e->src = p;
+        total_lut++;
+      }
+      if (stats) stats[1] += 1.0;
+    } else {
+      const po_lut_entry *e = lut + pos;
+      depth_prev = md_depth;
+      kmin_prev = md_kmin;
+      md_depth = e->depth;
+      md_kmin = e->kmin;
+      memcpy(prev, e->prev, sizeof prev);
+      model_error = best;
+      memcpy(out + p * PO_NOUT, out + e->src * PO_NOUT, PO_NOUT * sizeof(double));
+      out[p * PO_NOUT + 2] = best;
+      source[p] = e->src;
+      n_skipped += 1.0;
+      if (stats) stats[0] += 1.0;
+    }
+    hot = fabs(md_depth - depth_prev) / (eps + depth_prev) < continuity &&
+          fabs(md_kmin - kmin_prev) / (eps + kmin_prev) < continuity;
+    depth_prev = md_depth;
+    kmin_prev = md_kmin;
+    total_model_error += model_error;
+    n_modelled += 1.0;
+    nperc = (int)(1000 * ((double)++n_complete) / ((double)n));
+    if (nperc > nprev) {
+      if (n_opt > 0) {
+        const double error_mean = (float)(err_count ? err_total / ((double)err_count) : 0.0);
+        match += 0.75 * error_mean + 0.25 * total_model_error / n_modelled;
+        match /= 2.0;
+        entry = match;
+      }
+      if (n_skipped / n_modelled > 0.9925) {
+        match *= 0.75;
+        entry *= 0.75;
+      }
+      match = 1.5 > match ? 1.5 : match;
+      entry = 1.5 > entry ? 1.5 : entry;
+      nprev = nperc;
+      /* the statistics restart with every display (:1326-1352) */
+      total_model_error = 0.0;
+      n_modelled = 0.0;
+      n_skipped = 0.0;
+      n_opt = 0;
+      err_total = 0.0;
+      err_count = 0;
+    }
+  }
+  if (stats) {
+    stats[2] = match;
+    stats[3] = entry;
+  }
+  free(lut);
+}
+
+int po_lut_invert(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
+                  double h_tide, const float *rrs, int64_t npix, float nodata,
+                  const double *rrs_noise, double reqmin, int konvge, int kcount, int n_lut,
+                  int64_t n_chains, int nthreads, int64_t *order_out, int64_t *n_shallow_out,
+                  double *out, int64_t *source, double *chain_stats) {
+  po_scene sc;
+  po_fit fit;
+  po_key *keys;
+  int64_t p, S = 0, c;
+  const double *noise = NULL;
+  if (n_bands < 2 || n_bands > PO_MAX_BANDS || n_lut < 1 || n_chains < 1) return 1;
+  if (rrs_noise) {
+    int b, ok = 1;
+    for (b = 0; b < n_bands; b++)
+      if (rrs_noise[b] < 1.0e-6) ok = 0; /* model/samodel.c:590-600 */
+    if (ok) noise = rrs_noise;
+  }
+  scene_init(&sc, n_bands, wl, theta_sun_deg, theta_view_deg, h_tide);
+  fit.seed_step_scale = 1.0;
+  fit.reqmin = reqmin;
+  fit.konvge = konvge;
+  fit.kcount = kcount;
+  fit.n_hstarts = 8;
+  fit.hstarts = po_default_hstarts;
+  keys = (po_key *)malloc((size_t)(npix > 0 ? npix : 1) * sizeof(po_key));
+  for (p = 0; p < npix; p++) {
+    const float *r = rrs + p * n_bands;
+    memset(out + p * PO_NOUT, 0, PO_NOUT * sizeof(double));
+    if (masked(r, n_bands, nodata)) {
+      out[p * PO_NOUT + 9] = 1.0;
+      source[p] = -2;
+      continue;
+    }
+    keys[S].value = po_lut_key(r, n_bands, nodata, noise);
+    keys[S].idx = p;
+    S++;
+  }
+  qsort(keys, (size_t)S, sizeof(po_key), po_key_cmp);
+  for (p = 0; p < S; p++) order_out[p] = keys[p].idx;
+  free(keys);
+  *n_shallow_out = S;
+  if (n_chains > S) n_chains = S > 0 ? S : 1;
+  if (chain_stats) memset(chain_stats, 0, (size_t)n_chains * 4 * sizeof(double));
+#if _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+  for (c = 0; c < n_chains; c++) {
+    const int64_t a = c * S / n_chains, e = (c + 1) * S / n_chains;
+    lut_chain(&sc, &fit, rrs, n_bands, order_out + a, e - a, n_lut, out, source,
+              chain_stats ? chain_stats + 4 * c : NULL);
+  }
+  return 0;
 }

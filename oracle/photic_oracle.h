@@ -101,6 +101,20 @@ int po_depth_sigma(int n_bands, const double *wl, double theta_sun_deg, double t
 /* netCDF short packing (model/nc.c:251-320): see photic_oracle.c. */
 void po_nc_decompress(const int16_t *packed, int64_t n, float add_offset, float scale_factor,
                       int16_t missing_value, double spval, float *grid);
+/* Spatially coherent synthetic scene (smooth parameter fields) and the
+ * pixel loop with the dynamic lookup table (model/samodel.c:649-1215). */
+void po_field_truth(uint64_t seed, int64_t nrows, int64_t ncols, int64_t i, int64_t j,
+                    double *t5);
+void po_generate_field(uint64_t seed, int64_t nrows, int64_t ncols, int64_t row0, int64_t n_rows,
+                       int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
+                       double mask_frac, double noise_sigma, float nodata, float *rrs_out,
+                       double *truth_out);
+float po_lut_key(const float *r, int n_bands, float nodata, const double *noise);
+int po_lut_invert(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
+                  double h_tide, const float *rrs, int64_t npix, float nodata,
+                  const double *rrs_noise, double reqmin, int konvge, int kcount, int n_lut,
+                  int64_t n_chains, int nthreads, int64_t *order_out, int64_t *n_shallow_out,
+                  double *out, int64_t *source, double *chain_stats);
 void po_nc_compress(const float *grid, int64_t n, double spval, int16_t *packed,
                     float *add_offset, float *scale_factor, int16_t *missing_value);
 

@@ -536,13 +536,18 @@ double photic_ref_depth_sigma_stat(double *depths, int n) {
  * over one scene's [nrows][ncols][n_bands] float grid with its compiled-in
  * dynamic LUT, spectral ordering and hot starts (LUT 1, model/samodel.c:97),
  * run on one thread so that its order-dependent results are reproducible,
- * at the reference's own tolerances.  Outputs the depth grid (positive) and
- * the model-error grid as samodel() leaves them; its depth-uncertainty pass
- * and result files run as well (the netCDF stand-in keeps the files). */
+ * at the reference's own tolerances.  r_sigma (n_bands values or NULL for
+ * zeros) is the scene's noise spectrum, which orders the pixels when every
+ * band's is at least 1e-6 (:590-600, :749-767).  grids_out receives the ten
+ * result grids [10][nrows][ncols] exactly as samodel() leaves them: depth
+ * (negative below the datum), depth sigma, model error, bottom albedo,
+ * sand, seagrass, coral, K_min, bottom type, index of optical depth.  Its
+ * depth-uncertainty pass and result files run as well (the netCDF stand-in
+ * keeps the files in memory). */
 int photic_ref_samodel_grid(int n_bands, const double *wl, double theta_sun_deg,
                             double theta_view_deg, const float *grid, int nrows, int ncols,
-                            float nodata, int n_spatial, int n_bottoms, float *depth_out,
-                            float *error_out) {
+                            float nodata, const double *r_sigma, int n_spatial, int n_bottoms,
+                            float *grids_out) {
   scene sc;
   geogrid *gd, none;
   float **out[10];
@@ -560,6 +565,7 @@ int photic_ref_samodel_grid(int n_bands, const double *wl, double theta_sun_deg,
   for (b = 0; b < n_bands; b++) {
     sc.band_indexes[b] = b;
     sc.wavelengths[b] = (int)wl[b];
+    sc.R_sigma[b] = r_sigma ? r_sigma[b] : 0.0;
     gd[b].nrows = nrows;
     gd[b].ncols = ncols;
     gd[b].cellsize = 1.0f;
@@ -575,11 +581,10 @@ int photic_ref_samodel_grid(int n_bands, const double *wl, double theta_sun_deg,
 #endif
   samodel(&sc, gd, &idx, 1, false, none, 1, n_spatial, n_bottoms, out[0], out[1], out[2],
           out[3], out[4], out[5], out[6], out[7], out[8], out[9], 10.0f, 0, 1);
-  for (i = 0; i < nrows; i++)
-    for (j = 0; j < ncols; j++) {
-      depth_out[(size_t)i * ncols + j] = -out[0][i][j];
-      error_out[(size_t)i * ncols + j] = out[2][i][j];
-    }
+  for (k = 0; k < 10; k++)
+    for (i = 0; i < nrows; i++)
+      for (j = 0; j < ncols; j++)
+        grids_out[((size_t)k * nrows + i) * ncols + j] = out[k][i][j];
   for (k = 0; k < 10; k++) free_float_array_2d(out[k], nrows);
   for (b = 0; b < n_bands; b++) free_float_array_2d(gd[b].array, nrows);
   free(gd);

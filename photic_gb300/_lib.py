@@ -22,6 +22,8 @@ LAYOUT_REFERENCE, LAYOUT_SCENE_B = 0, 1
 TUNE_INVERT, TUNE_JOINT = 0, 1
 PX_FITTED, PX_MASKED, PX_INVALID = 0, 1, 2
 PX_CONVERGED = 0x100
+PX_SERVED = 0x200
+PX_HOT = 0x400
 
 
 class photic_config(C.Structure):
@@ -64,6 +66,15 @@ class photic_outputs(C.Structure):
         ("params", C.c_void_p),
         ("bottom_percent", C.c_void_p),
         ("bottom_type", C.c_void_p),
+    ]
+
+
+class photic_lut_config(C.Structure):
+    _fields_ = [
+        ("n_lut", C.c_int32),
+        ("n_chains", C.c_int64),
+        ("use_noise", C.c_int32),
+        ("rrs_noise", C.c_double * MAX_BANDS),
     ]
 
 
@@ -136,6 +147,13 @@ _SIGS = {
                                           C.POINTER(C.c_double), C.c_int32, C.c_int32,
                                           C.c_int32, C.c_int32, C.c_void_p,
                                           C.POINTER(photic_outputs), C.c_void_p]),
+    "photic_lut_config_default": (None, [C.POINTER(photic_lut_config)]),
+    "photic_lut_default_chains": (C.c_int64, [C.POINTER(photic_config)]),
+    "photic_lut_invert_batch": (C.c_int, [C.POINTER(photic_config), C.POINTER(photic_lut_config),
+                                          C.c_void_p, C.c_int64, C.POINTER(photic_outputs),
+                                          C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                          C.c_void_p]),
     "photic_depth_sigma": (C.c_int, [C.POINTER(photic_config), C.c_void_p, C.c_int64, C.c_void_p,
                                      C.POINTER(C.c_double), C.c_int32, C.c_uint64, C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -183,6 +183,56 @@ def invert(rrs: torch.Tensor, config: Optional[Config] = None, *,
     return out
 
 
+def lut_invert(rrs: torch.Tensor, config: Optional[Config] = None, *, n_lut: int = 16000,
+               n_chains: int = 0, rrs_noise: Optional[Sequence[float]] = None,
+               fields: Sequence[str] = OUTPUT_FIELDS, stream: Optional[torch.cuda.Stream] = None
+               ) -> Dict[str, torch.Tensor]:
+    """samodel()'s pixel loop with its dynamic lookup table
+    (model/samodel.c:649-1215) over ``rrs`` ([npix, n_bands] float32, CUDA):
+    the shallow pixels sorted by spectral index (times the spectral angle
+    to ``rrs_noise`` when every band of it is at least 1e-6), cut into
+    ``n_chains`` contiguous slices (0: one per resident lane), each run as
+    the reference runs them on one thread -- served from its table of
+    ``n_lut`` fits when a stored spectrum matches, else fitted (hot-started
+    from the previous pixel when the last two were continuous).  Use
+    ``Config.reference_default()`` for the reference's tolerances.  Returns
+    the outputs plus "source" (int64: -2 masked, -1 fitted, else the pixel
+    whose fit served it), "order" (the sorted shallow pixels) and
+    "chain_stats" ([n_chains, 4]: served, fitted, final match and entry
+    thresholds).  Synchronises the stream once (to size the order)."""
+    cfg = config or Config()
+    _check_cuda(rrs, "rrs", torch.float32)
+    if rrs.dim() != 2 or rrs.shape[1] != cfg.n_bands:
+        raise ValueError(f"rrs must be [npix, {cfg.n_bands}]")
+    if not rrs.is_contiguous():
+        raise ValueError("rrs must be contiguous")
+    npix = rrs.shape[0]
+    out = alloc_outputs(npix, rrs.device, fields)
+    source = torch.empty(npix, dtype=torch.int64, device=rrs.device)
+    order = torch.empty(max(npix, 1), dtype=torch.int64, device=rrs.device)
+    lc = L.photic_lut_config()
+    L.lib().photic_lut_config_default(C.byref(lc))
+    lc.n_lut = int(n_lut)
+    lc.n_chains = int(n_chains)
+    if rrs_noise is not None:
+        lc.use_noise = 1
+        for b, v in enumerate(rrs_noise):
+            lc.rrs_noise[b] = float(v)
+    c = cfg.to_c()
+    max_chains = int(n_chains) if n_chains else int(L.lib().photic_lut_default_chains(C.byref(c)))
+    stats = torch.zeros(max(1, min(max_chains, npix)), 4, dtype=torch.float64, device=rrs.device)
+    os_ = _outputs_struct(out)
+    n_sh, n_ch = C.c_int64(0), C.c_int64(0)
+    L.check(L.lib().photic_lut_invert_batch(C.byref(c), C.byref(lc), _ptr(rrs), npix,
+                                            C.byref(os_), _ptr(source), _ptr(order),
+                                            _ptr(stats), C.byref(n_sh), C.byref(n_ch),
+                                            _stream_handle(stream)))
+    out["source"] = source
+    out["order"] = order[:n_sh.value]
+    out["chain_stats"] = stats[:n_ch.value]
+    return out
+
+
 def region_invert(grid: torch.Tensor, config: Optional[Config] = None, *,
                   fields: Sequence[str] = OUTPUT_FIELDS,
                   stream: Optional[torch.cuda.Stream] = None) -> Dict[str, torch.Tensor]:

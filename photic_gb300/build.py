@@ -26,7 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["photic_host.cu", "photic_invert.cu", "photic_guarded.cu", "photic_joint.cu",
            "photic_joint_group.cu", "photic_region.cu",
            "photic_gemm.cu", "photic_mlp.cu", "photic_aux.cu", "photic_ncgrid.cu",
-           "photic_scene.cu"]
+           "photic_scene.cu", "photic_lut.cu"]
 
 
 def nvcc() -> str:

@@ -445,6 +445,129 @@ int photic_invert_batch_ordered(const photic_config *cfg, const float *d_rrs, in
   return PHOTIC_OK;
 }
 
+void photic_lut_config_default(photic_lut_config *lut) {
+  if (!lut) return;
+  memset(lut, 0, sizeof *lut);
+  lut->n_lut = 16000;  // model/samodel.c:650
+}
+
+int64_t photic_lut_default_chains(const photic_config *cfg) {
+  if (photic_config_check(cfg)) return 0;
+  unsigned int *err = nullptr;
+  int sms = 0;
+  if (device_state(&err, &sms)) return 0;
+  LutArgs a;
+  memset(&a, 0, sizeof a);
+  make_fit(*cfg, a.inv.fp);
+  return (int64_t)sms * lut_blocks_per_sm(a) * lut_block();
+}
+
+int photic_lut_invert_batch(const photic_config *cfg, const photic_lut_config *lut,
+                            const float *d_rrs, int64_t npix, const photic_outputs *out,
+                            int64_t *d_source, int64_t *d_order, double *d_chain_stats,
+                            int64_t *n_shallow, int64_t *n_chains_used, void *stream) {
+  int rc = photic_config_check(cfg);
+  if (rc) return rc;
+  if (n_shallow) *n_shallow = 0;
+  if (n_chains_used) *n_chains_used = 0;
+  if (!lut) return fail(PHOTIC_ERR_INVALID, "NULL lookup-table configuration");
+  if (lut->n_lut < 1 || lut->n_chains < 0)
+    return fail(PHOTIC_ERR_INVALID, "n_lut must be >= 1 and n_chains >= 0");
+  if (cfg->precision != PHOTIC_PREC_FP64)
+    return fail(PHOTIC_ERR_UNSUPPORTED, "the lookup-table loop runs in FP64 only");
+  if (npix < 0) return fail(PHOTIC_ERR_INVALID, "npix < 0");
+  if (npix == 0) return PHOTIC_OK;
+  if (!d_rrs || !out) return fail(PHOTIC_ERR_INVALID, "NULL input or output");
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned int *err = nullptr;
+  int sms = 0;
+  rc = device_state(&err, &sms);
+  if (rc) return rc;
+  const int nb = cfg->n_bands;
+
+  LutArgs a;
+  memset(&a, 0, sizeof a);
+  make_fit(*cfg, a.inv.fp);
+  make_scene(*cfg, cfg->theta_sun_deg, a.inv.sc);
+  a.inv.rrs = d_rrs;
+  a.inv.npix = npix;
+  a.inv.pixel_stride = nb;
+  a.inv.band_stride = 1;
+  a.inv.out = *out;
+  a.inv.error = err;
+  a.inv.early_exit = cfg->early_exit_per_scene * (double)(float)1;
+  a.source = d_source;
+  a.chain_stats = d_chain_stats;
+
+  // the order: keys, mask, stable sort (model/samodel.c:701-819)
+  LutKeyArgs ka;
+  memset(&ka, 0, sizeof ka);
+  ka.rrs = d_rrs;
+  ka.npix = npix;
+  ka.n_bands = nb;
+  ka.nodata = cfg->nodata_value;
+  bool noise = lut->use_noise != 0 && nb >= 4;
+  for (int b = 0; b < nb && noise; b++)
+    if (lut->rrs_noise[b] < 1.0e-6) noise = false;  // :590-600
+  ka.use_noise = noise ? 1 : 0;
+  for (int k = 0; k < 3; k++) ka.noise[k] = noise ? lut->rrs_noise[k + 1] : 0.0;
+  ka.out = *out;
+  ka.source = d_source;
+  int64_t *order = d_order;
+  cudaError_t e = cudaSuccess;
+  if (!order) {
+    e = cudaMallocAsync((void **)&order, npix * sizeof(int64_t), s);
+    if (e != cudaSuccess) return fail(PHOTIC_ERR_NOMEM, "order: %s", cudaGetErrorString(e));
+  }
+  int64_t S = 0;
+  e = lut_order(ka, order, &S, s);
+  if (e != cudaSuccess) {
+    if (!d_order) cudaFreeAsync(order, s);
+    return cuda_fail(e, "lookup-table order");
+  }
+  if (S > 0) {
+    const int per_sm = lut_blocks_per_sm(a);
+    if (per_sm < 1) {
+      if (!d_order) cudaFreeAsync(order, s);
+      return fail(PHOTIC_ERR_CUDA, "lookup-table kernel does not fit on the device");
+    }
+    const int block = lut_block();
+    const int64_t lanes = (int64_t)sms * per_sm * block;
+    int64_t C = lut->n_chains ? lut->n_chains : lanes;
+    if (C > S) C = S;
+    const int64_t per_chain = (S + C - 1) / C;
+    const int64_t cap = per_chain < lut->n_lut ? per_chain : (int64_t)lut->n_lut;
+    a.order = order;
+    a.n_shallow = S;
+    a.n_chains = C;
+    a.cap = cap;
+    unsigned long long *queue = nullptr;
+    e = cudaMallocAsync((void **)&a.ring, (size_t)C * 8 * cap * sizeof(double), s);
+    if (e == cudaSuccess)
+      e = cudaMallocAsync((void **)&a.ring_src, (size_t)C * cap * sizeof(int64_t), s);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)&queue, sizeof *queue, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(queue, 0, sizeof *queue, s);
+    if (e == cudaSuccess) {
+      a.queue = queue;
+      int64_t grid = (int64_t)sms * per_sm;
+      const int64_t need = (C + block - 1) / block;
+      if (grid > need) grid = need;
+      e = launch_lut(a, (int)grid, s);
+    }
+    cudaFreeAsync(a.ring, s);
+    cudaFreeAsync(a.ring_src, s);
+    cudaFreeAsync(queue, s);
+    if (e != cudaSuccess) {
+      if (!d_order) cudaFreeAsync(order, s);
+      return cuda_fail(e, "lookup-table kernel");
+    }
+    if (n_chains_used) *n_chains_used = C;
+  }
+  if (!d_order) cudaFreeAsync(order, s);
+  if (n_shallow) *n_shallow = S;
+  return PHOTIC_OK;
+}
+
 int photic_joint_invert_batch(const photic_config *cfg, const int32_t *d_offsets,
                               const double *d_theta_sun_deg, const float *d_rrs, int64_t npix,
                               int64_t n_obs, const photic_outputs *out, void *stream) {

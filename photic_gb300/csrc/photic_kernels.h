@@ -47,6 +47,35 @@ int invert_blocks_per_sm(const InvertArgs &a, int precision, int block);
 cudaError_t launch_guarded(const InvertArgs &a, int block, int grid, cudaStream_t s);
 int guarded_blocks_per_sm(const InvertArgs &a, int block);
 
+// samodel()'s pixel loop with the dynamic lookup table (photic_lut.cu).
+struct LutKeyArgs {
+  const float *rrs;  // [npix][n_bands]
+  int64_t npix;
+  int32_t n_bands;
+  float nodata;
+  int32_t use_noise;   // order by index x spectral angle to noise[] (blue, green, red)
+  double noise[3];
+  photic_outputs out;  // masked pixels' outputs are written here
+  int64_t *source;     // optional [npix]: -2 for masked pixels
+  float *keys;         // scratch [npix]
+  uint8_t *flags;      // scratch [npix]
+  int64_t *idx;        // scratch [npix]
+};
+struct LutArgs {
+  InvertArgs inv;         // fp, sc, rrs ([npix][n_bands]), out, error, early_exit
+  const int64_t *order;   // [n_shallow] sorted shallow pixels
+  int64_t n_shallow, n_chains, cap;  // cap = table slots per chain
+  double *ring;           // [n_chains][8][cap]
+  int64_t *ring_src;      // [n_chains][cap]
+  int64_t *source;        // optional [npix]: -1 fitted, else the pixel that served it
+  double *chain_stats;    // optional [n_chains][4]: served, fitted, match, entry
+  unsigned long long *queue;  // chain counter
+};
+cudaError_t lut_order(LutKeyArgs ka, int64_t *order, int64_t *n_shallow, cudaStream_t s);
+cudaError_t launch_lut(const LutArgs &a, int grid, cudaStream_t s);
+int lut_blocks_per_sm(const LutArgs &a);
+int lut_block();
+
 struct GenArgs {
   FitParams fp;
   SceneConsts sc;

@@ -2,7 +2,7 @@
 (sand, seagrass, coral), pixels alone or with 3 x 3 regions, empirical
 depths and scene stacks, against the reference-made golden fixture
 (tests/golden/bottoms.npz) and the oracle, itself pinned bit for bit to the
-reference (tests/test_oracle_vs_reference.py).  The bar is the benchmark spec's:
+reference (tests/test_oracle_vs_reference.py).  The bar is the
 median |dH| <= 1 cm and p99 <= 5 cm, with the bottom shares and types of the
 pixels whose fits agree."""
 import os

@@ -1,6 +1,6 @@
 """Distribution parity of every fit the GPU runs, against the FP64 oracle.
 
-The spec bar for each workload is median |dH| <= 1 cm and p99 |dH| <=
+The bar for each workload is median |dH| <= 1 cm and p99 |dH| <=
 5 cm against the FP64 oracle on the same inputs, with the relative errors of
 P, G, X and the bottom albedo stated beside it.  The oracle is the C
 restatement (oracle/photic_oracle.c), pinned bit for bit to the reference

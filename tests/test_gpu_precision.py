@@ -2,8 +2,7 @@
 
 FP64 is the drop-in and the headline: faithful to the oracle except on the
 last-ulp pixels (tests/test_gpu_invert.py).  The FP32 forward model with the
-special-function unit -- the north star's "bulk of the arithmetic in FP32" --
-keeps the simplex and every decision in FP64 but feeds them costs accurate to
+special-function unit -- the bulk of the arithmetic in FP32 -- keeps the simplex and every decision in FP64 but feeds them costs accurate to
 ~1e-6 relative, so the Nelder-Mead path departs from the oracle's wherever
 two vertex costs are that close; this test measures how far its fits land
 from the oracle's, and checks that it runs the same pixels to valid fits.
