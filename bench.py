@@ -240,6 +240,12 @@ def main():
                     help="pixels of the 4096x4096 temporal grid for the joint-fit leg (0: skip)")
     ap.add_argument("--region-side", type=int, default=96,
                     help="side of the square grid for the spatial-region leg (0: skip)")
+    ap.add_argument("--lut-side", type=int, default=4096,
+                    help="side of the coherent scene of the lookup-table leg (0: skip)")
+    ap.add_argument("--lut-oracle-chains", type=int, default=8,
+                    help="chains of the lookup-table leg re-run by the oracle")
+    ap.add_argument("--lut-cpu-side", type=int, default=128,
+                    help="side of the crop the lookup-table loop runs on one CPU thread")
     ap.add_argument("--nc-side", type=int, default=4096,
                     help="side of the scene written to and read from netCDF band files (0: off)")
     ap.add_argument("--serve-requests", type=int, default=12,
@@ -467,6 +473,9 @@ def main():
     serving = None
     if rank == 0 and args.serve_requests > 0:
         serving = serving_leg(args, net)
+    lutr = None
+    if rank == 0 and args.lut_side > 0:
+        lutr = lut_leg(args, dev)
     ncgrid = None
     if rank == 0 and args.nc_side > 0:
         try:
@@ -499,7 +508,8 @@ def main():
                 "seed_polish_ms_per_step": ms_step - ms_inv,
                 "plain_4096x4096": plain4096, "precision": precision,
                 "serving": serving, "temporal": temporal,
-                "regions": regions, "ncgrid": ncgrid, "e2e": e2e, "clocks": clk}
+                "regions": regions, "lut": lutr, "ncgrid": ncgrid, "e2e": e2e,
+                "clocks": clk}
         print(json.dumps(line))
     if pg_ is not None:
         pg_.destroy_process_group()
@@ -793,6 +803,95 @@ def region_leg(args, dev):
             "mean_evals": float(out["evals"].float().mean().item()),
             "oracle_sample": stats,
             "cpu_oracle_px_s": k * k / t_cpu, "cpu_threads": os.cpu_count() or 1}
+
+
+def lut_leg(args, dev):
+    """samodel()'s pixel loop with its dynamic lookup table (LUT 1) on a
+    spatially coherent scene at the reference's tolerances: the GPU's chains
+    against the plain cold-start inversion of the same scene, per-chain
+    parity against the oracle run on the same slices (each slice is the
+    reference's loop on one thread, pinned bit for bit to the reference's
+    samodel()), and that loop's CPU rate on one thread."""
+    import torch
+    import photic_gb300 as pg
+    from oracle import oracle as O
+    n = args.lut_side
+    cfg = pg.Config.reference_default()
+    rrs, _ = pg.generate_field(n, n, seed=SEED + 11, device=dev, with_truth=False)
+    small, _ = pg.generate_field(64, 64, seed=SEED + 12, device=dev, with_truth=False)
+    pg.lut_invert(small, cfg)  # warm-up
+    pg.invert(small, cfg, fields=("status",))
+    pg.sync()
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        o = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        pg.sync()
+        return o, e0.elapsed_time(e1) * 1e-3
+
+    fields = ("depth_f64", "status", "evals", "P", "G", "X", "bottom_albedo", "K_min")
+    lut, t_lut = timed(lambda: pg.lut_invert(rrs, cfg, fields=fields))
+    plain, t_plain = timed(lambda: pg.invert(rrs, cfg, fields=("depth_f64", "status", "evals")))
+    st = lut["status"].cpu().numpy()
+    src = lut["source"].cpu().numpy()
+    fit = (st & 0xFF) == 0
+    fitted = fit & (src == -1)
+    ev = lut["evals"].cpu().numpy()
+    pev = plain["evals"].cpu().numpy()
+    pst = plain["status"].cpu().numpy()
+    order = lut["order"].cpu().numpy()
+    C = int(lut["chain_stats"].shape[0])
+    S = order.size
+    h = lut["depth_f64"].cpu().numpy()
+    # parity: a sample of chains re-run by the oracle on the same slices
+    rng = np.random.default_rng(3)
+    chains = np.sort(rng.choice(C, size=min(args.lut_oracle_chains, C), replace=False))
+    r_np = rrs.cpu().numpy()
+    d_all, srv_g, srv_o = [], [], []
+    for c in chains:
+        sl = order[c * S // C:(c + 1) * S // C]
+        o, so, _, _ = O.lut_invert(r_np[sl], n_chains=1, nthreads=1)
+        d_all.append(np.abs(h[sl] - o[:, 0]))
+        srv_g.append(src[sl] >= 0)
+        srv_o.append(so >= 0)
+    d = np.concatenate(d_all) if d_all else np.zeros(0)
+    # the loop on the host, one chain on one thread (the reference's own
+    # schedule with OMP_NUM_THREADS=1), on a bounded crop of the scene
+    crop = r_np.reshape(n, n, 4)[:args.lut_cpu_side, :args.lut_cpu_side].reshape(-1, 4)
+    t0 = time.perf_counter()
+    oc, sc, _, _ = O.lut_invert(crop, n_chains=1, nthreads=1)
+    t_cpu = time.perf_counter() - t0
+    shallow_cpu = int(np.sum(oc[:, 9] == 0))
+    return {"workload": f"{n}x{n} spatially coherent scene (one water mass, smooth depth, "
+                        f"three bottom classes, noise 1e-4, 10 % masked), reference "
+                        f"tolerances (reqmin 1e-2, konvge 100, kcount 5000), LUT of 16000 "
+                        f"slots per chain",
+            "chains": C, "shallow_pixels": S, "pixels_per_chain": S / max(C, 1),
+            "px_s": float(fit.sum()) / t_lut, "seconds": t_lut,
+            "served_share": float(np.mean(src[fit] >= 0)),
+            "hot_share_of_fits": float(np.mean((st[fitted] & 0x400) != 0)),
+            "evals_per_fit": float(ev[fitted].mean()) if fitted.any() else 0.0,
+            "evals_per_pixel": float(ev[fit].mean()),
+            "plain_px_s": float(((pst & 0xFF) == 0).sum()) / t_plain, "plain_seconds": t_plain,
+            "plain_evals_per_pixel": float(pev[(pst & 0xFF) == 0].mean()),
+            "speedup_vs_plain": t_plain / t_lut,
+            "oracle_chains": {"chains": int(len(chains)), "pixels": int(d.size),
+                              "identical_depth": float(np.mean(d == 0)) if d.size else None,
+                              "median_abs_dH_m": float(np.median(d)) if d.size else None,
+                              "served_share_gpu": float(np.mean(np.concatenate(srv_g)))
+                              if srv_g else None,
+                              "served_share_oracle": float(np.mean(np.concatenate(srv_o)))
+                              if srv_o else None},
+            "cpu_one_thread": {"px_s": shallow_cpu / t_cpu, "seconds": t_cpu,
+                               "served_share": float(np.mean(sc[oc[:, 9] == 0] >= 0)),
+                               "sample": f"{args.lut_cpu_side}x{args.lut_cpu_side} corner of "
+                                         f"the scene, one chain, the oracle port (pinned bit "
+                                         f"for bit to the reference's samodel())"}}
 
 
 def ncgrid_leg(args, dev, rrs):

@@ -188,6 +188,17 @@ int photic_joint_invert_batch(const photic_config *cfg, const int32_t *d_offsets
 int photic_cost_batch(const photic_config *cfg, const float *d_rrs, const double *d_params,
                       int64_t n, double *d_cost, double *d_rrs_modelled, void *stream);
 
+/* Spatially coherent synthetic scene of nrows x ncols pixels (the workload
+ * of the lookup-table loop): one water mass (P, G, X within +/-10 % of
+ * values drawn once from the seed), depth a smooth field over 0.5-25 m, the
+ * bottom in three albedo classes with texture, N(0, noise_sigma) noise and
+ * mask_frac of the pixels masked.  Writes rows row0 .. row0+n_rows-1:
+ * [n_rows * ncols * n_bands] floats and, if d_truth != NULL,
+ * [n_rows * ncols * 5] doubles (H, P, G, X, B). */
+int photic_generate_field(const photic_config *cfg, uint64_t seed, int64_t nrows, int64_t ncols,
+                          int64_t row0, int64_t n_rows, double mask_frac, double noise_sigma,
+                          float *d_rrs, double *d_truth, void *stream);
+
 /* Synthetic scene of the plain-method workload (photic_aux.cu):
  * writes [npix * n_bands] floats and, if d_truth != NULL, [npix * 5]
  * doubles (H, P, G, X, B). Pixels pix0 .. pix0+npix-1 of the scene. */

@@ -11,17 +11,18 @@
  * clashes with the reference's own.
  *
  * Semantics kept: the per-pixel fit of samodel_optimise (cold multi-start,
- * or the single empirical depth start when empirical_depth_present), the
- * cost of samodel_error and the forward model of samodel_Rrs, for one
- * spatial region and the sand bottom; outputs are written where the
- * reference writes them.  Not reproduced: the reference samodel()'s
- * order-dependent shortcuts (lookup table of earlier fits, hot start from
- * the previous pixel, model/samodel.c:980-1109) and its netCDF writes --
- * samodel() here fits every unmasked pixel with the plain method and fills
- * the output grids in memory.  The functions return
- * void like the reference; each clears photic_last_error() on entry, and a
- * failure leaves the outputs untouched and its message there, so an empty
- * message after the call means success.
+ * the single empirical depth start when empirical_depth_present, or the hot
+ * start from md->prev), the cost of samodel_error and the forward model of
+ * samodel_Rrs, with one to three bottom types (sand, seagrass, coral) mixed
+ * per region and one or a 3 x 3 neighbourhood of regions; samodel()'s pixel
+ * loop, with its dynamic lookup table of earlier fits and hot starts
+ * (model/samodel.c:649-1215) where the lookup-table kernel covers the
+ * configuration (see samodel() below); outputs are written where the
+ * reference writes them, and samodel() ends with the reference's netCDF
+ * result files.  The functions return void like the reference; each clears
+ * photic_last_error() on entry, and a failure leaves the outputs untouched
+ * and its message there, so an empty message after the call means
+ * success.
  *
  * Rrs_measured is read at float precision (samodel() fills it from float
  * grids).  samodel_optimise honours start_at_previous for one scene (one
@@ -184,14 +185,25 @@ int photic_parse_scene(const char *line, photic_scene_spec *out);
 int photic_config_from_scene(const photic_scene *scene, photic_config *cfg);
 
 /* model/samodel.h:8-19.  Fits every pixel that has data in all bands of all
- * scenes (model/samodel.c:672-700); n_bottoms == 1 (sand) is required;
- * n_spatial <= 1 fits each pixel alone, n_spatial == 2 (one scene, no
- * empirical depths) fits it with its 3 x 3 neighbourhood
- * (photic_region_invert_batch, model/samodel.c:2957-3027); smoothing radius
- * 1 (none) only.  depth_sigma (one scene) is the reference's
- * Monte Carlo estimate computed by photic_depth_sigma with the scene's
- * R_sigma, 128 samples per 0.25 m interval and a fixed seed; 0 for more
- * scenes or n_spatial == 2.  Depth is written negative below the datum, as the reference does
+ * scenes (model/samodel.c:672-700), at the reference's tolerances
+ * (reqmin 1e-2, konvge 100, kcount 5000), smoothing radius 1 (none) only:
+ *   - one scene, n_bottoms == 1, n_spatial <= 1, no empirical depths: the
+ *     reference's pixel loop with its dynamic lookup table
+ *     (photic_lut_invert_batch): pixels in spectral-index order (times the
+ *     spectral angle to the scene's R_sigma when every band's is at least
+ *     1e-6), served from stored fits or fitted with hot starts; the order is
+ *     cut into PHOTIC_LUT_CHAINS contiguous chains (environment; 1 is the
+ *     reference on one thread), else one per lane the kernel keeps resident;
+ *   - one scene with empirical depths: every pixel fitted from its
+ *     empirical depth (no lookup table);
+ *   - n_bottoms 2..3, n_spatial == 2, or several scenes with empirical
+ *     depths: the general fit of photic_region_fit_batch (bottom mixtures,
+ *     3 x 3 regions, scene stacks; no lookup table);
+ *   - several scenes otherwise: the temporal joint fit.
+ * depth_sigma (one scene, the first two cases) is the reference's Monte
+ * Carlo estimate computed by photic_depth_sigma with the scene's R_sigma,
+ * 128 samples per 0.25 m interval and a fixed seed; 0 otherwise.  Depth is
+ * written negative below the datum, as the reference does
  * (model/samodel.c:1486).  Like the reference, it ends by writing the result
  * grids as netCDF files in the working directory (model/samodel.c:1492-1690):
  * <scene>_K_coastal/_K_blue/_K_green/_K_red/_P/_G/_X.nc per scene and the ten

@@ -482,7 +482,7 @@ _i64p = C.POINTER(C.c_int64)
 
 
 def generate_field(seed, nrows, ncols, *, row0=0, n_rows=None, wl=OLI_BANDS, theta_sun=35.0,
-                   theta_view=0.0, mask_frac=0.15, noise_sigma=2e-4, nodata=-9999.0):
+                   theta_view=0.0, mask_frac=0.1, noise_sigma=1e-4, nodata=-9999.0):
     """Rows [row0, row0 + n_rows) of a nrows x ncols scene whose parameters
     are smooth fields; returns ([n_rows*ncols, n_bands] float32 spectra,
     [n_rows*ncols, 5] truth H P G X B)."""

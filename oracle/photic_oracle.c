@@ -1717,12 +1717,12 @@ void po_generate_field(uint64_t seed, int64_t nrows, int64_t ncols, int64_t row0
  * samodel()'s pixel loop with its dynamic lookup table, one scene, one
  * region, one bottom type (model/samodel.c:649-660, 701-773, 901-1215).
  *
- *   order    the shallow pixels (no band nodata or negative, :933-947)
- *            sorted ascending by the spectral index |(Rrs_blue, Rrs_green,
- *            Rrs_red)| (bands 1, 2, 3), times the spectral angle to the
- *            noise spectrum when every band's noise is at least 1e-6
- *            (:706-770); the index is a float and ties keep the pixel
- *            order (glibc's qsort, a merge sort, is stable);
+ *   order    every pixel sorted ascending by the spectral index
+ *            |(Rrs_blue, Rrs_green, Rrs_red)| (bands 1, 2, 3), times the
+ *            spectral angle to the noise spectrum when every band's noise
+ *            is at least 1e-6 (:706-770), with glibc's merge sort (po_msort:
+ *            ties keep the pixel order); the shallow pixels (no band nodata
+ *            or negative, :933-947) in that order;
  *   chains   the sorted list cut into n_chains contiguous slices; each
  *            slice runs the reference's loop on its own, as one OpenMP
  *            thread of the reference runs it over the pixels it is given,
@@ -1754,11 +1754,30 @@ typedef struct {
   int64_t idx;
 } po_key;
 
-static int po_key_cmp(const void *a, const void *b) {
-  const po_key *x = (const po_key *)a, *y = (const po_key *)b;
-  if (x->value < y->value) return -1;
-  if (x->value > y->value) return 1;
-  return (x->idx > y->idx) - (x->idx < y->idx);
+/* sort_indexes_2d (model/common.c:180-209) sorts every pixel's index with
+ * glibc's qsort, a top-down merge sort: halves of n / 2 and n - n / 2, the
+ * merge taking the left element unless it compares greater.  The
+ * comparator (cmp_floats, model/common.c:165-177) calls a NaN equal to
+ * everything, so NaN indices -- pixels whose blue, green and red are all
+ * nodata or zero, under the spectral-angle order -- stay where the merges
+ * leave them; restating the same merge tree reproduces that order. */
+static void po_msort(po_key *b, po_key *tmp, size_t n) {
+  size_t n1, n2, i = 0, j, o = 0;
+  if (n <= 1) return;
+  n1 = n / 2;
+  n2 = n - n1;
+  po_msort(b, tmp, n1);
+  po_msort(b + n1, tmp, n2);
+  j = n1;
+  while (i < n1 && j < n) {
+    if (!(b[i].value > b[j].value))
+      tmp[o++] = b[i++];
+    else
+      tmp[o++] = b[j++];
+  }
+  while (i < n1) tmp[o++] = b[i++];
+  /* the right run's tail is already in place */
+  memcpy(b, tmp, o * sizeof(po_key));
 }
 
 /* approx_equal of model/common.c:392-394: float arguments, double product */
@@ -1841,7 +1860,7 @@ static void lut_chain(const po_scene *sc, const po_fit *fit, const float *rrs, i
         }
       }
     }
-    if (best > match) {
+    if (best > match || in_use == 0) { /* see photic_lut.cu on an empty table */
       po_pixel px;
       double seed[6], bestv[PO_MAX_PARAMS], *o = out + p * PO_NOUT;
       memset(&px, 0, sizeof px);
@@ -1959,20 +1978,27 @@ int po_lut_invert(int n_bands, const double *wl, double theta_sun_deg, double th
   fit.n_hstarts = 8;
   fit.hstarts = po_default_hstarts;
   keys = (po_key *)malloc((size_t)(npix > 0 ? npix : 1) * sizeof(po_key));
+  {
+    po_key *tmp = (po_key *)malloc((size_t)(npix > 0 ? npix : 1) * sizeof(po_key));
+    /* every pixel is keyed and sorted (:701-772); the masked ones are then
+     * left out of the shallow list (:790-812) */
+    for (p = 0; p < npix; p++) {
+      keys[p].value = po_lut_key(rrs + p * n_bands, n_bands, nodata, noise);
+      keys[p].idx = p;
+    }
+    po_msort(keys, tmp, (size_t)npix);
+    free(tmp);
+  }
   for (p = 0; p < npix; p++) {
-    const float *r = rrs + p * n_bands;
-    memset(out + p * PO_NOUT, 0, PO_NOUT * sizeof(double));
+    const float *r = rrs + keys[p].idx * n_bands;
+    memset(out + keys[p].idx * PO_NOUT, 0, PO_NOUT * sizeof(double));
     if (masked(r, n_bands, nodata)) {
-      out[p * PO_NOUT + 9] = 1.0;
-      source[p] = -2;
+      out[keys[p].idx * PO_NOUT + 9] = 1.0;
+      source[keys[p].idx] = -2;
       continue;
     }
-    keys[S].value = po_lut_key(r, n_bands, nodata, noise);
-    keys[S].idx = p;
-    S++;
+    order_out[S++] = keys[p].idx;
   }
-  qsort(keys, (size_t)S, sizeof(po_key), po_key_cmp);
-  for (p = 0; p < S; p++) order_out[p] = keys[p].idx;
   free(keys);
   *n_shallow_out = S;
   if (n_chains > S) n_chains = S > 0 ? S : 1;

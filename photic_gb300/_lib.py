@@ -124,6 +124,9 @@ _SIGS = {
     "photic_generate_scene": (C.c_int, [C.POINTER(photic_config), C.c_uint64, C.c_int64,
                                         C.c_int64, C.c_double, C.c_double, C.c_void_p,
                                         C.c_void_p, C.c_void_p]),
+    "photic_generate_field": (C.c_int, [C.POINTER(photic_config), C.c_uint64, C.c_int64,
+                                        C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_double,
+                                        C.c_void_p, C.c_void_p, C.c_void_p]),
     "photic_joint_counts": (C.c_int, [C.c_uint64, C.c_int64, C.c_int32, C.c_int32, C.c_void_p,
                                       C.c_void_p]),
     "photic_generate_joint": (C.c_int, [C.POINTER(photic_config), C.c_uint64, C.c_int64,

@@ -355,6 +355,26 @@ def generate_scene(npix: int, seed: int = 20260101, config: Optional[Config] = N
     return rrs, truth
 
 
+def generate_field(nrows: int, ncols: int, seed: int = 20261201, config: Optional[Config] = None,
+                   *, row0: int = 0, n_rows: Optional[int] = None, mask_frac: float = 0.1,
+                   noise_sigma: float = 1.0e-4, device="cuda", with_truth: bool = True,
+                   stream: Optional[torch.cuda.Stream] = None):
+    """Spatially coherent synthetic scene (smooth depth, one water mass,
+    three bottom classes), rows [row0, row0 + n_rows) of nrows x ncols,
+    generated on the GPU.  Returns (rrs [n_rows * ncols, n_bands] f32,
+    truth [n_rows * ncols, 5] f64 = H, P, G, X, B)."""
+    cfg = config or Config()
+    n_rows = nrows - row0 if n_rows is None else n_rows
+    n = n_rows * ncols
+    rrs = torch.empty(n, cfg.n_bands, dtype=torch.float32, device=device)
+    truth = torch.empty(n, 5, dtype=torch.float64, device=device) if with_truth else None
+    c = cfg.to_c()
+    L.check(L.lib().photic_generate_field(C.byref(c), seed, nrows, ncols, row0, n_rows,
+                                          mask_frac, noise_sigma, _ptr(rrs), _ptr(truth),
+                                          _stream_handle(stream)))
+    return rrs, truth
+
+
 def joint_invert(offsets: torch.Tensor, theta_sun: torch.Tensor, rrs: torch.Tensor,
                  config: Optional[Config] = None, *,
                  out: Optional[Dict[str, torch.Tensor]] = None,

@@ -61,6 +61,21 @@ __device__ void synthesise(const FitParams &fp, const SceneConsts &sc, double H,
   for (int b = 0; b < NB; b++) rrs[b] = cur[b];
 }
 
+// One smooth field over the scene in [0, 1]: three seeded harmonics.
+__device__ double field_value(uint64_t seed, uint32_t which, double u, double v) {
+  double s = 0.0, norm = 0.0;
+  for (int h = 0; h < 3; h++) {
+    double w[4];
+    const double amp = 1.0 / (double)(1 << h);
+    draw4(seed, (uint64_t)(which * 4u + (uint32_t)h), 7u, 1u, w);
+    const double fx = 1.0 + floor(4.0 * w[0]), fy = 1.0 + floor(4.0 * w[1]);
+    const double ph = 2.0 * kPi * w[2];
+    s += amp * sin(2.0 * kPi * (fx * u + fy * v) + ph);
+    norm += amp;
+  }
+  return 0.5 + 0.5 * s / norm;
+}
+
 template <int NB>
 __global__ void generate_kernel(GenArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -70,11 +85,30 @@ __global__ void generate_kernel(GenArgs a) {
   double u0[4], u1[4];
   draw4(a.seed, p, 0u, 0u, u0);
   draw4(a.seed, p, 1u, 0u, u1);
-  const double H = 0.5 + 24.5 * u0[0];
-  const double P = log_uniform(u0[1], 0.005, 0.1);
-  const double G = log_uniform(u0[2], 0.005, 0.2);
-  const double X = log_uniform(u0[3], 0.001, 0.05);
-  const double B = 0.05 + 0.45 * u1[0];
+  double H, P, G, X, B;
+  if (a.field_rows > 0) {
+    // the spatially coherent scene: one water mass (P, G, X within +/-10 %
+    // of values drawn once), depth a smooth field over 0.5-25 m, the bottom
+    // in three albedo classes with +/-5 % texture
+    const int64_t row = (int64_t)p / a.field_cols, col = (int64_t)p % a.field_cols;
+    const double u = ((double)row + 0.5) / (double)a.field_rows;
+    const double v = ((double)col + 0.5) / (double)a.field_cols;
+    double w[4];
+    draw4(a.seed, 0u, 9u, 1u, w);
+    const double tH = field_value(a.seed, 0u, u, v), tB = field_value(a.seed, 4u, u, v);
+    const double cls = tB < 0.4 ? 0.08 : (tB < 0.6 ? 0.2 : 0.4);
+    H = 0.5 + 24.5 * tH * tH;
+    P = log_uniform(w[0], 0.01, 0.05) * (0.9 + 0.2 * field_value(a.seed, 1u, u, v));
+    G = log_uniform(w[1], 0.01, 0.08) * (0.9 + 0.2 * field_value(a.seed, 2u, u, v));
+    X = log_uniform(w[2], 0.002, 0.02) * (0.9 + 0.2 * field_value(a.seed, 3u, u, v));
+    B = cls * (0.95 + 0.1 * field_value(a.seed, 5u, u, v));
+  } else {
+    H = 0.5 + 24.5 * u0[0];
+    P = log_uniform(u0[1], 0.005, 0.1);
+    G = log_uniform(u0[2], 0.005, 0.2);
+    X = log_uniform(u0[3], 0.001, 0.05);
+    B = 0.05 + 0.45 * u1[0];
+  }
   double r[NB];
   synthesise<NB>(a.fp, a.sc, H, P, G, X, B, r);
   for (int b = 0; b < nb; b += 2) {

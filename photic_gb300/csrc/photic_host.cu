@@ -672,6 +672,31 @@ int photic_generate_scene(const photic_config *cfg, uint64_t seed, int64_t pix0,
   return PHOTIC_OK;
 }
 
+int photic_generate_field(const photic_config *cfg, uint64_t seed, int64_t nrows, int64_t ncols,
+                          int64_t row0, int64_t n_rows, double mask_frac, double noise_sigma,
+                          float *d_rrs, double *d_truth, void *stream) {
+  int rc = photic_config_check(cfg);
+  if (rc) return rc;
+  if (nrows < 1 || ncols < 1 || row0 < 0 || n_rows < 0 || row0 + n_rows > nrows || !d_rrs)
+    return fail(PHOTIC_ERR_INVALID, "bad arguments");
+  GenArgs a;
+  memset(&a, 0, sizeof a);
+  make_fit(*cfg, a.fp);
+  make_scene(*cfg, cfg->theta_sun_deg, a.sc);
+  a.seed = seed;
+  a.pix0 = row0 * ncols;
+  a.npix = n_rows * ncols;
+  a.mask_frac = mask_frac;
+  a.noise_sigma = noise_sigma;
+  a.rrs = d_rrs;
+  a.truth = d_truth;
+  a.field_rows = nrows;
+  a.field_cols = ncols;
+  cudaError_t e = launch_generate(a, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "generator launch");
+  return PHOTIC_OK;
+}
+
 int photic_joint_counts(uint64_t seed, int64_t npix, int32_t kmin, int32_t kmax,
                         int32_t *d_counts, void *stream) {
   if (npix < 0 || !d_counts || kmin < 1 || kmax > PHOTIC_MAX_SCENES || kmin > kmax)
@@ -2264,8 +2289,21 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
         ea.npix = npix;
         ea.seeds = d_seeds;
         launch_empirical_seeds(ea, 0);
+        rc = photic_invert_batch(&cfg, d_rrs, npix, nb, 1, d_seeds, &o, 0);
+      } else {
+        // the reference's product path: the pixel loop with its dynamic
+        // lookup table (LUT 1, :649-1215), the sorted pixels cut into
+        // chains -- PHOTIC_LUT_CHAINS of them if set (1: the reference on
+        // one thread), else one per resident lane
+        photic_lut_config lc;
+        photic_lut_config_default(&lc);
+        const char *ch = getenv("PHOTIC_LUT_CHAINS");
+        if (ch && *ch) lc.n_chains = atoll(ch);
+        lc.use_noise = 1;
+        for (int b = 0; b < nb && b < PHOTIC_MAX_BANDS; b++) lc.rrs_noise[b] = s0.R_sigma[b];
+        rc = photic_lut_invert_batch(&cfg, &lc, d_rrs, npix, &o, nullptr, nullptr, nullptr,
+                                     nullptr, nullptr, 0);
       }
-      rc = photic_invert_batch(&cfg, d_rrs, npix, nb, 1, d_seeds, &o, 0);
     } else {
       std::vector<int32_t> offs((size_t)npix + 1);
       std::vector<double> th((size_t)nobs);

@@ -84,6 +84,7 @@ struct GenArgs {
   double mask_frac, noise_sigma;
   float *rrs;
   double *truth;
+  int64_t field_rows, field_cols;  // > 0: the spatially coherent scene of that size
 };
 cudaError_t launch_generate(const GenArgs &a, cudaStream_t s);
 

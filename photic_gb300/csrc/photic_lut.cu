@@ -6,8 +6,12 @@
 // sorted ascending by the spectral index |(Rrs_1, Rrs_2, Rrs_3)| (the blue,
 // green and red bands, :711-745), times the spectral angle to the scene's
 // noise spectrum when every band's noise is at least 1e-6 (:749-767).  The
-// index is a float; ties keep pixel order, as glibc's merge-sort qsort does
-// (:772): a stable radix sort.
+// index is a float, sorted over every pixel by glibc's merge-sort qsort
+// (:772, model/common.c:180-209): ties keep pixel order, so a stable radix
+// sort of the shallow pixels gives the same order -- except where a key is
+// NaN (a pixel whose blue, green and red are all nodata or zero, under the
+// spectral angle), which the comparator calls equal to everything; then the
+// reference's own merge tree is replayed level by level.
 //
 // Chains.  The sorted list is cut into contiguous slices.  Each slice runs
 // the reference's loop exactly as one of its OpenMP threads runs the pixels
@@ -106,6 +110,64 @@ __global__ void gather_keys_kernel(const float *keys, const int64_t *idx, int64_
                                    float *out) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) out[k] = keys[idx[k]];
+}
+
+__global__ void nan_count_kernel(const float *keys, int64_t n, unsigned long long *count) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n && isnan(keys[k])) atomicAdd(count, 1ull);
+}
+
+// One level of the reference's qsort (glibc's top-down merge sort: halves
+// of n / 2 and n - n / 2, the merge taking the left element unless it
+// compares greater), for key sets holding NaN: the comparator of
+// sort_indexes_2d calls a NaN equal to everything, so the order depends on
+// the merge tree and only the same tree reproduces it.  Thread t of level d
+// owns the node reached from the root by the bits of t (most significant
+// first: 0 left, 1 right) and merges its two halves from (kin, iin) into
+// (kout, iout); nodes of fewer than two elements are copied.
+__global__ void msort_level_kernel(const float *kin, const int64_t *iin, float *kout,
+                                   int64_t *iout, int64_t n, int depth) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ((int64_t)1 << depth)) return;
+  int64_t lo = 0, hi = n;
+  for (int b = depth - 1; b >= 0; b--) {
+    const int64_t mid = lo + (hi - lo) / 2;
+    if ((t >> b) & 1) lo = mid;
+    else hi = mid;
+  }
+  if (hi - lo < 2) {
+    for (int64_t k = lo; k < hi; k++) {
+      kout[k] = kin[k];
+      iout[k] = iin[k];
+    }
+    return;
+  }
+  const int64_t mid = lo + (hi - lo) / 2;
+  int64_t i = lo, j = mid, o = lo;
+  while (i < mid && j < hi) {
+    const float a = kin[i], b = kin[j];
+    if (!(a > b)) {
+      kout[o] = a;
+      iout[o++] = iin[i++];
+    } else {
+      kout[o] = b;
+      iout[o++] = iin[j++];
+    }
+  }
+  while (i < mid) {
+    kout[o] = kin[i];
+    iout[o++] = iin[i++];
+  }
+  while (j < hi) {
+    kout[o] = kin[j];
+    iout[o++] = iin[j++];
+  }
+}
+
+__global__ void gather_flags_kernel(const uint8_t *flags, const int64_t *idx, int64_t n,
+                                    uint8_t *out) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) out[k] = flags[idx[k]];
 }
 
 // ---------------------------------------------------------------------------
@@ -320,7 +382,9 @@ __global__ void __launch_bounds__(kLutBlock) lut_kernel(const __grid_constant__ 
             pos = op;
           }
         }
-        if (bestd > S.d[CD_MATCH][t]) {
+        // (an empty table with a threshold above 1e4 would make the
+        // reference serve an unused slot; that pixel is fitted here)
+        if (bestd > S.d[CD_MATCH][t] || n_in == 0) {
           // a fit (:1008-1063): set up on the owner lane
           if (lane == L) {
             float rf[NB];
@@ -515,7 +579,9 @@ int lut_blocks_per_sm(const LutArgs &a) {
 
 // The sorted shallow pixels: keys and mask (masked pixels' outputs written
 // there), the shallow pixels selected in pixel order, their keys gathered,
-// and a stable radix sort of (key, pixel) pairs.  order must hold npix
+// and a stable radix sort of (key, pixel) pairs -- the order of a stable
+// sort, which the reference's merge sort gives when no key is NaN; with NaN
+// keys, the reference's merge tree over every pixel instead.  order must hold npix
 // entries; *n_shallow receives the count (the call synchronises the stream
 // once to read it).  Scratch is stream-ordered.
 cudaError_t lut_order(LutKeyArgs ka, int64_t *order, int64_t *n_shallow, cudaStream_t s) {
@@ -548,13 +614,54 @@ cudaError_t lut_order(LutKeyArgs ka, int64_t *order, int64_t *n_shallow, cudaStr
     lut_key_kernel<<<(unsigned)((npix + bs - 1) / bs), bs, 0, s>>>(ka);
     e = cudaGetLastError();
   }
-  size_t bt = b_temp;
-  if (e == cudaSuccess)
-    e = cub::DeviceSelect::Flagged(temp, bt, idx, flags, sel_idx, d_count, npix, s);
-  int64_t S = 0;
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&S, d_count, sizeof S, cudaMemcpyDeviceToHost, s);
+  // NaN keys (pixels whose blue, green and red are all nodata or zero,
+  // under the spectral-angle order) need the reference's own merge tree
+  unsigned long long n_nan = 0;
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_count, 0, sizeof(int64_t), s);
+  if (e == cudaSuccess) {
+    const int bs = 256;
+    nan_count_kernel<<<(unsigned)((npix + bs - 1) / bs), bs, 0, s>>>(
+        keys, npix, reinterpret_cast<unsigned long long *>(d_count));
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&n_nan, d_count, sizeof n_nan, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e == cudaSuccess && S > 0) {
+  int64_t S = 0;
+  size_t bt = b_temp;
+  if (e == cudaSuccess && n_nan > 0) {
+    // merge-sort every pixel's (key, index) level by level, ping-ponging
+    // between (keys, idx) and (sorted_keys, sel_idx); then the shallow
+    // pixels in that order
+    int depth = 0;
+    while (((int64_t)1 << depth) < npix) depth++;
+    float *ka = keys, *kb = sorted_keys;
+    int64_t *ia = idx, *ib = sel_idx;
+    for (int d = depth - 1; d >= 0 && e == cudaSuccess; d--) {
+      const int64_t nt = (int64_t)1 << d;
+      const int bs = 128;
+      msort_level_kernel<<<(unsigned)((nt + bs - 1) / bs), bs, 0, s>>>(ka, ia, kb, ib, npix, d);
+      e = cudaGetLastError();
+      float *tk = ka; ka = kb; kb = tk;
+      int64_t *ti = ia; ia = ib; ib = ti;
+    }
+    uint8_t *sflags = reinterpret_cast<uint8_t *>(kb);  // the free key buffer
+    if (e == cudaSuccess) {
+      const int bs = 256;
+      gather_flags_kernel<<<(unsigned)((npix + bs - 1) / bs), bs, 0, s>>>(flags, ia, npix,
+                                                                        sflags);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+      e = cub::DeviceSelect::Flagged(temp, bt, ia, sflags, order, d_count, npix, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&S, d_count, sizeof S, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  } else {
+    if (e == cudaSuccess)
+      e = cub::DeviceSelect::Flagged(temp, bt, idx, flags, sel_idx, d_count, npix, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&S, d_count, sizeof S, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  if (e == cudaSuccess && S > 0 && n_nan == 0) {
     const int bs = 256;
     gather_keys_kernel<<<(unsigned)((S + bs - 1) / bs), bs, 0, s>>>(keys, sel_idx, S, sel_keys);
     e = cudaGetLastError();

@@ -4,7 +4,7 @@ Runs the reference's own samodel_optimise / samodel_error / nelmin, compiled
 from its sources by oracle/Makefile into oracle/_ref/libphotic_ref.so
 (needs the reference sources; run from the repository root):
 
-    make -C oracle all && python tests/golden/make_golden.py
+    make -C oracle all && python tests/golden/make_golden.py [fixture ...]
 
 Inputs are synthetic spectra of the plain-method workload (the reference
 publishes no test vectors).  Every fixture stores its inputs next to the
@@ -121,15 +121,35 @@ def bottoms():
                         stack_theta_sun=stack_th, **out)
 
 
+def lut():
+    """The reference's own samodel() with its dynamic lookup table (LUT 1),
+    one thread, reference tolerances, on two spatially coherent scenes: 64 x 64
+    ordered by the spectral index alone, and 48 x 48 with a noise spectrum
+    (R_sigma) so that the spectral angle enters the order.  Kept grids:
+    depth (negative below the datum), model error, bottom albedo, K_min and
+    index of optical depth, as samodel() leaves them."""
+    keep = [0, 2, 3, 7, 9]
+    out = {}
+    for name, n, rs in (("plain", 64, None), ("noise", 48, np.array([2e-4, 1.5e-4, 1e-4, 5e-5]))):
+        rrs, _ = O.generate_field(20261201 + n, n, n, mask_frac=0.1, noise_sigma=1e-4)
+        grid = rrs.reshape(n, n, 4)
+        g = O.reference_samodel_grid(grid, r_sigma=rs)
+        out[f"{name}_grid"] = grid
+        out[f"{name}_ref"] = g[keep]
+        if rs is not None:
+            out[f"{name}_r_sigma"] = rs
+    np.savez_compressed(os.path.join(OUT, "lut.npz"), grids=np.array(keep), **out)
+
+
+FIXTURES = {"single": single, "joint": joint, "cost_nelmin": cost_and_nelmin,
+            "regions": regions, "bottoms": bottoms, "lut": lut}
+
 if __name__ == "__main__":
     O.build(ref=True)
     if not O.reference_available():
         sys.exit("reference library not built; the reference sources are required")
-    single()
-    joint()
-    cost_and_nelmin()
-    regions()
-    bottoms()
+    for name in (sys.argv[1:] or list(FIXTURES)):
+        FIXTURES[name]()
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)), "bytes")

@@ -34,10 +34,10 @@ def _write_input(path, rrs, params=None, nrows=0, ncols=0):
         np.ascontiguousarray(params, dtype=np.float64).tofile(f)
 
 
-def _run(exe, mode, inp, out):
+def _run(exe, mode, inp, out, env=None):
     # samodel() writes its result files into the working directory
     r = subprocess.run([exe, mode, inp, out], capture_output=True, text=True, timeout=600,
-                       cwd=os.path.dirname(inp))
+                       cwd=os.path.dirname(inp), env=None if env is None else {**os.environ, **env})
     assert r.returncode == 0, (mode, r.returncode, r.stderr[-2000:])
 
 
@@ -193,6 +193,30 @@ def test_samodel_grid_matches_oracle(driver, port, tmp_path):
         v, step = decoded(name)
         m = fit & rest
         assert (v[m] > 0).all() and (v[m] <= 2.5 + step).all(), name
+
+
+def test_samodel_lookup_table_against_reference(driver, golden_dir, tmp_path):
+    """samodel() as the reference runs it -- the pixel loop with its dynamic
+    lookup table and hot starts -- on one chain (PHOTIC_LUT_CHAINS=1, the
+    reference on one thread), against the reference's own samodel() on the
+    same grid (tests/golden/lut.npz, LUT 1, one OpenMP thread)."""
+    g = np.load(os.path.join(golden_dir, "lut.npz"))
+    grid = g["plain_grid"]
+    n = grid.shape[0]
+    inp, out = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    _write_input(inp, grid.reshape(n * n, 4), nrows=n, ncols=n)
+    _run(driver, "grid", inp, out, env={"PHOTIC_LUT_CHAINS": "1"})
+    gr = np.fromfile(out, dtype=np.float32).reshape(10, n * n)
+    ref = g["plain_ref"].reshape(len(g["grids"]), n * n)  # depth, error, albedo, K_min, IOD
+    fit = ref[0] != 0
+    d = np.abs(gr[0, fit] - ref[0, fit])
+    same = d == 0
+    print(f"samodel() with the lookup table vs the reference's: {fit.sum()} px, identical "
+          f"depth {same.mean():.4f}, median |dH| {np.median(d):.3g} m")
+    assert np.median(d) == 0 and same.mean() >= 0.95
+    np.testing.assert_array_equal(gr[0, ~fit], 0)
+    for k, row in ((2, 1), (3, 2), (7, 3), (9, 4)):
+        np.testing.assert_array_equal(gr[k, fit][same], ref[row, fit][same], err_msg=str(k))
 
 
 def test_samodel_grid_regions_matches_oracle(driver, port, tmp_path):

@@ -1,0 +1,87 @@
+"""The oracle's restatement of samodel()'s pixel loop with its dynamic
+lookup table (model/samodel.c:649-1215) against the reference itself.
+
+The pin: the reference's own samodel() with LUT 1, run on one OpenMP thread
+(deterministic), on spatially coherent scenes -- tests/golden/lut.npz, made
+by tests/golden/make_golden.py -- and, where the reference sources are
+present, live on another scene.  One chain of the oracle is the reference
+on one thread; every grid must agree bit for bit.  Then the property the GPU
+path builds on: n chains are n independent runs of the same loop on
+contiguous slices of the sorted pixels."""
+import os
+
+import numpy as np
+import pytest
+
+# grids of samodel() kept in the fixture and the oracle record column of each
+GRID_COLS = {0: 0, 2: 3, 3: 1, 7: 4, 9: 5}  # depth, model error (Rrs), albedo, K_min, IOD
+
+
+def _compare_grids(out, ref_grids, kept, label):
+    fit = out[:, 9] == 0
+    for k, g in zip(kept, ref_grids):
+        col = GRID_COLS[int(k)]
+        mine = out[:, col].astype(np.float32)
+        want = g.reshape(-1)
+        if k == 0:
+            want = -want
+        same = mine[fit] == want[fit]
+        assert same.all(), (label, int(k), int((~same).sum()))
+
+
+@pytest.mark.parametrize("case", ["plain", "noise"])
+def test_oracle_lut_matches_reference_fixture(port, golden_dir, case):
+    g = np.load(os.path.join(golden_dir, "lut.npz"))
+    grid = g[f"{case}_grid"]
+    n = grid.shape[0]
+    rs = g[f"{case}_r_sigma"] if f"{case}_r_sigma" in g else None
+    out, src, order, stats = port.lut_invert(grid.reshape(n * n, 4), rrs_noise=rs, n_chains=1,
+                                             nthreads=1)
+    _compare_grids(out, g[f"{case}_ref"], g["grids"], case)
+    fit = out[:, 9] == 0
+    served = np.mean(src[fit] >= 0)
+    print(f"{case}: {fit.sum()} shallow pixels, served from the table {served:.4f}, "
+          f"final thresholds {stats[0, 2]:.3f}/{stats[0, 3]:.3f}")
+    assert served > 0.02
+    # served pixels carry their source's fit
+    s = np.where(src >= 0)[0]
+    np.testing.assert_array_equal(out[s, 0], out[src[s], 0])
+    assert np.all(src[src >= 0] != s) if s.size else True
+
+
+def test_oracle_lut_matches_reference_live(port):
+    if not port.reference_available():
+        pytest.skip("reference sources not available on this host")
+    n = 40
+    rrs, _ = port.generate_field(777, n, n)
+    ref = port.reference_samodel_grid(rrs.reshape(n, n, 4))
+    out, src, order, stats = port.lut_invert(rrs, n_chains=1, nthreads=1)
+    _compare_grids(out, ref[[0, 2, 3, 7, 9]], [0, 2, 3, 7, 9], "live")
+
+
+def test_oracle_order_is_the_stable_key_order(port):
+    rrs, _ = port.generate_field(31, 32, 32)
+    rrs[5] = rrs[9]  # a tie: equal spectra keep pixel order
+    out, src, order, _ = port.lut_invert(rrs, n_chains=1, nthreads=1)
+    keys = port.lut_key(rrs)
+    shallow = np.where(out[:, 9] == 0)[0]
+    want = shallow[np.argsort(keys[shallow], kind="stable")]
+    np.testing.assert_array_equal(order, want)
+    assert list(order).index(5) < list(order).index(9)
+    assert np.all(src[out[:, 9] == 1] == -2)
+
+
+def test_chains_are_independent_slices(port):
+    """n chains = the loop run alone on each contiguous slice of the order."""
+    n, C = 48, 5
+    rrs, _ = port.generate_field(4242, n, n)
+    out, src, order, stats = port.lut_invert(rrs, n_chains=C, nthreads=4)
+    S = order.size
+    for c in range(C):
+        sl = order[c * S // C:(c + 1) * S // C]
+        o1, s1, ord1, st1 = port.lut_invert(rrs[sl], n_chains=1, nthreads=1)
+        np.testing.assert_array_equal(ord1, np.arange(sl.size))  # the slice keeps its order
+        np.testing.assert_array_equal(out[sl], o1)
+        mapped = np.where(s1 >= 0, sl[np.maximum(s1, 0)], s1)
+        np.testing.assert_array_equal(src[sl], mapped)
+        np.testing.assert_array_equal(stats[c], st1[0])
