@@ -812,6 +812,7 @@ def lut_leg(args, dev):
     parity against the oracle run on the same slices (each slice is the
     reference's loop on one thread, pinned bit for bit to the reference's
     samodel()), and that loop's CPU rate on one thread."""
+    import ctypes as C
     import torch
     import photic_gb300 as pg
     from oracle import oracle as O
@@ -835,6 +836,20 @@ def lut_leg(args, dev):
         return o, e0.elapsed_time(e1) * 1e-3
 
     fields = ("depth_f64", "status", "evals", "P", "G", "X", "bottom_albedo", "K_min")
+    # fewer, longer chains: more of each chain's history to serve from, but
+    # the kernel lasts as long as its busiest lane
+    lanes = int(pg.api.L.lib().photic_lut_default_chains(C.byref(cfg.to_c()))) // 8
+    other = {}
+    for per_lane in (1, 32):
+        o, t = timed(lambda: pg.lut_invert(rrs, cfg, n_chains=per_lane * lanes,
+                                           fields=("status",)))
+        s_ = o["status"].cpu().numpy()
+        sr = o["source"].cpu().numpy()
+        f_ = (s_ & 0xFF) == 0
+        other[f"{per_lane}_per_lane"] = {"chains": int(o["chain_stats"].shape[0]),
+                                         "px_s": float(f_.sum()) / t,
+                                         "served_share": float(np.mean(sr[f_] >= 0))}
+        del o
     lut, t_lut = timed(lambda: pg.lut_invert(rrs, cfg, fields=fields))
     plain, t_plain = timed(lambda: pg.invert(rrs, cfg, fields=("depth_f64", "status", "evals")))
     st = lut["status"].cpu().numpy()
@@ -880,6 +895,7 @@ def lut_leg(args, dev):
             "plain_px_s": float(((pst & 0xFF) == 0).sum()) / t_plain, "plain_seconds": t_plain,
             "plain_evals_per_pixel": float(pev[(pst & 0xFF) == 0].mean()),
             "speedup_vs_plain": t_plain / t_lut,
+            "other_chain_counts": other,
             "oracle_chains": {"chains": int(len(chains)), "pixels": int(d.size),
                               "identical_depth": float(np.mean(d == 0)) if d.size else None,
                               "median_abs_dH_m": float(np.median(d)) if d.size else None,

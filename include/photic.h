@@ -273,7 +273,8 @@ int photic_region_fit_batch(const photic_config *cfg, const float *d_grid, int32
  * are sorted by the spectral index |(Rrs_1, Rrs_2, Rrs_3)| -- times the
  * spectral angle to rrs_noise[1..3] when use_noise and every band of
  * rrs_noise is at least 1e-6 (:590-600, 749-767) -- and the sorted list is
- * cut into n_chains contiguous slices (0: one per resident lane).  Each
+ * cut into n_chains contiguous slices (0: eight per resident lane, see
+ * photic_lut_default_chains).  Each
  * slice runs the reference's loop as one of its threads does: a pixel whose
  * spectrum matches a stored fit within the match threshold (entries within
  * 10 % of the previous pixel's depth and K_min, model_spectral_diff_mean
@@ -293,15 +294,17 @@ int photic_region_fit_batch(const photic_config *cfg, const float *d_grid, int32
  * PHOTIC_ERR_UNSUPPORTED). */
 typedef struct photic_lut_config {
   int32_t n_lut;                        /* slots per slice (the reference: 16000) */
-  int64_t n_chains;                     /* slices; 0: one per resident lane */
+  int64_t n_chains;                     /* slices; 0: eight per resident lane */
   int32_t use_noise;                    /* order by the spectral angle to rrs_noise */
   double rrs_noise[PHOTIC_MAX_BANDS];   /* the scene's noise spectrum (R_sigma) */
 } photic_lut_config;
 
 void photic_lut_config_default(photic_lut_config *lut);
 
-/* The slice count n_chains = 0 stands for: one per lane the kernel keeps
- * resident on this device (0 on error). */
+/* The slice count n_chains = 0 stands for: eight per lane the kernel keeps
+ * resident on this device (0 on error).  A slice is sequential; lanes that
+ * finish theirs take the next from a queue, so several per lane keep the
+ * kernel's tail to one short slice. */
 int64_t photic_lut_default_chains(const photic_config *cfg);
 
 int photic_lut_invert_batch(const photic_config *cfg, const photic_lut_config *lut,

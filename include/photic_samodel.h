@@ -193,7 +193,7 @@ int photic_config_from_scene(const photic_scene *scene, photic_config *cfg);
  *     spectral angle to the scene's R_sigma when every band's is at least
  *     1e-6), served from stored fits or fitted with hot starts; the order is
  *     cut into PHOTIC_LUT_CHAINS contiguous chains (environment; 1 is the
- *     reference on one thread), else one per lane the kernel keeps resident;
+ *     reference on one thread), else eight per lane the kernel keeps resident;
  *   - one scene with empirical depths: every pixel fitted from its
  *     empirical depth (no lookup table);
  *   - n_bottoms 2..3, n_spatial == 2, or several scenes with empirical

@@ -191,7 +191,7 @@ def lut_invert(rrs: torch.Tensor, config: Optional[Config] = None, *, n_lut: int
     (model/samodel.c:649-1215) over ``rrs`` ([npix, n_bands] float32, CUDA):
     the shallow pixels sorted by spectral index (times the spectral angle
     to ``rrs_noise`` when every band of it is at least 1e-6), cut into
-    ``n_chains`` contiguous slices (0: one per resident lane), each run as
+    ``n_chains`` contiguous slices (0: eight per resident lane), each run as
     the reference runs them on one thread -- served from its table of
     ``n_lut`` fits when a stored spectrum matches, else fitted (hot-started
     from the previous pixel when the last two were continuous).  Use

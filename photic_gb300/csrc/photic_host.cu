@@ -451,6 +451,13 @@ void photic_lut_config_default(photic_lut_config *lut) {
   lut->n_lut = 16000;  // model/samodel.c:650
 }
 
+// Default chains per resident lane.  A chain is sequential (every pixel
+// waits for the previous one's fit), so with one chain per lane the kernel
+// lasts as long as the lane with the most work; lanes that finish take the
+// next chain from the queue, and eight chains per lane bound that tail by
+// one short chain.
+constexpr int64_t kLutChainsPerLane = 8;
+
 int64_t photic_lut_default_chains(const photic_config *cfg) {
   if (photic_config_check(cfg)) return 0;
   unsigned int *err = nullptr;
@@ -459,7 +466,7 @@ int64_t photic_lut_default_chains(const photic_config *cfg) {
   LutArgs a;
   memset(&a, 0, sizeof a);
   make_fit(*cfg, a.inv.fp);
-  return (int64_t)sms * lut_blocks_per_sm(a) * lut_block();
+  return kLutChainsPerLane * sms * lut_blocks_per_sm(a) * lut_block();
 }
 
 int photic_lut_invert_batch(const photic_config *cfg, const photic_lut_config *lut,
@@ -533,7 +540,7 @@ int photic_lut_invert_batch(const photic_config *cfg, const photic_lut_config *l
     }
     const int block = lut_block();
     const int64_t lanes = (int64_t)sms * per_sm * block;
-    int64_t C = lut->n_chains ? lut->n_chains : lanes;
+    int64_t C = lut->n_chains ? lut->n_chains : kLutChainsPerLane * lanes;
     if (C > S) C = S;
     const int64_t per_chain = (S + C - 1) / C;
     const int64_t cap = per_chain < lut->n_lut ? per_chain : (int64_t)lut->n_lut;
@@ -2294,7 +2301,7 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
         // the reference's product path: the pixel loop with its dynamic
         // lookup table (LUT 1, :649-1215), the sorted pixels cut into
         // chains -- PHOTIC_LUT_CHAINS of them if set (1: the reference on
-        // one thread), else one per resident lane
+        // one thread), else eight per resident lane
         photic_lut_config lc;
         photic_lut_config_default(&lc);
         const char *ch = getenv("PHOTIC_LUT_CHAINS");
