@@ -285,6 +285,11 @@ int photic_region_fit_batch(const photic_config *cfg, const float *d_grid, int32
  * (PHOTIC_PX_HOT), and stored in the slice's table of n_lut slots (the
  * reference: 16000) when its model error is below the entry threshold and
  * its depth below 32 m; both thresholds adapt every 0.1 % of the slice.
+ * d_empirical (NULL, or device [npix] floats, empirical_nodata for none)
+ * is the reference's empirical depth grid (:702-710, 955-979): the pixels
+ * are then ordered by it, and a pixel with one starts its fit there (hot or
+ * cold, one start, depth = 1 m above -1 m, else |value|), a pixel without
+ * one is fitted cold.
  * Optional device outputs: d_source [npix] (-2 masked, -1 fitted, else the
  * pixel whose fit served it), d_order [npix] (the sorted shallow pixels,
  * first *n_shallow entries), d_chain_stats [n_chains][4] (served, fitted,
@@ -308,7 +313,8 @@ void photic_lut_config_default(photic_lut_config *lut);
 int64_t photic_lut_default_chains(const photic_config *cfg);
 
 int photic_lut_invert_batch(const photic_config *cfg, const photic_lut_config *lut,
-                            const float *d_rrs, int64_t npix, const photic_outputs *out,
+                            const float *d_rrs, int64_t npix, const float *d_empirical,
+                            float empirical_nodata, const photic_outputs *out,
                             int64_t *d_source, int64_t *d_order, double *d_chain_stats,
                             int64_t *n_shallow, int64_t *n_chains_used, void *stream);
 

@@ -187,15 +187,15 @@ int photic_config_from_scene(const photic_scene *scene, photic_config *cfg);
 /* model/samodel.h:8-19.  Fits every pixel that has data in all bands of all
  * scenes (model/samodel.c:672-700), at the reference's tolerances
  * (reqmin 1e-2, konvge 100, kcount 5000), smoothing radius 1 (none) only:
- *   - one scene, n_bottoms == 1, n_spatial <= 1, no empirical depths: the
- *     reference's pixel loop with its dynamic lookup table
- *     (photic_lut_invert_batch): pixels in spectral-index order (times the
- *     spectral angle to the scene's R_sigma when every band's is at least
- *     1e-6), served from stored fits or fitted with hot starts; the order is
- *     cut into PHOTIC_LUT_CHAINS contiguous chains (environment; 1 is the
- *     reference on one thread), else eight per lane the kernel keeps resident;
- *   - one scene with empirical depths: every pixel fitted from its
- *     empirical depth (no lookup table);
+ *   - one scene, n_bottoms == 1, n_spatial <= 1: the reference's pixel
+ *     loop with its dynamic lookup table (photic_lut_invert_batch): pixels
+ *     in spectral-index order (times the spectral angle to the scene's
+ *     R_sigma when every band's is at least 1e-6), or in the order of the
+ *     empirical depths when given, served from stored fits or fitted with
+ *     hot starts (from the empirical depth where a pixel has one); the order
+ *     is cut into PHOTIC_LUT_CHAINS contiguous chains (environment; 1 is the
+ *     reference on one thread), else eight per lane the kernel keeps
+ *     resident;
  *   - n_bottoms 2..3, n_spatial == 2, or several scenes with empirical
  *     depths: the general fit of photic_region_fit_batch (bottom mixtures,
  *     3 x 3 regions, scene stacks; no lookup table);

@@ -514,10 +514,12 @@ def lut_key(rrs, *, nodata=-9999.0, rrs_noise=None):
 
 
 def lut_invert(rrs, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0, h_tide=0.0,
-               nodata=-9999.0, rrs_noise=None, reqmin=None, konvge=100, kcount=2000,
-               n_lut=16000, n_chains=1, nthreads=0):
+               nodata=-9999.0, rrs_noise=None, empirical=None, empirical_nodata=-9999.0,
+               reqmin=None, konvge=100, kcount=2000, n_lut=16000, n_chains=1, nthreads=0):
     """samodel()'s loop with the dynamic lookup table over [npix, n_bands]
-    float32 spectra, the sorted shallow pixels cut into n_chains slices.
+    float32 spectra, the sorted shallow pixels cut into n_chains slices;
+    empirical ([npix] floats, empirical_nodata for none) orders the pixels and
+    starts their fits as the reference's empirical depth grid does.
     reqmin None: the reference's tolerances (1e-2 / 100 / 5000).  Returns
     (records [npix, NOUT], source [npix] (-1 fitted, -2 masked, else the
     pixel whose fit served it), order [n_shallow], chain_stats [n_chains, 4]
@@ -533,14 +535,16 @@ def lut_invert(rrs, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0, h_tide=0.0,
     n_sh = C.c_int64(0)
     stats = np.zeros((max(1, n_chains), 4))
     nz = _f64(rrs_noise) if rrs_noise is not None else None
+    em = _f32(empirical).reshape(-1) if empirical is not None else None
     L = port().lib
     L.po_lut_invert.argtypes = [C.c_int, _dp, C.c_double, C.c_double, C.c_double, _fp,
-                                C.c_int64, C.c_float, _dp, C.c_double, C.c_int, C.c_int, C.c_int,
-                                C.c_int64, C.c_int, _i64p, _i64p, _dp, _i64p, _dp]
+                                C.c_int64, C.c_float, _dp, _fp, C.c_float, C.c_double, C.c_int,
+                                C.c_int, C.c_int, C.c_int64, C.c_int, _i64p, _i64p, _dp, _i64p,
+                                _dp]
     rc = L.po_lut_invert(nb, _ptr(wl, _dp), theta_sun, theta_view, h_tide, _ptr(rrs, _fp), npix,
-                         nodata, _ptr(nz, _dp), reqmin, konvge, kcount, n_lut, n_chains,
-                         nthreads, _ptr(order, _i64p), C.byref(n_sh), _ptr(out, _dp),
-                         _ptr(source, _i64p), _ptr(stats, _dp))
+                         nodata, _ptr(nz, _dp), _ptr(em, _fp), empirical_nodata, reqmin, konvge,
+                         kcount, n_lut, n_chains, nthreads, _ptr(order, _i64p), C.byref(n_sh),
+                         _ptr(out, _dp), _ptr(source, _i64p), _ptr(stats, _dp))
     if rc:
         raise ValueError(f"po_lut_invert failed ({rc})")
     S = n_sh.value
@@ -548,7 +552,8 @@ def lut_invert(rrs, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0, h_tide=0.0,
 
 
 def reference_samodel_grid(grid, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0,
-                           nodata=-9999.0, r_sigma=None, n_spatial=1, n_bottoms=1):
+                           nodata=-9999.0, r_sigma=None, empirical=None,
+                           empirical_nodata=-9999.0, n_spatial=1, n_bottoms=1):
     """The reference's own samodel() with its lookup table over a
     [nrows, ncols, n_bands] grid on one thread; returns [10, nrows, ncols]
     float32 grids as samodel() leaves them (depth negative below the datum,
@@ -559,12 +564,14 @@ def reference_samodel_grid(grid, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0
     wl = _f64(wl)
     out = np.zeros((10, nr, nc), dtype=np.float32)
     rs = _f64(r_sigma) if r_sigma is not None else None
+    em = _f32(empirical).reshape(nr, nc) if empirical is not None else None
     L = reference().lib
     L.photic_ref_samodel_grid.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _fp, C.c_int,
-                                          C.c_int, C.c_float, _dp, C.c_int, C.c_int, _fp]
+                                          C.c_int, C.c_float, _dp, _fp, C.c_float, C.c_int,
+                                          C.c_int, _fp]
     rc = L.photic_ref_samodel_grid(nb, _ptr(wl, _dp), theta_sun, theta_view, _ptr(grid, _fp),
-                                   nr, nc, nodata, _ptr(rs, _dp), n_spatial, n_bottoms,
-                                   _ptr(out, _fp))
+                                   nr, nc, nodata, _ptr(rs, _dp), _ptr(em, _fp),
+                                   empirical_nodata, n_spatial, n_bottoms, _ptr(out, _fp))
     if rc:
         raise ValueError(f"photic_ref_samodel_grid failed ({rc})")
     return out

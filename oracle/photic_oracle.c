@@ -1830,8 +1830,8 @@ float po_lut_key(const float *r, int n_bands, float nodata, const double *noise)
 }
 
 static void lut_chain(const po_scene *sc, const po_fit *fit, const float *rrs, int nb,
-                      const int64_t *order, int64_t n, int n_lut, double *out, int64_t *source,
-                      double *stats) {
+                      const float *emp, float emp_nodata, const int64_t *order, int64_t n,
+                      int n_lut, double *out, int64_t *source, double *stats) {
   const double eps = (double)1.0e-4f; /* the reference's global float epsilon */
   const double continuity = 0.1;
   const int64_t cap = n < (int64_t)n_lut ? n : (int64_t)n_lut;
@@ -1862,7 +1862,17 @@ static void lut_chain(const po_scene *sc, const po_fit *fit, const float *rrs, i
     }
     if (best > match || in_use == 0) { /* see photic_lut.cu on an empty table */
       po_pixel px;
-      double seed[6], bestv[PO_MAX_PARAMS], *o = out + p * PO_NOUT;
+      double seed[6], bestv[PO_MAX_PARAMS], *o = out + p * PO_NOUT, h_emp = 0.0;
+      int emp_present = 0, use_hot = hot;
+      po_fit f1 = *fit;
+      if (emp) { /* the pixel's empirical depth (:955-979) */
+        if (!ref_approx_eq(emp[p], emp_nodata, 1.0e-6f)) {
+          emp_present = 1;
+          h_emp = emp[p] > -1.0 ? 1.0 : fabs(emp[p]);
+        } else {
+          use_hot = 0;
+        }
+      }
       memset(&px, 0, sizeof px);
       px.n_scenes = 1;
       px.n_bands = nb;
@@ -1871,15 +1881,18 @@ static void lut_chain(const po_scene *sc, const po_fit *fit, const float *rrs, i
       px.sc[0] = sc;
       for (b = 0; b < nb; b++) px.rrs[0][b] = meas[b];
       pixel_reference_rrs(&px);
-      if (hot) {
-        seed[0] = depth_prev;
+      if (use_hot) { /* :2234-2241: the empirical depth keeps its start */
+        seed[0] = emp_present ? h_emp : depth_prev;
         seed[1] = 100.0 * 4.0 * (px.r490[0] / (double)1);
         seed[2] = 1.0;
         seed[3] = prev[0];
         seed[4] = prev[1];
         seed[5] = prev[2];
+      } else if (emp_present) { /* one cold start at the empirical depth (:2221-2223) */
+        f1.n_hstarts = 1;
+        f1.hstarts = &h_emp;
       }
-      fit_pixel_ex(&px, fit, hot ? seed : NULL, o, bestv);
+      fit_pixel_ex(&px, &f1, use_hot ? seed : NULL, o, bestv);
       source[p] = -1;
       md_depth = o[0];
       md_kmin = o[4];
@@ -1955,9 +1968,10 @@ static void lut_chain(const po_scene *sc, const po_fit *fit, const float *rrs, i
 
 int po_lut_invert(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
                   double h_tide, const float *rrs, int64_t npix, float nodata,
-                  const double *rrs_noise, double reqmin, int konvge, int kcount, int n_lut,
-                  int64_t n_chains, int nthreads, int64_t *order_out, int64_t *n_shallow_out,
-                  double *out, int64_t *source, double *chain_stats) {
+                  const double *rrs_noise, const float *emp, float emp_nodata, double reqmin,
+                  int konvge, int kcount, int n_lut, int64_t n_chains, int nthreads,
+                  int64_t *order_out, int64_t *n_shallow_out, double *out, int64_t *source,
+                  double *chain_stats) {
   po_scene sc;
   po_fit fit;
   po_key *keys;
@@ -1983,7 +1997,8 @@ int po_lut_invert(int n_bands, const double *wl, double theta_sun_deg, double th
     /* every pixel is keyed and sorted (:701-772); the masked ones are then
      * left out of the shallow list (:790-812) */
     for (p = 0; p < npix; p++) {
-      keys[p].value = po_lut_key(rrs + p * n_bands, n_bands, nodata, noise);
+      /* the empirical depth itself when a grid of them is given (:708-710) */
+      keys[p].value = emp ? emp[p] : po_lut_key(rrs + p * n_bands, n_bands, nodata, noise);
       keys[p].idx = p;
     }
     po_msort(keys, tmp, (size_t)npix);
@@ -2009,8 +2024,8 @@ int po_lut_invert(int n_bands, const double *wl, double theta_sun_deg, double th
 #endif
   for (c = 0; c < n_chains; c++) {
     const int64_t a = c * S / n_chains, e = (c + 1) * S / n_chains;
-    lut_chain(&sc, &fit, rrs, n_bands, order_out + a, e - a, n_lut, out, source,
-              chain_stats ? chain_stats + 4 * c : NULL);
+    lut_chain(&sc, &fit, rrs, n_bands, emp, emp_nodata, order_out + a, e - a, n_lut, out,
+              source, chain_stats ? chain_stats + 4 * c : NULL);
   }
   return 0;
 }

@@ -112,9 +112,10 @@ void po_generate_field(uint64_t seed, int64_t nrows, int64_t ncols, int64_t row0
 float po_lut_key(const float *r, int n_bands, float nodata, const double *noise);
 int po_lut_invert(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
                   double h_tide, const float *rrs, int64_t npix, float nodata,
-                  const double *rrs_noise, double reqmin, int konvge, int kcount, int n_lut,
-                  int64_t n_chains, int nthreads, int64_t *order_out, int64_t *n_shallow_out,
-                  double *out, int64_t *source, double *chain_stats);
+                  const double *rrs_noise, const float *emp, float emp_nodata, double reqmin,
+                  int konvge, int kcount, int n_lut, int64_t n_chains, int nthreads,
+                  int64_t *order_out, int64_t *n_shallow_out, double *out, int64_t *source,
+                  double *chain_stats);
 void po_nc_compress(const float *grid, int64_t n, double spval, int16_t *packed,
                     float *add_offset, float *scale_factor, int16_t *missing_value);
 

@@ -538,7 +538,10 @@ double photic_ref_depth_sigma_stat(double *depths, int n) {
  * run on one thread so that its order-dependent results are reproducible,
  * at the reference's own tolerances.  r_sigma (n_bands values or NULL for
  * zeros) is the scene's noise spectrum, which orders the pixels when every
- * band's is at least 1e-6 (:590-600, :749-767).  grids_out receives the ten
+ * band's is at least 1e-6 (:590-600, :749-767); empirical (NULL or
+ * [nrows][ncols] floats, empirical_nodata for none) is an empirical depth
+ * grid, which then orders the pixels and starts their fits (:702-710,
+ * 955-979).  grids_out receives the ten
  * result grids [10][nrows][ncols] exactly as samodel() leaves them: depth
  * (negative below the datum), depth sigma, model error, bottom albedo,
  * sand, seagrass, coral, K_min, bottom type, index of optical depth.  Its
@@ -546,7 +549,8 @@ double photic_ref_depth_sigma_stat(double *depths, int n) {
  * keeps the files in memory). */
 int photic_ref_samodel_grid(int n_bands, const double *wl, double theta_sun_deg,
                             double theta_view_deg, const float *grid, int nrows, int ncols,
-                            float nodata, const double *r_sigma, int n_spatial, int n_bottoms,
+                            float nodata, const double *r_sigma, const float *empirical,
+                            float empirical_nodata, int n_spatial, int n_bottoms,
                             float *grids_out) {
   scene sc;
   geogrid *gd, none;
@@ -555,6 +559,15 @@ int photic_ref_samodel_grid(int n_bands, const double *wl, double theta_sun_deg,
   if (n_bands < 2 || n_bands > REF_MAX_BANDS) return 1;
   memset(&sc, 0, sizeof sc);
   memset(&none, 0, sizeof none);
+  if (empirical) { /* an empirical depth grid (model/samodel.c:702-710, 955-979) */
+    none.nrows = nrows;
+    none.ncols = ncols;
+    none.cellsize = 1.0f;
+    none.nodata_value = empirical_nodata;
+    allocate_float_array_2d(&none.array, nrows, ncols);
+    for (i = 0; i < nrows; i++)
+      for (j = 0; j < ncols; j++) none.array[i][j] = empirical[(size_t)i * ncols + j];
+  }
   strcpy(sc.scene_name, "harness");
   sc.n_bands = n_bands;
   sc.nrows = nrows;
@@ -579,12 +592,13 @@ int photic_ref_samodel_grid(int n_bands, const double *wl, double theta_sun_deg,
 #if _OPENMP
   omp_set_num_threads(1);
 #endif
-  samodel(&sc, gd, &idx, 1, false, none, 1, n_spatial, n_bottoms, out[0], out[1], out[2],
-          out[3], out[4], out[5], out[6], out[7], out[8], out[9], 10.0f, 0, 1);
+  samodel(&sc, gd, &idx, 1, empirical != NULL, none, 1, n_spatial, n_bottoms, out[0], out[1],
+          out[2], out[3], out[4], out[5], out[6], out[7], out[8], out[9], 10.0f, 0, 1);
   for (k = 0; k < 10; k++)
     for (i = 0; i < nrows; i++)
       for (j = 0; j < ncols; j++)
         grids_out[((size_t)k * nrows + i) * ncols + j] = out[k][i][j];
+  if (empirical) free_float_array_2d(none.array, nrows);
   for (k = 0; k < 10; k++) free_float_array_2d(out[k], nrows);
   for (b = 0; b < n_bands; b++) free_float_array_2d(gd[b].array, nrows);
   free(gd);

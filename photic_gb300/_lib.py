@@ -153,7 +153,8 @@ _SIGS = {
     "photic_lut_config_default": (None, [C.POINTER(photic_lut_config)]),
     "photic_lut_default_chains": (C.c_int64, [C.POINTER(photic_config)]),
     "photic_lut_invert_batch": (C.c_int, [C.POINTER(photic_config), C.POINTER(photic_lut_config),
-                                          C.c_void_p, C.c_int64, C.POINTER(photic_outputs),
+                                          C.c_void_p, C.c_int64, C.c_void_p, C.c_float,
+                                          C.POINTER(photic_outputs),
                                           C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                           C.c_void_p]),

@@ -185,6 +185,7 @@ def invert(rrs: torch.Tensor, config: Optional[Config] = None, *,
 
 def lut_invert(rrs: torch.Tensor, config: Optional[Config] = None, *, n_lut: int = 16000,
                n_chains: int = 0, rrs_noise: Optional[Sequence[float]] = None,
+               empirical: Optional[torch.Tensor] = None, empirical_nodata: float = -9999.0,
                fields: Sequence[str] = OUTPUT_FIELDS, stream: Optional[torch.cuda.Stream] = None
                ) -> Dict[str, torch.Tensor]:
     """samodel()'s pixel loop with its dynamic lookup table
@@ -199,7 +200,10 @@ def lut_invert(rrs: torch.Tensor, config: Optional[Config] = None, *, n_lut: int
     the outputs plus "source" (int64: -2 masked, -1 fitted, else the pixel
     whose fit served it), "order" (the sorted shallow pixels) and
     "chain_stats" ([n_chains, 4]: served, fitted, final match and entry
-    thresholds).  Synchronises the stream once (to size the order)."""
+    thresholds).  ``empirical`` ([npix] float32, CUDA; ``empirical_nodata``
+    for none) is the reference's empirical depth grid: it orders the pixels
+    and starts their fits.  Synchronises the stream once (to size the
+    order)."""
     cfg = config or Config()
     _check_cuda(rrs, "rrs", torch.float32)
     if rrs.dim() != 2 or rrs.shape[1] != cfg.n_bands:
@@ -207,6 +211,10 @@ def lut_invert(rrs: torch.Tensor, config: Optional[Config] = None, *, n_lut: int
     if not rrs.is_contiguous():
         raise ValueError("rrs must be contiguous")
     npix = rrs.shape[0]
+    if empirical is not None:
+        _check_cuda(empirical, "empirical", torch.float32)
+        if empirical.numel() != npix or not empirical.is_contiguous():
+            raise ValueError("empirical must be a contiguous [npix] tensor")
     out = alloc_outputs(npix, rrs.device, fields)
     source = torch.empty(npix, dtype=torch.int64, device=rrs.device)
     order = torch.empty(max(npix, 1), dtype=torch.int64, device=rrs.device)
@@ -224,6 +232,7 @@ def lut_invert(rrs: torch.Tensor, config: Optional[Config] = None, *, n_lut: int
     os_ = _outputs_struct(out)
     n_sh, n_ch = C.c_int64(0), C.c_int64(0)
     L.check(L.lib().photic_lut_invert_batch(C.byref(c), C.byref(lc), _ptr(rrs), npix,
+                                            _ptr(empirical), float(empirical_nodata),
                                             C.byref(os_), _ptr(source), _ptr(order),
                                             _ptr(stats), C.byref(n_sh), C.byref(n_ch),
                                             _stream_handle(stream)))

@@ -470,7 +470,8 @@ int64_t photic_lut_default_chains(const photic_config *cfg) {
 }
 
 int photic_lut_invert_batch(const photic_config *cfg, const photic_lut_config *lut,
-                            const float *d_rrs, int64_t npix, const photic_outputs *out,
+                            const float *d_rrs, int64_t npix, const float *d_empirical,
+                            float empirical_nodata, const photic_outputs *out,
                             int64_t *d_source, int64_t *d_order, double *d_chain_stats,
                             int64_t *n_shallow, int64_t *n_chains_used, void *stream) {
   int rc = photic_config_check(cfg);
@@ -505,6 +506,8 @@ int photic_lut_invert_batch(const photic_config *cfg, const photic_lut_config *l
   a.inv.early_exit = cfg->early_exit_per_scene * (double)(float)1;
   a.source = d_source;
   a.chain_stats = d_chain_stats;
+  a.emp = d_empirical;
+  a.emp_nodata = empirical_nodata;
 
   // the order: keys, mask, stable sort (model/samodel.c:701-819)
   LutKeyArgs ka;
@@ -520,6 +523,7 @@ int photic_lut_invert_batch(const photic_config *cfg, const photic_lut_config *l
   for (int k = 0; k < 3; k++) ka.noise[k] = noise ? lut->rrs_noise[k + 1] : 0.0;
   ka.out = *out;
   ka.source = d_source;
+  ka.emp = d_empirical;
   int64_t *order = d_order;
   cudaError_t e = cudaSuccess;
   if (!order) {
@@ -2283,34 +2287,34 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
       rc = photic_region_fit_batch(&cfg, d_rrs, nscenes, th, nrows, ncols, regions ? 2 : 1,
                                    n_bottoms, d_emp, &o, 0);
     } else if (nscenes == 1) {
-      if (!h_emp.empty()) {
-        cudaMalloc((void **)&d_emp, npix * sizeof(double));
-        cudaMalloc((void **)&d_seeds, npix * 6 * sizeof(double));
-        cudaMemcpy(d_emp, h_emp.data(), npix * sizeof(double), cudaMemcpyHostToDevice);
-        EmpSeedArgs ea;
-        memset(&ea, 0, sizeof ea);
-        make_fit(cfg, ea.fp);
-        make_scene(cfg, cfg.theta_sun_deg, ea.sc);
-        ea.rrs = d_rrs;
-        ea.h = d_emp;
-        ea.npix = npix;
-        ea.seeds = d_seeds;
-        launch_empirical_seeds(ea, 0);
-        rc = photic_invert_batch(&cfg, d_rrs, npix, nb, 1, d_seeds, &o, 0);
-      } else {
-        // the reference's product path: the pixel loop with its dynamic
-        // lookup table (LUT 1, :649-1215), the sorted pixels cut into
-        // chains -- PHOTIC_LUT_CHAINS of them if set (1: the reference on
-        // one thread), else eight per resident lane
-        photic_lut_config lc;
-        photic_lut_config_default(&lc);
-        const char *ch = getenv("PHOTIC_LUT_CHAINS");
-        if (ch && *ch) lc.n_chains = atoll(ch);
-        lc.use_noise = 1;
-        for (int b = 0; b < nb && b < PHOTIC_MAX_BANDS; b++) lc.rrs_noise[b] = s0.R_sigma[b];
-        rc = photic_lut_invert_batch(&cfg, &lc, d_rrs, npix, &o, nullptr, nullptr, nullptr,
-                                     nullptr, nullptr, 0);
+      // the reference's product path: the pixel loop with its dynamic
+      // lookup table (LUT 1, :649-1215), ordered by the spectral index or
+      // by the empirical depths when given (:702-710), the sorted pixels
+      // cut into chains -- PHOTIC_LUT_CHAINS of them if set (1: the
+      // reference on one thread), else eight per resident lane
+      photic_lut_config lc;
+      photic_lut_config_default(&lc);
+      const char *ch = getenv("PHOTIC_LUT_CHAINS");
+      if (ch && *ch) lc.n_chains = atoll(ch);
+      lc.use_noise = 1;
+      for (int b = 0; b < nb && b < PHOTIC_MAX_BANDS; b++) lc.rrs_noise[b] = s0.R_sigma[b];
+      float *d_raw = nullptr;
+      if (empirical_depth_present) {
+        std::vector<float> raw((size_t)npix);
+        for (int i = 0; i < nrows; i++)
+          for (int j = 0; j < ncols; j++) raw[(size_t)i * ncols + j] = empirical_depths.array[i][j];
+        if (cudaMalloc((void **)&d_raw, npix * sizeof(float)) == cudaSuccess)
+          cudaMemcpy(d_raw, raw.data(), npix * sizeof(float), cudaMemcpyHostToDevice);
       }
+      if (empirical_depth_present && !d_raw) {
+        rc = fail(PHOTIC_ERR_NOMEM, "samodel: empirical depth grid");
+      } else {
+        rc = photic_lut_invert_batch(&cfg, &lc, d_rrs, npix, d_raw,
+                                     empirical_depth_present ? empirical_depths.nodata_value : 0.0f,
+                                     &o, nullptr, nullptr, nullptr, nullptr, nullptr, 0);
+        if (rc == PHOTIC_OK) rc = photic_sync(0);
+      }
+      cudaFree(d_raw);
     } else {
       std::vector<int32_t> offs((size_t)npix + 1);
       std::vector<double> th((size_t)nobs);

@@ -55,6 +55,7 @@ struct LutKeyArgs {
   float nodata;
   int32_t use_noise;   // order by index x spectral angle to noise[] (blue, green, red)
   double noise[3];
+  const float *emp;    // optional [npix] empirical depths: the key itself
   photic_outputs out;  // masked pixels' outputs are written here
   int64_t *source;     // optional [npix]: -2 for masked pixels
   float *keys;         // scratch [npix]
@@ -70,6 +71,8 @@ struct LutArgs {
   int64_t *source;        // optional [npix]: -1 fitted, else the pixel that served it
   double *chain_stats;    // optional [n_chains][4]: served, fitted, match, entry
   unsigned long long *queue;  // chain counter
+  const float *emp;       // optional [npix] empirical depths, emp_nodata for none
+  float emp_nodata;
 };
 cudaError_t lut_order(LutKeyArgs ka, int64_t *order, int64_t *n_shallow, cudaStream_t s);
 cudaError_t launch_lut(const LutArgs &a, int grid, cudaStream_t s);

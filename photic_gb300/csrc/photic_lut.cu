@@ -85,6 +85,10 @@ __global__ void lut_key_kernel(LutKeyArgs a) {
     write_masked(a.out, p);
     if (a.source) a.source[p] = -2;
   }
+  if (a.emp) {  // the empirical depth itself (:708-710)
+    a.keys[p] = a.emp[p];
+    return;
+  }
   // :711-745 -- float sums, squares and root in double, stored as float
   float bs = 0.0f, gs = 0.0f, rs = 0.0f;
   if (a.n_bands > 1 && !ref_approx_eq(r[1], a.nodata, 1.0e-6f)) bs = __fadd_rn(bs, r[1]);
@@ -398,9 +402,20 @@ __global__ void __launch_bounds__(kLutBlock) lut_kernel(const __grid_constant__ 
 #pragma unroll
             for (int i = 0; i < kN; i++) best[i * BS] = 0.0;
             P::template cold_start<NB>(ia, px, m.start, m.step);
-            hot_fit = S.s[CS_HOT][t];
+            // the pixel's empirical depth (:955-979): its single start, hot
+            // or cold; a pixel without one is fitted cold
+            bool emp_present = false;
+            double h_emp = 0.0;
+            if (args.emp) {
+              const float e = args.emp[p];
+              if (!ref_approx_eq(e, args.emp_nodata, 1.0e-6f)) {
+                emp_present = true;
+                h_emp = (double)e > -1.0 ? 1.0 : fabs((double)e);
+              }
+            }
+            hot_fit = S.s[CS_HOT][t] && (args.emp == nullptr || emp_present);
             if (hot_fit) {  // :2234-2241, 2285-2305
-              const double h = S.d[CD_DPREV][t];
+              const double h = emp_present ? h_emp : S.d[CD_DPREV][t];
               m.start[0] = h;
               m.step[0] = P::h_step(h);
               m.start[3] = S.d[CD_PREV0][t];
@@ -408,6 +423,10 @@ __global__ void __launch_bounds__(kLutBlock) lut_kernel(const __grid_constant__ 
               m.start[5] = S.d[CD_PREV2][t];
 #pragma unroll
               for (int i = 3; i < 6; i++) m.step[i] = __dmul_rn(2.0, m.start[i]);
+              n_starts = 1;
+            } else if (emp_present) {  // :2221-2223
+              m.start[0] = h_emp;
+              m.step[0] = P::h_step(h_emp);
               n_starts = 1;
             } else {
               m.start[0] = P::hstart(ia, 0);

@@ -24,7 +24,9 @@
  *        grid     : samodel() over an nrows x ncols grid (grid2: with
  *                   n_spatial = 2, 3 x 3 regions per pixel; grid3: 3 x 3
  *                   regions and n_bottoms = 3, the reference's default call;
- *                   grid13: pixels alone, n_bottoms = 3); OUT = float
+ *                   grid13: pixels alone, n_bottoms = 3; gride: pixels
+ *                   alone with the empirical depth grid taken from params[0]
+ *                   as float, nodata -9999); OUT = float
  *                   [10][nrows][ncols] (depth, depth sigma, model error,
  *                   albedo, sand, seagrass, coral, K_min, type, IOD)
  *        optimise3: samodel_optimise with n_bottoms = 3 (sand, seagrass,
@@ -171,7 +173,7 @@ int main(int argc, char **argv) {
   if (!o) return 1;
 
   if (!strcmp(mode, "grid") || !strcmp(mode, "grid2") || !strcmp(mode, "grid3") ||
-      !strcmp(mode, "grid13")) {
+      !strcmp(mode, "grid13") || !strcmp(mode, "gride")) {
     const int n_spatial = (!strcmp(mode, "grid2") || !strcmp(mode, "grid3")) ? 2 : 0;
     const int n_bottoms = (!strcmp(mode, "grid3") || !strcmp(mode, "grid13")) ? 3 : 1;
     if (nrows * ncols != npix) return 1;
@@ -195,11 +197,20 @@ int main(int argc, char **argv) {
     }
     photic_geogrid none;
     memset(&none, 0, sizeof none);
+    const int emp = !strcmp(mode, "gride");
+    if (emp) {
+      none.nrows = nrows;
+      none.ncols = ncols;
+      none.nodata_value = -9999.0f;
+      none.array = fgrid(nrows, ncols);
+      for (int i = 0; i < nrows; i++)
+        for (int j = 0; j < ncols; j++) none.array[i][j] = (float)params[((size_t)i * ncols + j) * 6];
+    }
     float **g[10];
     for (int k = 0; k < 10; k++) g[k] = fgrid(nrows, ncols);
     int idx = 0;
-    samodel(sc, grids, &idx, 1, 0, none, 1, n_spatial, n_bottoms, g[0], g[1], g[2], g[3], g[4], g[5],
-            g[6], g[7], g[8], g[9], 0.0f, 0, 0);
+    samodel(sc, grids, &idx, 1, emp, none, 1, n_spatial, n_bottoms, g[0], g[1], g[2], g[3], g[4],
+            g[5], g[6], g[7], g[8], g[9], 0.0f, 0, 0);
     if (photic_last_error()[0]) {
       fprintf(stderr, "samodel: %s\n", photic_last_error());
       return 4;

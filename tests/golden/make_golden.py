@@ -123,9 +123,10 @@ def bottoms():
 
 def lut():
     """The reference's own samodel() with its dynamic lookup table (LUT 1),
-    one thread, reference tolerances, on two spatially coherent scenes: 64 x 64
-    ordered by the spectral index alone, and 48 x 48 with a noise spectrum
-    (R_sigma) so that the spectral angle enters the order.  Kept grids:
+    one thread, reference tolerances, on three spatially coherent scenes:
+    64 x 64 ordered by the spectral index alone, 48 x 48 with a noise
+    spectrum (R_sigma) so that the spectral angle enters the order, and
+    48 x 48 with an empirical depth grid.  Kept grids:
     depth (negative below the datum), model error, bottom albedo, K_min and
     index of optical depth, as samodel() leaves them."""
     keep = [0, 2, 3, 7, 9]
@@ -138,6 +139,18 @@ def lut():
         out[f"{name}_ref"] = g[keep]
         if rs is not None:
             out[f"{name}_r_sigma"] = rs
+    # an empirical depth grid (negative below the datum, 20 % nodata, some
+    # shallower than 1 m): it orders the pixels and starts their fits
+    n = 48
+    rrs, truth = O.generate_field(20261313, n, n, mask_frac=0.1, noise_sigma=1e-4)
+    rng = np.random.default_rng(9)
+    emp = (-truth[:, 0] * rng.uniform(0.8, 1.2, n * n)).astype(np.float32)
+    emp[rng.random(n * n) < 0.2] = -9999.0
+    emp[rng.random(n * n) < 0.05] = -0.5
+    grid = rrs.reshape(n, n, 4)
+    out["emp_grid"] = grid
+    out["emp_empirical"] = emp.reshape(n, n)
+    out["emp_ref"] = O.reference_samodel_grid(grid, empirical=emp.reshape(n, n))[keep]
     np.savez_compressed(os.path.join(OUT, "lut.npz"), grids=np.array(keep), **out)
 
 

@@ -18,6 +18,8 @@ import numpy as np
 import pytest
 import torch
 
+from tests.test_lut_oracle import fixture_case
+
 pytestmark = pytest.mark.gpu
 
 NTHREADS = os.cpu_count() or 1
@@ -27,9 +29,10 @@ def _ref_cfg(gpu):
     return gpu.Config.reference_default()
 
 
-def _run(gpu, rrs, n_chains, rrs_noise=None):
+def _run(gpu, rrs, n_chains, rrs_noise=None, empirical=None):
+    em = None if empirical is None else torch.tensor(empirical, device="cuda")
     out = gpu.lut_invert(torch.tensor(rrs, device="cuda"), _ref_cfg(gpu), n_chains=n_chains,
-                         rrs_noise=rrs_noise)
+                         rrs_noise=rrs_noise, empirical=em)
     gpu.sync()
     return {k: v.cpu().numpy() for k, v in out.items()}
 
@@ -56,31 +59,27 @@ def test_field_generator_matches_oracle(gpu, port):
     np.testing.assert_allclose(truth.cpu().numpy(), wt, rtol=1e-12)
 
 
-@pytest.mark.parametrize("case", ["plain", "noise"])
+@pytest.mark.parametrize("case", ["plain", "noise", "emp"])
 def test_order_matches_oracle(gpu, port, golden_dir, case):
     """The spectral-index order, with the reference's merge tree where NaN
-    keys (masked pixels under the spectral angle) occur, bit for bit."""
-    g = np.load(os.path.join(golden_dir, "lut.npz"))
-    n = g[f"{case}_grid"].shape[0]
-    rrs = g[f"{case}_grid"].reshape(n * n, 4)
-    rs = g[f"{case}_r_sigma"] if f"{case}_r_sigma" in g else None
-    o = _run(gpu, rrs, 1, rs)
-    ref, src, order, _ = port.lut_invert(rrs, rrs_noise=rs, n_chains=1, nthreads=1)
+    keys (masked pixels under the spectral angle) occur, or the empirical
+    depths' order, bit for bit."""
+    rrs, rs, em, _, _ = fixture_case(golden_dir, case)
+    o = _run(gpu, rrs, 1, rs, em)
+    ref, src, order, _ = port.lut_invert(rrs, rrs_noise=rs, empirical=em, n_chains=1,
+                                         nthreads=1)
     np.testing.assert_array_equal(o["order"], order)
     np.testing.assert_array_equal(o["source"] == -2, src == -2)
     np.testing.assert_array_equal(o["status"] & 0xFF, ref[:, 9].astype(np.int32))
 
 
-@pytest.mark.parametrize("case", ["plain", "noise"])
+@pytest.mark.parametrize("case", ["plain", "noise", "emp"])
 def test_one_chain_against_reference(gpu, port, golden_dir, case):
     """One chain is the reference's samodel() on one thread: its fixture."""
-    g = np.load(os.path.join(golden_dir, "lut.npz"))
-    n = g[f"{case}_grid"].shape[0]
-    rrs = g[f"{case}_grid"].reshape(n * n, 4)
-    rs = g[f"{case}_r_sigma"] if f"{case}_r_sigma" in g else None
-    o = _run(gpu, rrs, 1, rs)
-    ref_depth = -g[f"{case}_ref"][0].reshape(-1)
-    _, src_o, _, _ = port.lut_invert(rrs, rrs_noise=rs, n_chains=1, nthreads=1)
+    rrs, rs, em, ref_grids, _ = fixture_case(golden_dir, case)
+    o = _run(gpu, rrs, 1, rs, em)
+    ref_depth = -ref_grids[0].reshape(-1)
+    _, src_o, _, _ = port.lut_invert(rrs, rrs_noise=rs, empirical=em, n_chains=1, nthreads=1)
     fit = (o["status"] & 0xFF) == 0
     d, sg, sr = _stats(f"one chain vs reference ({case})", o["depth"], ref_depth, o["source"],
                        src_o, fit)
@@ -128,7 +127,7 @@ def test_served_pixels_carry_their_source(gpu, port):
 
 
 def test_default_chains(gpu, port):
-    """n_chains = 0: one chain per resident lane of the kernel."""
+    """n_chains = 0: eight chains per resident lane of the kernel."""
     n = 256
     rrs, _ = gpu.generate_field(n, n, seed=555)
     out = gpu.lut_invert(rrs, _ref_cfg(gpu))

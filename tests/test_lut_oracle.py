@@ -29,20 +29,28 @@ def _compare_grids(out, ref_grids, kept, label):
         assert same.all(), (label, int(k), int((~same).sum()))
 
 
-@pytest.mark.parametrize("case", ["plain", "noise"])
-def test_oracle_lut_matches_reference_fixture(port, golden_dir, case):
+def fixture_case(golden_dir, case):
+    """(spectra [npix, 4], noise spectrum or None, empirical depths or None,
+    the reference's grids, kept grid indices) of one case of lut.npz."""
     g = np.load(os.path.join(golden_dir, "lut.npz"))
     grid = g[f"{case}_grid"]
     n = grid.shape[0]
     rs = g[f"{case}_r_sigma"] if f"{case}_r_sigma" in g else None
-    out, src, order, stats = port.lut_invert(grid.reshape(n * n, 4), rrs_noise=rs, n_chains=1,
+    em = g[f"{case}_empirical"].reshape(-1) if f"{case}_empirical" in g else None
+    return grid.reshape(n * n, 4), rs, em, g[f"{case}_ref"], g["grids"]
+
+
+@pytest.mark.parametrize("case", ["plain", "noise", "emp"])
+def test_oracle_lut_matches_reference_fixture(port, golden_dir, case):
+    rrs, rs, em, ref_grids, kept = fixture_case(golden_dir, case)
+    out, src, order, stats = port.lut_invert(rrs, rrs_noise=rs, empirical=em, n_chains=1,
                                              nthreads=1)
-    _compare_grids(out, g[f"{case}_ref"], g["grids"], case)
+    _compare_grids(out, ref_grids, kept, case)
     fit = out[:, 9] == 0
     served = np.mean(src[fit] >= 0)
     print(f"{case}: {fit.sum()} shallow pixels, served from the table {served:.4f}, "
           f"final thresholds {stats[0, 2]:.3f}/{stats[0, 3]:.3f}")
-    assert served > 0.02
+    assert served > 0.01
     # served pixels carry their source's fit
     s = np.where(src >= 0)[0]
     np.testing.assert_array_equal(out[s, 0], out[src[s], 0])
