@@ -15,6 +15,8 @@
 #pragma once
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "photic_fastmath.cuh"
 #include "photic_params.h"
 
@@ -99,14 +101,26 @@ struct CostDetailsF64 {
   double Rm[kMaxBands];
 };
 
+// What a plain evaluation can keep, besides its cost, so that the products
+// at the kept optimum (model/samodel.c:2413, 1994-2079) follow from the same
+// evaluation: the bands' bottom and total subsurface reflectances and the
+// modelled Rrs, the Rrs error, K minimum and albedo.  NoKeep keeps nothing.
+struct NoKeep {};
+template <int NB>
+struct BandKeep {
+  double rrs_B[NB], rrs[NB], Rm[NB];
+  double E, K_min, qB;
+};
+
 // Cost of x = (H, 100B, q, 100P, 100G, 100X) for one scene, one region,
 // one bottom type: samodel_error (model/samodel.c:2432-2759) over
 // samodel_Rrs (model/samodel.c:2846-2949).  With one region the depth and
 // bottom continuity terms are identically zero and SAM is compiled out.
-template <bool kDetails, int NB>
+template <bool kDetails, int NB, class Keep = NoKeep>
 __device__ __forceinline__ double cost_f64(const FitParams &fp, const SceneConsts &sc,
                                            const PixelF64<NB> &px, const double *x,
-                                           CostDetailsF64 *det) {
+                                           CostDetailsF64 *det, Keep *keep = nullptr) {
+  constexpr bool kKeep = !std::is_same<Keep, NoKeep>::value;
   const int nb = fp.n_bands;
   const double H = fabs(x[0]);
   const double B = 0.01 * fabs(x[1]);
@@ -146,6 +160,11 @@ __device__ __forceinline__ double cost_f64(const FitParams &fp, const SceneConst
         iod = iod + rrs_B / rrs;
         det->Rm[b] = Rm;
       }
+      if constexpr (kKeep) {
+        keep->rrs_B[b] = rrs_B;
+        keep->rrs[b] = rrs;
+        keep->Rm[b] = Rm;
+      }
     }
   }
   const double E = 100.0 * sqrt(fm::div_count(err, nb)) / px.mean;
@@ -156,6 +175,11 @@ __device__ __forceinline__ double cost_f64(const FitParams &fp, const SceneConst
   }
   double model = 80.0 * E + 15.0 * Ke;
   model = fm::div_by(model, 120.0, fm::kInv120);
+  if constexpr (kKeep) {
+    keep->E = E;
+    keep->K_min = K_min;
+    keep->qB = qB;
+  }
   if (kDetails) {
     det->rrs_error = E;
     det->model_error = model;

@@ -51,6 +51,7 @@ struct PixelF32 {
 };
 
 struct PrecF32 : PrecF64 {
+  static constexpr bool kFused = false;  // its products come from an FP64 evaluation
   template <int NB>
   using Pixel = PixelF32<NB>;
   template <int NB>
@@ -139,6 +140,7 @@ struct PrecF32 : PrecF64 {
 };
 
 struct PrecDF {
+  static constexpr bool kFused = false;
   using T = df64;
   template <int NB>
   using Pixel = PixelDF<NB>;
@@ -315,9 +317,19 @@ __global__ void __launch_bounds__(BS) invert_kernel(const __grid_constant__ Inve
 
     // ---- one cost evaluation per lane, then the bookkeeping --------------
     if (has) {
-      if (m.phase == PH_FINAL) {
-        typename P::Details det;
-        P::template details<NB>(args, px, m.x, det);
+      const bool fin = m.phase == PH_FINAL;
+      typename P::Details det;
+      T y = P::zero();
+      if constexpr (P::kFused) {
+        // the kept optimum is evaluated together with the other lanes' points
+        typename P::template Keep<NB> keep;
+        y = P::template cost_keep<NB>(args, px, m.x, keep);
+        if (fin) P::template details_from_keep<NB>(args, keep, y, det);
+      } else {
+        if (fin) P::template details<NB>(args, px, m.x, det);
+        else y = P::template cost<NB>(args, px, m.x);
+      }
+      if (fin) {
         const int64_t p = pixel;
         const double H = fabs(P::to_double(m.x[0]));
         if (o.depth) o.depth[p] = (float)H;
@@ -339,7 +351,6 @@ __global__ void __launch_bounds__(BS) invert_kernel(const __grid_constant__ Inve
                         (kept_start << 16);
         has = false;
       } else {
-        const T y = P::template cost<NB>(args, px, m.x);
         if (++guard > guard_cap) {
           // Defensive cap: each nelmin call is bounded by kcount, so
           // reaching this means a defect; flag it instead of spinning.

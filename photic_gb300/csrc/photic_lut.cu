@@ -295,6 +295,7 @@ __global__ void __launch_bounds__(kLutBlock) lut_kernel(const __grid_constant__ 
   int64_t pixel = -1;
   int32_t start_k = 0, n_starts = 0, total = 0, kept_evals = 0, kept_start = 0, kept_fault = 0;
   int32_t guard = 0, hot_fit = 0;
+  int64_t pending = -1;  // a pixel of this lane's chain waiting for its fit
   double lowest = 0.0;
   bool has = false;
   const int32_t guard_cap = (fp.n_hstarts + 1) * (fp.kcount + 8 * kN + 16);
@@ -389,53 +390,9 @@ __global__ void __launch_bounds__(kLutBlock) lut_kernel(const __grid_constant__ 
         // (an empty table with a threshold above 1e4 would make the
         // reference serve an unused slot; that pixel is fitted here)
         if (bestd > S.d[CD_MATCH][t] || n_in == 0) {
-          // a fit (:1008-1063): set up on the owner lane
-          if (lane == L) {
-            float rf[NB];
-#pragma unroll
-            for (int b = 0; b < NB; b++) rf[b] = b < fp.n_bands ? __ldg(r + b) : 0.0f;
-            P::template setup<NB>(ia, rf, px);
-            pixel = p;
-            total = kept_evals = kept_start = kept_fault = guard = 0;
-            lowest = 1.0e4;
-            start_k = 0;
-#pragma unroll
-            for (int i = 0; i < kN; i++) best[i * BS] = 0.0;
-            P::template cold_start<NB>(ia, px, m.start, m.step);
-            // the pixel's empirical depth (:955-979): its single start, hot
-            // or cold; a pixel without one is fitted cold
-            bool emp_present = false;
-            double h_emp = 0.0;
-            if (args.emp) {
-              const float e = args.emp[p];
-              if (!ref_approx_eq(e, args.emp_nodata, 1.0e-6f)) {
-                emp_present = true;
-                h_emp = (double)e > -1.0 ? 1.0 : fabs((double)e);
-              }
-            }
-            hot_fit = S.s[CS_HOT][t] && (args.emp == nullptr || emp_present);
-            if (hot_fit) {  // :2234-2241, 2285-2305
-              const double h = emp_present ? h_emp : S.d[CD_DPREV][t];
-              m.start[0] = h;
-              m.step[0] = P::h_step(h);
-              m.start[3] = S.d[CD_PREV0][t];
-              m.start[4] = S.d[CD_PREV1][t];
-              m.start[5] = S.d[CD_PREV2][t];
-#pragma unroll
-              for (int i = 3; i < 6; i++) m.step[i] = __dmul_rn(2.0, m.start[i]);
-              n_starts = 1;
-            } else if (emp_present) {  // :2221-2223
-              m.start[0] = h_emp;
-              m.step[0] = P::h_step(h_emp);
-              n_starts = 1;
-            } else {
-              m.start[0] = P::hstart(ia, 0);
-              m.step[0] = P::h_step(m.start[0]);
-              n_starts = fp.n_hstarts;
-            }
-            m.begin(var_limit, fp.konvge, fp.kcount);
-            has = true;
-          }
+          // a fit (:1008-1063): set up below, every such lane of the warp
+          // at once
+          if (lane == L) pending = p;
           break;
         }
         // served (:1066-1073): the entry's outputs, lane k copying field k
@@ -477,13 +434,67 @@ __global__ void __launch_bounds__(kLutBlock) lut_kernel(const __grid_constant__ 
       }
       need &= ~(1u << L);
     }
+    if (pending >= 0) {
+      const int64_t p = pending;
+      const float *r = ia.rrs + p * fp.n_bands;
+      pending = -1;
+      float rf[NB];
+#pragma unroll
+      for (int b = 0; b < NB; b++) rf[b] = b < fp.n_bands ? __ldg(r + b) : 0.0f;
+      P::template setup<NB>(ia, rf, px);
+      pixel = p;
+      total = kept_evals = kept_start = kept_fault = guard = 0;
+      lowest = 1.0e4;
+      start_k = 0;
+#pragma unroll
+      for (int i = 0; i < kN; i++) best[i * BS] = 0.0;
+      P::template cold_start<NB>(ia, px, m.start, m.step);
+      // the pixel's empirical depth (:955-979): its single start, hot
+      // or cold; a pixel without one is fitted cold
+      bool emp_present = false;
+      double h_emp = 0.0;
+      if (args.emp) {
+        const float e = args.emp[p];
+        if (!ref_approx_eq(e, args.emp_nodata, 1.0e-6f)) {
+          emp_present = true;
+          h_emp = (double)e > -1.0 ? 1.0 : fabs((double)e);
+        }
+      }
+      hot_fit = S.s[CS_HOT][tid] && (args.emp == nullptr || emp_present);
+      if (hot_fit) {  // :2234-2241, 2285-2305
+        const double h = emp_present ? h_emp : S.d[CD_DPREV][tid];
+        m.start[0] = h;
+        m.step[0] = P::h_step(h);
+        m.start[3] = S.d[CD_PREV0][tid];
+        m.start[4] = S.d[CD_PREV1][tid];
+        m.start[5] = S.d[CD_PREV2][tid];
+#pragma unroll
+        for (int i = 3; i < 6; i++) m.step[i] = __dmul_rn(2.0, m.start[i]);
+        n_starts = 1;
+      } else if (emp_present) {  // :2221-2223
+        m.start[0] = h_emp;
+        m.step[0] = P::h_step(h_emp);
+        n_starts = 1;
+      } else {
+        m.start[0] = P::hstart(ia, 0);
+        m.step[0] = P::h_step(m.start[0]);
+        n_starts = fp.n_hstarts;
+      }
+      m.begin(var_limit, fp.konvge, fp.kcount);
+      has = true;
+    }
     if (!__any_sync(kFull, has)) break;
 
     // ---- one cost evaluation per lane, then the bookkeeping --------------
     if (has) {
+      // one evaluation for every lane; at the kept optimum its kept band
+      // values give the products (the final point is evaluated together
+      // with the other lanes' trial points)
+      BandKeep<NB> keep;
+      const double y = P::template cost_keep<NB>(ia, px, m.x, keep);
       if (m.phase == PH_FINAL) {
-        CostDetailsF64 det;
-        cost_f64<true, NB>(fp, ia.sc, px, m.x, &det);
+        typename P::Details det;
+        P::template details_from_keep<NB>(ia, keep, y, det);
         const int64_t p = pixel;
         const double H = fabs(m.x[0]);
         if (o.depth) o.depth[p] = (float)H;
@@ -523,9 +534,9 @@ __global__ void __launch_bounds__(kLutBlock) lut_kernel(const __grid_constant__ 
           double *R = args.ring + (size_t)c * 8 * cap;
           R[RG_DEPTH * cap + slot] = H;
           R[RG_KMIN * cap + slot] = det.K_min;
-          R[RG_RM1 * cap + slot] = fp.n_bands > 1 ? det.Rm[1] : 0.0;
-          R[RG_RM2 * cap + slot] = fp.n_bands > 2 ? det.Rm[2] : 0.0;
-          R[RG_RM3 * cap + slot] = fp.n_bands > 3 ? det.Rm[3] : 0.0;
+          R[RG_RM1 * cap + slot] = fp.n_bands > 1 ? keep.Rm[1] : 0.0;
+          R[RG_RM2 * cap + slot] = fp.n_bands > 2 ? keep.Rm[2] : 0.0;
+          R[RG_RM3 * cap + slot] = fp.n_bands > 3 ? keep.Rm[3] : 0.0;
           R[RG_PREV0 * cap + slot] = fabs(m.x[3]);
           R[RG_PREV1 * cap + slot] = fabs(m.x[4]);
           R[RG_PREV2 * cap + slot] = fabs(m.x[5]);
@@ -536,7 +547,6 @@ __global__ void __launch_bounds__(kLutBlock) lut_kernel(const __grid_constant__ 
         chain_tail(S, tid, me);
         has = false;
       } else {
-        const double y = P::template cost<NB>(ia, px, m.x);
         if (++guard > guard_cap) {
           // Defensive cap: each nelmin call is bounded by kcount, so
           // reaching this means a defect; flag it and drop the chain.

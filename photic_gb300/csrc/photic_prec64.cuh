@@ -61,6 +61,33 @@ struct PrecF64 {
   static __device__ __forceinline__ T cost(const InvertArgs &a, const Pixel<NB> &px, const T *x) {
     return cost_f64<false, NB>(a.fp, a.sc, px, x, nullptr);
   }
+  // One evaluation serves the Nelder-Mead and, at the kept optimum, the
+  // products: the kernel evaluates the final point with the other lanes'
+  // trial points instead of in a second, divergent cost evaluation.
+  static constexpr bool kFused = true;
+  template <int NB>
+  using Keep = BandKeep<NB>;
+  template <int NB>
+  static __device__ __forceinline__ T cost_keep(const InvertArgs &a, const Pixel<NB> &px,
+                                                const T *x, Keep<NB> &k) {
+    return cost_f64<false, NB, Keep<NB>>(a.fp, a.sc, px, x, nullptr, &k);
+  }
+  // The products of cost_f64<true> (photic_fp64.cuh) from a kept evaluation,
+  // the index of optical depth summed in band order.
+  template <int NB>
+  static __device__ __forceinline__ void details_from_keep(const InvertArgs &a,
+                                                           const Keep<NB> &k, T model,
+                                                           Details &d) {
+    double iod = 0.0;
+#pragma unroll
+    for (int b = 0; b < NB; b++)
+      if (b < a.fp.n_bands) iod = iod + k.rrs_B[b] / k.rrs[b];
+    d.rrs_error = k.E;
+    d.model_error = model;
+    d.bottom_albedo = k.qB;
+    d.K_min = k.K_min == 1.0e4 ? 0.0 : k.K_min;
+    d.iod = 100.0 * iod / (double)a.fp.n_bands;
+  }
   template <int NB>
   static __device__ __forceinline__ void details(const InvertArgs &a, const Pixel<NB> &px,
                                                  const T *x, Details &d) {
