@@ -142,3 +142,23 @@ def test_default_chains(gpu, port):
         __import__("ctypes").byref(_ref_cfg(gpu).to_c()))))
     print(f"default chains: {C} chains over {S} shallow pixels, served "
           f"{np.mean(src[fit] >= 0):.4f}")
+
+
+def test_eight_bands(gpu, port):
+    """The 8-band instantiation of the lookup-table kernel (bands 1..3 of an
+    OLCI-like set carry the spectral index and the difference)."""
+    wl8 = (412.5, 442.5, 490.0, 510.0, 560.0, 620.0, 665.0, 708.75)
+    n, C = 48, 4
+    rrs, _ = port.generate_field(4848, n, n, wl=wl8)
+    cfg = gpu.Config.reference_default(wavelengths=wl8)
+    out = gpu.lut_invert(torch.tensor(rrs, device="cuda"), cfg, n_chains=C)
+    gpu.sync()
+    o = {k: v.cpu().numpy() for k, v in out.items()}
+    ref, src, order, _ = port.lut_invert(rrs, wl=wl8, n_chains=C, nthreads=NTHREADS)
+    np.testing.assert_array_equal(o["order"], order)
+    fit = ref[:, 9] == 0
+    d, sg, sr = _stats("8 bands, 4 chains vs oracle", o["depth_f64"], ref[:, 0], o["source"], src,
+                       fit)
+    assert np.median(d) <= 0.01
+    assert np.mean(d == 0) >= 0.5
+    assert abs(sg - sr) <= 0.05
