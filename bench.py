@@ -1031,15 +1031,15 @@ FLOPS_PER_EVAL_F64 = 4 * 43 + 9
 # FP64 thread instructions per cost evaluation of the seeded headline fit
 # (cost + Nelder-Mead bookkeeping): 160.6 G over 307.75 M evaluations in the
 # ncu capture of invert_kernel<PrecF64, 4, 256> on a 1024 x 1024 tile
-# (profiles/invert_kernel_warm_1024x1024_full.md); issued as 779 lane-slots
-# of FP64 warp instructions (67 % of lanes live).
+# (profiles/invert_kernel_warm_1024x1024_full.md); issued as 741 lane-slots
+# of FP64 warp instructions (70 % of lanes live).
 FP64_INST_PER_EVAL = 522
 
 # dram__bytes_read.sum + dram__bytes_write.sum of the same capture
-# (76.49 MB + 5.50 MB over 1 048 576 seeded pixels), per pixel: the spectra
+# (76.75 MB + 5.47 MB over 1 048 576 seeded pixels), per pixel: the spectra
 # (16 B) and seed vector (48 B) read, depth, status and evaluation count
 # (16 B) written -- the algorithm's 80 B, no re-reads.
-TRAFFIC_BYTES_PER_PIXEL = (76.485888e6 + 5.499904e6) / 1048576
+TRAFFIC_BYTES_PER_PIXEL = (76.754688e6 + 5.472256e6) / 1048576
 TRAFFIC_NOTE = ("DRAM bytes per launch scaled by pixels from an ncu capture of this kernel on a "
                 "1048576-pixel seeded tile (78.2 B/pixel, against the 80 B/pixel the algorithm "
                 "moves: 16 B spectra + 48 B seed read, 16 B written)")
