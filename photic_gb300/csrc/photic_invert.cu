@@ -204,10 +204,13 @@ __global__ void __launch_bounds__(BS) invert_kernel(const __grid_constant__ Inve
   T *sv = reinterpret_cast<T *>(smem_raw);          // [(N+1)*N][BS]
   T *sf = sv + (kN + 1) * kN * BS;                  // [N+1][BS]
   T *sbest = sf + (kN + 1) * BS;                    // [N][BS]
-  float *schunk = reinterpret_cast<float *>(sbest + kN * BS);  // [BS/32][32][NB]
+  using Px = typename P::template Pixel<NB>;
+  Px *spx = reinterpret_cast<Px *>(sbest + kN * BS);  // [BS/32][32] set-ups of the chunk
+  float *schunk = reinterpret_cast<float *>(spx + BS);  // [BS/32][32][NB]
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   float *wchunk = schunk + warp * 32 * NB;
+  Px *wpx = spx + warp * 32;
   const unsigned lt_mask = (1u << lane) - 1u;
 
   NmLane<kN, P, BS> m;
@@ -259,6 +262,14 @@ __global__ void __launch_bounds__(BS) invert_kernel(const __grid_constant__ Inve
                   b < fp.n_bands ? __ldg(args.rrs + p * args.pixel_stride + b * args.band_stride)
                                  : 0.0f;
           }
+          // every lane sets up one pixel of the chunk (interpolated Rrs,
+          // Y and (440/lambda)^Y, model/samodel.c:1783-1799, 2897-2902)
+          // with the whole warp, instead of each lane alone when it takes
+          // the pixel; a masked pixel's set-up is never used
+          float r[NB];
+#pragma unroll
+          for (int b = 0; b < NB; b++) r[b] = wchunk[lane * NB + b];
+          P::template setup<NB>(args, r, wpx[lane]);
         }
         __syncwarp();
       }
@@ -279,7 +290,7 @@ __global__ void __launch_bounds__(BS) invert_kernel(const __grid_constant__ Inve
         if (masked) {
           write_masked(o, p);
         } else {
-          P::template setup<NB>(args, r, px);
+          px = wpx[q - chunk_base];
           pixel = p;
           total = kept_evals = kept_start = kept_fault = guard = 0;
           lowest = P::from_double(1.0e4);
@@ -390,7 +401,7 @@ __global__ void __launch_bounds__(BS) invert_kernel(const __grid_constant__ Inve
 
 template <class P, int NB, int BS>
 cudaError_t launch_one(const InvertArgs &a, int grid, cudaStream_t s, int *occupancy) {
-  const size_t smem = invert_smem_bytes(BS, NB);
+  const size_t smem = invert_smem_bytes(BS, NB) + (size_t)BS * sizeof(typename P::template Pixel<NB>);
   auto k = invert_kernel<P, NB, BS>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -416,6 +427,8 @@ cudaError_t launch_prec(const InvertArgs &a, int block, int grid, cudaStream_t s
 
 }  // namespace
 
+// Shared memory of the simplex and the staged spectra; launch_one adds the
+// chunk's pixel set-ups, whose size depends on the precision policy.
 size_t invert_smem_bytes(int block, int nb) {
   // double and double-float both take 8 bytes per value
   return (size_t)block * 8 * ((kN + 1) * kN + (kN + 1) + kN) +
