@@ -94,3 +94,37 @@ def test_gemm_strides_outside_the_tile_are_refused(lib, lbo, sbo):
                                       None)
     assert rc == L.ERR_INVALID
     assert b"stride" in lib.photic_last_error()
+
+
+def test_lookup_table_arguments_are_checked(lib):
+    """photic_lut_invert_batch refuses what it cannot run before it touches
+    the device: no configuration, an empty table, a negative chain count,
+    and every precision but FP64; an empty batch is a no-op."""
+    from photic_gb300 import _lib as L
+    c = L.photic_config()
+    lib.photic_config_default(C.byref(c))
+    lc = L.photic_lut_config()
+    lib.photic_lut_config_default(C.byref(lc))
+    assert lc.n_lut == 16000 and lc.n_chains == 0 and lc.use_noise == 0
+    o = L.photic_outputs()
+    n_sh, n_ch = C.c_int64(7), C.c_int64(7)
+    dummy = C.c_void_p(16)  # never dereferenced: the checks come first
+
+    def call(cfg, lut, npix=4):
+        return lib.photic_lut_invert_batch(C.byref(cfg), lut, dummy, npix, None, 0.0,
+                                           C.byref(o), None, None, None, C.byref(n_sh),
+                                           C.byref(n_ch), None)
+
+    assert call(c, None) == L.ERR_INVALID
+    lc.n_lut = 0
+    assert call(c, C.byref(lc)) == L.ERR_INVALID
+    lc.n_lut, lc.n_chains = 16000, -1
+    assert call(c, C.byref(lc)) == L.ERR_INVALID
+    lc.n_chains = 0
+    for prec in (L.PREC_DF64, L.PREC_FP32, L.PREC_GUARDED):
+        c.precision = prec
+        assert call(c, C.byref(lc)) == L.ERR_UNSUPPORTED
+        assert b"FP64" in lib.photic_last_error()
+    c.precision = L.PREC_FP64
+    assert call(c, C.byref(lc), npix=0) == L.OK
+    assert n_sh.value == 0 and n_ch.value == 0
