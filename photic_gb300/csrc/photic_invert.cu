@@ -154,6 +154,7 @@ struct PrecDF {
   static __device__ __forceinline__ T mul(T a, T b) { return df_mul(a, b); }
   static __device__ __forceinline__ T mul2(T a) { return df64{2.0f * a.hi, 2.0f * a.lo}; }
   static __device__ __forceinline__ T half(T a) { return df64{0.5f * a.hi, 0.5f * a.lo}; }
+  static __device__ __forceinline__ T scale2(T a, float c) { return df64{c * a.hi, c * a.lo}; }
   static __device__ __forceinline__ T div_n(T a, int n) { return df_div_f(a, (float)n); }
   static __device__ __forceinline__ bool lt(T a, T b) { return df_lt(a, b); }
   static __device__ __forceinline__ bool le(T a, T b) { return df_le(a, b); }

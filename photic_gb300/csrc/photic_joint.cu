@@ -35,6 +35,7 @@ struct PrecJ {
   static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
   static __device__ __forceinline__ T mul2(T a) { return 2.0 * a; }
   static __device__ __forceinline__ T half(T a) { return a * 0.5; }
+  static __device__ __forceinline__ T scale2(T a, float c) { return a * (double)c; }
   static __device__ __forceinline__ T div_n(T a, int n) { return fm::div_by(a, (double)n, 1.0 / (double)n); }
   static __device__ __forceinline__ bool lt(T a, T b) { return a < b; }
   static __device__ __forceinline__ bool le(T a, T b) { return a <= b; }

@@ -32,6 +32,9 @@ enum NmPhase : int32_t {
   PH_FINAL,           // re-evaluation at the kept optimum
 };
 
+// The kind of the pending simplex point of an iteration.
+enum NmPoint : int32_t { PK_NONE = 0, PK_REFL, PK_EXPAND, PK_CONTRACT_IN, PK_CONTRACT_OUT };
+
 // Loops over the simplex: fully unrolled for the single-scene simplex
 // (n <= 8), so that the lane's vectors stay in registers, and rolled for the
 // temporal fit (n up to 33).  (An unroll count that depends on a template
@@ -57,7 +60,7 @@ struct NmLane {
   T cen[N], refl[N], trial[N], xmin[N], start[N], step[N];
   T ylo, fr, scale, var_limit;
   long long floor_lo;
-  int32_t phase, jj, hi, lo, icount, numres, ifault, countdown;
+  int32_t phase, jj, hi, lo, icount, numres, ifault, countdown, pk;
   int32_t kcount, konvge;
 
   __device__ __forceinline__ T &V(int j, int i) { return v[(j * N + i) * BS]; }
@@ -96,9 +99,10 @@ struct NmLane {
   // Vertex j: the start point moved by step[j] * scale along coordinate j
   // (model/asa047.c:181-194).
   __device__ __forceinline__ void make_vertex(int j) {
+    // one moved coordinate: computed once and placed, not once per slot
+    const T sj = P::add(pick(start, j), P::mul(pick(step, j), scale));
     nm_for<0, N, kU>([&](int i) {
-      T s = start[i];
-      if (i == j) s = P::add(start[i], P::mul(step[i], scale));
+      const T s = i == j ? sj : start[i];
       x[i] = s;
       V(j, i) = s;
     });
@@ -119,7 +123,8 @@ struct NmLane {
   }
 
   // Top of the inner loop (model/asa047.c:213-250): budget check, worst
-  // vertex, centroid of the others, reflection.  false: the loop ends.
+  // vertex, centroid of the others; the reflection is left pending (pk).
+  // false: the loop ends.
   __device__ __forceinline__ bool inner_top() {
     if (kcount <= icount) return false;
     T yhi = F(0);
@@ -137,12 +142,32 @@ struct NmLane {
       z = P::sub(z, V(hi, i));
       cen[i] = P::div_n(z, N);
     });
-    nm_for<0, N, kU>([&](int i) {
-      refl[i] = P::add(cen[i], P::sub(cen[i], V(hi, i)));
-      x[i] = refl[i];
-    });
+    pk = PK_REFL;
     phase = PH_REFLECT;
     return true;
+  }
+
+  // The pending point of the iteration, cen + c (a - b) with
+  //   reflection          a = cen,   b = worst, c = 1   (model/asa047.c:251)
+  //   expansion           a = refl,  b = cen,   c = 2   (:262)
+  //   contraction inside  a = worst, b = cen,   c = 1/2 (:318)
+  //   contraction outside a = refl,  b = cen,   c = 1/2 (:369)
+  // c is a power of two, so the product is exact and each point equals the
+  // reference's coordinate by coordinate (rcoeff = 1 multiplies exactly).
+  // Written once for every kind, the lanes of a warp that need a point this
+  // trip compute it together, whichever kind it is.
+  __device__ __forceinline__ void make_point() {
+    const bool r = pk == PK_REFL;
+    const float c = pk == PK_EXPAND ? 2.0f : (r ? 1.0f : 0.5f);
+    nm_for<0, N, kU>([&](int i) {
+      const T w = V(hi, i);
+      const T a = r ? cen[i] : (pk == PK_CONTRACT_IN ? w : refl[i]);
+      const T b = r ? w : cen[i];
+      const T p = P::add(cen[i], P::scale2(P::sub(a, b), c));
+      x[i] = p;
+      if (r) refl[i] = p;
+      else trial[i] = p;
+    });
   }
 
   __device__ __forceinline__ void replace_hi(const T (&p)[N], T y) {
@@ -178,10 +203,16 @@ struct NmLane {
   // Consume the cost y of x[] and advance to the next point.  Returns true
   // when the nelmin call has returned (xmin, F(lo), icount, numres, ifault
   // hold its results); the caller then starts another call or finishes.
+  //
+  // The bookkeeping after the cost is a fixed sequence of stages, each
+  // guarded by the lane's state, so that the lanes of a warp needing the
+  // same stage in a trip (the centroid, the pending point) run it together
+  // instead of along one path per phase.
   __device__ __forceinline__ bool step_machine(T y) {
     enum { CS_NONE = -1, CS_READY, CS_TOP, CS_ITER_END, CS_END_INNER, CS_PROBE_PLUS,
            CS_PROBE_END, CS_NM_DONE };
     int cs = CS_NONE;
+    pk = PK_NONE;
     switch (phase) {
       case PH_INIT_BASE:
         F(N) = y;
@@ -198,10 +229,7 @@ struct NmLane {
         fr = y;
         icount++;
         if (P::lt(fr, ylo)) {
-          nm_for<0, N, kU>([&](int i) {
-            trial[i] = P::add(cen[i], P::mul2(P::sub(refl[i], cen[i])));
-            x[i] = trial[i];
-          });
+          pk = PK_EXPAND;
           phase = PH_EXPAND;
         } else {
           int worse = 0;
@@ -210,16 +238,10 @@ struct NmLane {
             replace_hi(refl, fr);
             cs = CS_ITER_END;
           } else if (worse == 0) {
-            nm_for<0, N, kU>([&](int i) {
-              trial[i] = P::add(cen[i], P::half(P::sub(V(hi, i), cen[i])));
-              x[i] = trial[i];
-            });
+            pk = PK_CONTRACT_IN;
             phase = PH_CONTRACT_IN;
           } else {
-            nm_for<0, N, kU>([&](int i) {
-              trial[i] = P::add(cen[i], P::half(P::sub(refl[i], cen[i])));
-              x[i] = trial[i];
-            });
+            pk = PK_CONTRACT_OUT;
             phase = PH_CONTRACT_OUT;
           }
         }
@@ -296,59 +318,49 @@ struct NmLane {
       default:
         break;
     }
-    // Bookkeeping until the next point to evaluate.
-    while (cs != CS_NONE) {
-      switch (cs) {
-        case CS_READY:
-          find_lo();
-          cs = CS_TOP;
-          break;
-        case CS_TOP:
-          cs = inner_top() ? CS_NONE : CS_END_INNER;
-          break;
-        case CS_ITER_END:
-          cs = iteration_end() ? CS_END_INNER : CS_TOP;
-          break;
-        case CS_END_INNER:
-          nm_for<0, N, kU>([&](int i) { xmin[i] = V(lo, i); });
-          floor_lo = P::trunc10(F(lo));
-          if (kcount < icount) {
-            ifault = 2;
-            cs = CS_NM_DONE;
-          } else {
-            ifault = 0;
-            jj = 0;
-            cs = CS_PROBE_PLUS;
-          }
-          break;
-        case CS_PROBE_PLUS: {
-          const T del = P::eps_step(pick(step, jj));
-          put(xmin, jj, P::add(pick(xmin, jj), del));
-          nm_for<0, N, kU>([&](int i) { x[i] = xmin[i]; });
-          phase = PH_PROBE_PLUS;
-          cs = CS_NONE;
-          break;
-        }
-        case CS_PROBE_END:
-          if (ifault == 0) {
-            cs = CS_NM_DONE;
-          } else {
-            // restart from the probe point with a 1e-6 simplex
-            nm_for<0, N, kU>([&](int i) { start[i] = xmin[i]; });
-            scale = P::eps_scale();
-            numres++;
-            restart_simplex();
-            cs = CS_NONE;
-          }
-          break;
-        case CS_NM_DONE:
-          return true;
-        default:
-          cs = CS_NONE;
-          break;
+    // The transitions between the stages below only go forward
+    // (READY -> TOP, ITER_END -> TOP | END_INNER, TOP -> END_INNER,
+    // END_INNER -> PROBE_PLUS | NM_DONE), so one pass in this order
+    // follows every chain the reference's loops can take.
+    if (cs == CS_READY) {
+      find_lo();
+      cs = CS_TOP;
+    }
+    if (cs == CS_ITER_END) cs = iteration_end() ? CS_END_INNER : CS_TOP;
+    if (cs == CS_TOP) cs = inner_top() ? CS_NONE : CS_END_INNER;
+    if (cs == CS_END_INNER) {
+      nm_for<0, N, kU>([&](int i) { xmin[i] = V(lo, i); });
+      floor_lo = P::trunc10(F(lo));
+      if (kcount < icount) {
+        ifault = 2;
+        cs = CS_NM_DONE;
+      } else {
+        ifault = 0;
+        jj = 0;
+        cs = CS_PROBE_PLUS;
       }
     }
-    return false;
+    if (cs == CS_PROBE_PLUS) {
+      const T del = P::eps_step(pick(step, jj));
+      put(xmin, jj, P::add(pick(xmin, jj), del));
+      nm_for<0, N, kU>([&](int i) { x[i] = xmin[i]; });
+      phase = PH_PROBE_PLUS;
+      cs = CS_NONE;
+    }
+    if (cs == CS_PROBE_END) {
+      if (ifault == 0) {
+        cs = CS_NM_DONE;
+      } else {
+        // restart from the probe point with a 1e-6 simplex
+        nm_for<0, N, kU>([&](int i) { start[i] = xmin[i]; });
+        scale = P::eps_scale();
+        numres++;
+        restart_simplex();
+        cs = CS_NONE;
+      }
+    }
+    if (pk != PK_NONE) make_point();
+    return cs == CS_NM_DONE;
   }
 };
 

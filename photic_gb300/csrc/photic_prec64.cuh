@@ -28,6 +28,8 @@ struct PrecF64 {
   static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
   static __device__ __forceinline__ T mul2(T a) { return 2.0 * a; }
   static __device__ __forceinline__ T half(T a) { return a * 0.5; }
+  // a * c for c in {1/2, 1, 2}: exact
+  static __device__ __forceinline__ T scale2(T a, float c) { return a * (double)c; }
   // z / n for the simplex size n, a compile-time constant here
   static __device__ __forceinline__ T div_n(T a, int n) { return fm::div_by(a, (double)n, 1.0 / (double)n); }
   static __device__ __forceinline__ bool lt(T a, T b) { return a < b; }

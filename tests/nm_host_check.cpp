@@ -37,6 +37,7 @@ struct HostF64 {
   static T mul(T a, T b) { return a * b; }
   static T mul2(T a) { return 2.0 * a; }
   static T half(T a) { return a * 0.5; }
+  static T scale2(T a, float c) { return a * (double)c; }
   static T div_n(T a, int n) { return photic::fm::div_by(a, (double)n, 1.0 / (double)n); }
   static bool lt(T a, T b) { return a < b; }
   static bool le(T a, T b) { return a <= b; }
