@@ -551,6 +551,77 @@ def lut_invert(rrs, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0, h_tide=0.0,
     return out, source, order[:S], stats[:min(n_chains, max(S, 1))]
 
 
+def glut_invert(grid, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0, h_tide=0.0,
+                nodata=-9999.0, n_spatial=2, n_bottoms=3, rrs_noise=None, empirical=None,
+                empirical_nodata=-9999.0, reqmin=None, konvge=100, kcount=2000, n_lut=16000,
+                n_chains=1, nthreads=0):
+    """samodel()'s loop with the dynamic lookup table in the general
+    configuration: grid [nrows, ncols, n_bands] or [n_scenes, nrows, ncols,
+    n_bands] float32, 3 x 3 regions (n_spatial 2), n_bottoms bottom types,
+    one sun zenith per scene (theta_sun scalar or sequence), rrs_noise
+    [n_scenes, n_bands] (the spectral-angle order), empirical [nrows,
+    ncols].  Returns (records [npix, NOUT], source, order, chain_stats) as
+    lut_invert."""
+    g = _f32(grid)
+    if g.ndim == 3:
+        g = g[None]
+    S, nr, nc, nb = g.shape
+    npix = nr * nc
+    wl = _f64(wl)
+    th = _f64(np.broadcast_to(np.asarray(theta_sun, dtype=np.float64), (S,)))
+    if reqmin is None:
+        reqmin, konvge, kcount = 1e-2, 100, 5000
+    out = np.zeros((npix, NOUT))
+    source = np.zeros(npix, dtype=np.int64)
+    order = np.zeros(max(npix, 1), dtype=np.int64)
+    n_sh = C.c_int64(0)
+    stats = np.zeros((max(1, n_chains), 4))
+    nz = _f64(np.asarray(rrs_noise, dtype=np.float64).reshape(S, nb)) if rrs_noise is not None \
+        else None
+    em = _f32(empirical).reshape(-1) if empirical is not None else None
+    L = port().lib
+    L.po_glut_invert.argtypes = [C.c_int, _dp, _dp, C.c_double, C.c_double, _fp, C.c_int,
+                                 C.c_int, C.c_int, C.c_float, C.c_int, C.c_int, _dp, _fp,
+                                 C.c_float, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int64,
+                                 C.c_int, _i64p, _i64p, _dp, _i64p, _dp]
+    rc = L.po_glut_invert(nb, _ptr(wl, _dp), _ptr(th, _dp), theta_view, h_tide, _ptr(g, _fp), S,
+                          nr, nc, nodata, n_spatial, n_bottoms, _ptr(nz, _dp), _ptr(em, _fp),
+                          empirical_nodata, reqmin, konvge, kcount, n_lut, n_chains, nthreads,
+                          _ptr(order, _i64p), C.byref(n_sh), _ptr(out, _dp), _ptr(source, _i64p),
+                          _ptr(stats, _dp))
+    if rc:
+        raise ValueError(f"po_glut_invert failed ({rc})")
+    S_ = n_sh.value
+    return out, source, order[:S_], stats[:min(n_chains, max(S_, 1))]
+
+
+def reference_samodel_stack(grid, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0,
+                            nodata=-9999.0, r_sigma=None, empirical=None,
+                            empirical_nodata=-9999.0, n_spatial=1, n_bottoms=1):
+    """The reference's own samodel() over [n_scenes, nrows, ncols, n_bands]
+    co-registered scenes (one sun zenith each, r_sigma [n_scenes, n_bands])
+    on one thread; returns the [10, nrows, ncols] grids as
+    reference_samodel_grid."""
+    g = _f32(grid)
+    S, nr, nc, nb = g.shape
+    wl = _f64(wl)
+    th = _f64(np.broadcast_to(np.asarray(theta_sun, dtype=np.float64), (S,)))
+    out = np.zeros((10, nr, nc), dtype=np.float32)
+    rs = _f64(np.asarray(r_sigma, dtype=np.float64).reshape(S, nb)) if r_sigma is not None \
+        else None
+    em = _f32(empirical).reshape(nr, nc) if empirical is not None else None
+    L = reference().lib
+    L.photic_ref_samodel_stack.argtypes = [C.c_int, _dp, _dp, C.c_double, _fp, C.c_int, C.c_int,
+                                           C.c_int, C.c_float, _dp, _fp, C.c_float, C.c_int,
+                                           C.c_int, _fp]
+    rc = L.photic_ref_samodel_stack(nb, _ptr(wl, _dp), _ptr(th, _dp), theta_view, _ptr(g, _fp),
+                                    S, nr, nc, nodata, _ptr(rs, _dp), _ptr(em, _fp),
+                                    empirical_nodata, n_spatial, n_bottoms, _ptr(out, _fp))
+    if rc:
+        raise ValueError(f"photic_ref_samodel_stack failed ({rc})")
+    return out
+
+
 def reference_samodel_grid(grid, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0,
                            nodata=-9999.0, r_sigma=None, empirical=None,
                            empirical_nodata=-9999.0, n_spatial=1, n_bottoms=1):

@@ -1187,6 +1187,7 @@ typedef struct {
   double K[PO_MAX_SCENES][PO_MAX_BANDS]; /* md->K[scene][band]: the last region's */
   double rrs_mod[PO_MAX_REGIONS][PO_MAX_SCENES][PO_MAX_BANDS];
   double rrs_bot[PO_MAX_REGIONS][PO_MAX_SCENES][PO_MAX_BANDS];
+  double Rm[PO_MAX_REGIONS][PO_MAX_SCENES][PO_MAX_BANDS]; /* md->Rrs_modelled */
   double bottom_albedo, rrs_error, model_error;
 } po_rpixel;
 
@@ -1240,6 +1241,7 @@ static double region_cost(const double *x, void *ctx) {
         px->bottom_albedo = albedo;
         Rm = hope_band(sc, b, P, G, X, rho, Hr, 0.0, px->r440[r][s], px->r490[r][s],
                        &px->K[s][b], &px->rrs_bot[r][s][b], &px->rrs_mod[r][s][b]);
+        px->Rm[r][s][b] = Rm;
         d = Rm - px->rrs[r][s][b];
         err += pow(d, 2.0);
         tot += px->rrs[r][s][b];
@@ -1373,8 +1375,13 @@ static void region_reference_rrs(po_rpixel *px) {
 
 /* samodel_optimise for one pixel's regions (model/samodel.c:1768-2115):
  * depth starts, nelmin, early exit, the final re-evaluation and the post-fit
- * products.  h_emp: the empirical depth, or NaN for the 8 cold starts. */
-static void region_fit(po_rpixel *px, const po_fit *fit, double h_emp, double *o) {
+ * products.  h_emp: the single depth start (an empirical depth, or the
+ * previous pixel's under a hot start), or NaN for the 8 cold starts.
+ * hot_prev (3 per scene, or NULL): the hot start's P, G, X, each with twice
+ * itself as step (model/samodel.c:2234-2241, 2288-2309).  best_out
+ * (optional) receives the kept parameter vector. */
+static void region_fit(po_rpixel *px, const po_fit *fit, double h_emp, const double *hot_prev,
+                       double *o, double *best_out) {
   const int R = px->R, S = px->S, n = region_n_params(px), nb = px->nb, off = R + 2 * nb * R;
   double start[PO_MAX_PARAMS], step[PO_MAX_PARAMS], xm[PO_MAX_PARAMS], best[PO_MAX_PARAMS];
   double lowest = 1.0e4, y = 0.0;
@@ -1386,6 +1393,11 @@ static void region_fit(po_rpixel *px, const po_fit *fit, double h_emp, double *o
   nst = isnan(h_emp) ? fit->n_hstarts : 1;
   for (k = 0; k < nst; k++) {
     region_cold_start(px, isnan(h_emp) ? fit->hstarts[k] : h_emp, start, step);
+    if (hot_prev)
+      for (s = 0; s < 3 * S; s++) {
+        start[off + s] = hot_prev[s];
+        step[off + s] = 2.0 * start[off + s];
+      }
     po_nelmin(region_cost, px, n, start, xm, &y, fit->reqmin, step, fit->konvge, fit->kcount,
               &icount, &numres, &ifault);
     total += icount;
@@ -1401,6 +1413,7 @@ static void region_fit(po_rpixel *px, const po_fit *fit, double h_emp, double *o
     }
   }
   region_cost(best, px);
+  if (best_out) memcpy(best_out, best, n * sizeof(double));
   {
     double K_min = 1.0e10, iod = 0.0, nobs = 0.0, depth = 0.0, ow = sqrt((double)R);
     double q_sum = 0.0, pct[PO_MAX_MIX], largest = 0.0, type = 0.0;
@@ -1460,6 +1473,38 @@ static void region_fit(po_rpixel *px, const po_fit *fit, double h_emp, double *o
   o[39] = (double)px->origin;
 }
 
+/* extract_Rrs_data (model/samodel.c:2957-3027) for pixel p of a
+ * [n_scenes][nrows][ncols][n_bands] grid: the regions' spectra, their count
+ * and the origin's slot. */
+static void region_extract(const float *grid, int n_scenes, int nrows, int ncols, int n_bands,
+                           float nodata, int n_spatial, int64_t p, po_rpixel *px) {
+  const int64_t npix = (int64_t)nrows * ncols;
+  const int i = (int)(p / ncols), j = (int)(p % ncols), w = n_spatial - 1;
+  int ii, jj, sk, b;
+  px->R = 0;
+  px->origin = 0;
+  for (ii = -w; ii <= w; ii++) {
+    const int iii = i + ii < 0 ? 0 : (i + ii > nrows - 1 ? nrows - 1 : i + ii);
+    for (jj = -w; jj <= w; jj++) {
+      const int jjj = j + jj < 0 ? 0 : (j + jj > ncols - 1 ? ncols - 1 : j + jj);
+      int nodata_region = 0;
+      for (sk = 0; sk < n_scenes && !nodata_region; sk++) {
+        const float *q = grid + ((int64_t)sk * npix + (int64_t)iii * ncols + jjj) * n_bands;
+        for (b = 0; b < n_bands; b++) {
+          if (!f_close(q[b], nodata, 1.0e-6f)) {
+            px->rrs[px->R][sk][b] = q[b];
+          } else {
+            nodata_region = 1;
+            break;
+          }
+        }
+      }
+      if (i == iii && j == jjj) px->origin = px->R;
+      if (!nodata_region) px->R++;
+    }
+  }
+}
+
 /* grid: [n_scenes][nrows][ncols][n_bands]; theta_sun_deg: [n_scenes]. */
 int po_region_fit_batch(int n_bands, const double *wl, const double *theta_sun_deg,
                         double theta_view_deg, double h_tide, const float *grid, int n_scenes,
@@ -1486,12 +1531,10 @@ int po_region_fit_batch(int n_bands, const double *wl, const double *theta_sun_d
 #pragma omp parallel for schedule(dynamic, 4)
 #endif
   for (p = 0; p < npix; p++) {
-    const int i = (int)(p / ncols), j = (int)(p % ncols);
-    const int w = n_spatial - 1;
     double *o = out + p * PO_NOUT;
     double h_emp = NAN;
     po_rpixel px;
-    int ii, jj, b, sk, bad = 0;
+    int sk, bad = 0;
     memset(o, 0, PO_NOUT * sizeof(double));
     for (sk = 0; sk < n_scenes && !bad; sk++) /* model/samodel.c:933-947 */
       bad = masked(grid + ((int64_t)sk * npix + p) * n_bands, n_bands, nodata);
@@ -1508,29 +1551,9 @@ int po_region_fit_batch(int n_bands, const double *wl, const double *theta_sun_d
       h_emp = h_empirical[p];
       if (h_emp > 8.0) px.nb = 1; /* model/samodel.c:1781, 1826-1830 */
     }
-    /* extract_Rrs_data, model/samodel.c:2957-3027 */
-    for (ii = -w; ii <= w; ii++) {
-      const int iii = i + ii < 0 ? 0 : (i + ii > nrows - 1 ? nrows - 1 : i + ii);
-      for (jj = -w; jj <= w; jj++) {
-        const int jjj = j + jj < 0 ? 0 : (j + jj > ncols - 1 ? ncols - 1 : j + jj);
-        int nodata_region = 0;
-        for (sk = 0; sk < n_scenes && !nodata_region; sk++) {
-          const float *q = grid + ((int64_t)sk * npix + (int64_t)iii * ncols + jjj) * n_bands;
-          for (b = 0; b < n_bands; b++) {
-            if (!f_close(q[b], nodata, 1.0e-6f)) {
-              px.rrs[px.R][sk][b] = q[b];
-            } else {
-              nodata_region = 1;
-              break;
-            }
-          }
-        }
-        if (i == iii && j == jjj) px.origin = px.R;
-        if (!nodata_region) px.R++;
-      }
-    }
+    region_extract(grid, n_scenes, nrows, ncols, n_bands, nodata, n_spatial, p, &px);
     if (px.R == 0) continue;
-    region_fit(&px, &fit, h_emp, o);
+    region_fit(&px, &fit, h_emp, NULL, o, NULL);
   }
   return 0;
 }
@@ -2026,6 +2049,320 @@ int po_lut_invert(int n_bands, const double *wl, double theta_sun_deg, double th
     const int64_t a = c * S / n_chains, e = (c + 1) * S / n_chains;
     lut_chain(&sc, &fit, rrs, n_bands, emp, emp_nodata, order_out + a, e - a, n_lut, out,
               source, chain_stats ? chain_stats + 4 * c : NULL);
+  }
+  return 0;
+}
+
+/* ---- the pixel loop with its lookup table, general configuration -------
+ * samodel() with LUT 1 (model/samodel.c:649-1352) for 3 x 3 regions, bottom
+ * mixtures and stacks of scenes: the loop of lut_chain above with
+ *   keys     blue, green and red summed over the scenes, each value that is
+ *            not nodata, and the noise spectra summed over the scenes for
+ *            the spectral angle (:711-767);
+ *   shallow  every band of every scene neither nodata nor negative;
+ *   lookup   entries with the pixel's region count (:985), the mean over
+ *            scenes and regions of the measured and modelled Rrs of bands
+ *            1..3 where both are non-zero (model_spectral_diff_mean,
+ *            :2792-2842, scene-major sums);
+ *   fit      samodel_optimise over the regions (region_fit), hot-started
+ *            from the previous pixel when the last two were continuous: one
+ *            depth start at the previous depth (or the empirical depth) for
+ *            every region, cold albedos and mixing weights, each scene's
+ *            P, G, X from the previous fit (:2234-2241, 2288-2309);
+ *   entry    the fit's region count, depth, K_min, modelled Rrs of bands
+ *            1..3 per region and scene, and P, G, X (partial_copy_md,
+ *            :3031-3139).
+ * h_empirical, which selects sand alone above 8 m (:1826), is set only by
+ * a pixel with an empirical depth and kept by the pixels after it; before
+ * the first such pixel the reference leaves it unset (md is allocated with
+ * malloc, :375): it is taken as 0 here, i.e. every bottom type is fitted,
+ * as in the reference runs the fixtures come from. */
+typedef struct {
+  int R;
+  double depth, kmin;
+  double rm[PO_MAX_REGIONS][PO_MAX_SCENES][3];
+  double prev[3 * PO_MAX_SCENES];
+  int64_t src;
+} po_glut_entry;
+
+static float glut_spectral_diff(const po_rpixel *px, const po_glut_entry *e) {
+  double error = 0.0;
+  int k, r, s, n_total = 0;
+  for (k = 1; k <= 3 && k < px->n_bands; k++) {
+    double current = 0.0, previous = 0.0, nobs = 0.0;
+    for (s = 0; s < px->S; s++)
+      for (r = 0; r < px->R; r++)
+        if (!ref_approx_eq((float)px->rrs[r][s][k], 0.0f, 1.0e-6f) &&
+            !ref_approx_eq((float)e->rm[r][s][k - 1], 0.0f, 1.0e-6f)) {
+          current += px->rrs[r][s][k];
+          previous += e->rm[r][s][k - 1];
+          nobs += 1.0;
+        }
+    if (nobs > 0.5) {
+      current /= nobs;
+      previous /= nobs;
+    }
+    error += pow((current - previous) / current, 2.0);
+    n_total++;
+  }
+  error = 100.0 * sqrt(error / ((double)n_total));
+  return (float)error;
+}
+
+/* The spectral index of pixel p over n_scenes scenes (model/samodel.c:
+ * 711-767); noise: [n_scenes][n_bands] or NULL. */
+float po_glut_key(const float *grid, int n_scenes, int64_t npix, int64_t p, int n_bands,
+                  float nodata, const double *noise) {
+  float blue_sum = 0.0f, green_sum = 0.0f, red_sum = 0.0f, index;
+  int s;
+  for (s = 0; s < n_scenes; s++) {
+    const float *r = grid + ((int64_t)s * npix + p) * n_bands;
+    if (n_bands > 1 && !ref_approx_eq(r[1], nodata, 1.0e-6f)) blue_sum += r[1];
+    if (n_bands > 2 && !ref_approx_eq(r[2], nodata, 1.0e-6f)) green_sum += r[2];
+    if (n_bands > 3 && !ref_approx_eq(r[3], nodata, 1.0e-6f)) red_sum += r[3];
+  }
+  index = (float)sqrt(pow(blue_sum, 2) + pow(green_sum, 2) + pow(red_sum, 2));
+  if (noise) {
+    double bn = 0.0, gn = 0.0, rn = 0.0, angle;
+    for (s = 0; s < n_scenes; s++) {
+      bn += noise[s * n_bands + 1];
+      gn += noise[s * n_bands + 2];
+      rn += noise[s * n_bands + 3];
+    }
+    angle = blue_sum * bn + green_sum * gn + red_sum * rn;
+    angle /= index * sqrt(pow(bn, 2) + pow(gn, 2) + pow(rn, 2));
+    angle = acos(angle);
+    index *= angle;
+  }
+  return index;
+}
+
+typedef struct {
+  const po_scene *sc;
+  const po_fit *fit;
+  const float *grid;
+  int S, nrows, ncols, nb, n_spatial, n_bottoms;
+  float nodata;
+  const float *emp;
+  float emp_nodata;
+  int n_lut;
+} po_glut_ctx;
+
+static void glut_chain(const po_glut_ctx *g, const int64_t *order, int64_t n, double *out,
+                       int64_t *source, double *stats) {
+  const double eps = (double)1.0e-4f;
+  const double continuity = 0.1;
+  const int S = g->S;
+  const int64_t cap = n < (int64_t)g->n_lut ? n : (int64_t)g->n_lut;
+  po_glut_entry *lut =
+      (po_glut_entry *)calloc((size_t)(cap > 0 ? cap : 1), sizeof(po_glut_entry));
+  int64_t total_lut = 0, k, n_complete = 0, err_count = 0, n_opt = 0;
+  double md_depth = 0.0, md_kmin = 0.0, depth_prev = 0.0, kmin_prev = 0.0;
+  double prev[3 * PO_MAX_SCENES], h_emp_state = 0.0;
+  double match = 1.125 * (double)S > 1.5 ? 1.125 * (double)S : 1.5, entry;
+  double n_modelled = 0.0, n_skipped = 0.0, total_model_error = 0.0, err_total = 0.0;
+  int hot = 0, nprev = 0, nperc, i;
+  memset(prev, 0, sizeof prev);
+  entry = match;
+  for (k = 0; k < n; k++) {
+    const int64_t p = order[k];
+    po_rpixel px;
+    double best = 1.0e4, model_error, h_emp = NAN;
+    int64_t pos = 0, j, in_use = total_lut < cap ? total_lut : cap;
+    int emp_present = 0, s;
+    memset(&px, 0, sizeof px);
+    px.n_bands = g->nb;
+    px.S = S;
+    px.nb = g->n_bottoms;
+    for (s = 0; s < S; s++) px.sc[s] = &g->sc[s];
+    region_extract(g->grid, S, g->nrows, g->ncols, g->nb, g->nodata, g->n_spatial, p, &px);
+    if (px.R == 0) continue; /* :951-953 (a shallow pixel keeps its own region) */
+    if (g->emp) { /* :955-976 */
+      if (!ref_approx_eq(g->emp[p], g->emp_nodata, 1.0e-6f)) {
+        emp_present = 1;
+        h_emp_state = g->emp[p] > -1.0 ? 1.0 : fabs(g->emp[p]);
+        h_emp = h_emp_state;
+      } else {
+        hot = 0;
+      }
+    }
+    for (j = 0; j < in_use; j++) {
+      const po_glut_entry *e = lut + j;
+      if (e->R == px.R && fabs(e->depth - md_depth) / (md_depth + eps) < continuity &&
+          fabs(e->kmin - md_kmin) / (md_kmin + eps) < continuity) {
+        double d = (double)glut_spectral_diff(&px, e);
+        if (d < best) {
+          best = d;
+          pos = j;
+        }
+      }
+    }
+    if (best > match || in_use == 0) {
+      double bestv[PO_MAX_PARAMS], *o = out + p * PO_NOUT, h0 = h_emp;
+      int off;
+      if (h_emp_state > 8.0) px.nb = 1; /* :1826-1830 */
+      off = px.R + 2 * px.nb * px.R;
+      if (hot && !emp_present) h0 = depth_prev;
+      region_fit(&px, g->fit, h0, hot ? prev : NULL, o, bestv);
+      source[p] = -1;
+      md_depth = o[0];
+      md_kmin = o[4];
+      model_error = o[2];
+      for (i = 0; i < 3 * S; i++) prev[i] = fabs(bestv[off + i]); /* :2086-2099 */
+      n_opt++;
+      if (!ref_approx_eq((float)model_error, 0.0f, 1.0e-4f)) {
+        err_total += model_error;
+        err_count++;
+      }
+      if (model_error < entry && md_depth < 32.0) {
+        po_glut_entry *e = lut + (total_lut % cap);
+        int r, b;
+        e->R = px.R;
+        e->depth = md_depth;
+        e->kmin = md_kmin;
+        for (r = 0; r < px.R; r++)
+          for (s = 0; s < S; s++)
+            for (b = 0; b < 3; b++) e->rm[r][s][b] = b + 1 < g->nb ? px.Rm[r][s][b + 1] : 0.0;
+        memcpy(e->prev, prev, sizeof prev);
+        e->src = p;
+        total_lut++;
+      }
+      if (stats) stats[1] += 1.0;
+    } else {
+      const po_glut_entry *e = lut + pos;
+      depth_prev = md_depth;
+      kmin_prev = md_kmin;
+      md_depth = e->depth;
+      md_kmin = e->kmin;
+      memcpy(prev, e->prev, sizeof prev);
+      model_error = best;
+      memcpy(out + p * PO_NOUT, out + e->src * PO_NOUT, PO_NOUT * sizeof(double));
+      out[p * PO_NOUT + 2] = best;
+      source[p] = e->src;
+      n_skipped += 1.0;
+      if (stats) stats[0] += 1.0;
+    }
+    hot = fabs(md_depth - depth_prev) / (eps + depth_prev) < continuity &&
+          fabs(md_kmin - kmin_prev) / (eps + kmin_prev) < continuity;
+    depth_prev = md_depth;
+    kmin_prev = md_kmin;
+    total_model_error += model_error;
+    n_modelled += 1.0;
+    nperc = (int)(1000 * ((double)++n_complete) / ((double)n));
+    if (nperc > nprev) {
+      if (n_opt > 0) {
+        const double error_mean = (float)(err_count ? err_total / ((double)err_count) : 0.0);
+        match += 0.75 * error_mean + 0.25 * total_model_error / n_modelled;
+        match /= 2.0;
+        entry = match;
+      }
+      if (n_skipped / n_modelled > 0.9925) {
+        match *= 0.75;
+        entry *= 0.75;
+      }
+      match = 1.5 > match ? 1.5 : match;
+      entry = 1.5 > entry ? 1.5 : entry;
+      nprev = nperc;
+      total_model_error = 0.0;
+      n_modelled = 0.0;
+      n_skipped = 0.0;
+      n_opt = 0;
+      err_total = 0.0;
+      err_count = 0;
+    }
+  }
+  if (stats) {
+    stats[2] = match;
+    stats[3] = entry;
+  }
+  free(lut);
+}
+
+/* grid: [n_scenes][nrows][ncols][n_bands]; theta_sun_deg, rrs_noise:
+ * per scene ([n_scenes], [n_scenes][n_bands]; the noise only when every
+ * value is at least 1e-6, :590-600, and n_bands >= 4); emp: [nrows][ncols]
+ * empirical depths or NULL.  Outputs as po_lut_invert. */
+int po_glut_invert(int n_bands, const double *wl, const double *theta_sun_deg,
+                   double theta_view_deg, double h_tide, const float *grid, int n_scenes,
+                   int nrows, int ncols, float nodata, int n_spatial, int n_bottoms,
+                   const double *rrs_noise, const float *emp, float emp_nodata, double reqmin,
+                   int konvge, int kcount, int n_lut, int64_t n_chains, int nthreads,
+                   int64_t *order_out, int64_t *n_shallow_out, double *out, int64_t *source,
+                   double *chain_stats) {
+  po_scene sc[PO_MAX_SCENES];
+  po_fit fit;
+  po_glut_ctx g;
+  po_key *keys;
+  const int64_t npix = (int64_t)nrows * ncols;
+  int64_t p, S = 0, c;
+  const double *noise = NULL;
+  int s;
+  if (n_bands < 2 || n_bands > PO_MAX_BANDS || n_lut < 1 || n_chains < 1 || n_scenes < 1 ||
+      n_scenes > PO_MAX_SCENES || n_spatial < 1 || n_spatial > 2 || n_bottoms < 1 ||
+      n_bottoms > PO_MAX_MIX)
+    return 1;
+  if (rrs_noise && n_bands >= 4) {
+    int b, ok = 1;
+    for (s = 0; s < n_scenes; s++)
+      for (b = 0; b < n_bands; b++)
+        if (rrs_noise[s * n_bands + b] < 1.0e-6) ok = 0;
+    if (ok) noise = rrs_noise;
+  }
+  for (s = 0; s < n_scenes; s++)
+    scene_init(&sc[s], n_bands, wl, theta_sun_deg[s], theta_view_deg, h_tide);
+  fit.seed_step_scale = 1.0;
+  fit.reqmin = reqmin;
+  fit.konvge = konvge;
+  fit.kcount = kcount;
+  fit.n_hstarts = 8;
+  fit.hstarts = po_default_hstarts;
+  keys = (po_key *)malloc((size_t)(npix > 0 ? npix : 1) * sizeof(po_key));
+  {
+    po_key *tmp = (po_key *)malloc((size_t)(npix > 0 ? npix : 1) * sizeof(po_key));
+    for (p = 0; p < npix; p++) {
+      keys[p].value = emp ? emp[p] : po_glut_key(grid, n_scenes, npix, p, n_bands, nodata, noise);
+      keys[p].idx = p;
+    }
+    po_msort(keys, tmp, (size_t)npix);
+    free(tmp);
+  }
+  for (p = 0; p < npix; p++) {
+    const int64_t q = keys[p].idx;
+    int bad = 0;
+    memset(out + q * PO_NOUT, 0, PO_NOUT * sizeof(double));
+    for (s = 0; s < n_scenes && !bad; s++)
+      bad = masked(grid + ((int64_t)s * npix + q) * n_bands, n_bands, nodata);
+    if (bad) {
+      out[q * PO_NOUT + 9] = 1.0;
+      source[q] = -2;
+      continue;
+    }
+    order_out[S++] = q;
+  }
+  free(keys);
+  *n_shallow_out = S;
+  if (n_chains > S) n_chains = S > 0 ? S : 1;
+  if (chain_stats) memset(chain_stats, 0, (size_t)n_chains * 4 * sizeof(double));
+  g.sc = sc;
+  g.fit = &fit;
+  g.grid = grid;
+  g.S = n_scenes;
+  g.nrows = nrows;
+  g.ncols = ncols;
+  g.nb = n_bands;
+  g.n_spatial = n_spatial;
+  g.n_bottoms = n_bottoms;
+  g.nodata = nodata;
+  g.emp = emp;
+  g.emp_nodata = emp_nodata;
+  g.n_lut = n_lut;
+#if _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+  for (c = 0; c < n_chains; c++) {
+    const int64_t a = c * S / n_chains, e = (c + 1) * S / n_chains;
+    glut_chain(&g, order_out + a, e - a, out, source, chain_stats ? chain_stats + 4 * c : NULL);
   }
   return 0;
 }

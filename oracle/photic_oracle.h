@@ -110,6 +110,15 @@ void po_generate_field(uint64_t seed, int64_t nrows, int64_t ncols, int64_t row0
                        double mask_frac, double noise_sigma, float nodata, float *rrs_out,
                        double *truth_out);
 float po_lut_key(const float *r, int n_bands, float nodata, const double *noise);
+float po_glut_key(const float *grid, int n_scenes, int64_t npix, int64_t p, int n_bands,
+                  float nodata, const double *noise);
+int po_glut_invert(int n_bands, const double *wl, const double *theta_sun_deg,
+                   double theta_view_deg, double h_tide, const float *grid, int n_scenes,
+                   int nrows, int ncols, float nodata, int n_spatial, int n_bottoms,
+                   const double *rrs_noise, const float *emp, float emp_nodata, double reqmin,
+                   int konvge, int kcount, int n_lut, int64_t n_chains, int nthreads,
+                   int64_t *order_out, int64_t *n_shallow_out, double *out, int64_t *source,
+                   double *chain_stats);
 int po_lut_invert(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
                   double h_tide, const float *rrs, int64_t npix, float nodata,
                   const double *rrs_noise, const float *emp, float emp_nodata, double reqmin,

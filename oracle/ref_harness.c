@@ -547,17 +547,22 @@ double photic_ref_depth_sigma_stat(double *depths, int n) {
  * sand, seagrass, coral, K_min, bottom type, index of optical depth.  Its
  * depth-uncertainty pass and result files run as well (the netCDF stand-in
  * keeps the files in memory). */
-int photic_ref_samodel_grid(int n_bands, const double *wl, double theta_sun_deg,
-                            double theta_view_deg, const float *grid, int nrows, int ncols,
-                            float nodata, const double *r_sigma, const float *empirical,
-                            float empirical_nodata, int n_spatial, int n_bottoms,
-                            float *grids_out) {
-  scene sc;
+/* samodel() over n_scenes co-registered scenes of the same bands:
+ * grid [n_scenes][nrows][ncols][n_bands], theta_sun_deg and r_sigma per
+ * scene ([n_scenes], [n_scenes][n_bands] or NULL); one thread. */
+int photic_ref_samodel_stack(int n_bands, const double *wl, const double *theta_sun_deg,
+                             double theta_view_deg, const float *grid, int n_scenes, int nrows,
+                             int ncols, float nodata, const double *r_sigma,
+                             const float *empirical, float empirical_nodata, int n_spatial,
+                             int n_bottoms, float *grids_out) {
+  scene *sc;
   geogrid *gd, none;
   float **out[10];
-  int b, i, j, k, idx = 0;
-  if (n_bands < 2 || n_bands > REF_MAX_BANDS) return 1;
-  memset(&sc, 0, sizeof sc);
+  int b, i, j, k, s, *idx;
+  const size_t npix = (size_t)nrows * ncols;
+  if (n_bands < 2 || n_bands > REF_MAX_BANDS || n_scenes < 1) return 1;
+  sc = (scene *)calloc(n_scenes, sizeof(scene));
+  idx = (int *)calloc(n_scenes, sizeof(int));
   memset(&none, 0, sizeof none);
   if (empirical) { /* an empirical depth grid (model/samodel.c:702-710, 955-979) */
     none.nrows = nrows;
@@ -568,39 +573,57 @@ int photic_ref_samodel_grid(int n_bands, const double *wl, double theta_sun_deg,
     for (i = 0; i < nrows; i++)
       for (j = 0; j < ncols; j++) none.array[i][j] = empirical[(size_t)i * ncols + j];
   }
-  strcpy(sc.scene_name, "harness");
-  sc.n_bands = n_bands;
-  sc.nrows = nrows;
-  sc.ncols = ncols;
-  sc.theta_w = theta_sun_deg;
-  sc.theta_v = theta_view_deg;
-  gd = (geogrid *)calloc(n_bands, sizeof(geogrid));
-  for (b = 0; b < n_bands; b++) {
-    sc.band_indexes[b] = b;
-    sc.wavelengths[b] = (int)wl[b];
-    sc.R_sigma[b] = r_sigma ? r_sigma[b] : 0.0;
-    gd[b].nrows = nrows;
-    gd[b].ncols = ncols;
-    gd[b].cellsize = 1.0f;
-    gd[b].nodata_value = nodata;
-    allocate_float_array_2d(&gd[b].array, nrows, ncols);
-    for (i = 0; i < nrows; i++)
-      for (j = 0; j < ncols; j++) gd[b].array[i][j] = grid[((size_t)i * ncols + j) * n_bands + b];
+  gd = (geogrid *)calloc((size_t)n_scenes * n_bands, sizeof(geogrid));
+  for (s = 0; s < n_scenes; s++) {
+    idx[s] = s;
+    snprintf(sc[s].scene_name, sizeof sc[s].scene_name, "harness%d", s);
+    sc[s].n_bands = n_bands;
+    sc[s].nrows = nrows;
+    sc[s].ncols = ncols;
+    sc[s].theta_w = theta_sun_deg[s];
+    sc[s].theta_v = theta_view_deg;
+    for (b = 0; b < n_bands; b++) {
+      geogrid *g = gd + s * n_bands + b;
+      sc[s].band_indexes[b] = s * n_bands + b;
+      sc[s].wavelengths[b] = (int)wl[b];
+      sc[s].R_sigma[b] = r_sigma ? r_sigma[s * n_bands + b] : 0.0;
+      g->nrows = nrows;
+      g->ncols = ncols;
+      g->cellsize = 1.0f;
+      g->nodata_value = nodata;
+      allocate_float_array_2d(&g->array, nrows, ncols);
+      for (i = 0; i < nrows; i++)
+        for (j = 0; j < ncols; j++)
+          g->array[i][j] = grid[(s * npix + (size_t)i * ncols + j) * n_bands + b];
+    }
   }
   for (k = 0; k < 10; k++) allocate_float_array_2d(&out[k], nrows, ncols);
   set_tol(0, 0.0, 0, 0);
 #if _OPENMP
   omp_set_num_threads(1);
 #endif
-  samodel(&sc, gd, &idx, 1, empirical != NULL, none, 1, n_spatial, n_bottoms, out[0], out[1],
-          out[2], out[3], out[4], out[5], out[6], out[7], out[8], out[9], 10.0f, 0, 1);
+  samodel(sc, gd, idx, n_scenes, empirical != NULL, none, 1, n_spatial, n_bottoms, out[0],
+          out[1], out[2], out[3], out[4], out[5], out[6], out[7], out[8], out[9], 10.0f, 0, 1);
   for (k = 0; k < 10; k++)
     for (i = 0; i < nrows; i++)
       for (j = 0; j < ncols; j++)
         grids_out[((size_t)k * nrows + i) * ncols + j] = out[k][i][j];
   if (empirical) free_float_array_2d(none.array, nrows);
   for (k = 0; k < 10; k++) free_float_array_2d(out[k], nrows);
-  for (b = 0; b < n_bands; b++) free_float_array_2d(gd[b].array, nrows);
+  for (b = 0; b < n_scenes * n_bands; b++) free_float_array_2d(gd[b].array, nrows);
   free(gd);
+  free(sc);
+  free(idx);
   return 0;
+}
+
+/* samodel() over one scene (photic_ref_samodel_stack with n_scenes = 1). */
+int photic_ref_samodel_grid(int n_bands, const double *wl, double theta_sun_deg,
+                            double theta_view_deg, const float *grid, int nrows, int ncols,
+                            float nodata, const double *r_sigma, const float *empirical,
+                            float empirical_nodata, int n_spatial, int n_bottoms,
+                            float *grids_out) {
+  return photic_ref_samodel_stack(n_bands, wl, &theta_sun_deg, theta_view_deg, grid, 1, nrows,
+                                  ncols, nodata, r_sigma, empirical, empirical_nodata, n_spatial,
+                                  n_bottoms, grids_out);
 }

@@ -154,8 +154,55 @@ def lut():
     np.savez_compressed(os.path.join(OUT, "lut.npz"), grids=np.array(keep), **out)
 
 
+# the general configurations of the lookup-table loop: (name, side,
+# n_spatial, n_bottoms, sun zeniths of the scenes, noise, empirical grid)
+GLUT_CASES = (("r2b3", 20, 2, 3, (35.0,), False, False),
+              ("r1b3", 24, 1, 3, (35.0,), False, False),
+              ("r2b2_noise", 18, 2, 2, (35.0,), True, False),
+              ("r2b3_emp", 18, 2, 3, (35.0,), False, True),
+              ("r2b3_s2", 12, 2, 3, (35.0, 50.0), False, False))
+
+
+def glut():
+    """The reference's own samodel() with LUT 1 in its general
+    configurations -- 3 x 3 regions, mixtures of 1-3 bottom types, a noise
+    spectrum, an empirical depth grid (15 % nodata), a stack of two scenes
+    -- one thread, reference tolerances, on spatially coherent scenes (a
+    stack: the same place under two sun zeniths).  Kept grids: all but the
+    depth sigma.  The empirical grid's nodata value is positive, so that its
+    nodata pixels sort after the pixels with an empirical depth: the
+    reference sets h_empirical (which picks sand alone above 8 m) only from
+    a pixel with one and never initialises it (model/samodel.c:375,
+    960-967), so nodata pixels sorted first would see an undefined value."""
+    keep = [0, 2, 3, 4, 5, 6, 7, 8, 9]
+    out = {}
+    for name, n, ns, nbt, ths, noise, emp in GLUT_CASES:
+        grids = np.stack([O.generate_field(20261401 + n, n, n, theta_sun=t, mask_frac=0.1,
+                                           noise_sigma=1e-4)[0].reshape(n, n, 4) for t in ths])
+        rs = np.array([[2e-4, 1.5e-4, 1e-4, 5e-5]] * len(ths)) if noise else None
+        em = None
+        if emp:
+            _, truth = O.generate_field(20261401 + n, n, n, theta_sun=ths[0])
+            rng = np.random.default_rng(11)
+            em = (-truth[:, 0] * rng.uniform(0.8, 1.2, n * n)).astype(np.float32)
+            em[rng.random(n * n) < 0.15] = 9999.0
+            em = em.reshape(n, n)
+        g = O.reference_samodel_stack(grids, theta_sun=ths, n_spatial=ns, n_bottoms=nbt,
+                                      r_sigma=rs, empirical=em, empirical_nodata=9999.0)
+        out[f"{name}_grid"] = grids
+        out[f"{name}_theta_sun"] = np.array(ths)
+        out[f"{name}_config"] = np.array([ns, nbt])
+        out[f"{name}_ref"] = g[keep]
+        if rs is not None:
+            out[f"{name}_r_sigma"] = rs
+        if em is not None:
+            out[f"{name}_empirical"] = em
+    np.savez_compressed(os.path.join(OUT, "glut.npz"), grids=np.array(keep),
+                        cases=np.array([c[0] for c in GLUT_CASES]), **out)
+
+
 FIXTURES = {"single": single, "joint": joint, "cost_nelmin": cost_and_nelmin,
-            "regions": regions, "bottoms": bottoms, "lut": lut}
+            "regions": regions, "bottoms": bottoms, "lut": lut, "glut": glut}
 
 if __name__ == "__main__":
     O.build(ref=True)

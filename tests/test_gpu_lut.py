@@ -162,3 +162,28 @@ def test_eight_bands(gpu, port):
     assert np.median(d) <= 0.01
     assert np.mean(d == 0) >= 0.5
     assert abs(sg - sr) <= 0.05
+
+
+def test_edges(gpu, port):
+    """No pixels, every pixel masked, and more chains than shallow pixels
+    (the chain count clamps to the pixels, as in the oracle)."""
+    cfg = _ref_cfg(gpu)
+    out = gpu.lut_invert(torch.empty(0, 4, device="cuda"), cfg)
+    gpu.sync()
+    assert out["order"].numel() == 0 and out["chain_stats"].shape[0] == 0
+    assert out["depth"].numel() == 0
+    o = _run(gpu, np.full((50, 4), -9999.0, np.float32), 0)
+    assert o["order"].size == 0 and o["chain_stats"].shape[0] == 0
+    assert np.all(o["source"] == -2) and np.all((o["status"] & 0xFF) == 1)
+    rrs, _ = port.generate_field(99, 3, 3)
+    rrs[4] = -9999.0
+    for C in (1, 64):
+        o = _run(gpu, rrs, C)
+        ref, src, order, st = port.lut_invert(rrs, n_chains=C, nthreads=1)
+        np.testing.assert_array_equal(o["order"], order)
+        assert o["chain_stats"].shape[0] == st.shape[0] == min(C, order.size)
+        np.testing.assert_array_equal(o["source"] < 0, src < 0)
+        np.testing.assert_array_equal(o["status"] & 0xFF, ref[:, 9].astype(np.int32))
+        fit = ref[:, 9] == 0
+        d = np.abs(o["depth_f64"][fit] - ref[fit, 0])
+        assert np.median(d) <= 0.01, d
