@@ -318,6 +318,48 @@ int photic_lut_invert_batch(const photic_config *cfg, const photic_lut_config *l
                             int64_t *d_source, int64_t *d_order, double *d_chain_stats,
                             int64_t *n_shallow, int64_t *n_chains_used, void *stream);
 
+/* samodel()'s pixel loop with its dynamic lookup table in the general
+ * configuration: the fit of photic_region_fit_batch (3 x 3 regions,
+ * mixtures of n_bottoms bottom types, stacks of n_scenes scenes) inside the
+ * loop of photic_lut_invert_batch (model/samodel.c:649-1352).  d_grid
+ * (device, float) is [n_scenes][nrows][ncols][n_bands]; theta_sun_deg as
+ * for photic_region_fit_batch.  The shallow pixels (no band of any scene
+ * nodata or negative) are sorted by |(sum over scenes of Rrs_1, Rrs_2,
+ * Rrs_3)| -- times the spectral angle to the noise summed over the scenes
+ * when rrs_noise (host, [n_scenes][n_bands]) is given, n_bands >= 4 and
+ * every value is at least 1e-6 -- or by d_empirical (device [nrows *
+ * ncols] floats, empirical_nodata for none).  Each slice of the sorted list
+ * (lut->n_chains of them; 0: eight per resident warp, see
+ * photic_region_lut_default_chains) runs the reference's loop on one warp:
+ * a pixel whose table holds an entry with the same region count, within
+ * 10 % of the previous pixel's depth and K_min, whose modelled Rrs of bands
+ * 1..3 (averaged over scenes and regions where both are non-zero) differ
+ * from the measured by at most the match threshold takes that fit's
+ * outputs (PHOTIC_PX_SERVED, model_error = the difference, evals 0); any
+ * other pixel is fitted -- hot-started from the previous pixel when the
+ * last two were continuous (PHOTIC_PX_HOT: every region's depth at the
+ * previous depth or the empirical one, each scene's P, G, X from the
+ * previous fit) -- and entered into the table below the entry threshold
+ * and 32 m.  A pixel with an empirical depth starts there; the depth that
+ * selects sand alone above 8 m is the latest pixel's empirical depth in the
+ * slice (0 before the first).  Outputs, d_source, d_order, d_chain_stats,
+ * *n_shallow and *n_chains_used as for photic_lut_invert_batch, in the
+ * layout of photic_region_fit_batch.  FP64 only. */
+int photic_region_lut_invert_batch(const photic_config *cfg, const photic_lut_config *lut,
+                                   const float *d_grid, int32_t n_scenes,
+                                   const double *theta_sun_deg, int32_t nrows, int32_t ncols,
+                                   int32_t n_spatial, int32_t n_bottoms, const double *rrs_noise,
+                                   const float *d_empirical, float empirical_nodata,
+                                   const photic_outputs *out, int64_t *d_source,
+                                   int64_t *d_order, double *d_chain_stats, int64_t *n_shallow,
+                                   int64_t *n_chains_used, void *stream);
+
+/* Default slices of photic_region_lut_invert_batch for a configuration:
+ * eight per warp of the general fit's kernel resident on this device (0 on
+ * error or an unsupported configuration). */
+int64_t photic_region_lut_default_chains(const photic_config *cfg, int32_t n_scenes,
+                                         int32_t n_spatial, int32_t n_bottoms);
+
 /* Depth uncertainty, the reference's ad hoc estimate (model/samodel.c:
  * 1368-1479): for each 0.25 m interval up to the deepest fitted depth (whole
  * metres, at most 30 m), n_samples pixels of the interval are drawn (up to

@@ -158,6 +158,17 @@ _SIGS = {
                                           C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                           C.c_void_p]),
+    "photic_region_lut_invert_batch": (C.c_int, [C.POINTER(photic_config),
+                                                 C.POINTER(photic_lut_config), C.c_void_p,
+                                                 C.c_int32, C.POINTER(C.c_double), C.c_int32,
+                                                 C.c_int32, C.c_int32, C.c_int32,
+                                                 C.POINTER(C.c_double), C.c_void_p, C.c_float,
+                                                 C.POINTER(photic_outputs), C.c_void_p,
+                                                 C.c_void_p, C.c_void_p,
+                                                 C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                                 C.c_void_p]),
+    "photic_region_lut_default_chains": (C.c_int64, [C.POINTER(photic_config), C.c_int32,
+                                                     C.c_int32, C.c_int32]),
     "photic_depth_sigma": (C.c_int, [C.POINTER(photic_config), C.c_void_p, C.c_int64, C.c_void_p,
                                      C.POINTER(C.c_double), C.c_int32, C.c_uint64, C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -303,6 +303,72 @@ def region_fit(grid: torch.Tensor, config: Optional[Config] = None, *, n_spatial
     return out
 
 
+def region_lut_invert(grid: torch.Tensor, config: Optional[Config] = None, *,
+                      n_spatial: int = 2, n_bottoms: int = 3,
+                      theta_sun: Optional[Sequence[float]] = None, n_lut: int = 16000,
+                      n_chains: int = 0, rrs_noise=None, empirical: Optional[torch.Tensor] = None,
+                      empirical_nodata: float = -9999.0,
+                      fields: Sequence[str] = OUTPUT_FIELDS + MIX_FIELDS,
+                      stream: Optional[torch.cuda.Stream] = None) -> Dict[str, torch.Tensor]:
+    """samodel()'s pixel loop with its dynamic lookup table in the general
+    configuration (model/samodel.c:649-1352): the fit of ``region_fit``
+    (``n_spatial``, ``n_bottoms``, the scenes of a [n_scenes, nrows, ncols,
+    n_bands] grid with sun zeniths ``theta_sun``) for each pixel its table
+    cannot serve, the sorted shallow pixels cut into ``n_chains`` slices (0:
+    eight per resident warp), each run as the reference runs them on one
+    thread.  ``rrs_noise`` ([n_scenes, n_bands]) orders by the spectral
+    angle too; ``empirical`` ([nrows * ncols] float32, CUDA) is the
+    reference's empirical depth grid.  Use ``Config.reference_default()``
+    for the reference's tolerances.  Returns the outputs (P, G, X: [npix,
+    n_scenes]) plus "source", "order" and "chain_stats" as ``lut_invert``.
+    Synchronises the stream once (to size the order)."""
+    cfg = config or Config()
+    _check_cuda(grid, "grid", torch.float32)
+    g4 = grid if grid.dim() == 4 else grid.unsqueeze(0)
+    if g4.dim() != 4 or g4.shape[3] != cfg.n_bands or not g4.is_contiguous():
+        raise ValueError(f"grid must be a contiguous [(n_scenes,) nrows, ncols, {cfg.n_bands}]")
+    S, nrows, ncols = int(g4.shape[0]), int(g4.shape[1]), int(g4.shape[2])
+    npix = nrows * ncols
+    if empirical is not None:
+        _check_cuda(empirical, "empirical", torch.float32)
+        if empirical.numel() != npix or not empirical.is_contiguous():
+            raise ValueError("empirical must be a contiguous [nrows * ncols] tensor")
+    out = alloc_outputs(npix, grid.device, [f for f in fields if f != "params"],
+                        n_obs=npix * S if S > 1 else None)
+    source = torch.empty(npix, dtype=torch.int64, device=grid.device)
+    order = torch.empty(max(npix, 1), dtype=torch.int64, device=grid.device)
+    lc = L.photic_lut_config()
+    L.lib().photic_lut_config_default(C.byref(lc))
+    lc.n_lut = int(n_lut)
+    lc.n_chains = int(n_chains)
+    c = cfg.to_c()
+    th = (C.c_double * S)(*([cfg.theta_sun_deg] * S if theta_sun is None else
+                            [float(t) for t in theta_sun]))
+    noise = None
+    if rrs_noise is not None:
+        vals = [float(v) for row in rrs_noise for v in row]
+        if len(vals) != S * cfg.n_bands:
+            raise ValueError("rrs_noise must be [n_scenes, n_bands]")
+        noise = (C.c_double * len(vals))(*vals)
+    max_chains = int(n_chains) if n_chains else int(L.lib().photic_region_lut_default_chains(
+        C.byref(c), S, int(n_spatial), int(n_bottoms)))
+    stats = torch.zeros(max(1, min(max_chains, npix)), 4, dtype=torch.float64, device=grid.device)
+    os_ = _outputs_struct(out)
+    n_sh, n_ch = C.c_int64(0), C.c_int64(0)
+    L.check(L.lib().photic_region_lut_invert_batch(
+        C.byref(c), C.byref(lc), _ptr(g4), S, th, nrows, ncols, int(n_spatial), int(n_bottoms),
+        noise, _ptr(empirical), float(empirical_nodata), C.byref(os_), _ptr(source),
+        _ptr(order), _ptr(stats), C.byref(n_sh), C.byref(n_ch), _stream_handle(stream)))
+    if S > 1:
+        for f in ("P", "G", "X"):
+            if f in out:
+                out[f] = out[f].view(npix, S)
+    out["source"] = source
+    out["order"] = order[:n_sh.value]
+    out["chain_stats"] = stats[:n_ch.value]
+    return out
+
+
 def depth_sigma(rrs: torch.Tensor, depth: torch.Tensor, r_sigma: Sequence[float],
                 config: Optional[Config] = None, *, n_samples: int = 128, seed: int = 1,
                 stream: Optional[torch.cuda.Stream] = None) -> Dict[str, torch.Tensor]:

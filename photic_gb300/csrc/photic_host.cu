@@ -515,6 +515,7 @@ int photic_lut_invert_batch(const photic_config *cfg, const photic_lut_config *l
   ka.rrs = d_rrs;
   ka.npix = npix;
   ka.n_bands = nb;
+  ka.n_scenes = 1;
   ka.nodata = cfg->nodata_value;
   bool noise = lut->use_noise != 0 && nb >= 4;
   for (int b = 0; b < nb && noise; b++)
@@ -2219,10 +2220,9 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
         }
     }
   }
-  // The general fit (bottom mixtures, 3 x 3 regions, or a scene stack with
-  // empirical depths) takes scene-major grids; the plain single-pixel and
-  // joint paths take [pixel][scene][band].
-  const bool general = n_bottoms > 1 || regions || (nscenes > 1 && empirical_depth_present);
+  // The general loop (bottom mixtures, 3 x 3 regions, stacks of scenes)
+  // takes scene-major grids; the single-scene loop takes [pixel][band].
+  const bool general = n_bottoms > 1 || regions || nscenes > 1;
   std::vector<float> h_grid;
   if (general) {
     h_grid.resize(h_rrs.size());
@@ -2231,22 +2231,12 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
         for (int b = 0; b < nb; b++)
           h_grid[((size_t)k * npix + p) * nb + b] = h_rrs[((size_t)p * nscenes + k) * nb + b];
   }
-  std::vector<double> h_emp;
-  if (empirical_depth_present) {
-    h_emp.assign((size_t)npix, NAN);
-    for (int i = 0; i < nrows; i++)
-      for (int j = 0; j < ncols; j++) {
-        const float e = empirical_depths.array[i][j];
-        if (!f_close_ref(e, empirical_depths.nodata_value))  // model/samodel.c:960-967
-          h_emp[(size_t)i * ncols + j] = e > -1.0f ? 1.0 : fabs((double)e);
-      }
-  }
   // device buffers
   float *d_rrs = nullptr;
-  double *d_depth = nullptr, *d_seeds = nullptr, *d_emp = nullptr, *d_th = nullptr;
-  float *d_f = nullptr, *d_pgx = nullptr, *d_mix = nullptr;
+  double *d_depth = nullptr;
+  float *d_f = nullptr, *d_pgx = nullptr, *d_mix = nullptr, *d_raw = nullptr;
   double *d_params = nullptr;
-  int32_t *d_status = nullptr, *d_off = nullptr;
+  int32_t *d_status = nullptr;
   const bool one_by_one = nscenes == 1 && !general;
   bool ok = cudaMalloc((void **)&d_rrs, h_rrs.size() * sizeof(float)) == cudaSuccess &&
             cudaMalloc((void **)&d_depth, npix * sizeof(double)) == cudaSuccess &&
@@ -2273,60 +2263,47 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
     o.G = d_pgx + nobs;
     o.X = d_pgx + 2 * nobs;
     o.params = d_params;
-    int rc;
-    if (general) {
-      // P, G, X come out as [pixel][scene], the joint fit's layout
+    int rc = PHOTIC_OK;
+    // The reference's product path is its pixel loop with the dynamic
+    // lookup table (LUT 1, :649-1352) in every configuration, ordered by the
+    // spectral index (times the spectral angle to the scenes' R_sigma) or by
+    // the empirical depths when given (:702-767), the sorted pixels cut into
+    // chains -- PHOTIC_LUT_CHAINS of them if set (1: the reference on one
+    // thread), else eight per resident lane (one scene, one region, one
+    // bottom type) or warp (the general fit).
+    photic_lut_config lc;
+    photic_lut_config_default(&lc);
+    const char *ch = getenv("PHOTIC_LUT_CHAINS");
+    if (ch && *ch) lc.n_chains = atoll(ch);
+    if (empirical_depth_present) {
+      std::vector<float> raw((size_t)npix);
+      for (int i = 0; i < nrows; i++)
+        for (int j = 0; j < ncols; j++) raw[(size_t)i * ncols + j] = empirical_depths.array[i][j];
+      if (cudaMalloc((void **)&d_raw, npix * sizeof(float)) == cudaSuccess)
+        cudaMemcpy(d_raw, raw.data(), npix * sizeof(float), cudaMemcpyHostToDevice);
+      else
+        rc = fail(PHOTIC_ERR_NOMEM, "samodel: empirical depth grid");
+    }
+    const float emp_nodata = empirical_depth_present ? empirical_depths.nodata_value : 0.0f;
+    if (rc != PHOTIC_OK) {
+    } else if (general) {
+      // P, G, X come out as [pixel][scene]
       o.bottom_percent = d_mix;
       o.bottom_type = d_mix + 3 * npix;
-      double th[PHOTIC_MAX_SCENES];
-      for (int k = 0; k < nscenes; k++) th[k] = scene_data[scene_indexes[k]].theta_w;
-      if (!h_emp.empty()) {
-        cudaMalloc((void **)&d_emp, npix * sizeof(double));
-        cudaMemcpy(d_emp, h_emp.data(), npix * sizeof(double), cudaMemcpyHostToDevice);
+      double th[PHOTIC_MAX_SCENES], noise[PHOTIC_MAX_SCENES * PHOTIC_MAX_BANDS];
+      for (int k = 0; k < nscenes; k++) {
+        const photic_scene &sk = scene_data[scene_indexes[k]];
+        th[k] = sk.theta_w;
+        for (int b = 0; b < nb; b++) noise[k * nb + b] = sk.R_sigma[b];
       }
-      rc = photic_region_fit_batch(&cfg, d_rrs, nscenes, th, nrows, ncols, regions ? 2 : 1,
-                                   n_bottoms, d_emp, &o, 0);
-    } else if (nscenes == 1) {
-      // the reference's product path: the pixel loop with its dynamic
-      // lookup table (LUT 1, :649-1215), ordered by the spectral index or
-      // by the empirical depths when given (:702-710), the sorted pixels
-      // cut into chains -- PHOTIC_LUT_CHAINS of them if set (1: the
-      // reference on one thread), else eight per resident lane
-      photic_lut_config lc;
-      photic_lut_config_default(&lc);
-      const char *ch = getenv("PHOTIC_LUT_CHAINS");
-      if (ch && *ch) lc.n_chains = atoll(ch);
+      rc = photic_region_lut_invert_batch(&cfg, &lc, d_rrs, nscenes, th, nrows, ncols,
+                                          regions ? 2 : 1, n_bottoms, noise, d_raw, emp_nodata,
+                                          &o, nullptr, nullptr, nullptr, nullptr, nullptr, 0);
+    } else {
       lc.use_noise = 1;
       for (int b = 0; b < nb && b < PHOTIC_MAX_BANDS; b++) lc.rrs_noise[b] = s0.R_sigma[b];
-      float *d_raw = nullptr;
-      if (empirical_depth_present) {
-        std::vector<float> raw((size_t)npix);
-        for (int i = 0; i < nrows; i++)
-          for (int j = 0; j < ncols; j++) raw[(size_t)i * ncols + j] = empirical_depths.array[i][j];
-        if (cudaMalloc((void **)&d_raw, npix * sizeof(float)) == cudaSuccess)
-          cudaMemcpy(d_raw, raw.data(), npix * sizeof(float), cudaMemcpyHostToDevice);
-      }
-      if (empirical_depth_present && !d_raw) {
-        rc = fail(PHOTIC_ERR_NOMEM, "samodel: empirical depth grid");
-      } else {
-        rc = photic_lut_invert_batch(&cfg, &lc, d_rrs, npix, d_raw,
-                                     empirical_depth_present ? empirical_depths.nodata_value : 0.0f,
-                                     &o, nullptr, nullptr, nullptr, nullptr, nullptr, 0);
-        if (rc == PHOTIC_OK) rc = photic_sync(0);
-      }
-      cudaFree(d_raw);
-    } else {
-      std::vector<int32_t> offs((size_t)npix + 1);
-      std::vector<double> th((size_t)nobs);
-      for (int64_t p = 0; p <= npix; p++) offs[p] = (int32_t)(p * nscenes);
-      for (int64_t p = 0; p < npix; p++)
-        for (int k = 0; k < nscenes; k++)
-          th[(size_t)(p * nscenes + k)] = scene_data[scene_indexes[k]].theta_w;
-      cudaMalloc((void **)&d_off, offs.size() * sizeof(int32_t));
-      cudaMalloc((void **)&d_th, th.size() * sizeof(double));
-      cudaMemcpy(d_off, offs.data(), offs.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
-      cudaMemcpy(d_th, th.data(), th.size() * sizeof(double), cudaMemcpyHostToDevice);
-      rc = photic_joint_invert_batch(&cfg, d_off, d_th, d_rrs, npix, nobs, &o, 0);
+      rc = photic_lut_invert_batch(&cfg, &lc, d_rrs, npix, d_raw, emp_nodata, &o, nullptr,
+                                   nullptr, nullptr, nullptr, nullptr, 0);
     }
     if (rc == PHOTIC_OK) rc = photic_sync(0);
     if (rc == PHOTIC_OK) {
@@ -2430,10 +2407,7 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
   cudaFree(d_params);
   cudaFree(d_status);
   if (d_mix) cudaFree(d_mix);
-  if (d_emp) cudaFree(d_emp);
-  if (d_seeds) cudaFree(d_seeds);
-  if (d_off) cudaFree(d_off);
-  if (d_th) cudaFree(d_th);
+  if (d_raw) cudaFree(d_raw);
 }
 
 }  // extern "C"
@@ -2618,11 +2592,12 @@ extern "C" int photic_depth_sigma(const photic_config *cfg, const float *d_rrs, 
 // Spatial-region fit (model/samodel.c:2957-3027 with n_spatial = 2).
 // ---------------------------------------------------------------------------
 
-extern "C" int photic_region_fit_batch(const photic_config *cfg, const float *d_grid,
-                                       int32_t n_scenes, const double *theta_sun_deg,
-                                       int32_t nrows, int32_t ncols, int32_t n_spatial,
-                                       int32_t n_bottoms, const double *d_h_empirical,
-                                       const photic_outputs *out, void *stream) {
+namespace {
+
+// Checks shared by the general fit and its lookup-table loop; *nmax
+// receives the largest parameter count.
+int region_config_check(const photic_config *cfg, int32_t n_scenes, int32_t n_spatial,
+                        int32_t n_bottoms, int *nmax) {
   int rc = photic_config_check(cfg);
   if (rc) return rc;
   if (n_spatial < 1 || n_spatial > 2)
@@ -2634,12 +2609,14 @@ extern "C" int photic_region_fit_batch(const photic_config *cfg, const float *d_
   const int Rmax = n_spatial == 2 ? kRegionMaxR : 1;
   if (Rmax * n_scenes * cfg->n_bands > 128 || Rmax * n_scenes > 64)
     return fail(PHOTIC_ERR_UNSUPPORTED, "regions x scenes x bands beyond 128");
-  const int nmax = region_max_params(Rmax, n_bottoms, n_scenes);
-  if (nmax > 96) return fail(PHOTIC_ERR_UNSUPPORTED, "%d unknowns beyond 96", nmax);
-  if (nrows < 0 || ncols < 0 || !out || ((int64_t)nrows * ncols > 0 && !d_grid))
-    return fail(PHOTIC_ERR_INVALID, "bad arguments");
-  if ((int64_t)nrows * ncols == 0) return PHOTIC_OK;
-  RegionArgs a;
+  *nmax = region_max_params(Rmax, n_bottoms, n_scenes);
+  if (*nmax > 96) return fail(PHOTIC_ERR_UNSUPPORTED, "%d unknowns beyond 96", *nmax);
+  return PHOTIC_OK;
+}
+
+void region_args(const photic_config *cfg, const float *d_grid, int32_t n_scenes,
+                 const double *theta_sun_deg, int32_t nrows, int32_t ncols, int32_t n_spatial,
+                 int32_t n_bottoms, const photic_outputs *out, RegionArgs &a) {
   memset(&a, 0, sizeof a);
   make_fit(*cfg, a.fp);
   make_scene(*cfg, cfg->theta_sun_deg, a.sc);
@@ -2655,9 +2632,155 @@ extern "C" int photic_region_fit_batch(const photic_config *cfg, const float *d_
   a.n_scenes = n_scenes;
   a.n_spatial = n_spatial;
   a.n_bottoms = n_bottoms;
-  a.h_emp = d_h_empirical;
   a.out = *out;
+}
+
+// Default chains of the general loop per resident warp (one chain runs on
+// a warp): as for the single-scene loop's lanes.
+constexpr int64_t kRegionChainsPerWarp = 8;
+
+}  // namespace
+
+extern "C" int photic_region_fit_batch(const photic_config *cfg, const float *d_grid,
+                                       int32_t n_scenes, const double *theta_sun_deg,
+                                       int32_t nrows, int32_t ncols, int32_t n_spatial,
+                                       int32_t n_bottoms, const double *d_h_empirical,
+                                       const photic_outputs *out, void *stream) {
+  int nmax = 0;
+  int rc = region_config_check(cfg, n_scenes, n_spatial, n_bottoms, &nmax);
+  if (rc) return rc;
+  if (nrows < 0 || ncols < 0 || !out || ((int64_t)nrows * ncols > 0 && !d_grid))
+    return fail(PHOTIC_ERR_INVALID, "bad arguments");
+  if ((int64_t)nrows * ncols == 0) return PHOTIC_OK;
+  RegionArgs a;
+  region_args(cfg, d_grid, n_scenes, theta_sun_deg, nrows, ncols, n_spatial, n_bottoms, out, a);
+  a.h_emp = d_h_empirical;
   return run_region(a, nmax, cfg->blocks_per_sm, (cudaStream_t)stream);
+}
+
+
+extern "C" int64_t photic_region_lut_default_chains(const photic_config *cfg, int32_t n_scenes,
+                                                    int32_t n_spatial, int32_t n_bottoms) {
+  int nmax = 0;
+  if (region_config_check(cfg, n_scenes, n_spatial, n_bottoms, &nmax)) return 0;
+  unsigned int *err = nullptr;
+  int sms = 0;
+  if (device_state(&err, &sms)) return 0;
+  RegionArgs a;
+  memset(&a, 0, sizeof a);
+  make_fit(*cfg, a.fp);
+  int64_t warps = 0;
+  if (launch_region(a, nmax, sms, cfg->blocks_per_sm, 0, &warps) != cudaSuccess) return 0;
+  return kRegionChainsPerWarp * warps;
+}
+
+extern "C" int photic_region_lut_invert_batch(
+    const photic_config *cfg, const photic_lut_config *lut, const float *d_grid, int32_t n_scenes,
+    const double *theta_sun_deg, int32_t nrows, int32_t ncols, int32_t n_spatial,
+    int32_t n_bottoms, const double *rrs_noise, const float *d_empirical, float empirical_nodata,
+    const photic_outputs *out, int64_t *d_source, int64_t *d_order, double *d_chain_stats,
+    int64_t *n_shallow, int64_t *n_chains_used, void *stream) {
+  int nmax = 0;
+  int rc = region_config_check(cfg, n_scenes, n_spatial, n_bottoms, &nmax);
+  if (rc) return rc;
+  if (n_shallow) *n_shallow = 0;
+  if (n_chains_used) *n_chains_used = 0;
+  if (!lut) return fail(PHOTIC_ERR_INVALID, "NULL lookup-table configuration");
+  if (lut->n_lut < 1 || lut->n_chains < 0)
+    return fail(PHOTIC_ERR_INVALID, "n_lut must be >= 1 and n_chains >= 0");
+  if (cfg->precision != PHOTIC_PREC_FP64)
+    return fail(PHOTIC_ERR_UNSUPPORTED, "the lookup-table loop runs in FP64 only");
+  if (nrows < 0 || ncols < 0) return fail(PHOTIC_ERR_INVALID, "nrows / ncols < 0");
+  const int64_t npix = (int64_t)nrows * ncols;
+  if (npix == 0) return PHOTIC_OK;
+  if (!d_grid || !out) return fail(PHOTIC_ERR_INVALID, "NULL input or output");
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned int *err = nullptr;
+  int sms = 0;
+  rc = device_state(&err, &sms);
+  if (rc) return rc;
+  const int nb = cfg->n_bands;
+  RegionArgs a;
+  region_args(cfg, d_grid, n_scenes, theta_sun_deg, nrows, ncols, n_spatial, n_bottoms, out, a);
+  a.error = err;
+  a.source = d_source;
+  a.chain_stats = d_chain_stats;
+  a.emp = d_empirical;
+  a.emp_nodata = empirical_nodata;
+
+  // the order (model/samodel.c:701-819): keys summed over the scenes
+  LutKeyArgs ka;
+  memset(&ka, 0, sizeof ka);
+  ka.rrs = d_grid;
+  ka.npix = npix;
+  ka.n_bands = nb;
+  ka.n_scenes = n_scenes;
+  ka.general = 1;
+  ka.nodata = cfg->nodata_value;
+  bool noise = rrs_noise != nullptr && nb >= 4;
+  for (int k = 0; k < n_scenes * nb && noise; k++)
+    if (rrs_noise[k] < 1.0e-6) noise = false;  // :590-600
+  ka.use_noise = noise ? 1 : 0;
+  for (int c = 0; c < 3 && noise; c++) {
+    double t = 0.0;
+    for (int k = 0; k < n_scenes; k++) t += rrs_noise[k * nb + c + 1];  // :752-756
+    ka.noise[c] = t;
+  }
+  ka.out = *out;
+  ka.source = d_source;
+  ka.emp = d_empirical;
+  int64_t *order = d_order;
+  cudaError_t e = cudaSuccess;
+  if (!order) {
+    e = cudaMallocAsync((void **)&order, npix * sizeof(int64_t), s);
+    if (e != cudaSuccess) return fail(PHOTIC_ERR_NOMEM, "order: %s", cudaGetErrorString(e));
+  }
+  int64_t S = 0;
+  e = lut_order(ka, order, &S, s);
+  if (e != cudaSuccess) {
+    if (!d_order) cudaFreeAsync(order, s);
+    return cuda_fail(e, "lookup-table order");
+  }
+  if (S > 0) {
+    int64_t warps = 0;
+    e = launch_region(a, nmax, sms, cfg->blocks_per_sm, s, &warps);
+    if (e != cudaSuccess || warps < 1) {
+      if (!d_order) cudaFreeAsync(order, s);
+      return fail(PHOTIC_ERR_CUDA, "region kernel does not fit on the device");
+    }
+    int64_t C = lut->n_chains ? lut->n_chains : kRegionChainsPerWarp * warps;
+    if (C > S) C = S;
+    const int64_t per_chain = (S + C - 1) / C;
+    const int64_t cap = per_chain < lut->n_lut ? per_chain : (int64_t)lut->n_lut;
+    a.order = order;
+    a.n_shallow = S;
+    a.n_chains = C;
+    a.cap = cap;
+    a.entry_stride = region_entry_stride(n_scenes);
+    unsigned long long *queue = nullptr;
+    e = cudaMallocAsync((void **)&a.ring, (size_t)C * cap * a.entry_stride * sizeof(double), s);
+    if (e == cudaSuccess)
+      e = cudaMallocAsync((void **)&a.ring_src, (size_t)C * cap * sizeof(int64_t), s);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)&queue, sizeof *queue, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(queue, 0, sizeof *queue, s);
+    if (e == cudaSuccess && d_chain_stats)
+      e = cudaMemsetAsync(d_chain_stats, 0, (size_t)C * 4 * sizeof(double), s);
+    if (e == cudaSuccess) {
+      a.queue = queue;
+      e = launch_region(a, nmax, sms, cfg->blocks_per_sm, s);
+    }
+    cudaFreeAsync(a.ring, s);
+    cudaFreeAsync(a.ring_src, s);
+    cudaFreeAsync(queue, s);
+    if (e != cudaSuccess) {
+      if (!d_order) cudaFreeAsync(order, s);
+      return cuda_fail(e, "lookup-table region kernel");
+    }
+    if (n_chains_used) *n_chains_used = C;
+  }
+  if (!d_order) cudaFreeAsync(order, s);
+  if (n_shallow) *n_shallow = S;
+  return PHOTIC_OK;
 }
 
 extern "C" int photic_region_invert_batch(const photic_config *cfg, const float *d_grid,

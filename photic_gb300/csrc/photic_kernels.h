@@ -49,12 +49,14 @@ int guarded_blocks_per_sm(const InvertArgs &a, int block);
 
 // samodel()'s pixel loop with the dynamic lookup table (photic_lut.cu).
 struct LutKeyArgs {
-  const float *rrs;  // [npix][n_bands]
+  const float *rrs;  // [n_scenes][npix][n_bands]
   int64_t npix;
   int32_t n_bands;
+  int32_t n_scenes;    // the keys sum blue, green and red over the scenes
+  int32_t general;     // masked outputs in the region fit's layout (P, G, X per scene)
   float nodata;
-  int32_t use_noise;   // order by index x spectral angle to noise[] (blue, green, red)
-  double noise[3];
+  int32_t use_noise;   // order by index x spectral angle to noise[] (blue, green, red,
+  double noise[3];     // each summed over the scenes)
   const float *emp;    // optional [npix] empirical depths: the key itself
   photic_outputs out;  // masked pixels' outputs are written here
   int64_t *source;     // optional [npix]: -2 for masked pixels
@@ -283,16 +285,33 @@ struct RegionArgs {
   double *eval_det;             // [npix][8]: Rrs error, model error, albedo, the last
                                 // scene's K_min (the cost's), IOD, K_min over all
                                 // scenes (the post-fit product's)
-  unsigned long long *queue;    // work-queue head (zeroed)
+  unsigned long long *queue;    // work-queue head (zeroed): pixels, or chains
   photic_outputs out;           // per pixel (P, G, X: [npix][n_scenes]); status carries
                                 // the region count << 24
   unsigned int *error;
+  // chain mode (samodel()'s pixel loop with its lookup table, grid mode):
+  // the sorted shallow pixels cut into n_chains contiguous slices, one warp
+  // per slice at a time
+  const int64_t *order;         // [n_shallow]; NULL: every pixel from the queue
+  int64_t n_shallow, n_chains, cap;  // cap: table slots per chain
+  int32_t entry_stride;         // doubles per table entry
+  double *ring;                 // [n_chains][cap][entry_stride]
+  int64_t *ring_src;            // [n_chains][cap]: the pixel whose fit an entry holds
+  int64_t *source;              // optional [npix]: -1 fitted, else the serving pixel
+  double *chain_stats;          // optional [n_chains][4]: served, fitted, match, entry
+  const float *emp;             // optional [npix] empirical depths (emp_nodata: none)
+  float emp_nodata;
 };
+// Doubles of one table entry of the general loop: region count, depth,
+// K_min, P, G, X per scene, modelled Rrs of bands 1..3 per region and scene.
+constexpr int region_entry_stride(int n_scenes) { return 3 + 3 * n_scenes + 27 * n_scenes; }
 // Parameters of a fit with up to max_regions regions, n_bottoms types and
 // n_scenes scenes.
 int region_max_params(int max_regions, int n_bottoms, int n_scenes);
+// warps: when non-NULL, no launch -- the number of resident warps of the
+// kernel that max_params selects is returned there.
 cudaError_t launch_region(const RegionArgs &a, int max_params, int sms, int per_sm,
-                          cudaStream_t s);
+                          cudaStream_t s, int64_t *warps = nullptr);
 
 // Depth uncertainty by re-inversion of perturbed samples (photic_aux.cu).
 constexpr int kDsMaxIntervals = 120;  // 30 m in 0.25 m steps

@@ -72,28 +72,59 @@ __device__ __forceinline__ bool ref_approx_eq(float a, float b, float eps) {
 // ---------------------------------------------------------------------------
 // Order
 // ---------------------------------------------------------------------------
+// The masked outputs of the general loop: the region fit's layout, with P,
+// G, X per scene and the bottom shares.
+__device__ void write_masked_general(const photic_outputs &o, int64_t p, int S) {
+  if (o.depth) o.depth[p] = 0.0f;
+  if (o.depth_f64) o.depth_f64[p] = 0.0;
+  for (int s = 0; s < S; s++) {
+    if (o.P) o.P[p * S + s] = 0.0f;
+    if (o.G) o.G[p * S + s] = 0.0f;
+    if (o.X) o.X[p * S + s] = 0.0f;
+  }
+  if (o.bottom_albedo) o.bottom_albedo[p] = 0.0f;
+  if (o.model_error) o.model_error[p] = 0.0f;
+  if (o.rrs_error) o.rrs_error[p] = 0.0f;
+  if (o.K_min) o.K_min[p] = 0.0f;
+  if (o.iod) o.iod[p] = 0.0f;
+  if (o.evals) o.evals[p] = 0;
+  if (o.evals_kept) o.evals_kept[p] = 0;
+  if (o.status) o.status[p] = PHOTIC_PX_MASKED;
+  if (o.bottom_percent)
+    for (int k = 0; k < 3; k++) o.bottom_percent[p * 3 + k] = 0.0f;
+  if (o.bottom_type) o.bottom_type[p] = 0.0f;
+}
+
 __global__ void lut_key_kernel(LutKeyArgs a) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= a.npix) return;
-  const float *r = a.rrs + p * a.n_bands;
+  const int S = a.n_scenes;
   bool masked = false;
-  for (int b = 0; b < a.n_bands; b++)
-    if (band_masked(r[b], a.nodata)) masked = true;
+  for (int s = 0; s < S; s++) {  // every band of every scene (:933-947)
+    const float *r = a.rrs + (s * a.npix + p) * a.n_bands;
+    for (int b = 0; b < a.n_bands; b++)
+      if (band_masked(r[b], a.nodata)) masked = true;
+  }
   a.flags[p] = masked ? 0 : 1;
   a.idx[p] = p;
   if (masked) {
-    write_masked(a.out, p);
+    if (a.general) write_masked_general(a.out, p, S);
+    else write_masked(a.out, p);
     if (a.source) a.source[p] = -2;
   }
   if (a.emp) {  // the empirical depth itself (:708-710)
     a.keys[p] = a.emp[p];
     return;
   }
-  // :711-745 -- float sums, squares and root in double, stored as float
+  // :711-745 -- float sums over the scenes, squares and root in double,
+  // stored as float
   float bs = 0.0f, gs = 0.0f, rs = 0.0f;
-  if (a.n_bands > 1 && !ref_approx_eq(r[1], a.nodata, 1.0e-6f)) bs = __fadd_rn(bs, r[1]);
-  if (a.n_bands > 2 && !ref_approx_eq(r[2], a.nodata, 1.0e-6f)) gs = __fadd_rn(gs, r[2]);
-  if (a.n_bands > 3 && !ref_approx_eq(r[3], a.nodata, 1.0e-6f)) rs = __fadd_rn(rs, r[3]);
+  for (int s = 0; s < S; s++) {
+    const float *r = a.rrs + (s * a.npix + p) * a.n_bands;
+    if (a.n_bands > 1 && !ref_approx_eq(r[1], a.nodata, 1.0e-6f)) bs = __fadd_rn(bs, r[1]);
+    if (a.n_bands > 2 && !ref_approx_eq(r[2], a.nodata, 1.0e-6f)) gs = __fadd_rn(gs, r[2]);
+    if (a.n_bands > 3 && !ref_approx_eq(r[3], a.nodata, 1.0e-6f)) rs = __fadd_rn(rs, r[3]);
+  }
   const double b2 = __dmul_rn((double)bs, (double)bs), g2 = __dmul_rn((double)gs, (double)gs),
                r2 = __dmul_rn((double)rs, (double)rs);
   float key = (float)sqrt(__dadd_rn(__dadd_rn(b2, g2), r2));

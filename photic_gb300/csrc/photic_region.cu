@@ -41,6 +41,9 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kMaxR = kRegionMaxR, kTerms = 128, kHT = kTerms / 32, kShares = 32, kRS = 64;
+// chain mode, per warp: the measured bands 1..3 of every region and scene,
+// the modelled Rrs of the final evaluation, the chain's P, G, X and state
+constexpr int kChainD = 3 * kRS + kTerms + 3 * kMaxScenes + 24;
 
 // Launch shapes: C coordinates per lane, vertex row stride CG.
 template <int C, int CG>
@@ -50,9 +53,10 @@ struct Shape {
   // doubles of shared memory per warp: vertices (n+1) x CG, per-lane vertex
   // costs, the evaluation point, band terms (residual^2, K, bottom share of
   // the reflectance), per-region Rrs(490/550/640), final details and
-  // per-(region, bottom) shares of the bottom-continuity term
+  // per-(region, bottom) shares of the bottom-continuity term, and the
+  // chain mode's arrays
   static constexpr int kSmem =
-      (kMaxN + 1) * CG + kNF * 32 + 32 * C + 3 * kTerms + 3 * kRS + 8 + kShares;
+      (kMaxN + 1) * CG + kNF * 32 + 32 * C + 3 * kTerms + 3 * kRS + 8 + kShares + kChainD;
 };
 
 __device__ __forceinline__ bool nodata_value(float v, float nodata) {
@@ -117,8 +121,157 @@ __device__ __forceinline__ void write_masked(const photic_outputs &o, int64_t p,
   if (o.bottom_type) o.bottom_type[p] = 0.0f;
 }
 
+// ---- chain mode: samodel()'s loop with its lookup table (model/samodel.c:
+// 649-1352) over the region fit.  A warp runs one chain (a contiguous slice
+// of the sorted shallow pixels) as one thread of the reference runs its
+// pixels: the table scan by the 32 lanes, a served pixel's outputs copied
+// from its entry's pixel, a fit hot-started from the previous pixel when the
+// last two were continuous, the entry and the adaptive thresholds.
+//
+// The chain's state, in the warp's shared memory, written by lane 0:
+enum : int { G_DEPTH, G_KMIN, G_DPREV, G_KPREV, G_HEMP, G_MATCH, G_ENTRY, G_NMOD, G_NSKIP,
+             G_TOTME, G_ERRTOT, G_ERRCNT, G_NOPT, G_TOTLUT, G_NCOMP, G_NPREV, G_HOT, G_K,
+             G_KBEG, G_KEND, G_CHAIN, G_COUNT };
+static_assert(G_COUNT <= 24, "chain state");
+constexpr double kEps = (double)1.0e-4f;  // the reference's float epsilon (model/common.c:93)
+constexpr double kContinuity = 0.1;       // :981
+constexpr double kMinThreshold = 1.5;     // :892
+constexpr double kMaxSkip = 0.9925;       // :880
+
+// A new chain c (:871-899): empty table, thresholds MAX(1.5, 1.125 S), no
+// previous pixel; h_empirical, which the reference leaves unset until a
+// pixel with an empirical depth, is 0 (every bottom type fitted).
+__device__ __forceinline__ void chain_begin(const RegionArgs &a, double *cst, double *cprev,
+                                            int64_t c, int S) {
+  for (int k = 0; k < G_COUNT; k++) cst[k] = 0.0;
+  const double m0 = 1.125 * (double)S;
+  cst[G_MATCH] = m0 > kMinThreshold ? m0 : kMinThreshold;
+  cst[G_ENTRY] = cst[G_MATCH];
+  cst[G_CHAIN] = (double)c;
+  cst[G_KBEG] = (double)(c * a.n_shallow / a.n_chains);
+  cst[G_KEND] = (double)((c + 1) * a.n_shallow / a.n_chains);
+  cst[G_K] = cst[G_KBEG];
+  for (int i = 0; i < 3 * kMaxScenes; i++) cprev[i] = 0.0;
+}
+
+// After a pixel, served or fitted (:1102-1211, the statistics restarting at
+// every update, :1326-1352): the hot-start decision, the previous pixel,
+// the thresholds every 0.1 % of the chain.  Lane 0.
+__device__ __forceinline__ void chain_post(const RegionArgs &a, double *cst, double me) {
+  const double depth = cst[G_DEPTH], kmin = cst[G_KMIN];
+  const double dprev = cst[G_DPREV], kprev = cst[G_KPREV];
+  cst[G_HOT] = (fabs(depth - dprev) / (kEps + dprev) < kContinuity &&
+                fabs(kmin - kprev) / (kEps + kprev) < kContinuity)
+                   ? 1.0
+                   : 0.0;
+  cst[G_DPREV] = depth;
+  cst[G_KPREV] = kmin;
+  cst[G_TOTME] = cst[G_TOTME] + me;
+  cst[G_NMOD] = cst[G_NMOD] + 1.0;
+  cst[G_NCOMP] += 1.0;
+  const int nperc = (int)((1000.0 * cst[G_NCOMP]) / (cst[G_KEND] - cst[G_KBEG]));
+  if ((double)nperc > cst[G_NPREV]) {
+    double match = cst[G_MATCH], entry = cst[G_ENTRY];
+    const double n_mod = cst[G_NMOD];
+    if (cst[G_NOPT] > 0.0) {
+      const double cnt = cst[G_ERRCNT];
+      // vec_mean2_double (model/common.c:877-891) returns a float
+      const double error_mean = (double)(float)(cnt > 0.0 ? cst[G_ERRTOT] / cnt : 0.0);
+      match = match + (0.75 * error_mean + (0.25 * cst[G_TOTME]) / n_mod);
+      match = match / 2.0;
+      entry = match;
+    }
+    if (cst[G_NSKIP] / n_mod > kMaxSkip) {
+      match = match * 0.75;
+      entry = entry * 0.75;
+    }
+    cst[G_MATCH] = kMinThreshold > match ? kMinThreshold : match;
+    cst[G_ENTRY] = kMinThreshold > entry ? kMinThreshold : entry;
+    cst[G_NPREV] = (double)nperc;
+    cst[G_TOTME] = 0.0;
+    cst[G_NMOD] = 0.0;
+    cst[G_NSKIP] = 0.0;
+    cst[G_NOPT] = 0.0;
+    cst[G_ERRTOT] = 0.0;
+    cst[G_ERRCNT] = 0.0;
+  }
+  cst[G_K] += 1.0;
+  if (a.chain_stats) {
+    const int64_t c = (int64_t)cst[G_CHAIN];
+    a.chain_stats[c * 4 + 2] = cst[G_MATCH];
+    a.chain_stats[c * 4 + 3] = cst[G_ENTRY];
+  }
+}
+
+// model_spectral_diff_mean (model/samodel.c:2792-2842): bands 1..3 below
+// n_bands, the measured (meas, scene-major) and the entry's modelled Rrs
+// (rm, region-major) averaged over the scenes and regions where both are
+// non-zero; the square by a multiply where the reference calls pow(x, 2).
+__device__ __forceinline__ float glut_diff(const double *meas, const double *rm, int R, int S,
+                                           int nb) {
+  double error = 0.0;
+  int n_total = 0;
+  for (int k = 1; k <= 3; k++) {
+    if (k >= nb) break;
+    double current = 0.0, previous = 0.0, nobs = 0.0;
+    for (int s = 0; s < S; s++)
+      for (int r = 0; r < R; r++) {
+        const double mv = meas[(s * R + r) * 3 + k - 1], lv = rm[(r * S + s) * 3 + k - 1];
+        if ((float)mv != 0.0f && (float)lv != 0.0f) {
+          current = current + mv;
+          previous = previous + lv;
+          nobs = nobs + 1.0;
+        }
+      }
+    if (nobs > 0.5) {
+      current = current / nobs;
+      previous = previous / nobs;
+    }
+    const double t = (current - previous) / current;
+    error = error + t * t;
+    n_total++;
+  }
+  error = 100.0 * sqrt(error / (double)n_total);
+  return (float)error;
+}
+
+// A served pixel's outputs (partial_copy_md, model/samodel.c:3031-3139, then
+// the grids of :1118-1166): those of the pixel whose fit the entry holds,
+// with the spectral difference as model error; the lanes copy one field
+// each.
+__device__ __noinline__ void serve_copy(const RegionArgs &a, int64_t p, int64_t src, float diff,
+                                        int S, int lane) {
+  const photic_outputs &o = a.out;
+  for (int f = lane; f < 15 + 3 * S; f += 32) {
+    if (f == 0) { if (o.depth) o.depth[p] = o.depth[src]; }
+    else if (f == 1) { if (o.depth_f64) o.depth_f64[p] = o.depth_f64[src]; }
+    else if (f == 2) { if (o.bottom_albedo) o.bottom_albedo[p] = o.bottom_albedo[src]; }
+    else if (f == 3) { if (o.model_error) o.model_error[p] = diff; }
+    else if (f == 4) { if (o.rrs_error) o.rrs_error[p] = o.rrs_error[src]; }
+    else if (f == 5) { if (o.K_min) o.K_min[p] = o.K_min[src]; }
+    else if (f == 6) { if (o.iod) o.iod[p] = o.iod[src]; }
+    else if (f == 7) { if (o.evals) o.evals[p] = 0; }
+    else if (f == 8) { if (o.evals_kept) o.evals_kept[p] = 0; }
+    else if (f == 9) {
+      if (o.status)
+        o.status[p] = PHOTIC_PX_FITTED | PHOTIC_PX_SERVED |
+                      (o.status[src] & (PHOTIC_PX_CONVERGED | (0xF << 24)));
+    } else if (f == 10) { if (a.source) a.source[p] = src; }
+    else if (f == 11) { if (o.bottom_type) o.bottom_type[p] = o.bottom_type[src]; }
+    else if (f < 15) {
+      if (o.bottom_percent) o.bottom_percent[p * 3 + f - 12] = o.bottom_percent[src * 3 + f - 12];
+    } else {
+      const int j = f - 15, s = j % S;
+      float *v = j < S ? o.P : (j < 2 * S ? o.G : o.X);
+      if (v) v[p * S + s] = v[src * S + s];
+    }
+  }
+}
+
+// (One block per SM as the launch bound's minimum: without it the compiler
+// held the kernel to 128 registers and spilled.)
 template <int C, int CG, int BLOCK>
-__global__ void __launch_bounds__(BLOCK) region_kernel(const __grid_constant__ RegionArgs a) {
+__global__ void __launch_bounds__(BLOCK, 1) region_kernel(const __grid_constant__ RegionArgs a) {
   using Sh = Shape<C, CG>;
   constexpr int kMaxN = Sh::kMaxN, kNF = Sh::kNF;
   extern __shared__ double smem[];
@@ -132,6 +285,8 @@ __global__ void __launch_bounds__(BLOCK) region_kernel(const __grid_constant__ R
          *kk = dd + kTerms, *io = kk + kTerms, *s490 = io + kTerms, *s550 = s490 + kRS,
          *s640 = s550 + kRS, *misc = s640 + kRS;
   double *share = misc + 8;
+  double *meas = share + kShares, *rmv = meas + 3 * kRS, *cprev = rmv + kTerms,
+         *cst = cprev + 3 * kMaxScenes;
   const bool list = a.list_R != nullptr;
   // spectrum of scene s of region slot q (a pixel index of the grid, or a
   // region row of the list)
@@ -149,46 +304,157 @@ __global__ void __launch_bounds__(BLOCK) region_kernel(const __grid_constant__ R
   m.nrt = 6;
 
   const double early = fp.early_exit_per_scene * (double)(float)S;
+  const double kNaN = __longlong_as_double(0x7ff8000000000000LL);
+  const bool chained = a.order != nullptr;
+  if (chained) {
+    if (lane == 0) {
+      cst[G_K] = 0.0;
+      cst[G_KEND] = 0.0;
+    }
+    __syncwarp();
+  }
 
   for (;;) {
-    unsigned long long t = 0;
-    if (lane == 0) t = atomicAdd(a.queue, 1ull);
-    t = __shfl_sync(kFull, t, 0);
-    if (t >= (unsigned long long)a.npix) break;
-    const int64_t p = (int64_t)t;
-
-    // the pixel loop's mask test on the centre, every scene
-    // (model/samodel.c:933-947); samodel_optimise called directly has none
-    if (!a.no_mask) {
-      bool masked = false;
-      for (int s = 0; s < S; s++)
-        for (int b = 0; b < nb; b++) {
-          const float v = spec(p, s)[b];
-          if (nodata_value(v, fp.nodata) || v < 0.0f) masked = true;
-        }
-      if (masked) {
-        if (lane == 0) write_masked(o, p, S, PHOTIC_PX_MASKED);
-        continue;
-      }
-    }
-
-    // ---- set-up: regions, bottom types, per-term inputs
+    int64_t p = 0;
     int64_t rp[kMaxR];
-    int origin = 0;
-    const int R = regions_of(a, p, rp, origin);
-    int nbt = a.n_bottoms;
-    double hemp = __longlong_as_double(0x7ff8000000000000LL);
-    if (a.h_emp) {
-      hemp = a.h_emp[p];
-      if (!isnan(hemp) && hemp > 8.0) nbt = 1;  // model/samodel.c:1781, 1826-1830
+    int origin = 0, R = 0;
+    bool hot = false;
+    // the depth start (NaN: the cold starts) and the depth that picks sand
+    // alone above 8 m (model/samodel.c:1781, 1826-1830)
+    double hemp = kNaN, hbot = kNaN;
+    if (chained) {
+      // ---- the chain's next pixel that its table cannot serve
+      bool done = false;
+      for (;;) {
+        if (cst[G_K] >= cst[G_KEND]) {
+          unsigned long long c = 0;
+          if (lane == 0) c = atomicAdd(a.queue, 1ull);
+          c = __shfl_sync(kFull, c, 0);
+          if (c >= (unsigned long long)a.n_chains) {
+            done = true;
+            break;
+          }
+          __syncwarp();
+          if (lane == 0) chain_begin(a, cst, cprev, (int64_t)c, S);
+          __syncwarp();
+          continue;
+        }
+        p = a.order[(int64_t)cst[G_K]];
+        R = regions_of(a, p, rp, origin);
+        // the pixel's empirical depth (:955-976)
+        bool emp_present = false;
+        double h_emp = 0.0;
+        if (a.emp) {
+          const float e = a.emp[p];
+          if (!nodata_value(e, a.emp_nodata)) {
+            emp_present = true;
+            h_emp = (double)e > -1.0 ? 1.0 : fabs((double)e);
+          }
+        }
+        // measured bands 1..3 of every region and scene, scene-major
+        for (int t = lane; t < R * S * 3; t += 32) {
+          const int s = t / (R * 3), r = (t / 3) % R, k = t % 3 + 1;
+          meas[t] = k < nb ? (double)spec(rp[r], s)[k] : 0.0;
+        }
+        __syncwarp();
+        if (lane == 0 && a.emp) {
+          if (emp_present) cst[G_HEMP] = h_emp;
+          else cst[G_HOT] = 0.0;
+        }
+        // lookup (:980-999): among the entries with the pixel's region
+        // count and within 10 % of the previous pixel's depth and K_min,
+        // the first slot of least spectral difference
+        const int64_t c = (int64_t)cst[G_CHAIN];
+        const int64_t tl = (int64_t)cst[G_TOTLUT];
+        const int64_t n_in = tl < a.cap ? tl : a.cap;
+        const double dep = cst[G_DEPTH], km = cst[G_KMIN];
+        const double *ring = a.ring + (size_t)c * a.cap * a.entry_stride;
+        double bestd = 1.0e4;
+        int64_t pos = 0;
+        for (int64_t j = lane; j < n_in; j += 32) {
+          const double *e = ring + j * a.entry_stride;
+          if ((int)e[0] == R && fabs(e[1] - dep) / (dep + kEps) < kContinuity &&
+              fabs(e[2] - km) / (km + kEps) < kContinuity) {
+            const double d = (double)glut_diff(meas, e + 3 + 3 * S, R, S, nb);
+            if (d < bestd) {
+              bestd = d;
+              pos = j;
+            }
+          }
+        }
+#pragma unroll
+        for (int w = 16; w > 0; w >>= 1) {
+          const double ob = __shfl_xor_sync(kFull, bestd, w);
+          const int64_t op = __shfl_xor_sync(kFull, pos, w);
+          if (ob < bestd || (ob == bestd && op < pos)) {
+            bestd = ob;
+            pos = op;
+          }
+        }
+        __syncwarp();
+        if (bestd > cst[G_MATCH] || n_in == 0) {
+          // a fit (:1008-1063), hot when the last two pixels were
+          // continuous (:2234-2241: the empirical depth keeps its start)
+          hot = cst[G_HOT] != 0.0;
+          hbot = cst[G_HEMP];
+          hemp = emp_present ? h_emp : (hot ? cst[G_DPREV] : kNaN);
+          break;
+        }
+        // served (:1066-1073): the entry's pixel's outputs
+        const int64_t src = a.ring_src[(size_t)c * a.cap + pos];
+        const double *e = ring + pos * a.entry_stride;
+        serve_copy(a, p, src, (float)bestd, S, lane);
+        for (int i = lane; i < 3 * S; i += 32) cprev[i] = e[3 + i];
+        __syncwarp();
+        if (lane == 0) {
+          cst[G_DPREV] = cst[G_DEPTH];
+          cst[G_KPREV] = cst[G_KMIN];
+          cst[G_DEPTH] = e[1];
+          cst[G_KMIN] = e[2];
+          cst[G_NSKIP] = cst[G_NSKIP] + 1.0;
+          if (a.chain_stats) a.chain_stats[c * 4 + 0] += 1.0;
+          chain_post(a, cst, bestd);
+        }
+        __syncwarp();
+      }
+      if (done) break;
+    } else {
+      unsigned long long t = 0;
+      if (lane == 0) t = atomicAdd(a.queue, 1ull);
+      t = __shfl_sync(kFull, t, 0);
+      if (t >= (unsigned long long)a.npix) break;
+      p = (int64_t)t;
+
+      // the pixel loop's mask test on the centre, every scene
+      // (model/samodel.c:933-947); samodel_optimise called directly has none
+      if (!a.no_mask) {
+        bool masked = false;
+        for (int s = 0; s < S; s++)
+          for (int b = 0; b < nb; b++) {
+            const float v = spec(p, s)[b];
+            if (nodata_value(v, fp.nodata) || v < 0.0f) masked = true;
+          }
+        if (masked) {
+          if (lane == 0) write_masked(o, p, S, PHOTIC_PX_MASKED);
+          continue;
+        }
+      }
+      R = regions_of(a, p, rp, origin);
+      if (a.h_emp) hemp = hbot = a.h_emp[p];
     }
+
+    // ---- set-up: bottom types, per-term inputs
+    int nbt = a.n_bottoms;
+    if (!isnan(hbot) && hbot > 8.0) nbt = 1;  // model/samodel.c:1781, 1826-1830
     const int N = R + 2 * nbt * R + 3 * S, nterm = R * S * nb;
     const int qo = R + R * nbt, off = R + 2 * nbt * R;
     if (R < 1 || N > kMaxN || nterm > kTerms || R * S > kRS) {
       if (lane == 0) {
         atomicOr(a.error, PHOTIC_DEVERR_EVAL_CAP);
         write_masked(o, p, S, PHOTIC_PX_INVALID);
+        if (chained) cst[G_K] += 1.0;
       }
+      __syncwarp();
       continue;
     }
     m.nrt = N;
@@ -277,6 +543,10 @@ __global__ void __launch_bounds__(BLOCK) region_kernel(const __grid_constant__ R
           st = j == 0 ? P : j == 1 ? 1.5 * P : 100.0 * 30.0 * fp.aw640 * m640;
           sp = 2.0 * st;
         }
+        if (hot && c >= off && c < N) {  // the previous fit's P, G, X (:2288-2309)
+          st = cprev[c - off];
+          sp = 2.0 * st;
+        }
         m.start[tt] = st;
         m.step[tt] = sp;
       }
@@ -290,7 +560,7 @@ __global__ void __launch_bounds__(BLOCK) region_kernel(const __grid_constant__ R
     double lowest = 1.0e4, best[C];
 #pragma unroll
     for (int tt = 0; tt < C; tt++) best[tt] = 0.0;
-    bool final_eval = eval_only;
+    bool final_eval = eval_only, fitted = false;
     if (eval_only) {
       for (int c = lane; c < N; c += 32) X[c] = a.eval_params[p * a.eval_stride + c];
     } else {
@@ -351,6 +621,7 @@ __global__ void __launch_bounds__(BLOCK) region_kernel(const __grid_constant__ R
         if (final_eval) {
           io[tau] = rrs_B / rrs;
           if (eval_only && a.eval_rm) a.eval_rm[((p * kMaxR + r) * S + s) * nb + b] = Rm;
+          if (chained) rmv[tau] = Rm;
         }
       }
       // each (region, bottom) share |100 B| |q| / sum |q| on its own lane
@@ -474,6 +745,7 @@ __global__ void __launch_bounds__(BLOCK) region_kernel(const __grid_constant__ R
             else depth += h;
           }
           depth /= ow + ((double)R) - 1.0;
+          misc[6] = depth;
           // bottom shares of the origin region and the bottom type
           // (model/samodel.c:2021-2047)
           double qs = 0.0, pct[3] = {0.0, 0.0, 0.0}, largest = 0.0, type = 0.0;
@@ -508,10 +780,11 @@ __global__ void __launch_bounds__(BLOCK) region_kernel(const __grid_constant__ R
           if (o.bottom_type) o.bottom_type[p] = (float)type;
           if (o.status)
             o.status[p] = PHOTIC_PX_FITTED | (kept_fault == 0 ? PHOTIC_PX_CONVERGED : 0) |
-                          (kept_start << 16) | (R << 24);
+                          (hot ? PHOTIC_PX_HOT : 0) | (kept_start << 16) | (R << 24);
         }
         if (a.list_params)
           for (int c = lane; c < N; c += 32) a.list_params[p * a.eval_stride + c] = X[c];
+        fitted = true;
         break;
       }
       if (++guard > guard_cap) {
@@ -551,11 +824,59 @@ __global__ void __launch_bounds__(BLOCK) region_kernel(const __grid_constant__ R
       }
     }
     __syncwarp();
+    if (chained) {
+      // the fit's P, G, X for the next hot start (:2086-2099); the entry
+      // (:1035-1063): region count, depth, K_min, P, G, X and the modelled
+      // Rrs of bands 1..3 when the model error is below the entry
+      // threshold and the depth below 32 m, into the oldest slot
+      const int64_t c = (int64_t)cst[G_CHAIN];
+      const double depth = misc[6], kmin = misc[3], me = misc[1];
+      const bool ins = fitted && me < cst[G_ENTRY] && depth < 32.0;
+      const int64_t slot = (int64_t)cst[G_TOTLUT] % a.cap;
+      if (fitted)
+        for (int i = lane; i < 3 * S; i += 32) cprev[i] = fabs(X[off + i]);
+      __syncwarp();
+      if (ins) {
+        double *e = a.ring + ((size_t)c * a.cap + slot) * a.entry_stride;
+        for (int i = lane; i < 3 * S; i += 32) e[3 + i] = cprev[i];
+        for (int t = lane; t < R * S * 3; t += 32) {
+          const int r = t / (S * 3), s = (t / 3) % S, k = t % 3 + 1;
+          e[3 + 3 * S + t] = k < nb ? rmv[(r * S + s) * nb + k] : 0.0;
+        }
+        if (lane == 0) {
+          e[0] = (double)R;
+          e[1] = depth;
+          e[2] = kmin;
+          a.ring_src[(size_t)c * a.cap + slot] = p;
+        }
+      }
+      __syncwarp();
+      if (lane == 0) {
+        if (fitted) {
+          if (a.source) a.source[p] = -1;
+          cst[G_DEPTH] = depth;
+          cst[G_KMIN] = kmin;
+          cst[G_NOPT] += 1.0;
+          if ((float)me != 0.0f) {  // vec_mean2_double leaves zeros out
+            cst[G_ERRTOT] = cst[G_ERRTOT] + me;
+            cst[G_ERRCNT] += 1.0;
+          }
+          if (ins) cst[G_TOTLUT] += 1.0;
+          if (a.chain_stats) a.chain_stats[c * 4 + 1] += 1.0;
+          chain_post(a, cst, me);
+        } else {
+          cst[G_K] += 1.0;  // an invalid pixel leaves the chain's state alone
+        }
+      }
+      __syncwarp();
+    }
   }
 }
 
+// warps: when non-NULL, only the number of resident warps is returned.
 template <int C, int CG, int BLOCK>
-cudaError_t launch_shape(const RegionArgs &a, int sms, int per_sm, cudaStream_t s) {
+cudaError_t launch_shape(const RegionArgs &a, int sms, int per_sm, cudaStream_t s,
+                         int64_t *warps) {
   const size_t bytes = (size_t)(BLOCK / 32) * Shape<C, CG>::kSmem * sizeof(double);
   auto k = region_kernel<C, CG, BLOCK>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
@@ -566,7 +887,12 @@ cudaError_t launch_shape(const RegionArgs &a, int sms, int per_sm, cudaStream_t 
   if (occ < 1) return cudaErrorInvalidConfiguration;
   const int use = per_sm > 0 && per_sm < occ ? per_sm : occ;
   int64_t grid = (int64_t)sms * use;
-  const int64_t need = (a.npix + BLOCK / 32 - 1) / (BLOCK / 32);
+  if (warps) {
+    *warps = grid * (BLOCK / 32);
+    return cudaSuccess;
+  }
+  const int64_t units = a.order ? a.n_chains : a.npix;  // chains, or pixels
+  const int64_t need = (units + BLOCK / 32 - 1) / (BLOCK / 32);
   if (grid > need) grid = need;
   k<<<(int)grid, BLOCK, bytes, s>>>(a);
   return cudaGetLastError();
@@ -579,11 +905,11 @@ int region_max_params(int max_regions, int n_bottoms, int n_scenes) {
 }
 
 cudaError_t launch_region(const RegionArgs &a, int max_params, int sms, int per_sm,
-                          cudaStream_t s) {
-  if (max_params <= Shape<1, 32>::kMaxN) return launch_shape<1, 32, 128>(a, sms, per_sm, s);
+                          cudaStream_t s, int64_t *warps) {
+  if (max_params <= Shape<1, 32>::kMaxN) return launch_shape<1, 32, 128>(a, sms, per_sm, s, warps);
   if (max_params <= Shape<3, kRegionMaxParams>::kMaxN)
-    return launch_shape<3, kRegionMaxParams, 32>(a, sms, per_sm, s);
-  if (max_params <= Shape<3, 96>::kMaxN) return launch_shape<3, 96, 32>(a, sms, per_sm, s);
+    return launch_shape<3, kRegionMaxParams, 32>(a, sms, per_sm, s, warps);
+  if (max_params <= Shape<3, 96>::kMaxN) return launch_shape<3, 96, 32>(a, sms, per_sm, s, warps);
   return cudaErrorInvalidValue;
 }
 

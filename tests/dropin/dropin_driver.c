@@ -221,6 +221,63 @@ int main(int argc, char **argv) {
     return 0;
   }
 
+  int xs = 0, xb = 0, xS = 0, xe = 0;
+  if (sscanf(mode, "gridx:%d:%d:%d:%d", &xs, &xb, &xS, &xe) == 4) {
+    /* a stack of xS scenes ([scene][row][col][band] in rrs), n_spatial xs,
+     * n_bottoms xb; scene s's sun zenith in params[s * 6 + 1] and its R_sigma
+     * in params[s * 6 + 2 ..] (four bands); with xe, the empirical depths in
+     * params[p * 6] (nodata 9999) */
+    const int np1 = nrows * ncols;
+    if (xS < 1 || np1 * xS != npix || nb > 4) return 1;
+    photic_scene *sc = xcalloc((size_t)xS, sizeof *sc);
+    photic_geogrid *grids = xcalloc((size_t)xS * nb, sizeof *grids);
+    int *idx = xcalloc((size_t)xS, sizeof(int));
+    for (int k = 0; k < xS; k++) {
+      idx[k] = k;
+      snprintf(sc[k].scene_name, sizeof sc[k].scene_name, "synthetic%d", k);
+      sc[k].n_bands = nb;
+      sc[k].nrows = nrows;
+      sc[k].ncols = ncols;
+      sc[k].theta_w = params[k * 6 + 1];
+      sc[k].theta_v = th[1];
+      for (int b = 0; b < nb; b++) {
+        photic_geogrid *gr = grids + k * nb + b;
+        sc[k].band_indexes[b] = k * nb + b;
+        sc[k].wavelengths[b] = (int)wl[b];
+        sc[k].R_sigma[b] = params[k * 6 + 2 + b];
+        gr->nrows = nrows;
+        gr->ncols = ncols;
+        gr->nodata_value = -9999.0f;
+        gr->array = fgrid(nrows, ncols);
+        for (int i = 0; i < nrows; i++)
+          for (int j = 0; j < ncols; j++)
+            gr->array[i][j] = rrs[(((size_t)k * nrows + i) * ncols + j) * nb + b];
+      }
+    }
+    photic_geogrid none;
+    memset(&none, 0, sizeof none);
+    if (xe) {
+      none.nrows = nrows;
+      none.ncols = ncols;
+      none.nodata_value = 9999.0f;
+      none.array = fgrid(nrows, ncols);
+      for (int i = 0; i < nrows; i++)
+        for (int j = 0; j < ncols; j++) none.array[i][j] = (float)params[((size_t)i * ncols + j) * 6];
+    }
+    float **g[10];
+    for (int k = 0; k < 10; k++) g[k] = fgrid(nrows, ncols);
+    samodel(sc, grids, idx, xS, xe, none, 1, xs, xb, g[0], g[1], g[2], g[3], g[4], g[5], g[6],
+            g[7], g[8], g[9], 0.0f, 0, 0);
+    if (photic_last_error()[0]) {
+      fprintf(stderr, "samodel: %s\n", photic_last_error());
+      return 4;
+    }
+    for (int k = 0; k < 10; k++)
+      for (int i = 0; i < nrows; i++) fwrite(g[k][i], sizeof(float), (size_t)ncols, o);
+    fclose(o);
+    return 0;
+  }
+
   photic_model_data *md = md_new(nb, wl, th[0], th[1]);
   for (int p = 0; p < npix; p++) {
     for (int b = 0; b < nb; b++) md->Rrs_measured[0][0][b] = rrs[(size_t)p * nb + b];

@@ -128,3 +128,37 @@ def test_lookup_table_arguments_are_checked(lib):
     c.precision = L.PREC_FP64
     assert call(c, C.byref(lc), npix=0) == L.OK
     assert n_sh.value == 0 and n_ch.value == 0
+
+
+def test_general_lookup_table_arguments_are_checked(lib):
+    """photic_region_lut_invert_batch refuses unsupported configurations
+    and bad table settings before it touches the device; an empty grid is a
+    no-op."""
+    from photic_gb300 import _lib as L
+    c = L.photic_config()
+    lib.photic_config_default(C.byref(c))
+    lc = L.photic_lut_config()
+    lib.photic_lut_config_default(C.byref(lc))
+    o = L.photic_outputs()
+    n_sh, n_ch = C.c_int64(7), C.c_int64(7)
+    dummy = C.c_void_p(16)  # never dereferenced: the checks come first
+    th = (C.c_double * 2)(35.0, 40.0)
+
+    def call(cfg, lut, S=1, ns=2, nbt=3, nrows=4, ncols=4):
+        return lib.photic_region_lut_invert_batch(C.byref(cfg), lut, dummy, S, th, nrows, ncols,
+                                                  ns, nbt, None, None, 0.0, C.byref(o), None,
+                                                  None, None, C.byref(n_sh), C.byref(n_ch), None)
+
+    assert call(c, C.byref(lc), ns=3) == L.ERR_UNSUPPORTED
+    assert call(c, C.byref(lc), nbt=4) == L.ERR_UNSUPPORTED
+    assert call(c, C.byref(lc), S=9) == L.ERR_UNSUPPORTED
+    assert call(c, C.byref(lc), S=4) == L.ERR_UNSUPPORTED  # 9 regions x 4 scenes x 4 bands > 128
+    assert call(c, None) == L.ERR_INVALID
+    lc.n_lut = 0
+    assert call(c, C.byref(lc)) == L.ERR_INVALID
+    lc.n_lut = 16000
+    c.precision = L.PREC_DF64
+    assert call(c, C.byref(lc)) == L.ERR_UNSUPPORTED
+    c.precision = L.PREC_FP64
+    assert call(c, C.byref(lc), nrows=0) == L.OK
+    assert n_sh.value == 0 and n_ch.value == 0
