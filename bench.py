@@ -246,6 +246,10 @@ def main():
                     help="chains of the lookup-table leg re-run by the oracle")
     ap.add_argument("--lut-cpu-side", type=int, default=128,
                     help="side of the crop the lookup-table loop runs on one CPU thread")
+    ap.add_argument("--glut-side", type=int, default=96,
+                    help="side of the coherent scene of the general lookup-table leg (0: skip)")
+    ap.add_argument("--glut-cpu-side", type=int, default=20,
+                    help="side of the crop the general loop runs on one CPU thread")
     ap.add_argument("--nc-side", type=int, default=4096,
                     help="side of the scene written to and read from netCDF band files (0: off)")
     ap.add_argument("--serve-requests", type=int, default=12,
@@ -476,6 +480,9 @@ def main():
     lutr = None
     if rank == 0 and args.lut_side > 0:
         lutr = lut_leg(args, dev)
+    glut = None
+    if rank == 0 and args.glut_side > 0:
+        glut = glut_leg(args, dev)
     ncgrid = None
     if rank == 0 and args.nc_side > 0:
         try:
@@ -508,7 +515,7 @@ def main():
                 "seed_polish_ms_per_step": ms_step - ms_inv,
                 "plain_4096x4096": plain4096, "precision": precision,
                 "serving": serving, "temporal": temporal,
-                "regions": regions, "lut": lutr, "ncgrid": ncgrid, "e2e": e2e,
+                "regions": regions, "lut": lutr, "general_lut": glut, "ncgrid": ncgrid, "e2e": e2e,
                 "clocks": clk}
         print(json.dumps(line))
     if pg_ is not None:
@@ -908,6 +915,90 @@ def lut_leg(args, dev):
                                "sample": f"{args.lut_cpu_side}x{args.lut_cpu_side} corner of "
                                          f"the scene, one chain, the oracle port (pinned bit "
                                          f"for bit to the reference's samodel())"}}
+
+
+def glut_leg(args, dev):
+    """samodel()'s pixel loop with its lookup table in the reference's
+    default configuration (3 x 3 regions, sand, seagrass and coral mixed in
+    each: model/bam.c:3236-3241, model/common.c:152) on a spatially
+    coherent scene at the reference's tolerances: the GPU's chains (eight
+    and one per resident warp) against the general fit of every pixel, and
+    on a corner crop the loop on one chain against the oracle's (pinned bit
+    for bit to the reference's samodel()), whose time is the CPU rate."""
+    import ctypes as C
+    import torch
+    import photic_gb300 as pg
+    from oracle import oracle as O
+    n = args.glut_side
+    cfg = pg.Config.reference_default()
+    rrs, _ = pg.generate_field(n, n, seed=SEED + 13, device=dev, with_truth=False)
+    grid = rrs.reshape(1, n, n, 4).contiguous()
+    small = grid[:, :8, :8].contiguous()
+    pg.region_lut_invert(small, cfg, fields=("status",))  # warm-up
+    pg.region_fit(small, cfg, fields=("status",))
+    pg.sync()
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        o = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        pg.sync()
+        return o, e0.elapsed_time(e1) * 1e-3
+
+    fields = ("depth_f64", "status", "evals")
+    warps = int(pg.api.L.lib().photic_region_lut_default_chains(C.byref(cfg.to_c()), 1, 2,
+                                                                 3)) // 8
+    one, t_one = timed(lambda: pg.region_lut_invert(grid, cfg, n_chains=warps, fields=fields))
+    lut, t_lut = timed(lambda: pg.region_lut_invert(grid, cfg, fields=fields))
+    plain, t_plain = timed(lambda: pg.region_fit(grid, cfg, fields=fields))
+
+    def summary(o, t):
+        st = o["status"].cpu().numpy()
+        src = o["source"].cpu().numpy()
+        ev = o["evals"].cpu().numpy()
+        fit = (st & 0xFF) == 0
+        fitted = fit & (src == -1)
+        return {"chains": int(o["chain_stats"].shape[0]), "px_s": float(fit.sum()) / t,
+                "seconds": t, "served_share": float(np.mean(src[fit] >= 0)),
+                "hot_share_of_fits": float(np.mean((st[fitted] & 0x400) != 0)),
+                "evals_per_pixel": float(ev[fit].mean())}
+
+    pst = plain["status"].cpu().numpy()
+    pfit = (pst & 0xFF) == 0
+    res = summary(lut, t_lut)
+    res.update({"workload": f"{n}x{n} spatially coherent scene, 3x3 regions, sand, seagrass "
+                            f"and coral (n = 66 unknowns), reference tolerances, LUT of 16000 "
+                            f"slots per chain",
+                "one_chain_per_warp": summary(one, t_one),
+                "plain_px_s": float(pfit.sum()) / t_plain, "plain_seconds": t_plain,
+                "plain_evals_per_pixel": float(plain["evals"].cpu().numpy()[pfit].mean()),
+                "speedup_vs_plain": t_plain / t_lut})
+    # one chain on a corner crop: the GPU against the oracle, and the
+    # oracle's time as the loop's CPU rate on one thread
+    k = args.glut_cpu_side
+    crop = grid[:, :k, :k].contiguous()
+    g1 = pg.region_lut_invert(crop, cfg, n_chains=1, fields=("depth_f64", "status"))
+    pg.sync()
+    t0 = time.perf_counter()
+    oc, sc, _, _ = O.glut_invert(crop.cpu().numpy(), n_spatial=2, n_bottoms=3, n_chains=1,
+                                 nthreads=1)
+    t_cpu = time.perf_counter() - t0
+    f1 = (g1["status"].cpu().numpy() & 0xFF) == 0
+    d = np.abs(g1["depth_f64"].cpu().numpy()[f1] - oc[f1, 0])
+    s1 = g1["source"].cpu().numpy()
+    res["one_chain_crop"] = {"pixels": int(f1.sum()), "identical_depth": float(np.mean(d == 0)),
+                             "median_abs_dH_m": float(np.median(d)),
+                             "served_share_gpu": float(np.mean(s1[f1] >= 0)),
+                             "served_share_oracle": float(np.mean(sc[oc[:, 9] == 0] >= 0))}
+    res["cpu_one_thread"] = {"px_s": float(np.sum(oc[:, 9] == 0)) / t_cpu, "seconds": t_cpu,
+                             "sample": f"{k}x{k} corner of the scene, one chain, the oracle "
+                                       f"port (pinned bit for bit to the reference's "
+                                       f"samodel())"}
+    return res
 
 
 def ncgrid_leg(args, dev, rrs):
