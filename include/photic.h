@@ -378,6 +378,21 @@ int photic_depth_sigma(const photic_config *cfg, const float *d_rrs, int64_t npi
                        uint64_t seed, float *d_depth_sigma, double *d_table,
                        int32_t *d_sample_pixel, double *d_sample_depth, void *stream);
 
+/* The same estimate for the general fit (model/samodel.c:1368-1479 as
+ * samodel() runs it with regions, bottom mixtures or scene stacks): the
+ * samples are drawn as photic_depth_sigma draws them, each sampled pixel's
+ * regions (extract_Rrs_data) of every scene of d_grid ([n_scenes][nrows]
+ * [ncols][n_bands], device) have every band moved by n * r_sigma[scene]
+ * [band] (host, [n_scenes][n_bands]) and are refitted by the general fit
+ * (photic_region_fit_batch's; cold depth starts, every bottom type: the
+ * reference's h_empirical of 5 m, :1448).  Outputs as photic_depth_sigma. */
+int photic_region_depth_sigma(const photic_config *cfg, const float *d_grid, int32_t n_scenes,
+                              const double *theta_sun_deg, int32_t nrows, int32_t ncols,
+                              int32_t n_spatial, int32_t n_bottoms, const float *d_depth,
+                              const double *r_sigma, int32_t n_samples, uint64_t seed,
+                              float *d_depth_sigma, double *d_table, int32_t *d_sample_pixel,
+                              double *d_sample_depth, void *stream);
+
 /* Launch-shape autotuner (new; no reference counterpart).  Times the
  * inversion (kind PHOTIC_TUNE_INVERT: block_threads 64/128/256 x blocks per
  * SM 0 (occupancy limit)/2/3/4) or the temporal joint fit (PHOTIC_TUNE_JOINT:

@@ -335,6 +335,45 @@ def depth_sigma(rrs, depth, r_sigma, *, n_samples=128, seed=1, wl=OLI_BANDS, the
     return sig, table, spix, sdep
 
 
+def region_depth_sigma(grid, depth, r_sigma, *, n_spatial=2, n_bottoms=3, n_samples=128,
+                       seed=1, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0, nodata=-9999.0,
+                       reqmin=None, konvge=100, kcount=2000, sample_depth=None, nthreads=0):
+    """The depth uncertainty for the general fit: grid [(n_scenes,) nrows,
+    ncols, n_bands], depth [nrows*ncols] (positive, 0 not fitted), r_sigma
+    [n_scenes, n_bands]; reqmin None: the reference's tolerances.  Returns
+    (depth_sigma, table [120], sample_pixel [120*n], sample_depth)."""
+    g = _f32(grid)
+    if g.ndim == 3:
+        g = g[None]
+    S, nr, nc, nb = g.shape
+    npix = nr * nc
+    dep = np.ascontiguousarray(depth, dtype=np.float32).reshape(-1)
+    rs = _f64(np.asarray(r_sigma, dtype=np.float64).reshape(S, nb))
+    th = _f64(np.broadcast_to(np.asarray(theta_sun, dtype=np.float64), (S,)))
+    wl = _f64(wl)
+    if reqmin is None:
+        reqmin, konvge, kcount = 1e-2, 100, 5000
+    ns = 120 * n_samples
+    spix = np.zeros(ns, dtype=np.int32)
+    sdep = np.zeros(ns)
+    table = np.zeros(120)
+    sig = np.zeros(npix, dtype=np.float32)
+    sin = _f64(sample_depth) if sample_depth is not None else None
+    L = port().lib
+    L.po_region_depth_sigma.argtypes = [C.c_int, _dp, _dp, C.c_double, _fp, C.c_int, C.c_int,
+                                        C.c_int, C.c_float, C.c_int, C.c_int, _fp, _dp, C.c_int,
+                                        C.c_uint64, C.c_double, C.c_int, C.c_int, C.c_int, _dp,
+                                        _i32p, _dp, _dp, _fp]
+    rc = L.po_region_depth_sigma(nb, _ptr(wl, _dp), _ptr(th, _dp), theta_view, _ptr(g, _fp), S,
+                                 nr, nc, nodata, n_spatial, n_bottoms, dep.ctypes.data_as(_fp),
+                                 _ptr(rs, _dp), n_samples, seed, reqmin, konvge, kcount,
+                                 nthreads, _ptr(sin, _dp), spix.ctypes.data_as(_i32p),
+                                 _ptr(sdep, _dp), _ptr(table, _dp), sig.ctypes.data_as(_fp))
+    if rc:
+        raise ValueError("po_region_depth_sigma failed")
+    return sig, table, spix, sdep
+
+
 def region_invert_batch(grid, *, wl=OLI_BANDS, theta_sun=35.0, theta_view=0.0, h_tide=0.0,
                         nodata=-9999.0, reqmin=1e-10, konvge=100, kcount=2000, n_spatial=2,
                         n_bottoms=1, h_empirical=None, nthreads=0, which="port"):

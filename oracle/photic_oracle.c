@@ -1048,18 +1048,12 @@ static int po_approx_f(float a, float b, float eps) {
   return d <= ((fabsf(a) < fabsf(b) ? fabsf(b) : fabsf(a)) * eps);
 }
 
-int po_depth_sigma(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
-                   const float *rrs, int64_t npix, const float *depth, const double *r_sigma,
-                   int n_samples, uint64_t seed, double reqmin, int konvge, int kcount,
-                   int nthreads, const double *sample_depth_in, int32_t *sample_pixel,
-                   double *sample_depth, double *table, float *depth_sigma) {
-  const double interval = 0.25;
-  const int64_t ns = (int64_t)PO_DS_MAX * n_samples;
+/* The deepest fitted depth's interval count (model/samodel.c:1383-1387). */
+static int ds_intervals_host(const float *depth, int64_t npix, double interval) {
   float mx = 0.0f;
-  int64_t p, g;
-  int k, n_int, n_trials = (int)sqrt((double)npix);
   double m;
-  float *srrs;
+  int64_t p;
+  int n_int;
   for (p = 0; p < npix; p++) {
     float v = depth[p];
     if (!(v > 0.0f) || po_approx_f(v, 0.0f, 1.0e-4f)) continue;
@@ -1068,13 +1062,20 @@ int po_depth_sigma(int n_bands, const double *wl, double theta_sun_deg, double t
   m = interval * (double)((int)mx / interval);
   if (m > 30.0) m = 30.0;
   n_int = (int)(m / interval);
-  if (n_int > PO_DS_MAX) n_int = PO_DS_MAX;
-  srrs = (float *)malloc((size_t)ns * n_bands * sizeof(float));
-  if (!srrs) return 1;
+  return n_int > PO_DS_MAX ? PO_DS_MAX : n_int;
+}
+
+/* The samples: per (interval, sample) a pixel of the interval found by up
+ * to n_trials uniform probes (-1: none) and the draw n of frand2(1.0)
+ * (model/samodel.c:1402-1424, model/common.c:220), from Philox. */
+static void ds_select_host(const float *depth, int64_t npix, int n_samples, uint64_t seed,
+                           int n_int, double interval, int32_t *sample_pixel, float *sample_n) {
+  const int64_t ns = (int64_t)PO_DS_MAX * n_samples;
+  const int n_trials = (int)sqrt((double)npix);
+  int64_t g;
   for (g = 0; g < ns; g++) {
     int64_t found = -1;
-    int t2, b;
-    k = (int)(g / n_samples);
+    int t2, k = (int)(g / n_samples);
     if (k < n_int) {
       double d = k * interval;
       for (t2 = 0; t2 < n_trials && found < 0; t2++) {
@@ -1087,43 +1088,25 @@ int po_depth_sigma(int n_bands, const double *wl, double theta_sun_deg, double t
       }
     }
     sample_pixel[g] = (int32_t)found;
-    if (found < 0) {
-      for (b = 0; b < n_bands; b++) srrs[g * n_bands + b] = -9999.0f;
-    } else {
+    sample_n[g] = 0.0f;
+    if (found >= 0) {
       uint32_t w[4];
       double u0, u1;
-      float n;
       po_philox4x32((uint32_t)g, (uint32_t)(g >> 32), 0xFFFFFFFFu, 0xD6u, (uint32_t)seed,
                     (uint32_t)(seed >> 32), w);
       u0 = ((double)w[0] + 0.5) * 2.3283064365386963e-10;
       u1 = ((double)w[1] + 0.5) * 2.3283064365386963e-10;
-      n = u0 < 0.5 ? (float)u1 : -1.0f * (float)u1; /* frand2(1.0), model/common.c:220 */
-      for (b = 0; b < n_bands; b++) {
-        double v = (double)rrs[found * n_bands + b];
-        if (!po_approx_f(n, 0.0f, 1.0e-6f)) v += (double)n * r_sigma[b];
-        srrs[g * n_bands + b] = (float)v;
-      }
+      sample_n[g] = u0 < 0.5 ? (float)u1 : -1.0f * (float)u1;
     }
   }
-  if (sample_depth_in) {
-    memcpy(sample_depth, sample_depth_in, (size_t)ns * sizeof(double));
-  } else {
-    double *out = (double *)malloc((size_t)ns * PO_NOUT * sizeof(double));
-    if (!out) {
-      free(srrs);
-      return 1;
-    }
-    if (po_invert_batch(n_bands, wl, theta_sun_deg, theta_view_deg, 0.0, srrs, ns, -9999.0f,
-                        reqmin, konvge, kcount, 0, NULL, NULL, 1.0, nthreads, out)) {
-      free(out);
-      free(srrs);
-      return 1;
-    }
-    for (g = 0; g < ns; g++) sample_depth[g] = out[g * PO_NOUT + 0];
-    free(out);
-  }
-  free(srrs);
-  /* vec_mean2_double / vec_stddev_double (model/common.c:877-940) */
+}
+
+/* vec_mean2_double / vec_stddev_double of each interval's non-zero
+ * refitted depths (model/common.c:877-940) and the map (:1462-1476). */
+static void ds_finish_host(const double *sample_depth, int n_samples, int n_int, double interval,
+                           const float *depth, int64_t npix, double *table, float *depth_sigma) {
+  int64_t p;
+  int k;
   for (k = 0; k < PO_DS_MAX; k++) {
     double sigma = 0.0;
     if (k < n_int) {
@@ -1156,6 +1139,59 @@ int po_depth_sigma(int n_bands, const double *wl, double theta_sun_deg, double t
     }
     depth_sigma[p] = s;
   }
+}
+
+int po_depth_sigma(int n_bands, const double *wl, double theta_sun_deg, double theta_view_deg,
+                   const float *rrs, int64_t npix, const float *depth, const double *r_sigma,
+                   int n_samples, uint64_t seed, double reqmin, int konvge, int kcount,
+                   int nthreads, const double *sample_depth_in, int32_t *sample_pixel,
+                   double *sample_depth, double *table, float *depth_sigma) {
+  const double interval = 0.25;
+  const int64_t ns = (int64_t)PO_DS_MAX * n_samples;
+  const int n_int = ds_intervals_host(depth, npix, interval);
+  int64_t g;
+  float *srrs = (float *)malloc((size_t)ns * n_bands * sizeof(float));
+  float *sn = (float *)malloc((size_t)ns * sizeof(float));
+  if (!srrs || !sn) {
+    free(srrs);
+    free(sn);
+    return 1;
+  }
+  ds_select_host(depth, npix, n_samples, seed, n_int, interval, sample_pixel, sn);
+  for (g = 0; g < ns; g++) {
+    const int64_t found = sample_pixel[g];
+    int b;
+    for (b = 0; b < n_bands; b++) {
+      double v;
+      if (found < 0) {
+        srrs[g * n_bands + b] = -9999.0f;
+        continue;
+      }
+      v = (double)rrs[found * n_bands + b];
+      if (!po_approx_f(sn[g], 0.0f, 1.0e-6f)) v += (double)sn[g] * r_sigma[b];
+      srrs[g * n_bands + b] = (float)v;
+    }
+  }
+  free(sn);
+  if (sample_depth_in) {
+    memcpy(sample_depth, sample_depth_in, (size_t)ns * sizeof(double));
+  } else {
+    double *out = (double *)malloc((size_t)ns * PO_NOUT * sizeof(double));
+    if (!out) {
+      free(srrs);
+      return 1;
+    }
+    if (po_invert_batch(n_bands, wl, theta_sun_deg, theta_view_deg, 0.0, srrs, ns, -9999.0f,
+                        reqmin, konvge, kcount, 0, NULL, NULL, 1.0, nthreads, out)) {
+      free(out);
+      free(srrs);
+      return 1;
+    }
+    for (g = 0; g < ns; g++) sample_depth[g] = out[g * PO_NOUT + 0];
+    free(out);
+  }
+  free(srrs);
+  ds_finish_host(sample_depth, n_samples, n_int, interval, depth, npix, table, depth_sigma);
   return 0;
 }
 
@@ -2364,5 +2400,79 @@ int po_glut_invert(int n_bands, const double *wl, const double *theta_sun_deg,
     const int64_t a = c * S / n_chains, e = (c + 1) * S / n_chains;
     glut_chain(&g, order_out + a, e - a, out, source, chain_stats ? chain_stats + 4 * c : NULL);
   }
+  return 0;
+}
+
+/* The depth uncertainty for the general fit (model/samodel.c:1368-1479
+ * with regions, bottom mixtures or scene stacks): the samples of
+ * po_depth_sigma, each sampled pixel's regions (extract_Rrs_data) with
+ * every band of every scene moved by n r_sigma[scene][band] in double and
+ * stored as float (as the GPU's region lists hold them), refitted cold by
+ * the general fit with every bottom type (h_empirical 5 m, :1448).  grid:
+ * [n_scenes][nrows][ncols][n_bands]; r_sigma: [n_scenes][n_bands]. */
+int po_region_depth_sigma(int n_bands, const double *wl, const double *theta_sun_deg,
+                          double theta_view_deg, const float *grid, int n_scenes, int nrows,
+                          int ncols, float nodata, int n_spatial, int n_bottoms,
+                          const float *depth, const double *r_sigma, int n_samples,
+                          uint64_t seed, double reqmin, int konvge, int kcount, int nthreads,
+                          const double *sample_depth_in, int32_t *sample_pixel,
+                          double *sample_depth, double *table, float *depth_sigma) {
+  const double interval = 0.25;
+  const int64_t npix = (int64_t)nrows * ncols, ns = (int64_t)PO_DS_MAX * n_samples;
+  const int n_int = ds_intervals_host(depth, npix, interval);
+  po_scene sc[PO_MAX_SCENES];
+  po_fit fit;
+  int64_t g;
+  int s;
+  float *sn;
+  if (n_bands < 2 || n_bands > PO_MAX_BANDS || n_scenes < 1 || n_scenes > PO_MAX_SCENES ||
+      n_spatial < 1 || n_spatial > 2 || n_bottoms < 1 || n_bottoms > PO_MAX_MIX)
+    return 1;
+  sn = (float *)malloc((size_t)ns * sizeof(float));
+  if (!sn) return 1;
+  ds_select_host(depth, npix, n_samples, seed, n_int, interval, sample_pixel, sn);
+  if (sample_depth_in) {
+    memcpy(sample_depth, sample_depth_in, (size_t)ns * sizeof(double));
+  } else {
+    for (s = 0; s < n_scenes; s++)
+      scene_init(&sc[s], n_bands, wl, theta_sun_deg[s], theta_view_deg, 0.0);
+    fit.seed_step_scale = 1.0;
+    fit.reqmin = reqmin;
+    fit.konvge = konvge;
+    fit.kcount = kcount;
+    fit.n_hstarts = 8;
+    fit.hstarts = po_default_hstarts;
+#if _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 4)
+#endif
+    for (g = 0; g < ns; g++) {
+      po_rpixel px;
+      double o[PO_NOUT];
+      int r, k, b;
+      const int moved = !po_approx_f(sn[g], 0.0f, 1.0e-6f);
+      sample_depth[g] = 0.0;
+      if (sample_pixel[g] < 0) continue;
+      memset(&px, 0, sizeof px);
+      px.n_bands = n_bands;
+      px.S = n_scenes;
+      px.nb = n_bottoms;
+      for (k = 0; k < n_scenes; k++) px.sc[k] = &sc[k];
+      region_extract(grid, n_scenes, nrows, ncols, n_bands, nodata, n_spatial, sample_pixel[g],
+                     &px);
+      if (px.R == 0) continue;
+      for (r = 0; r < px.R; r++)
+        for (k = 0; k < n_scenes; k++)
+          for (b = 0; b < n_bands; b++) {
+            double v = px.rrs[r][k][b];
+            if (moved) v += (double)sn[g] * r_sigma[k * n_bands + b];
+            px.rrs[r][k][b] = (double)(float)v;
+          }
+      region_fit(&px, &fit, NAN, NULL, o, NULL);
+      sample_depth[g] = o[0];
+    }
+  }
+  free(sn);
+  ds_finish_host(sample_depth, n_samples, n_int, interval, depth, npix, table, depth_sigma);
   return 0;
 }

@@ -110,6 +110,13 @@ void po_generate_field(uint64_t seed, int64_t nrows, int64_t ncols, int64_t row0
                        double mask_frac, double noise_sigma, float nodata, float *rrs_out,
                        double *truth_out);
 float po_lut_key(const float *r, int n_bands, float nodata, const double *noise);
+int po_region_depth_sigma(int n_bands, const double *wl, const double *theta_sun_deg,
+                          double theta_view_deg, const float *grid, int n_scenes, int nrows,
+                          int ncols, float nodata, int n_spatial, int n_bottoms,
+                          const float *depth, const double *r_sigma, int n_samples,
+                          uint64_t seed, double reqmin, int konvge, int kcount, int nthreads,
+                          const double *sample_depth_in, int32_t *sample_pixel,
+                          double *sample_depth, double *table, float *depth_sigma);
 float po_glut_key(const float *grid, int n_scenes, int64_t npix, int64_t p, int n_bands,
                   float nodata, const double *noise);
 int po_glut_invert(int n_bands, const double *wl, const double *theta_sun_deg,

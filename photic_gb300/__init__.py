@@ -7,5 +7,5 @@ from . import api  # noqa: F401
 from . import ncgrid  # noqa: F401
 from .api import (Config, JointGraph, PhoticError, alloc_outputs, cost,  # noqa: F401
                   depth_sigma, fallbacks_first, generate_field, generate_joint, generate_scene,
-                  invert, joint_invert, lut_invert, region_fit, region_invert,
+                  invert, joint_invert, lut_invert, region_depth_sigma, region_fit, region_invert,
                   region_lut_invert, sync, version)

@@ -169,6 +169,12 @@ _SIGS = {
                                                  C.c_void_p]),
     "photic_region_lut_default_chains": (C.c_int64, [C.POINTER(photic_config), C.c_int32,
                                                      C.c_int32, C.c_int32]),
+    "photic_region_depth_sigma": (C.c_int, [C.POINTER(photic_config), C.c_void_p, C.c_int32,
+                                            C.POINTER(C.c_double), C.c_int32, C.c_int32,
+                                            C.c_int32, C.c_int32, C.c_void_p,
+                                            C.POINTER(C.c_double), C.c_int32, C.c_uint64,
+                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_void_p]),
     "photic_depth_sigma": (C.c_int, [C.POINTER(photic_config), C.c_void_p, C.c_int64, C.c_void_p,
                                      C.POINTER(C.c_double), C.c_int32, C.c_uint64, C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

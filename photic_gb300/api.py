@@ -242,6 +242,45 @@ def lut_invert(rrs: torch.Tensor, config: Optional[Config] = None, *, n_lut: int
     return out
 
 
+def region_depth_sigma(grid: torch.Tensor, depth: torch.Tensor, r_sigma,
+                       config: Optional[Config] = None, *, n_spatial: int = 2,
+                       n_bottoms: int = 3, theta_sun: Optional[Sequence[float]] = None,
+                       n_samples: int = 128, seed: int = 1,
+                       stream: Optional[torch.cuda.Stream] = None) -> Dict[str, torch.Tensor]:
+    """The reference's depth uncertainty for the general fit
+    (model/samodel.c:1368-1479 with regions, mixtures or scene stacks): the
+    samples of ``depth_sigma``, each sampled pixel's regions of every scene
+    of ``grid`` ([(n_scenes,) nrows, ncols, n_bands]) moved by n *
+    ``r_sigma`` ([n_scenes, n_bands]) and refitted by the general fit.
+    ``depth``: [nrows * ncols] float32, positive, 0 = not fitted.  Returns
+    sigma, table, sample_pixel and sample_depth as ``depth_sigma``."""
+    cfg = config or Config()
+    _check_cuda(grid, "grid", torch.float32)
+    _check_cuda(depth, "depth", torch.float32)
+    g4 = grid if grid.dim() == 4 else grid.unsqueeze(0)
+    if g4.dim() != 4 or g4.shape[3] != cfg.n_bands or not g4.is_contiguous():
+        raise ValueError(f"grid must be a contiguous [(n_scenes,) nrows, ncols, {cfg.n_bands}]")
+    S, nrows, ncols = int(g4.shape[0]), int(g4.shape[1]), int(g4.shape[2])
+    vals = [float(v) for row in r_sigma for v in row]
+    if len(vals) != S * cfg.n_bands:
+        raise ValueError("r_sigma must be [n_scenes, n_bands]")
+    ns = 120 * n_samples
+    dev = grid.device
+    out = {"sigma": torch.empty(nrows * ncols, dtype=torch.float32, device=dev),
+           "table": torch.empty(120, dtype=torch.float64, device=dev),
+           "sample_pixel": torch.empty(ns, dtype=torch.int32, device=dev),
+           "sample_depth": torch.empty(ns, dtype=torch.float64, device=dev)}
+    c = cfg.to_c()
+    th = (C.c_double * S)(*([cfg.theta_sun_deg] * S if theta_sun is None else
+                            [float(t) for t in theta_sun]))
+    rs = (C.c_double * len(vals))(*vals)
+    L.check(L.lib().photic_region_depth_sigma(
+        C.byref(c), _ptr(g4), S, th, nrows, ncols, int(n_spatial), int(n_bottoms), _ptr(depth),
+        rs, int(n_samples), int(seed), _ptr(out["sigma"]), _ptr(out["table"]),
+        _ptr(out["sample_pixel"]), _ptr(out["sample_depth"]), _stream_handle(stream)))
+    return out
+
+
 def region_invert(grid: torch.Tensor, config: Optional[Config] = None, *,
                   fields: Sequence[str] = OUTPUT_FIELDS,
                   stream: Optional[torch.cuda.Stream] = None) -> Dict[str, torch.Tensor]:

@@ -358,9 +358,11 @@ __global__ void ds_select_kernel(const __grid_constant__ DepthSigmaArgs a) {
     }
   }
   a.sample_pixel[g] = (int32_t)found;
-  float *out = a.sample_rrs + g * nb;
+  float *out = a.sample_rrs ? a.sample_rrs + g * nb : nullptr;
   if (found < 0) {
-    for (int b = 0; b < nb; b++) out[b] = a.nodata;
+    if (out)
+      for (int b = 0; b < nb; b++) out[b] = a.nodata;
+    if (a.sample_n) a.sample_n[g] = 0.0f;
     return;
   }
   uint32_t c[4] = {(uint32_t)g, (uint32_t)(g >> 32), 0xFFFFFFFFu, 0xD6u};
@@ -368,6 +370,8 @@ __global__ void ds_select_kernel(const __grid_constant__ DepthSigmaArgs a) {
   const double u0 = ((double)c[0] + 0.5) * 2.3283064365386963e-10;
   const double u1 = ((double)c[1] + 0.5) * 2.3283064365386963e-10;
   const float n = u0 < 0.5 ? (float)u1 : -1.0f * (float)u1;  // frand2(1.0)
+  if (a.sample_n) a.sample_n[g] = n;
+  if (!out) return;
   for (int b = 0; b < nb; b++) {
     const float refl = a.rrs[found * nb + b];
     double v = (double)refl;

@@ -2285,17 +2285,19 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
         rc = fail(PHOTIC_ERR_NOMEM, "samodel: empirical depth grid");
     }
     const float emp_nodata = empirical_depth_present ? empirical_depths.nodata_value : 0.0f;
+    // per scene: sun zenith and R_sigma (the noise of the order and of the
+    // depth uncertainty)
+    double th[PHOTIC_MAX_SCENES], noise[PHOTIC_MAX_SCENES * PHOTIC_MAX_BANDS];
+    for (int k = 0; k < nscenes; k++) {
+      const photic_scene &sk = scene_data[scene_indexes[k]];
+      th[k] = sk.theta_w;
+      for (int b = 0; b < nb; b++) noise[k * nb + b] = sk.R_sigma[b];
+    }
     if (rc != PHOTIC_OK) {
     } else if (general) {
       // P, G, X come out as [pixel][scene]
       o.bottom_percent = d_mix;
       o.bottom_type = d_mix + 3 * npix;
-      double th[PHOTIC_MAX_SCENES], noise[PHOTIC_MAX_SCENES * PHOTIC_MAX_BANDS];
-      for (int k = 0; k < nscenes; k++) {
-        const photic_scene &sk = scene_data[scene_indexes[k]];
-        th[k] = sk.theta_w;
-        for (int b = 0; b < nb; b++) noise[k * nb + b] = sk.R_sigma[b];
-      }
       rc = photic_region_lut_invert_batch(&cfg, &lc, d_rrs, nscenes, th, nrows, ncols,
                                           regions ? 2 : 1, n_bottoms, noise, d_raw, emp_nodata,
                                           &o, nullptr, nullptr, nullptr, nullptr, nullptr, 0);
@@ -2318,9 +2320,9 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
       cudaMemcpy(H.data(), d_depth, npix * sizeof(double), cudaMemcpyDeviceToHost);
       cudaMemcpy(f.data(), d_f, 4 * npix * sizeof(float), cudaMemcpyDeviceToHost);
       cudaMemcpy(st.data(), d_status, npix * sizeof(int32_t), cudaMemcpyDeviceToHost);
-      // depth uncertainty of the fitted grid (:1368-1479), one scene
+      // depth uncertainty of the fitted grid (:1368-1479)
       std::vector<float> sig((size_t)npix, 0.0f);
-      if (depth_sigma && nscenes == 1 && !general) {
+      if (depth_sigma) {
         std::vector<float> hpos((size_t)npix);
         for (int64_t p = 0; p < npix; p++)
           hpos[p] = (st[p] & 0xFF) == PHOTIC_PX_FITTED ? (float)H[p] : 0.0f;
@@ -2328,10 +2330,13 @@ void samodel(photic_scene scene_data[], photic_geogrid gridded_data[], int *scen
         if (cudaMalloc((void **)&d_hpos, npix * sizeof(float)) == cudaSuccess &&
             cudaMalloc((void **)&d_sig, npix * sizeof(float)) == cudaSuccess) {
           cudaMemcpy(d_hpos, hpos.data(), npix * sizeof(float), cudaMemcpyHostToDevice);
-          double rs[PHOTIC_MAX_BANDS];
-          for (int b = 0; b < nb; b++) rs[b] = s0.R_sigma[b];
-          rc = photic_depth_sigma(&cfg, d_rrs, npix, d_hpos, rs, 128, 1, d_sig, nullptr,
-                                  nullptr, nullptr, nullptr);
+          if (general)  // the general fit's refits of each sample's regions
+            rc = photic_region_depth_sigma(&cfg, d_rrs, nscenes, th, nrows, ncols,
+                                           regions ? 2 : 1, n_bottoms, d_hpos, noise, 128, 1,
+                                           d_sig, nullptr, nullptr, nullptr, nullptr);
+          else
+            rc = photic_depth_sigma(&cfg, d_rrs, npix, d_hpos, noise, 128, 1, d_sig, nullptr,
+                                    nullptr, nullptr, nullptr);
           if (rc == PHOTIC_OK) rc = photic_sync(nullptr);
           if (rc == PHOTIC_OK)
             cudaMemcpy(sig.data(), d_sig, npix * sizeof(float), cudaMemcpyDeviceToHost);
@@ -2780,6 +2785,95 @@ extern "C" int photic_region_lut_invert_batch(
   }
   if (!d_order) cudaFreeAsync(order, s);
   if (n_shallow) *n_shallow = S;
+  return PHOTIC_OK;
+}
+
+extern "C" int photic_region_depth_sigma(const photic_config *cfg, const float *d_grid,
+                                         int32_t n_scenes, const double *theta_sun_deg,
+                                         int32_t nrows, int32_t ncols, int32_t n_spatial,
+                                         int32_t n_bottoms, const float *d_depth,
+                                         const double *r_sigma, int32_t n_samples, uint64_t seed,
+                                         float *d_depth_sigma, double *d_table,
+                                         int32_t *d_sample_pixel, double *d_sample_depth,
+                                         void *stream) {
+  int nmax = 0;
+  int rc = region_config_check(cfg, n_scenes, n_spatial, n_bottoms, &nmax);
+  if (rc) return rc;
+  const int64_t npix = (int64_t)nrows * ncols;
+  if (nrows < 0 || ncols < 0 || (npix > 0 && (!d_grid || !d_depth || !d_depth_sigma)) ||
+      !r_sigma || n_samples < 1 || n_samples > 4096 || npix > 0xffffffffLL)
+    return fail(PHOTIC_ERR_INVALID, "bad arguments");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nb = cfg->n_bands;
+  const int64_t ns = (int64_t)kDsMaxIntervals * n_samples;
+  // scratch: max bits, sample pixels, draws, sample depths, table, region lists
+  const size_t off_pix = 256, off_n = off_pix + ((ns * 4 + 255) / 256) * 256;
+  const size_t off_dep = off_n + ((ns * 4 + 255) / 256) * 256;
+  const size_t off_tab = off_dep + ((ns * 8 + 255) / 256) * 256;
+  const size_t off_R = off_tab + ((kDsMaxIntervals * 8 + 255) / 256) * 256;
+  const size_t off_o = off_R + ((ns * 4 + 255) / 256) * 256;
+  const size_t off_rrs = off_o + ((ns * 4 + 255) / 256) * 256;
+  const size_t bytes = off_rrs + (size_t)ns * kRegionMaxR * n_scenes * nb * 4;
+  unsigned char *ws = nullptr;
+  cudaError_t e = cudaMallocAsync((void **)&ws, bytes, s);
+  if (e != cudaSuccess) return fail(PHOTIC_ERR_NOMEM, "depth-sigma workspace");
+  cudaMemsetAsync(ws, 0, 256, s);
+  DepthSigmaArgs a;
+  memset(&a, 0, sizeof a);
+  a.rrs = d_grid;
+  a.depth = d_depth;
+  a.npix = npix;
+  a.n_bands = nb;
+  a.n_samples = n_samples;
+  a.n_trials = (int)sqrt((double)npix);  // (int) sqrt(nrows * ncols)
+  a.interval = 0.25;
+  a.nodata = cfg->nodata_value;
+  a.seed = seed;
+  a.max_bits = (unsigned int *)ws;
+  a.sample_pixel = d_sample_pixel ? d_sample_pixel : (int32_t *)(ws + off_pix);
+  a.sample_n = (float *)(ws + off_n);
+  double *sdep = d_sample_depth ? d_sample_depth : (double *)(ws + off_dep);
+  a.sample_depth = sdep;
+  a.table = d_table ? d_table : (double *)(ws + off_tab);
+  a.depth_sigma = d_depth_sigma;
+  e = launch_depth_sigma_select(a, s);
+  RegionSampleArgs ra;
+  memset(&ra, 0, sizeof ra);
+  ra.grid = d_grid;
+  ra.nrows = nrows;
+  ra.ncols = ncols;
+  ra.n_scenes = n_scenes;
+  ra.n_bands = nb;
+  ra.n_spatial = n_spatial;
+  ra.nodata = cfg->nodata_value;
+  for (int k = 0; k < n_scenes; k++)
+    for (int b = 0; b < nb; b++) ra.r_sigma[k * 8 + b] = r_sigma[k * nb + b];
+  ra.sample_pixel = a.sample_pixel;
+  ra.sample_n = a.sample_n;
+  ra.ns = ns;
+  ra.list_rrs = (float *)(ws + off_rrs);
+  ra.list_R = (int32_t *)(ws + off_R);
+  ra.list_origin = (int32_t *)(ws + off_o);
+  if (e == cudaSuccess) e = launch_region_samples(ra, s);
+  if (e == cudaSuccess) {
+    // the refits: the general fit of every sample's regions, cold, with
+    // the reference's h_empirical of 5 m (every bottom type; :1448)
+    photic_outputs o;
+    memset(&o, 0, sizeof o);
+    o.depth_f64 = sdep;
+    RegionArgs r;
+    region_args(cfg, nullptr, n_scenes, theta_sun_deg, 0, 0, n_spatial, n_bottoms, &o, r);
+    r.npix = ns;
+    r.no_mask = 1;
+    r.list_rrs = ra.list_rrs;
+    r.list_R = ra.list_R;
+    r.list_origin = ra.list_origin;
+    rc = run_region(r, nmax, cfg->blocks_per_sm, s);
+    if (rc == PHOTIC_OK) e = launch_depth_sigma_finish(a, s);
+  }
+  cudaFreeAsync(ws, s);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(e, "depth-sigma kernels");
   return PHOTIC_OK;
 }
 

@@ -326,12 +326,28 @@ struct DepthSigmaArgs {
   uint64_t seed;
   unsigned int *max_bits;    // scratch: deepest depth (float bits), zeroed
   int32_t *sample_pixel;     // [kDsMaxIntervals * n_samples], -1 = none
-  float *sample_rrs;         // [kDsMaxIntervals * n_samples][n_bands]
+  float *sample_rrs;         // optional [kDsMaxIntervals * n_samples][n_bands]
+  float *sample_n;           // optional [kDsMaxIntervals * n_samples]: the draws n
   const double *sample_depth;  // refitted depths of the samples
   double *table;             // [kDsMaxIntervals]
   float *depth_sigma;        // [npix]
 };
 cudaError_t launch_depth_sigma_select(const DepthSigmaArgs &a, cudaStream_t s);
+// The depth uncertainty's samples for the general fit: each sampled pixel's
+// regions (extract_Rrs_data, model/samodel.c:2957-3027) with every band of
+// every scene moved by n R_sigma[scene][band], as region lists.
+struct RegionSampleArgs {
+  const float *grid;           // [n_scenes][nrows][ncols][n_bands]
+  int nrows, ncols, n_scenes, n_bands, n_spatial;
+  float nodata;
+  double r_sigma[kMaxScenes * 8];  // [scene][band]
+  const int32_t *sample_pixel;  // [ns], -1 = none (no regions)
+  const float *sample_n;        // [ns]
+  int64_t ns;
+  float *list_rrs;              // [ns][9][n_scenes][n_bands]
+  int32_t *list_R, *list_origin;  // [ns]
+};
+cudaError_t launch_region_samples(const RegionSampleArgs &a, cudaStream_t s);
 cudaError_t launch_depth_sigma_finish(const DepthSigmaArgs &a, cudaStream_t s);
 
 // Throughput probes (TFLOP/s of FP64 and FP32 FMA, Tops/s of MUFU ex2).

@@ -448,6 +448,13 @@ __global__ void __launch_bounds__(BLOCK, 1) region_kernel(const __grid_constant_
     if (!isnan(hbot) && hbot > 8.0) nbt = 1;  // model/samodel.c:1781, 1826-1830
     const int N = R + 2 * nbt * R + 3 * S, nterm = R * S * nb;
     const int qo = R + R * nbt, off = R + 2 * nbt * R;
+    if (R < 1 && a.list_R) {
+      // a problem without regions (md->n_regions == 0: the reference's
+      // loops skip it, model/samodel.c:951-953, 1428-1430)
+      if (lane == 0) write_masked(o, p, S, PHOTIC_PX_MASKED);
+      __syncwarp();
+      continue;
+    }
     if (R < 1 || N > kMaxN || nterm > kTerms || R * S > kRS) {
       if (lane == 0) {
         atomicOr(a.error, PHOTIC_DEVERR_EVAL_CAP);
@@ -898,7 +905,57 @@ cudaError_t launch_shape(const RegionArgs &a, int sms, int per_sm, cudaStream_t 
   return cudaGetLastError();
 }
 
+// One thread per sample: the sampled pixel's regions in extract_Rrs_data's
+// order with the perturbation of the depth-uncertainty refit (:1426-1427,
+// 3003-3006: value + n R_sigma when n is not within 1e-6 of 0, in double,
+// stored as float); no pixel: no regions.
+__global__ void region_samples_kernel(const __grid_constant__ RegionSampleArgs a) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= a.ns) return;
+  const int64_t p = a.sample_pixel[g];
+  const int S = a.n_scenes, nb = a.n_bands;
+  if (p < 0) {
+    a.list_R[g] = 0;
+    a.list_origin[g] = 0;
+    return;
+  }
+  const int64_t npix = (int64_t)a.nrows * a.ncols;
+  const int i = (int)(p / a.ncols), j = (int)(p % a.ncols), w = a.n_spatial - 1;
+  const float n = a.sample_n[g];
+  const bool move = !(fabsf(n - 0.0f) <= fabsf(n) * 1.0e-6f);
+  int R = 0, origin = 0;
+  for (int ii = -w; ii <= w; ii++) {
+    const int iii = i + ii < 0 ? 0 : (i + ii > a.nrows - 1 ? a.nrows - 1 : i + ii);
+    for (int jj = -w; jj <= w; jj++) {
+      const int jjj = j + jj < 0 ? 0 : (j + jj > a.ncols - 1 ? a.ncols - 1 : j + jj);
+      const int64_t q = (int64_t)iii * a.ncols + jjj;
+      bool nodata = false;
+      for (int s = 0; s < S && !nodata; s++)
+        for (int b = 0; b < nb; b++) {
+          const float refl = a.grid[(s * npix + q) * nb + b];
+          if (nodata_value(refl, a.nodata)) {
+            nodata = true;
+            break;
+          }
+          double v = (double)refl;
+          if (move) v += (double)n * a.r_sigma[s * 8 + b];
+          a.list_rrs[((g * kMaxR + R) * S + s) * nb + b] = (float)v;
+        }
+      if (i == iii && j == jjj) origin = R;
+      if (!nodata) R++;
+    }
+  }
+  a.list_R[g] = R;
+  a.list_origin[g] = origin;
+}
+
 }  // namespace
+
+cudaError_t launch_region_samples(const RegionSampleArgs &a, cudaStream_t s) {
+  if (a.ns <= 0) return cudaSuccess;
+  region_samples_kernel<<<(unsigned)((a.ns + 127) / 128), 128, 0, s>>>(a);
+  return cudaGetLastError();
+}
 
 int region_max_params(int max_regions, int n_bottoms, int n_scenes) {
   return max_regions + 2 * n_bottoms * max_regions + 3 * n_scenes;

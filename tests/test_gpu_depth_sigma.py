@@ -42,3 +42,41 @@ def test_depth_sigma_matches_oracle(gpu, port):
     close = np.isclose(g["table"][:n_int], table[:n_int], rtol=1e-6)
     assert close.mean() >= 0.8, (close.mean(), g["table"][:n_int], table[:n_int])
     assert (g["sigma"][depth <= 0] == 0).all()
+
+
+def test_region_depth_sigma_matches_oracle(gpu, port):
+    """The general fit's depth uncertainty (3 x 3 regions, three bottom
+    types, a stack of two scenes): the same draws bit for bit, every sampled
+    pixel's perturbed regions refitted by the general fit, the statistics of
+    the GPU's refits restated by the oracle, and end to end the refits
+    agree on most samples (reference tolerances)."""
+    n = 24
+    ths = (35.0, 50.0)
+    grid = np.stack([port.generate_field(777, n, n, theta_sun=t)[0].reshape(n, n, 4)
+                     for t in ths])
+    _, truth = port.generate_field(777, n, n)
+    masked = (grid < 0).any(axis=(0, 3)).reshape(-1)
+    depth = np.where(masked, 0.0, np.minimum(truth[:, 0], 6.0)).astype(np.float32)
+    rs = np.array([R_SIGMA, [2.5e-4, 2.0e-4, 1.5e-4, 1.0e-4]])
+    cfg = gpu.Config.reference_default()
+    g = gpu.region_depth_sigma(torch.tensor(grid, device="cuda"),
+                               torch.tensor(depth, device="cuda"), rs, cfg, n_spatial=2,
+                               n_bottoms=3, theta_sun=list(ths), n_samples=8, seed=5)
+    gpu.sync()
+    g = {k: v.cpu().numpy() for k, v in g.items()}
+    sig, table, spix, sdep = port.region_depth_sigma(grid, depth, rs, n_samples=8, seed=5,
+                                                     theta_sun=ths,
+                                                     nthreads=os.cpu_count() or 1)
+    np.testing.assert_array_equal(g["sample_pixel"], spix)
+    found = spix >= 0
+    assert found.sum() > 20
+    sig2, table2, _, _ = port.region_depth_sigma(grid, depth, rs, n_samples=8, seed=5,
+                                                 theta_sun=ths, sample_depth=g["sample_depth"])
+    np.testing.assert_allclose(g["table"], table2, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(g["sigma"], sig2, rtol=1e-6, atol=0)
+    np.testing.assert_array_equal(g["sample_depth"][~found], 0.0)
+    d = np.abs(g["sample_depth"][found] - sdep[found])
+    print(f"general depth sigma: {found.sum()} refits, identical {np.mean(d == 0):.4f}, "
+          f"median |dH| {np.median(d):.3g} m")
+    assert np.median(d) <= 0.01 and np.mean(d == 0) >= 0.5
+    assert (g["sigma"][depth <= 0] == 0).all() and (g["sigma"][depth > 0] > 0).any()
