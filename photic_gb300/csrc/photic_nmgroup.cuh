@@ -4,8 +4,10 @@
 // coordinate l (and l + G, ... up to C slots) of every vertex, the centroid
 // and the trial points; the vertex costs and every decision taken on them
 // are replicated in all lanes of the group, each lane keeping its own copy
-// of the costs.  The simplex size is a template constant (NT > 0) or set at
-// run time (NT = 0, member nrt), for pixels whose parameter count varies.
+// of the costs -- or, with kSharedF (a group of a whole warp), one copy
+// that every write reaches between two warp barriers.  The simplex size is a
+// template constant (NT > 0) or set at run time (NT = 0, member nrt), for
+// pixels whose parameter count varies.
 #pragma once
 #include <stdint.h>
 
@@ -16,10 +18,11 @@ namespace photic {
 
 // Group-distributed Nelder-Mead: the state machine of NmLane with the
 // coordinate loops cut to the lane's own coordinates.
-template <int NT, int C, int G, int CG>
+template <int NT, int C, int G, int CG, bool kSharedF = false>
 struct NmGroup {
   int nrt;             // the simplex size when NT <= 0 (set before begin)
-  double *V, *Fv, *X;  // shared: V[j * CG + i], this lane's costs Fv[j * G], X[i]
+  double *V, *Fv, *X;  // shared: V[j * CG + i], this lane's costs Fv[j * G] (or the
+                       // group's Fv[j] with kSharedF), X[i]
   int gl;              // lane within the group
   unsigned gmask;      // the group's lanes
   double cen[C], refl[C], trial[C], xmin[C], start[C], step[C];
@@ -37,7 +40,23 @@ struct NmGroup {
   // coordinate came out unstepped.)
   __device__ __forceinline__ int slot_of(int i) const { return (i % G) == gl ? i / G : -1; }
   __device__ __forceinline__ double &Vv(int j, int i) { return V[j * CG + i]; }
-  __device__ __forceinline__ double &F(int j) { return Fv[j * G]; }
+  __device__ __forceinline__ double &F(int j) { return Fv[kSharedF ? j : j * G]; }
+  // A cost write.  With one copy for the warp, every lane has made the
+  // step's reads before any lane writes, and sees the write after it:
+  // the lanes take the same decisions, so they all reach both barriers.
+  __device__ __forceinline__ void setF(int j, double y) {
+    if constexpr (kSharedF) {
+#if defined(__CUDA_ARCH__)
+      __syncwarp(gmask);
+#endif
+      Fv[j] = y;
+#if defined(__CUDA_ARCH__)
+      __syncwarp(gmask);
+#endif
+    } else {
+      Fv[j * G] = y;
+    }
+  }
 
   // Every slot gets a defined value, also those of coordinates the lane
   // does not own (they are computed on but never stored).
@@ -137,12 +156,13 @@ struct NmGroup {
 
   // Each lane keeps its own copy of the vertex costs (the same values in
   // every lane of the group), so no lane ever reads a cost another lane is
-  // writing, whatever the lanes' relative progress.
+  // writing, whatever the lanes' relative progress; or one shared copy
+  // written between barriers (setF).
   __device__ __forceinline__ void replace_hi(const double (&p)[C], double y) {
 #pragma unroll
     for (int t = 0; t < C; t++)
       if (own(t)) Vv(hi, coord(t)) = p[t];
-    F(hi) = y;
+    setF(hi, y);
   }
 
   __device__ __forceinline__ bool iteration_end() {
@@ -193,12 +213,12 @@ struct NmGroup {
     int cs = CS_NONE;
     switch (phase) {
       case PH_INIT_BASE:
-        F(dim()) = y;
+        setF(dim(), y);
         icount++;
         make_vertex(0);
         break;
       case PH_INIT_VERT:
-        F(jj) = y;
+        setF(jj, y);
         icount++;
         if (jj + 1 < dim()) make_vertex(jj + 1);
         else cs = CS_READY;
@@ -259,7 +279,7 @@ struct NmGroup {
         break;
       }
       case PH_SHRINK:
-        F(jj) = y;
+        setF(jj, y);
         icount++;
         if (jj < dim()) {
           const int j = jj + 1;

@@ -44,19 +44,23 @@ constexpr int kMaxR = kRegionMaxR, kTerms = 128, kHT = kTerms / 32, kShares = 32
 // chain mode, per warp: the measured bands 1..3 of every region and scene,
 // the modelled Rrs of the final evaluation, the chain's P, G, X and state
 constexpr int kChainD = 3 * kRS + kTerms + 3 * kMaxScenes + 24;
+// the cost's staging, per warp: |H| and depth deviations per region, bottom
+// deviations per (type, region), K penalty and smallest K per scene, mean
+// share per type
+constexpr int kStage = 64;
 
 // Launch shapes: C coordinates per lane, vertex row stride CG.
 template <int C, int CG>
 struct Shape {
   static constexpr int kMaxN = C == 1 ? 32 : CG;
   static constexpr int kNF = kMaxN + 2;
-  // doubles of shared memory per warp: vertices (n+1) x CG, per-lane vertex
-  // costs, the evaluation point, band terms (residual^2, K, bottom share of
+  // doubles of shared memory per warp: vertices (n+1) x CG, the vertex
+  // costs (one copy for the warp), the evaluation point, band terms (residual^2, K, bottom share of
   // the reflectance), per-region Rrs(490/550/640), final details and
   // per-(region, bottom) shares of the bottom-continuity term, and the
   // chain mode's arrays
   static constexpr int kSmem =
-      (kMaxN + 1) * CG + kNF * 32 + 32 * C + 3 * kTerms + 3 * kRS + 8 + kShares + kChainD;
+      (kMaxN + 1) * CG + kNF + 32 * C + 3 * kTerms + 3 * kRS + 8 + kShares + kChainD + kStage;
 };
 
 __device__ __forceinline__ bool nodata_value(float v, float nodata) {
@@ -281,12 +285,12 @@ __global__ void __launch_bounds__(BLOCK, 1) region_kernel(const __grid_constant_
   const int nb = fp.n_bands, S = a.n_scenes;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   double *base = smem + warp * Sh::kSmem;
-  double *V = base, *Fb = V + (kMaxN + 1) * CG, *X = Fb + kNF * 32, *dd = X + 32 * C,
+  double *V = base, *Fb = V + (kMaxN + 1) * CG, *X = Fb + kNF, *dd = X + 32 * C,
          *kk = dd + kTerms, *io = kk + kTerms, *s490 = io + kTerms, *s550 = s490 + kRS,
          *s640 = s550 + kRS, *misc = s640 + kRS;
   double *share = misc + 8;
   double *meas = share + kShares, *rmv = meas + 3 * kRS, *cprev = rmv + kTerms,
-         *cst = cprev + 3 * kMaxScenes;
+         *cst = cprev + 3 * kMaxScenes, *stg = cst + 24;
   const bool list = a.list_R != nullptr;
   // spectrum of scene s of region slot q (a pixel index of the grid, or a
   // region row of the list)
@@ -294,9 +298,9 @@ __global__ void __launch_bounds__(BLOCK, 1) region_kernel(const __grid_constant_
     return list ? a.list_rrs + (q * S + s) * nb : a.grid + ((int64_t)s * a.npix + q) * nb;
   };
 
-  NmGroup<0, C, 32, CG> m;
+  NmGroup<0, C, 32, CG, true> m;
   m.V = V;
-  m.Fv = Fb + lane;
+  m.Fv = Fb;
   m.X = X;
   m.gl = lane;
   m.gmask = kFull;
@@ -640,61 +644,101 @@ __global__ void __launch_bounds__(BLOCK, 1) region_kernel(const __grid_constant_
         share[lane] = fabs(X[R + r * nbt + k]) * fabs(X[qo + r * nbt + k]) / qs;
       }
       __syncwarp();
-      // ---- the cost on the head lane (model/samodel.c:2432-2759)
+      // ---- the cost (model/samodel.c:2432-2759).  Every sum keeps the
+      // reference's order on one lane; the sums that do not depend on one
+      // another run on different lanes together, and the terms they add
+      // (|H| per region, the squared deviations, each scene's K penalty)
+      // are formed by the lanes in parallel.  An outside-the-band term that
+      // the reference skips is added here as +0, which leaves every partial
+      // sum unchanged (the terms are >= 0).
+      double *habs = stg, *dv2d = stg + 9, *dv2b = stg + 18, *kpen = stg + 45, *bmv = stg + 53,
+             *kms = stg + 56;
+      if (lane < R) habs[lane] = fabs(X[lane]);
+      if (lane < S) {  // each scene's smallest K over the last region's bands (:2696-2701)
+        double km = 1.0e4;
+        for (int b = 0; b < nb; b++) {
+          const double Kb = kk[((R - 1) * S + lane) * nb + b];
+          if (__double2float_rn(Kb) != 0.0f && Kb < km) km = Kb;
+        }
+        kms[lane] = km;
+      }
+      __syncwarp();
+      // ordered sums: lane 0 the squared residuals (:2571), lane 1 the
+      // depths (:2597-2600), lane 2 + k the bottom shares of type k (:2652)
+      double z = 0.0;
+      {
+        const double *src = dd;
+        int cnt = 0, str = 1;
+        if (lane == 0) {
+          cnt = nterm;
+        } else if (lane == 1) {
+          src = habs;
+          cnt = R;
+        } else if (lane < 2 + nbt) {
+          src = share + (lane - 2);
+          cnt = R;
+          str = nbt;
+        }
+        for (int i = 0; i < cnt; i++) z = z + src[i * str];
+      }
+      const double err = __shfl_sync(kFull, z, 0);
+      const double dmean = __shfl_sync(kFull, z, 1) / (double)R;
+      if (lane >= 2 && lane < 2 + nbt) bmv[lane - 2] = z / (double)R;
+      const double thd = dmean < 4.0 ? 0.4 : dmean < 8.0 ? 0.2 : dmean < 12.0 ? 0.1 : 0.05;
+      const double thb = dmean < 5.0 ? 0.25 : dmean < 10.0 ? 0.1 : dmean < 15.0 ? 0.05 : 0.01;
+      bool outd = false, outb = false;
+      if (lane < R) {  // depth continuity, one region per lane (:2604-2617)
+        const double h = habs[lane];
+        outd = h < (1.0 - thd) * dmean || h > (1.0 + thd) * dmean;
+        const double dv = h - dmean;
+        dv2d[lane] = outd ? dv * dv : 0.0;
+      }
+      __syncwarp();
+      if (lane < nbt * R) {  // bottom continuity, one (type, region) per lane (:2655-2668)
+        const int k = lane / R, r = lane % R;
+        const double bm = bmv[k], bt = share[r * nbt + k];
+        outb = bt < (1.0 - thb) * bm || bt > (1.0 + thb) * bm;
+        const double dv = bt - bm;
+        dv2b[lane] = outb ? dv * dv : 0.0;
+      }
+      if (lane < S) kpen[lane] = k_penalty_f64(fp.kp, habs[origin], kms[lane]);
+      const double nd = (double)__popc(__ballot_sync(kFull, outd));
+      const double nbo = (double)__popc(__ballot_sync(kFull, outb));
+      __syncwarp();
+      // ordered sums: lane 0 the depth deviations, lane 1 the bottom
+      // deviations (type-major), lane 2 the scenes' K penalties, lane 3 the
+      // types' mean shares
+      double z2 = 0.0;
+      {
+        const double *src = dv2d;
+        int cnt = 0;
+        if (lane == 0) {
+          cnt = R;
+        } else if (lane == 1) {
+          src = dv2b;
+          cnt = nbt * R;
+        } else if (lane == 2) {
+          src = kpen;
+          cnt = S;
+        } else if (lane == 3) {
+          src = bmv;
+          cnt = nbt;
+        }
+        for (int i = 0; i < cnt; i++) z2 = z2 + src[i];
+      }
+      double Ed = __shfl_sync(kFull, z2, 0), Eb = __shfl_sync(kFull, z2, 1);
+      double Ke = __shfl_sync(kFull, z2, 2);
+      const double btotal = __shfl_sync(kFull, z2, 3);
       double y = 0.0;
       if (lane == 0) {
-        double err = 0.0;
-        for (int tau = 0; tau < nterm; tau++) err = err + dd[tau];
         const double E = 100.0 * sqrt(fm::div_count(err, nterm)) / mean;
-        // depth continuity
-        double dmean = 0.0;
-        for (int r = 0; r < R; r++) dmean += fabs(X[r]);
-        dmean /= (double)R;
-        double th = dmean < 4.0 ? 0.4 : dmean < 8.0 ? 0.2 : dmean < 12.0 ? 0.1 : 0.05;
-        double Ed = 0.0, nout = 0.0;
-        for (int r = 0; r < R; r++) {
-          const double h = fabs(X[r]);
-          if (h < (1.0 - th) * dmean || h > (1.0 + th) * dmean) {
-            const double dv = h - dmean;
-            Ed += dv * dv;
-            nout += 1.0;
-          }
-        }
-        if (nout > 0.5) Ed = 100.0 * sqrt(Ed / nout) / dmean;
-        // bottom continuity, per bottom type
-        th = dmean < 5.0 ? 0.25 : dmean < 10.0 ? 0.1 : dmean < 15.0 ? 0.05 : 0.01;
-        double Eb = 0.0, btotal = 0.0;
-        nout = 0.0;
-        for (int k = 0; k < nbt; k++) {
-          double bmean = 0.0;
-          for (int r = 0; r < R; r++) bmean += share[r * nbt + k];
-          bmean /= (double)R;
-          btotal += bmean;
-          for (int r = 0; r < R; r++) {
-            const double bt = share[r * nbt + k];
-            if (bt < (1.0 - th) * bmean || bt > (1.0 + th) * bmean) {
-              const double dv = bt - bmean;
-              Eb += dv * dv;
-              nout += 1.0;
-            }
-          }
-        }
-        if (nout > 0.5) {
+        if (nd > 0.5) Ed = 100.0 * sqrt(Ed / nd) / dmean;
+        if (nbo > 0.5) {
           const double bmean = btotal / ((double)nbt);
-          Eb = 100.0 * sqrt(Eb / nout) / bmean;
+          Eb = 100.0 * sqrt(Eb / nbo) / bmean;
         }
-        // K terms: the origin's depth and each scene's K (the last region's
-        // bands); the very-high-K term on the last scene's
-        double km = 1.0e4, Ke = 0.0;
-        const double Ho = fabs(X[origin]);
-        for (int s = 0; s < S; s++) {
-          km = 1.0e4;
-          for (int b = 0; b < nb; b++) {
-            const double Kb = kk[((R - 1) * S + s) * nb + b];
-            if (__double2float_rn(Kb) != 0.0f && Kb < km) km = Kb;
-          }
-          Ke = Ke + k_penalty_f64(fp.kp, Ho, km);
-        }
+        // the very-high-K term on the last scene's K (:2728-2732)
+        const double km = kms[S - 1];
         if (km > 0.7) {
           const double dk = 4.0 * (km - 0.7);
           Ke = Ke + 100.0 * (dk * dk);
