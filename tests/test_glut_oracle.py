@@ -104,3 +104,21 @@ def test_glut_chains_are_independent_slices(port, golden_dir):
         assert np.all(src[sl][src[sl] >= 0] >= 0)
         assert set(src[sl][src[sl] >= 0]).issubset(set(sl))  # served from its own chain
         np.testing.assert_array_equal(stats[c, 0] + stats[c, 1], sl.size)
+
+
+def test_oracle_glut_eight_bands_matches_reference_live(port):
+    """Eight OLCI-like bands (the order and the spectral difference use
+    bands 1..3 of them), 3 x 3 regions, two bottom types, against the
+    reference's own samodel().  The wavelengths are whole nanometres: a
+    scene record holds them as int (model/common.h:200)."""
+    if not port.reference_available():
+        pytest.skip("reference sources not available on this host")
+    wl8 = (412.0, 442.0, 490.0, 510.0, 560.0, 620.0, 665.0, 709.0)
+    n = 10
+    grid = port.generate_field(8181, n, n, wl=wl8)[0].reshape(1, n, n, 8)
+    ref = port.reference_samodel_stack(grid, wl=wl8, n_spatial=2, n_bottoms=2)
+    out, src, order, stats = port.glut_invert(grid, wl=wl8, n_spatial=2, n_bottoms=2,
+                                              n_chains=1, nthreads=1)
+    keep = [0, 2, 3, 4, 5, 6, 7, 8, 9]
+    compare_grids(out, ref[keep], keep, "eight bands")
+    assert (out[:, 9] == 0).sum() > 50
