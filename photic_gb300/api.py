@@ -228,6 +228,9 @@ def lut_invert(rrs: torch.Tensor, config: Optional[Config] = None, *, n_lut: int
             lc.rrs_noise[b] = float(v)
     c = cfg.to_c()
     max_chains = int(n_chains) if n_chains else int(L.lib().photic_lut_default_chains(C.byref(c)))
+    if max_chains < 1:
+        raise PhoticError(L.ERR_CUDA, "no chain count for this configuration: "
+                          + L.lib().photic_last_error().decode(errors="replace"))
     stats = torch.zeros(max(1, min(max_chains, npix)), 4, dtype=torch.float64, device=rrs.device)
     os_ = _outputs_struct(out)
     n_sh, n_ch = C.c_int64(0), C.c_int64(0)
@@ -391,6 +394,9 @@ def region_lut_invert(grid: torch.Tensor, config: Optional[Config] = None, *,
         noise = (C.c_double * len(vals))(*vals)
     max_chains = int(n_chains) if n_chains else int(L.lib().photic_region_lut_default_chains(
         C.byref(c), S, int(n_spatial), int(n_bottoms)))
+    if max_chains < 1:
+        raise PhoticError(L.ERR_CUDA, "no chain count for this configuration: "
+                          + L.lib().photic_last_error().decode(errors="replace"))
     stats = torch.zeros(max(1, min(max_chains, npix)), 4, dtype=torch.float64, device=grid.device)
     os_ = _outputs_struct(out)
     n_sh, n_ch = C.c_int64(0), C.c_int64(0)
