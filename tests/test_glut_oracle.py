@@ -122,3 +122,30 @@ def test_oracle_glut_eight_bands_matches_reference_live(port):
     keep = [0, 2, 3, 4, 5, 6, 7, 8, 9]
     compare_grids(out, ref[keep], keep, "eight bands")
     assert (out[:, 9] == 0).sum() > 50
+
+
+def test_oracle_glut_edges_match_reference_live(port):
+    """Edges of the general loop against the reference: a 3 x 3 grid, whose
+    clamped neighbourhoods repeat pixels (the corner's 3 x 3 region list
+    holds its own spectrum four times, extract_Rrs_data's clamping,
+    model/samodel.c:2974-2992), with a nodata pixel in the middle that every
+    neighbourhood leaves out."""
+    if not port.reference_available():
+        pytest.skip("reference sources not available on this host")
+    n = 3
+    grid = port.generate_field(3131, n, n, mask_frac=0.0)[0].reshape(1, n, n, 4)
+    grid[0, 1, 1, 2] = -9999.0
+    ref = port.reference_samodel_stack(grid, n_spatial=2, n_bottoms=3)
+    out, src, order, stats = port.glut_invert(grid, n_spatial=2, n_bottoms=3, n_chains=1,
+                                              nthreads=1)
+    keep = [0, 2, 3, 4, 5, 6, 7, 8, 9]
+    compare_grids(out, ref[keep], keep, "3x3")
+    assert order.size == 8 and src[4] == -2
+    assert out[0, 38] == 8  # the corner: 9 clamped slots less the nodata centre
+
+
+def test_oracle_glut_all_masked(port):
+    n = 4
+    grid = np.full((1, n, n, 4), -9999.0, np.float32)
+    out, src, order, stats = port.glut_invert(grid, n_chains=3, nthreads=1)
+    assert order.size == 0 and np.all(src == -2) and np.all(out[:, 9] == 1)
