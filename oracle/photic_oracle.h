@@ -12,11 +12,15 @@
  *   nelmin             model/asa047.c:10-502       (modified AS 47)
  *   samodel_optimise   model/samodel.c:1768-2115   (per-pixel driver) with
  *   samodel_optimise_one_bottom_combination  model/samodel.c:2119-2427
+ *   extract_Rrs_data   model/samodel.c:2957-3027   (3 x 3 regions)
+ *   samodel()'s pixel loop with its lookup table, model/samodel.c:649-1352
+ *   the depth uncertainty, model/samodel.c:1368-1479
  *   interp_1d          model/common.c:298-335
- * restricted to one spatial region per pixel (n_spatial <= 1), which is what
- * every synthetic configuration uses.  It is pinned bit-for-bit against the
- * reference compiled from its own sources (oracle/_ref, built by
- * oracle/Makefile) and against the committed fixtures in tests/golden/.
+ *   the netCDF packing, model/nc.c:14-320
+ * for one pixel or a 3 x 3 neighbourhood, one to three bottom types and
+ * stacks of scenes.  It is pinned bit for bit against the reference
+ * compiled from its own sources (oracle/_ref, built by oracle/Makefile) and
+ * against the committed fixtures in tests/golden/.
  */
 #ifndef PHOTIC_ORACLE_H
 #define PHOTIC_ORACLE_H
