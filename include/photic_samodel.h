@@ -186,23 +186,24 @@ int photic_config_from_scene(const photic_scene *scene, photic_config *cfg);
 
 /* model/samodel.h:8-19.  Fits every pixel that has data in all bands of all
  * scenes (model/samodel.c:672-700), at the reference's tolerances
- * (reqmin 1e-2, konvge 100, kcount 5000), smoothing radius 1 (none) only:
- *   - one scene, n_bottoms == 1, n_spatial <= 1: the reference's pixel
- *     loop with its dynamic lookup table (photic_lut_invert_batch): pixels
- *     in spectral-index order (times the spectral angle to the scene's
- *     R_sigma when every band's is at least 1e-6), or in the order of the
- *     empirical depths when given, served from stored fits or fitted with
- *     hot starts (from the empirical depth where a pixel has one); the order
- *     is cut into PHOTIC_LUT_CHAINS contiguous chains (environment; 1 is the
- *     reference on one thread), else eight per lane the kernel keeps
- *     resident;
- *   - n_bottoms 2..3, n_spatial == 2, or several scenes with empirical
- *     depths: the general fit of photic_region_fit_batch (bottom mixtures,
- *     3 x 3 regions, scene stacks; no lookup table);
- *   - several scenes otherwise: the temporal joint fit.
- * depth_sigma (one scene, the first two cases) is the reference's Monte
- * Carlo estimate computed by photic_depth_sigma with the scene's R_sigma,
- * 128 samples per 0.25 m interval and a fixed seed; 0 otherwise.  Depth is
+ * (reqmin 1e-2, konvge 100, kcount 5000), smoothing radius 1 (none) only,
+ * through the reference's pixel loop with its dynamic lookup table: pixels
+ * in spectral-index order (blue, green and red summed over the scenes; times
+ * the spectral angle to the scenes' R_sigma when every band's is at least
+ * 1e-6), or in the order of the empirical depths when given, served from
+ * stored fits or fitted with hot starts (from the empirical depth where a
+ * pixel has one); the order is cut into PHOTIC_LUT_CHAINS contiguous chains
+ * (environment; 1 is the reference on one thread), else eight per lane or
+ * warp the kernel keeps resident.  The fit is
+ *   - one scene, n_bottoms == 1, n_spatial <= 1: the single-pixel fit
+ *     (photic_lut_invert_batch, a lane per chain);
+ *   - otherwise (n_bottoms 2..3, n_spatial == 2, stacks of scenes): the
+ *     general fit of photic_region_fit_batch -- bottom mixtures, 3 x 3
+ *     regions, each scene's P, G, X (photic_region_lut_invert_batch, a warp
+ *     per chain).
+ * depth_sigma is the reference's Monte Carlo estimate, computed by
+ * photic_depth_sigma or photic_region_depth_sigma with the scenes' R_sigma,
+ * 128 samples per 0.25 m interval and a fixed seed.  Depth is
  * written negative below the datum, as the reference does
  * (model/samodel.c:1486).  Like the reference, it ends by writing the result
  * grids as netCDF files in the working directory (model/samodel.c:1492-1690):
