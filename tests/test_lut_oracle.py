@@ -93,3 +93,18 @@ def test_chains_are_independent_slices(port):
         mapped = np.where(s1 >= 0, sl[np.maximum(s1, 0)], s1)
         np.testing.assert_array_equal(src[sl], mapped)
         np.testing.assert_array_equal(stats[c], st1[0])
+
+
+def test_oracle_lut_eight_bands_matches_reference_live(port):
+    """Eight OLCI-like bands, whole nanometres (a scene record holds them as
+    int, model/common.h:200): the order and the spectral difference use
+    bands 1..3 of them."""
+    if not port.reference_available():
+        pytest.skip("reference sources not available on this host")
+    wl8 = (412.0, 442.0, 490.0, 510.0, 560.0, 620.0, 665.0, 709.0)
+    n = 32
+    rrs, _ = port.generate_field(8282, n, n, wl=wl8)
+    ref = port.reference_samodel_grid(rrs.reshape(n, n, 8), wl=wl8)
+    out, src, order, stats = port.lut_invert(rrs, wl=wl8, n_chains=1, nthreads=1)
+    _compare_grids(out, ref[[0, 2, 3, 7, 9]], [0, 2, 3, 7, 9], "eight bands")
+    assert np.mean(src[out[:, 9] == 0] >= 0) > 0.01
