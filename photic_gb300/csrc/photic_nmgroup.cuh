@@ -128,17 +128,70 @@ struct NmGroup {
     }
   }
 
-  __device__ __forceinline__ bool inner_top() {
-    if (kcount <= icount) return false;
+  // The worst vertex: the first index of the largest cost, a NaN cost
+  // never replacing the running one (a NaN at index 0 is kept, model/
+  // asa047.c:221-231).  With one cost copy for the warp, each lane scans
+  // the vertices j = lane, lane + 32, ... and the warp combines the lanes'
+  // (cost, index) by the larger cost, the smaller index on a tie.
+  __device__ __forceinline__ int worst_vertex() {
+    if constexpr (kSharedF) {
+#if defined(__CUDA_ARCH__)
+      const double f0 = F(0);
+      if (f0 != f0) return 0;
+      double v = 0.0;
+      int idx = 0x7fffffff;
+      for (int j = gl; j <= dim(); j += G) {
+        const double f = F(j);
+        if (f == f && (idx == 0x7fffffff || v < f)) {
+          v = f;
+          idx = j;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ov = __shfl_xor_sync(gmask, v, o);
+        const int oi = __shfl_xor_sync(gmask, idx, o);
+        if (oi != 0x7fffffff &&
+            (idx == 0x7fffffff || v < ov || (!(ov < v) && oi < idx))) {
+          v = ov;
+          idx = oi;
+        }
+      }
+      return idx;
+#endif
+    }
     double yhi = F(0);
-    hi = 0;
+    int h = 0;
     for (int j = 1; j <= dim(); j++) {
       const double fj = F(j);
       if (yhi < fj) {
         yhi = fj;
-        hi = j;
+        h = j;
       }
     }
+    return h;
+  }
+
+  // How many vertices cost more than fr (model/asa047.c:294-301): a count,
+  // so with one cost copy the lanes count their vertices and the warp adds.
+  __device__ __forceinline__ int count_worse(double fr_) {
+    if constexpr (kSharedF) {
+#if defined(__CUDA_ARCH__)
+      int c = 0;
+      for (int j = gl; j <= dim(); j += G)
+        if (fr_ < F(j)) c++;
+      return (int)__reduce_add_sync(gmask, (unsigned)c);
+#endif
+    }
+    int worse = 0;
+    for (int j = 0; j <= dim(); j++)
+      if (fr_ < F(j)) worse++;
+    return worse;
+  }
+
+  __device__ __forceinline__ bool inner_top() {
+    if (kcount <= icount) return false;
+    hi = worst_vertex();
 #pragma unroll
     for (int t = 0; t < C; t++)
       if (own(t)) {
@@ -232,9 +285,7 @@ struct NmGroup {
           set_x_from(trial);
           phase = PH_EXPAND;
         } else {
-          int worse = 0;
-          for (int j = 0; j <= dim(); j++)
-            if (fr < F(j)) worse++;
+          const int worse = count_worse(fr);
           if (worse > 1) {
             replace_hi(refl, fr);
             cs = CS_ITER_END;
